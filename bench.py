@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Benchmark: atom-timesteps/s of the 1M-atom LJ NVE step (mixed precision vs FP64).
+
+Workload (the benchmark's configuration 1): N = 1,048,576 LJ atoms
+(eps = 1, sigma = 1, cut 2.5 sigma') on a 128x128x64 simple-cubic lattice at
+number density 0.8 sigma'^-3 with a +-0.05 sigma' jitter, Gaussian velocities
+at T = 1, neighbour-list skin 0.3 sigma', CollectionVerlet with dt = 0.002.
+A "step" is one time step of the whole system (drift, pair forces, kick,
+rebuild test, and the list rebuild whenever the test fires).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun every rank runs an independent
+replica of the system (the single-system step has no data-parallel split).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "atom-timesteps/s (1M LJ, mixed vs FP64) at stated error"
+UNIT = "atom-timesteps/s"
+DT = 0.002
+SHAPE = (128, 128, 64)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles():
+    """dram bytes per launch of the force kernel from the committed ncu summary (if any)."""
+    p = ROOT / "profiles" / "force32_lj1m_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_1M:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """Sample nvidia-smi clocks / throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_system(w, precision, device):
+    from parm_gb300 import System
+    s = System(w.sizes, ndim=w.ndim, precision=precision)
+    s.set_boxes(w.L)
+    s.set_atoms(x=w.x, v=w.v, a=np.zeros_like(w.x), f=np.zeros_like(w.x), m=w.m)
+    s.set_interaction(w.kind, w.params, w.skin)
+    # Collection::initialize
+    s.nlist_update(False)
+    s.set_forces(True)
+    s.nlist_update(False)
+    return s
+
+
+def cpu_baseline_sample(w, max_steps=3):
+    """Time the oracle (a single-threaded restatement of the reference step) on the same system.
+
+    The reference's O(N^2) list build is infeasible at 1M atoms; the list is
+    installed through the oracle's cell-list construction (same pair set, not
+    timed) and only time steps without a rebuild are timed.  The O(N^2)
+    rebuild cost is measured at 16384 atoms and extrapolated by N^2.
+    """
+    from oracle.oracle import Oracle
+    o = Oracle(w.n, 3)
+    o.set_box(w.L[0])
+    o.set_state(x=w.x, v=w.v, a=np.zeros_like(w.x), f=np.zeros_like(w.x), m=w.m)
+    o.set_interaction(w.kind, w.params, w.skin)
+    o.build_fast()
+    o.set_forces(True)
+    which0 = o.which()
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        o.verlet(DT, 1)
+        steps += 1
+        if time.perf_counter() - t0 > 25:
+            break
+    dt = time.perf_counter() - t0
+    rebuilt = o.which() != which0
+    # O(N^2) rebuild at 16384 atoms
+    from parm_gb300 import workloads as W
+    ws = W.lj_lattice(shape=(32, 32, 16), skin_prime=0.3)
+    os_ = Oracle(ws.n, 3)
+    os_.set_box(ws.L[0])
+    os_.set_state(x=ws.x, v=ws.v, m=ws.m)
+    os_.set_interaction(ws.kind, ws.params, ws.skin)
+    t1 = time.perf_counter()
+    os_.nl_update(True)
+    tb = time.perf_counter() - t1
+    t_rebuild_1m = tb * (w.n / ws.n) ** 2
+    del o, os_
+    return {"value": w.n * steps / dt, "steps": steps, "seconds": dt, "rebuilt": rebuilt,
+            "rebuild_s_16k": tb, "rebuild_s_extrapolated": t_rebuild_1m}
+
+
+def run_reference(args, rank):
+    from parm_gb300 import workloads as W
+    w = W.lj_lattice(shape=SHAPE, skin_prime=0.3)
+    s = cpu_baseline_sample(w, max_steps=max(1, min(args.steps, 5)))
+    sample = (f"oracle port of the reference step on the full {w.n}-atom system, 1 host thread: "
+              f"{s['steps']} CollectionVerlet steps without a list rebuild in {s['seconds']:.1f} s; the "
+              f"reference's O(N^2) rebuild measured {s['rebuild_s_16k']:.2f} s at 16384 atoms, "
+              f"extrapolated {s['rebuild_s_extrapolated']:.0f} s at {w.n} atoms (not included)")
+    out = {"metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": s["steps"],
+           "warmup": 0, "ms_per_step": 1000 * s["seconds"] / s["steps"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": f"lj_nve_{w.n}_atoms", "n_atoms": w.n, "dt": DT,
+                      "skin_sigma": w.skin, "lattice": list(SHAPE)},
+           "cpu_baseline": {"value": s["value"], "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+           "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from parm_gb300 import capi, workloads as W
+    from parm_gb300.system import System
+    lib = capi.load()
+    capi.check(lib.parm_use_device(local_rank))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    w = W.lj_lattice(shape=SHAPE, skin_prime=0.3, seed=12345 + rank)
+    n = w.n
+    log(f"[rank {rank}] building mixed system, n={n}")
+    g = make_system(w, "mixed", local_rank)
+    g.set_graph_steps(50)
+    g.verlet(DT, args.warmup)
+    g.sync()
+    e_start = g.energy()[0] + g.kinetic_energy()[0]
+    stream = torch.cuda.ExternalStream(g.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local_rank)
+    g.timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    g.verlet(DT, args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = g.last_launches()
+    tr = g.timing_read()
+    g.timing(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    e_end = g.energy()[0] + g.kinetic_energy()[0]
+    value = world * n * args.steps / (ms / 1000.0)
+    npairs = int(g.numpairs()[0])
+
+    # --- roofline of the dominant kernel (the mixed pair-force kernel) ---
+    force_ms = tr["force_ms"] / max(1, tr["force_launches"])
+    nnb = 2.0 * npairs / n   # full-list entries per atom
+    bytes_per_atom = 232.0 + 4.0 * nnb
+    algo_bytes = n * bytes_per_atom
+    achieved = algo_bytes / (force_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = traffic_from_profiles()
+
+    result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)", "data": "synthetic",
+              "config": {"workload": f"lj_nve_{n}_atoms_mixed", "n_atoms": n, "lattice": list(SHAPE),
+                         "box": [float(v) for v in w.L[0]], "dt": DT, "skin_sigma": w.skin,
+                         "cutoff_sigma": float(w.params[0, 2]), "precision": "mixed",
+                         "parallelism": f"replicas{world}" if world > 1 else "single",
+                         "l2": "inputs larger than L2 (state + neighbour lists ~1 GB)",
+                         "steps_per_graph": 50},
+              "clocks": ck,
+              "gpu_launches": launches,
+              "rebuilds": tr["rebuilds"]}
+    result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "traffic": traffic,
+                          "kernel": "k_force32 (pair forces + kick + rebuild test)",
+                          "algorithmic_bytes_per_atom": bytes_per_atom, "force_ms_per_launch": force_ms,
+                          "peak_source": f"{peak_kind} hbm_gbs"}
+    result["energy_drift_rel"] = {"per_1e5_steps": abs(e_end - e_start) / abs(e_start) * 1e5 / args.steps,
+                                  "steps": args.steps}
+
+    # --- FP64 path on the same system, and mixed-vs-FP64 error at one state ---
+    st = g.get_atoms(capi.X | capi.V | capi.A)
+    w64 = W.lj_lattice(shape=SHAPE, skin_prime=0.3, seed=12345 + rank)
+    w64.x, w64.v = st["x"], st["v"]
+    g64 = make_system(w64, "fp64", local_rank)
+    g64.set_graph_steps(10)
+    k64 = max(3, min(40, args.steps // 10))
+    g64.verlet(DT, 2)
+    torch.cuda.synchronize()
+    s64 = torch.cuda.ExternalStream(g64.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s64)
+    g64.verlet(DT, k64)
+    e1.record(s64)
+    e1.synchronize()
+    v64 = n * k64 / (e0.elapsed_time(e1) / 1000.0)
+    # forces at one common state
+    st64 = g64.get_atoms(capi.X)
+    g.set_atoms(x=st64["x"])
+    g.nlist_update(True)
+    g64.nlist_update(True)
+    g.set_forces(False)
+    g64.set_forces(False)
+    F32 = g.get_atoms(capi.F)["f"]
+    F64 = g64.get_atoms(capi.F)["f"]
+    ferr = float(np.sqrt(((F32 - F64) ** 2).sum(1)).max() / np.sqrt((F64 ** 2).sum(1).mean()))
+    E32, E64 = g.energy()[0], g64.energy()[0]
+    result["fp64_value"] = world * v64
+    result["mixed_vs_fp64"] = value / (world * v64)
+    result["accuracy"] = {"max_force_err_over_rms_force": ferr, "rel_energy_err": abs(E32 - E64) / abs(E64)}
+    g64.close()
+
+    # --- end to end through the C ABI with host buffers ---
+    stride = 4 * 3 + 1
+    nbytes = n * stride * 8
+    import ctypes as C
+    hp = C.c_void_p()
+    capi.check(lib.parm_host_alloc(C.byref(hp), nbytes))
+    buf = np.ctypeslib.as_array((C.c_double * (n * stride)).from_address(hp.value)).reshape(n, stride)
+    cur = g.get_atoms(capi.X | capi.V | capi.A)
+    buf[:, 0:3], buf[:, 3:6], buf[:, 6:9] = cur["x"], cur["v"], cur["a"]
+    fields = capi.X | capi.V | capi.A
+    dptr = buf.ctypes.data_as(C.POINTER(C.c_double))
+    n_e2e = max(3, min(args.e2e_steps, args.steps))
+    for _ in range(2):
+        capi.check(lib.parm_set_atoms(g.h, dptr, stride, fields))
+        capi.check(lib.parm_verlet(g.h, DT, 1))
+        capi.check(lib.parm_get_atoms(g.h, dptr, stride, fields))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        capi.check(lib.parm_set_atoms(g.h, dptr, stride, fields))
+        capi.check(lib.parm_verlet(g.h, DT, 1))
+        capi.check(lib.parm_get_atoms(g.h, dptr, stride, fields))
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    result["e2e"] = {"value": world * n * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * 9 * 8,
+                     "d2h_bytes_per_step": n * 9 * 8, "steps": n_e2e,
+                     "api": "parm_set_atoms(x,v,a) + parm_verlet(dt, 1) + parm_get_atoms(x,v,a), pinned host AoS"}
+    lib.parm_host_free(hp)
+    g.close()
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        log("[rank 0] timing the CPU oracle sample")
+        s = cpu_baseline_sample(w)
+        result["cpu_baseline"] = {
+            "value": s["value"], "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": (f"oracle port, {s['steps']} CollectionVerlet steps of the same {n}-atom system on one "
+                       f"host thread ({s['seconds']:.1f} s), list installed by the cell-list construction "
+                       f"(untimed); reference O(N^2) rebuild: {s['rebuild_s_16k']:.2f} s at 16384 atoms, "
+                       f"~{s['rebuild_s_extrapolated']:.0f} s extrapolated to {n} (excluded)")}
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * parm_gb300 — C ABI of the GB300 MD time-step library.
+ *
+ * This is the boundary a host binding (C++, ctypes, SWIG, cgo, ...) links
+ * against: plain pointers and sizes, integer status codes, no C++ or CUDA
+ * types.  Every function returns PARM_OK (0) or a negative status; the text of
+ * the last error of the calling thread is available from parm_last_error().
+ *
+ * One handle (parm_system) owns the GPU state of `nsys` independent periodic
+ * systems (a single simulation is nsys == 1).  Atoms are addressed by their
+ * global index: system s owns indices [off_s, off_s + natoms[s]) with off_s the
+ * sum of the earlier systems' sizes.  Each entry point names the reference
+ * interface (wackywendell/parm, src/...) whose behaviour it provides.
+ *
+ * Threading: a handle is used from one host thread at a time; all GPU work of
+ * a handle runs on the handle's own CUDA stream.
+ */
+#ifndef PARM_GB300_H
+#define PARM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference raises the matching C++ exceptions) */
+#define PARM_OK 0
+#define PARM_ERR_ARG (-1)      /* std::invalid_argument */
+#define PARM_ERR_RUNTIME (-2)  /* std::runtime_error */
+#define PARM_ERR_CUDA (-3)     /* CUDA failure (no device, out of memory, ...) */
+#define PARM_ERR_CAPACITY (-4) /* neighbour list capacity exceeded; state after the call is invalid */
+
+/* arithmetic of the pair kernels */
+#define PARM_FP64 0  /* bit-exact with the reference CPU code */
+#define PARM_MIXED 1 /* FP32 pair forces, FP64 integration and reductions */
+
+/* pair interactions (the NListed<A,P> instantiations) */
+#define PARM_LJCUT 0     /* NListed<EpsSigCutAtom, LennardJonesCutPair>; params (epsilon, sigma, sigcut) */
+#define PARM_REPULSION 1 /* NListed<EpsSigExpAtom, RepulsionPair>;      params (eps, sigma, exponent) */
+#define PARM_LJREPULSE 2 /* NListed<EpsSigAtom, LJRepulsePair>;         params (epsilon, sigma, unused) */
+
+/* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
+#define PARM_X 1u
+#define PARM_V 2u
+#define PARM_A 4u
+#define PARM_F 8u
+#define PARM_M 16u
+
+/* parm_evaluate quantities (per system) */
+#define PARM_EVAL_ENERGY 0   /* NListed::energy            src/interaction.hpp:2152-2163 */
+#define PARM_EVAL_VIRIAL 1   /* NListed::pressure          src/interaction.hpp:2247-2260 */
+#define PARM_EVAL_STRESS 2   /* NListed::stress (ndim*ndim) src/interaction.hpp:2278-2291 */
+#define PARM_EVAL_CONTACTS 3 /* NListed::contacts          src/interaction.hpp:2124-2137 */
+#define PARM_EVAL_OVERLAPS 4 /* NListed::overlaps          src/interaction.hpp:2139-2150 */
+
+#define PARM_NOT_MEMBER 0xFFFFFFFFu
+
+typedef struct parm_system parm_system;
+
+/* Text of the calling thread's last error ("" when none). */
+const char* parm_last_error(void);
+
+/* Library ABI version (major * 100 + minor). */
+int parm_version(void);
+
+/* Select the CUDA device used by handles created afterwards on this thread. */
+int parm_use_device(int device);
+
+/* Create a handle for nsys systems of natoms[s] atoms in ndim (2 or 3)
+ * dimensions.  Replaces the reference's per-simulation storage:
+ * AtomVec(N, mass) (src/box.hpp:441-479) — masses start at 1, all vectors at 0. */
+int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* natoms, int precision);
+int parm_destroy(parm_system* s);
+
+/* Box side lengths, nsys*ndim doubles.  OriginBox(Vec size) and
+ * OriginBox::resize_to(Vec) without moving atoms (src/box.hpp:97-158, box.cpp:17-20). */
+int parm_set_boxes(parm_system* s, const double* L);
+
+/* Copy fields between the handle and host records laid out like the
+ * reference's AtomVec storage: record of atom i at atoms + i*stride (stride in
+ * doubles, >= 4*ndim+1) holding x[ndim], v[ndim], a[ndim], f[ndim], m.
+ * `fields` is an OR of PARM_X..PARM_M.  (AtomVec::operator[], src/box.hpp:470-471) */
+int parm_set_atoms(parm_system* s, const double* atoms, uint64_t stride, uint32_t fields);
+int parm_get_atoms(parm_system* s, double* atoms, uint64_t stride, uint32_t fields);
+
+/* Install the pair interaction and its neighbour list:
+ *   NListed<A,P>(box, atoms, skin) + NListed::add(A) for every atom with
+ *   rank[i] != PARM_NOT_MEMBER (src/interaction.hpp:1902-1914).
+ * params: natoms*3 doubles per kind (see PARM_LJCUT..).  rank[i] is the atom's
+ * position in the NeighborList (its insertion order, src/trackers.hpp:194-201),
+ * which fixes the reference's pair order; pass NULL for rank[i] = local index.
+ * Marks the list for a rebuild on the next update (ignorechanged = true). */
+int parm_set_interaction(parm_system* s, int kind, const double* params, const uint32_t* rank,
+                         double skin);
+
+/* NeighborList::ignore(a, b) (src/trackers.hpp:190-193). */
+int parm_nlist_ignore(parm_system* s, uint32_t a, uint32_t b);
+
+/* NeighborList::update_list(force) (src/trackers.cpp:19-85).  rebuilt (nsys
+ * bytes, may be NULL) receives 1 for systems whose list was rebuilt. */
+int parm_nlist_update(parm_system* s, int force, uint8_t* rebuilt);
+
+/* NeighborList::which() and numpairs() per system (src/trackers.hpp:186-187). */
+int parm_nlist_which(parm_system* s, uint32_t* which);
+int parm_nlist_numpairs(parm_system* s, uint64_t* numpairs);
+
+/* The pair list of system `sys` in the reference's order (NeighborList::begin()
+ * .. end(), get(i)): pairs[2k] = first (the later-added atom), pairs[2k+1] =
+ * last.  Writes min(cap, npairs) pairs and stores the total in *npairs. */
+int parm_nlist_pairs(parm_system* s, uint32_t sys, uint32_t* pairs, uint64_t cap, uint64_t* npairs);
+
+/* Collection::set_forces(constraints_and_a) (src/collection.cpp:159-179). */
+int parm_set_forces(parm_system* s, int constraints_and_a);
+
+/* Per-system interaction quantities (PARM_EVAL_*); out holds nsys values
+ * (nsys*ndim*ndim for the stress). */
+int parm_evaluate(parm_system* s, int what, double* out);
+
+/* Time steps (each equals `nsteps` calls of the reference's timestep()):
+ *   CollectionVerlet::timestep  src/collection.cpp:442-469
+ *   CollectionDamped::timestep  src/collection.cpp:356-381 (constants 339-354)
+ *   CollectionSol::timestep     src/collection.cpp:265-322 (constants 230-263)
+ * CollectionSol draws its Gaussian pairs from a counter-based generator
+ * (Philox4x32-10 keyed by splitmix64(seed + s), counter = (atom, step)), not
+ * from the reference's global Mersenne twister. */
+int parm_verlet(parm_system* s, double dt, uint32_t nsteps);
+int parm_damped(parm_system* s, double dt, double damping, uint32_t nsteps);
+int parm_sol(parm_system* s, double dt, double damping, double T, uint64_t seed, uint32_t nsteps);
+
+/* AtomGroup::kinetic_energy(origin) per system (src/box.cpp:401-411);
+ * origin: nsys*ndim doubles or NULL. */
+int parm_kinetic_energy(parm_system* s, const double* origin, double* out);
+/* AtomGroup::momentum() and mass() per system (src/box.cpp:237-258). */
+int parm_momentum(parm_system* s, double* momentum, double* mass);
+/* max over mobile atoms of |f|^2, per system (minimisation convergence). */
+int parm_max_force_sq(parm_system* s, double* out);
+
+/* Langevin step counter (advanced once per parm_sol step; the counter used
+ * by a step is the value after the advance). */
+int parm_get_step(parm_system* s, uint64_t* step);
+int parm_set_step(parm_system* s, uint64_t step);
+
+/* Neighbour capacity per atom (grown automatically at set-up from the density). */
+int parm_set_nlist_capacity(parm_system* s, uint32_t maxnb);
+int parm_get_nlist_capacity(parm_system* s, uint32_t* maxnb);
+
+/* Steps captured per CUDA graph launch (default 16). */
+int parm_set_graph_steps(parm_system* s, uint32_t k);
+
+/* Kernel timing: when enabled, time-step calls record CUDA events around the
+ * pair-force kernel of every step and accumulate their durations. */
+int parm_timing(parm_system* s, int enable);
+int parm_timing_read(parm_system* s, double* force_ms, uint64_t* force_launches, double* drift_ms,
+                     uint64_t* rebuilds);
+
+/* Number of kernel launches issued by the last time-step call. */
+int parm_last_launches(parm_system* s, uint64_t* launches);
+
+/* Wait for all GPU work of the handle. */
+int parm_sync(parm_system* s);
+/* The handle's cudaStream_t, as an opaque pointer. */
+void* parm_stream(parm_system* s);
+
+/* Page-locked host memory for fast parm_set_atoms / parm_get_atoms. */
+int parm_host_alloc(void** p, uint64_t bytes);
+int parm_host_free(void* p);
+
+/* Evaluate the library's minimum-image routine remainder(d[i], L[i]) on the
+ * GPU (test hook for the exact IEEE remainder used by OriginBox::diff). */
+int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

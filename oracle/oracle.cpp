@@ -1,0 +1,679 @@
+// ORACLE — test infrastructure only, never part of the product path.
+//
+// A scalar CPU restatement of ParM's MD hot path (wackywendell/parm), written
+// to reproduce the reference's floating-point evaluation order exactly so that
+// the CUDA FP64 path can be checked bit-for-bit.  Only the test-suite, the
+// smoke check and bench.py's CPU-baseline leg load this library.
+//
+// Parity status: pinned.  The fixtures under tests/golden/ are produced by the
+// reference's own sources (src/box.cpp, src/trackers.cpp, src/collection.cpp,
+// src/vecrand.cpp and the NListed templates of src/interaction.hpp) compiled
+// against a small restatement of the Eigen/Boost subset they use
+// (oracle/refbuild/), and tests/test_oracle_golden.py checks this file
+// against them.  The Langevin noise stream is the project's counter-based
+// generator (the reference draws from Boost's mt19937, which cannot be
+// reproduced), so Langevin parity with the reference is statistical.
+//
+// Evaluation-order facts taken from the reference (all FP64, no FMA; build
+// with -ffp-contract=off):
+//   * OriginBox::diff = remainder(r1 - r2, L) per component (box.hpp:68-78,103)
+//   * Eigen fixed-size 3-vector squaredNorm/dot reduce as ((v0 + v1) + v2)
+//     (2-wide packet pre-reduction followed by the tail element)
+//   * norm = sqrt(squaredNorm)
+//   * coefficient-wise expressions evaluate left to right per component.
+//
+// Build:  g++ -O2 -ffp-contract=off -fPIC -shared -std=c++17 oracle.cpp
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <algorithm>
+#include <set>
+#include <vector>
+#include <utility>
+
+namespace {
+
+enum PairKind { LJCUT = 0, REPULSION = 1, LJREPULSE = 2 };
+
+struct V3 {
+    double c[3] = {0, 0, 0};
+};
+
+// Eigen squaredNorm / dot order for NDIM=3: ((a0*b0 + a1*b1) + a2*b2);
+// for NDIM=2: a0*b0 + a1*b1.
+inline double dotv(const double* a, const double* b, int nd) {
+    double s = a[0] * b[0] + a[1] * b[1];
+    if (nd == 3) s = s + a[2] * b[2];
+    return s;
+}
+
+struct AtomParams {
+    double p0 = 0, p1 = 0, p2 = 0;  // kind-dependent (eps, sigma, sigcut|exponent)
+};
+
+struct PairConst {
+    // LennardJonesCutPair / RepulsionPair / LJRepulsePair constructor outputs
+    double eps, sig, third, cut_energy;
+};
+
+struct System {
+    int nd;
+    uint32_t n;
+    double L[3] = {1, 1, 1};
+    std::vector<double> x, v, a, f, m;  // n*nd each (AoS of Vec)
+
+    // NListed<A,P> + NeighborList state (interaction.hpp:1876-1945, trackers.hpp:157-214)
+    int kind = -1;
+    double skin = 0;
+    std::vector<uint32_t> members;      // SubGroup order (insertion order)
+    std::vector<double> diameters;      // A::max_size() per member
+    std::vector<double> lastlocs;       // per member
+    std::vector<AtomParams> params;     // indexed by AtomVec index
+    std::vector<uint8_t> has_params;
+    std::vector<std::pair<uint32_t, uint32_t>> curpairs;  // (first.n, last.n)
+    std::set<std::pair<uint32_t, uint32_t>> ignored;      // (max, min) by AtomVec index
+    uint32_t updatenum = 0;
+    bool ignorechanged = true;
+
+    System(int nd_, uint32_t n_) : nd(nd_), n(n_), x(n_ * nd_), v(n_ * nd_), a(n_ * nd_),
+                                   f(n_ * nd_), m(n_, 1.0), params(n_), has_params(n_, 0) {}
+
+    // OriginBox::diff (box.hpp:103) with vec_mod (box.hpp:68-78)
+    inline void diff(const double* r1, const double* r2, double* out) const {
+        for (int d = 0; d < nd; d++) out[d] = std::remainder(r1[d] - r2[d], L[d]);
+    }
+
+    PairConst pair_const(uint32_t i, uint32_t j) const {
+        // P(atoms[first], atoms[last]) with first = i (interaction.hpp:2109-2113)
+        const AtomParams& A = params[i];
+        const AtomParams& B = params[j];
+        PairConst pc{};
+        if (kind == LJCUT) {
+            // LennardJonesCutPair(EpsSigCutAtom, EpsSigCutAtom) (interaction.hpp:967-976)
+            // and LennardJonesCut ctor (interaction.hpp:250-255)
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2;
+            pc.third = std::max(A.p2, B.p2);
+            double rsix = std::pow(pc.third, 6);
+            double mid = (1 - 1 / rsix);
+            pc.cut_energy = pc.eps * (mid * mid - 1);
+        } else if (kind == REPULSION) {
+            // RepulsionPair(EpsSigExpAtom, EpsSigExpAtom) (interaction.hpp:1532-1537)
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2.0;
+            pc.third = (A.p2 + B.p2) / 2.0;
+            pc.cut_energy = 0;
+        } else {
+            // LJRepulsePair(EpsSigAtom, EpsSigAtom) (interaction.hpp:875-880)
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2;
+            pc.third = 0;
+            pc.cut_energy = 0;
+        }
+        return pc;
+    }
+
+    // P::energy(box) for the three pair kinds
+    double pair_energy(const PairConst& pc, const double* rij) const {
+        double dsq = dotv(rij, rij, nd);
+        if (kind == LJCUT) {
+            // LennardJonesCut::energy (interaction.hpp:256-262)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > (pc.third * pc.third)) return 0;
+            double rsix = rsq * rsq * rsq;
+            double mid = (1 - 1 / rsix);
+            return pc.eps * (mid * mid - 1) - pc.cut_energy;
+        } else if (kind == REPULSION) {
+            // RepulsionPair::energy (interaction.hpp:1544-1550)
+            if (dsq > pc.sig * pc.sig) return 0.0;
+            double R = std::sqrt(dsq);
+            return pc.eps * std::pow(1.0 - (R / pc.sig), pc.third) / pc.third;
+        } else {
+            // LJRepulsive::energy (interaction.hpp:127-134)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > 1) return 0;
+            double rsix = rsq * rsq * rsq;
+            double mid = (1 - 1 / rsix);
+            return pc.eps * (mid * mid);
+        }
+    }
+
+    // P::forces(box); returns false when the pair is beyond its cutoff (force = 0)
+    bool pair_force(const PairConst& pc, const double* rij, double* fo) const {
+        double dsq = dotv(rij, rij, nd);
+        double s;
+        if (kind == LJCUT) {
+            // LennardJonesCut::forces (interaction.hpp:263-271)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > (pc.third * pc.third)) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double rsix = rsq * rsq * rsq;
+            double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
+            s = fmagTimesR / dsq;
+        } else if (kind == REPULSION) {
+            // RepulsionPair::forces (interaction.hpp:1551-1556)
+            if (dsq > pc.sig * pc.sig) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double R = std::sqrt(dsq);
+            s = pc.eps * std::pow(1.0 - (R / pc.sig), pc.third - 1) / pc.sig / R;
+        } else {
+            // LJRepulsive::forces (interaction.hpp:136-150)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > 1) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double rsix = rsq * rsq * rsq;
+            double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
+            s = fmagTimesR / dsq;
+        }
+        for (int d = 0; d < nd; d++) fo[d] = rij[d] * s;
+        return true;
+    }
+
+    double max_size(uint32_t i) const {
+        // EpsSigCutAtom::max_size (interaction.hpp:904), EpsSigExpAtom (1464), EpsSigAtom (864)
+        if (kind == LJCUT) return params[i].p1 * params[i].p2;
+        return params[i].p1;
+    }
+
+    bool is_ignored(uint32_t i, uint32_t j) const {
+        uint32_t hi = std::max(i, j), lo = std::min(i, j);
+        return ignored.count({hi, lo}) > 0;
+    }
+
+    // NeighborList::update_list (trackers.cpp:19-85)
+    bool update_list(bool force) {
+        const size_t M = members.size();
+        if (!force && !ignorechanged) {
+            double bigdist = 0, biggestdist = 0;
+            for (size_t k = 0; k < M; k++) {
+                const double* xi = &x[members[k] * nd];
+                double dd[3];
+                for (int d = 0; d < nd; d++) dd[d] = xi[d] - lastlocs[k * nd + d];
+                double curdist = std::sqrt(dotv(dd, dd, nd));
+                if (curdist > biggestdist) {
+                    bigdist = biggestdist;
+                    biggestdist = curdist;
+                } else if (curdist > bigdist) {
+                    bigdist = curdist;
+                } else
+                    continue;
+                if (bigdist + biggestdist >= skin) {
+                    force = true;
+                    break;
+                }
+            }
+            if (!force) return false;
+        }
+        updatenum++;
+        ignorechanged = false;
+        curpairs.clear();
+        for (size_t i = 0; i < M; i++) {
+            uint32_t ai = members[i];
+            const double* xi = &x[ai * nd];
+            for (int d = 0; d < nd; d++) lastlocs[i * nd + d] = xi[d];
+            for (size_t j = 0; j < i; j++) {
+                uint32_t aj = members[j];
+                if (is_ignored(ai, aj)) continue;
+                double diam = (diameters[i] + diameters[j]) / 2;
+                double r[3];
+                diff(xi, &x[aj * nd], r);
+                if (std::sqrt(dotv(r, r, nd)) < (diam + skin)) curpairs.push_back({ai, aj});
+            }
+        }
+        return true;
+    }
+
+    // NListed::set_forces (interaction.hpp:2165-2175); adds into f
+    void nlisted_set_forces(bool want_p, double* p_out, double* stress_out) {
+        double p = 0;
+        double st[9] = {0};
+        for (auto& pr : curpairs) {
+            PairConst pc = pair_const(pr.first, pr.second);
+            double r[3], fo[3];
+            diff(&x[pr.first * nd], &x[pr.second * nd], r);
+            pair_force(pc, r, fo);
+            for (int d = 0; d < nd; d++) {
+                f[pr.first * nd + d] += fo[d];
+                f[pr.second * nd + d] -= fo[d];
+            }
+            if (want_p) {
+                // set_forces_get_pressure (2231-2245) / set_forces_get_stress (2262-2276)
+                p += dotv(r, fo, nd);
+                for (int aa = 0; aa < nd; aa++)
+                    for (int bb = 0; bb < nd; bb++) st[aa * nd + bb] += r[aa] * fo[bb];
+            }
+        }
+        if (p_out) *p_out = p;
+        if (stress_out) std::memcpy(stress_out, st, sizeof(double) * nd * nd);
+    }
+
+    // NListed::energy (2152-2163)
+    double nlisted_energy() const {
+        double E = 0;
+        for (auto& pr : curpairs) {
+            PairConst pc = pair_const(pr.first, pr.second);
+            double r[3];
+            diff(&x[pr.first * nd], &x[pr.second * nd], r);
+            E += pair_energy(pc, r);
+        }
+        return E;
+    }
+
+    // NListed::pressure (2247-2260) and stress (2278-2291)
+    double nlisted_pressure(double* stress_out) const {
+        double p = 0;
+        double st[9] = {0};
+        for (auto& pr : curpairs) {
+            PairConst pc = pair_const(pr.first, pr.second);
+            double r[3], fo[3];
+            diff(&x[pr.first * nd], &x[pr.second * nd], r);
+            pair_force(pc, r, fo);
+            p += dotv(r, fo, nd);
+            for (int aa = 0; aa < nd; aa++)
+                for (int bb = 0; bb < nd; bb++) st[aa * nd + bb] += r[aa] * fo[bb];
+        }
+        if (stress_out) std::memcpy(stress_out, st, sizeof(double) * nd * nd);
+        return p;
+    }
+
+    // NListed::contacts / overlaps (2124-2150)
+    uint64_t nlisted_count(bool overlaps) const {
+        uint64_t c = 0;
+        for (auto& pr : curpairs) {
+            PairConst pc = pair_const(pr.first, pr.second);
+            double r[3];
+            diff(&x[pr.first * nd], &x[pr.second * nd], r);
+            double E = pair_energy(pc, r);
+            if (overlaps ? (E > 0.0) : (E != 0.0)) c++;
+        }
+        return c;
+    }
+
+    static bool mobile(double mm) { return !(mm <= 0 || std::isinf(mm)); }
+
+    // AtomGroup::reset_forces (box.cpp:427-431) + Collection::set_forces (collection.cpp:159-179)
+    void collection_set_forces(bool constraints_and_a) {
+        std::fill(f.begin(), f.end(), 0.0);
+        if (kind >= 0) nlisted_set_forces(false, nullptr, nullptr);
+        if (!constraints_and_a) return;
+        for (uint32_t i = 0; i < n; i++) {
+            if (!mobile(m[i])) {
+                for (int d = 0; d < nd; d++) a[i * nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < nd; d++) a[i * nd + d] = f[i * nd + d] / m[i];
+        }
+    }
+
+    void update_trackers() {
+        if (kind >= 0) update_list(false);
+    }
+
+    // CollectionVerlet::timestep (collection.cpp:442-469)
+    void verlet(double dt) {
+        for (uint32_t i = 0; i < n; i++) {
+            if (!mobile(m[i])) {
+                for (int d = 0; d < nd; d++) v[i * nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < nd; d++) {
+                x[i * nd + d] += v[i * nd + d] * dt + a[i * nd + d] * (dt * dt / 2);
+                v[i * nd + d] += a[i * nd + d] * (dt / 2);
+            }
+        }
+        collection_set_forces(false);
+        for (uint32_t i = 0; i < n; i++) {
+            if (!mobile(m[i])) {
+                for (int d = 0; d < nd; d++) a[i * nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < nd; d++) {
+                a[i * nd + d] = f[i * nd + d] / m[i];
+                v[i * nd + d] += a[i * nd + d] * (dt / 2);
+            }
+        }
+        update_trackers();
+    }
+
+    // CollectionDamped::timestep (collection.cpp:356-381); c0,c1,c2 from set_constants (339-354)
+    void damped(double dt, double c0, double c1, double c2) {
+        for (uint32_t i = 0; i < n; i++) {
+            if (!mobile(m[i])) {
+                for (int d = 0; d < nd; d++) v[i * nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < nd; d++) {
+                x[i * nd + d] += v[i * nd + d] * (c1 * dt) + a[i * nd + d] * (c2 * dt * dt);
+                v[i * nd + d] = v[i * nd + d] * c0 + a[i * nd + d] * (dt * (c1 - c2));
+            }
+        }
+        collection_set_forces(true);
+        for (uint32_t i = 0; i < n; i++) {
+            if (!mobile(m[i])) continue;
+            for (int d = 0; d < nd; d++) v[i * nd + d] += a[i * nd + d] * (dt * c2);
+        }
+        update_trackers();
+    }
+
+    // CollectionSol::timestep (collection.cpp:265-322) with the counter-based
+    // Gaussian pair generator standing in for BivariateGauss::gen_vecs.
+    void sol(double dt, double damping, double T, double c0, double c1, double c2,
+             double x11, double x21, double x22, uint64_t seed, uint64_t step);
+};
+
+// ---- counter-based normal generator (Philox4x32-10, Salmon et al. SC'11) ----
+inline void philox_round(uint32_t c[4], const uint32_t k[2]) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c[1] ^ k[0];
+    uint32_t n2 = hi0 ^ c[3] ^ k[1];
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+}
+
+inline void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    uint32_t k[2] = {k0, k1};
+    for (int r = 0; r < 10; r++) {
+        philox_round(c, k);
+        k[0] += 0x9E3779B9u;
+        k[1] += 0xBB67AE85u;
+    }
+}
+
+inline double u53(uint32_t a, uint32_t b) {
+    uint64_t v = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    return ((double)v + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// Six standard normals for (seed, step, atom): Philox blocks 0..2, Box-Muller.
+void normals6(uint64_t seed, uint64_t step, uint32_t atom, double out[6]) {
+    for (uint32_t blk = 0; blk < 3; blk++) {
+        uint32_t c[4] = {atom, (uint32_t)step, (uint32_t)(step >> 32), blk};
+        philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        double u1 = u53(c[0], c[1]);
+        double u2 = u53(c[2], c[3]);
+        double r = std::sqrt(-2.0 * std::log(u1));
+        double th = 6.283185307179586 * u2;
+        out[2 * blk] = r * std::cos(th);
+        out[2 * blk + 1] = r * std::sin(th);
+    }
+}
+
+void System::sol(double dt, double damping, double T, double c0, double c1, double c2,
+                 double x11, double x21, double x22, uint64_t seed, uint64_t step) {
+    for (uint32_t i = 0; i < n; i++) {
+        if (m[i] <= 0 || std::isinf(m[i])) {
+            for (int d = 0; d < nd; d++) v[i * nd + d] = 0;
+            continue;
+        }
+        double v0 = std::sqrt(T / m[i]);
+        double r0 = dt * v0;
+        double g[6] = {0, 0, 0, 0, 0, 0};
+        double drG[3] = {0, 0, 0}, dvG[3] = {0, 0, 0};
+        if (damping > 0) {
+            normals6(seed, step, i, g);
+            // BivariateGauss::gen_vecs (vecrand.cpp:73-85): x1 = g[0..nd), x2 = g[nd..2nd)
+            for (int d = 0; d < nd; d++) {
+                drG[d] = g[d] * x11;
+                dvG[d] = g[d] * x21 + g[nd + d] * x22;
+            }
+        }
+        for (int d = 0; d < nd; d++) {
+            x[i * nd + d] += v[i * nd + d] * (c1 * dt) + a[i * nd + d] * (c2 * dt * dt) + drG[d] * r0;
+            v[i * nd + d] = v[i * nd + d] * c0 + a[i * nd + d] * (dt * (c1 - c2)) + dvG[d] * v0;
+        }
+    }
+    collection_set_forces(false);
+    for (uint32_t i = 0; i < n; i++) {
+        if (m[i] == 0 || std::isinf(m[i])) {
+            for (int d = 0; d < nd; d++) a[i * nd + d] = 0;
+            continue;
+        }
+        for (int d = 0; d < nd; d++) a[i * nd + d] = f[i * nd + d] / m[i];
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        if (m[i] == 0 || std::isinf(m[i])) {
+            for (int d = 0; d < nd; d++) v[i * nd + d] = 0;
+            continue;
+        }
+        for (int d = 0; d < nd; d++) v[i * nd + d] += a[i * nd + d] * (dt * c2);
+    }
+    update_trackers();
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_create(int ndim, uint32_t n) {
+    if (ndim != 2 && ndim != 3) return nullptr;
+    return new System(ndim, n);
+}
+void orc_destroy(void* s) { delete static_cast<System*>(s); }
+
+void orc_set_box(void* s, const double* L) {
+    System* S = static_cast<System*>(s);
+    for (int d = 0; d < S->nd; d++) S->L[d] = L[d];
+}
+
+// arrays are (n, ndim) row-major (an AtomVec's x/v/a/f fields), m is (n,)
+void orc_set_state(void* s, const double* x, const double* v, const double* a, const double* f,
+                   const double* m) {
+    System* S = static_cast<System*>(s);
+    size_t k = (size_t)S->n * S->nd;
+    if (x) std::memcpy(S->x.data(), x, k * 8);
+    if (v) std::memcpy(S->v.data(), v, k * 8);
+    if (a) std::memcpy(S->a.data(), a, k * 8);
+    if (f) std::memcpy(S->f.data(), f, k * 8);
+    if (m) std::memcpy(S->m.data(), m, (size_t)S->n * 8);
+}
+
+void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* m) {
+    System* S = static_cast<System*>(s);
+    size_t k = (size_t)S->n * S->nd;
+    if (x) std::memcpy(x, S->x.data(), k * 8);
+    if (v) std::memcpy(v, S->v.data(), k * 8);
+    if (a) std::memcpy(a, S->a.data(), k * 8);
+    if (f) std::memcpy(f, S->f.data(), k * 8);
+    if (m) std::memcpy(m, S->m.data(), (size_t)S->n * 8);
+}
+
+// NListed(box, atoms, skin) (interaction.hpp:1911-1914)
+int orc_set_interaction(void* s, int kind, double skin) {
+    System* S = static_cast<System*>(s);
+    if (kind < 0 || kind > 2) return -1;
+    S->kind = kind;
+    S->skin = skin;
+    return 0;
+}
+
+// NListed::add(A) -> NeighborList::add(atm, atm.max_size()) (interaction.hpp:1906-1910,
+// trackers.hpp:194-201)
+int orc_add_atom(void* s, uint32_t i, const double* p) {
+    System* S = static_cast<System*>(s);
+    if (i >= S->n || S->has_params[i]) return -1;
+    S->params[i].p0 = p[0];
+    S->params[i].p1 = p[1];
+    S->params[i].p2 = (S->kind == LJREPULSE) ? 0.0 : p[2];
+    S->has_params[i] = 1;
+    S->members.push_back(i);
+    S->diameters.push_back(S->max_size(i));
+    for (int d = 0; d < S->nd; d++) S->lastlocs.push_back(S->x[i * S->nd + d]);
+    S->ignorechanged = true;
+    return 0;
+}
+
+// NeighborList::ignore (trackers.hpp:190-193)
+void orc_ignore(void* s, uint32_t i, uint32_t j) {
+    System* S = static_cast<System*>(s);
+    S->ignored.insert({std::max(i, j), std::min(i, j)});
+    S->ignorechanged = true;
+}
+
+int orc_nl_update(void* s, int force) { return static_cast<System*>(s)->update_list(force != 0) ? 1 : 0; }
+uint32_t orc_nl_which(void* s) { return static_cast<System*>(s)->updatenum; }
+uint64_t orc_nl_numpairs(void* s) { return static_cast<System*>(s)->curpairs.size(); }
+void orc_nl_get_pairs(void* s, uint32_t* out) {
+    System* S = static_cast<System*>(s);
+    for (size_t k = 0; k < S->curpairs.size(); k++) {
+        out[2 * k] = S->curpairs[k].first;
+        out[2 * k + 1] = S->curpairs[k].second;
+    }
+}
+
+double orc_energy(void* s) { return static_cast<System*>(s)->nlisted_energy(); }
+double orc_pressure(void* s, double* stress) { return static_cast<System*>(s)->nlisted_pressure(stress); }
+uint64_t orc_contacts(void* s) { return static_cast<System*>(s)->nlisted_count(false); }
+uint64_t orc_overlaps(void* s) { return static_cast<System*>(s)->nlisted_count(true); }
+
+// Collection::set_forces(constraints_and_a); when p/stress given, the
+// NListed::set_forces_get_pressure / set_forces_get_stress accumulations too.
+void orc_set_forces(void* s, int constraints_and_a, double* p, double* stress) {
+    System* S = static_cast<System*>(s);
+    std::fill(S->f.begin(), S->f.end(), 0.0);
+    S->nlisted_set_forces(p || stress, p, stress);
+    if (!constraints_and_a) return;
+    for (uint32_t i = 0; i < S->n; i++) {
+        for (int d = 0; d < S->nd; d++)
+            S->a[i * S->nd + d] = System::mobile(S->m[i]) ? S->f[i * S->nd + d] / S->m[i] : 0.0;
+    }
+}
+
+// Collection::initialize (collection.cpp:13-19)
+void orc_initialize(void* s) {
+    System* S = static_cast<System*>(s);
+    S->update_trackers();
+    S->collection_set_forces(true);
+    S->update_trackers();
+}
+
+void orc_update_trackers(void* s) { static_cast<System*>(s)->update_trackers(); }
+
+void orc_verlet(void* s, double dt, uint32_t nsteps) {
+    System* S = static_cast<System*>(s);
+    for (uint32_t k = 0; k < nsteps; k++) S->verlet(dt);
+}
+
+void orc_damped(void* s, double dt, double c0, double c1, double c2, uint32_t nsteps) {
+    System* S = static_cast<System*>(s);
+    for (uint32_t k = 0; k < nsteps; k++) S->damped(dt, c0, c1, c2);
+}
+
+void orc_sol(void* s, double dt, double damping, double T, double c0, double c1, double c2,
+             double x11, double x21, double x22, uint64_t seed, uint64_t step0, uint32_t nsteps) {
+    System* S = static_cast<System*>(s);
+    for (uint32_t k = 0; k < nsteps; k++)
+        S->sol(dt, damping, T, c0, c1, c2, x11, x21, x22, seed, step0 + k);
+}
+
+void orc_normals6(uint64_t seed, uint64_t step, uint32_t atom, double* out) {
+    normals6(seed, step, atom, out);
+}
+
+// AtomGroup::kinetic_energy(originvelocity) (box.cpp:401-411)
+double orc_kinetic_energy(void* s, const double* origin) {
+    System* S = static_cast<System*>(s);
+    double totE = 0;
+    for (uint32_t i = 0; i < S->n; i++) {
+        double mm = S->m[i];
+        if (mm == 0 || std::isinf(mm)) continue;
+        double cv[3] = {0, 0, 0};
+        for (int d = 0; d < S->nd; d++) cv[d] = S->v[i * S->nd + d] - (origin ? origin[d] : 0.0);
+        totE += mm / 2 * dotv(cv, cv, S->nd);
+    }
+    return totE;
+}
+
+// AtomGroup::momentum (box.cpp:249-258) and mass (237-245)
+double orc_momentum(void* s, double* out) {
+    System* S = static_cast<System*>(s);
+    double tot[3] = {0, 0, 0};
+    double mass = 0;
+    for (uint32_t i = 0; i < S->n; i++) {
+        double mm = S->m[i];
+        if (mm <= 0 || std::isinf(mm)) continue;
+        for (int d = 0; d < S->nd; d++) tot[d] += S->v[i * S->nd + d] * mm;
+        mass += mm;
+    }
+    for (int d = 0; d < S->nd; d++) out[d] = tot[d];
+    return mass;
+}
+
+// A cell-list construction of the same pair set as update_list(true), for
+// sizes where the reference's O(N^2) loop is too slow to use as a checker.
+// Output order matches curpairs: i ascending over members, j ascending < i.
+// Returns the number of pairs written (or required, when cap is too small).
+uint64_t orc_pairs_celllist(void* s, uint32_t* out, uint64_t cap) {
+    System* S = static_cast<System*>(s);
+    const int nd = S->nd;
+    const size_t M = S->members.size();
+    double dmax = 0;
+    for (double d : S->diameters) dmax = std::max(dmax, d);
+    const double rl = dmax + S->skin;
+    int nc[3] = {1, 1, 1};
+    for (int d = 0; d < nd; d++) {
+        int c = (int)std::floor(S->L[d] / rl);
+        nc[d] = c >= 3 ? c : 1;
+    }
+    size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
+    std::vector<std::vector<uint32_t>> cells(ncell);
+    std::vector<int> cellof(M * 3);
+    for (size_t k = 0; k < M; k++) {
+        const double* xi = &S->x[S->members[k] * nd];
+        int ci[3] = {0, 0, 0};
+        for (int d = 0; d < nd; d++) {
+            double w = xi[d] - std::floor(xi[d] / S->L[d]) * S->L[d];
+            int c = (int)std::floor(w / S->L[d] * nc[d]);
+            if (c < 0) c = 0;
+            if (c >= nc[d]) c = nc[d] - 1;
+            ci[d] = c;
+            cellof[k * 3 + d] = c;
+        }
+        cells[(size_t)(ci[2] * nc[1] + ci[1]) * nc[0] + ci[0]].push_back((uint32_t)k);
+    }
+    uint64_t cnt = 0;
+    std::vector<uint32_t> nb;
+    for (size_t i = 0; i < M; i++) {
+        nb.clear();
+        int r[3] = {nc[0] >= 3 ? 1 : 0, nc[1] >= 3 ? 1 : 0, (nd == 3 && nc[2] >= 3) ? 1 : 0};
+        for (int dz = -r[2]; dz <= r[2]; dz++)
+            for (int dy = -r[1]; dy <= r[1]; dy++)
+                for (int dx = -r[0]; dx <= r[0]; dx++) {
+                    int c0 = (cellof[i * 3] + dx + nc[0]) % nc[0];
+                    int c1 = (cellof[i * 3 + 1] + dy + nc[1]) % nc[1];
+                    int c2 = (cellof[i * 3 + 2] + dz + nc[2]) % nc[2];
+                    for (uint32_t j : cells[(size_t)(c2 * nc[1] + c1) * nc[0] + c0])
+                        if (j < i) nb.push_back(j);
+                }
+        std::sort(nb.begin(), nb.end());
+        uint32_t ai = S->members[i];
+        for (uint32_t j : nb) {
+            uint32_t aj = S->members[j];
+            if (S->is_ignored(ai, aj)) continue;
+            double diam = (S->diameters[i] + S->diameters[j]) / 2;
+            double rr[3];
+            S->diff(&S->x[ai * nd], &S->x[aj * nd], rr);
+            if (std::sqrt(dotv(rr, rr, nd)) < (diam + S->skin)) {
+                if (cnt < cap) {
+                    out[2 * cnt] = ai;
+                    out[2 * cnt + 1] = aj;
+                }
+                cnt++;
+            }
+        }
+    }
+    return cnt;
+}
+
+// Install a pair list directly (used with orc_pairs_celllist for large N):
+// equivalent to the state after update_list(true) at the current positions.
+void orc_nl_install(void* s, const uint32_t* pairs, uint64_t npairs) {
+    System* S = static_cast<System*>(s);
+    S->curpairs.resize(npairs);
+    for (uint64_t k = 0; k < npairs; k++) S->curpairs[k] = {pairs[2 * k], pairs[2 * k + 1]};
+    for (size_t k = 0; k < S->members.size(); k++)
+        for (int d = 0; d < S->nd; d++) S->lastlocs[k * S->nd + d] = S->x[S->members[k] * S->nd + d];
+    S->updatenum++;
+    S->ignorechanged = false;
+}
+
+}  // extern "C"

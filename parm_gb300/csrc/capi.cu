@@ -1,0 +1,1102 @@
+// Host side of the C ABI declared in include/parm_gb300.h: handle
+// management, layout conversion, neighbour-list bookkeeping and the
+// graph-captured time-step loops.
+//
+// A time step is captured once per (integrator, steps-per-launch) as a CUDA
+// graph:  arm -> IF(rebuild needed) { rebuild chain } -> drift -> pair forces.
+// The arm kernel consumes the displacement test accumulated by the previous
+// step's force kernel and sets the conditional node's value, so a step without
+// a rebuild costs three kernel launches and no host round trip.  The reference
+// runs its rebuild test at the end of a step (Collection::update_trackers);
+// here it is resolved at the start of the next step, which sees identical
+// positions.  Calls that need the reference's post-step list state (queries,
+// uploads, force evaluations) first resolve a pending test ("flush").
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "parm_ctx.cuh"
+#include "parm_gb300.h"
+
+using namespace parm;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (expr);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(PARM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define TRY(expr)                 \
+    do {                          \
+        int r_ = (expr);          \
+        if (r_ != PARM_OK) return r_; \
+    } while (0)
+
+uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+struct GraphEntry {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> ev;  // per step: drift start, force start, force end
+    uint32_t k = 0;
+};
+
+enum StepMode { SM_VERLET = 0, SM_DAMPED = 1, SM_SOL = 2 };
+}  // namespace
+
+struct parm_system {
+    DevCtx c{};
+    int nd = 3, prec = 0;
+    uint32_t nsys = 0, n = 0;
+    std::vector<uint32_t> natoms, off;
+    std::vector<SysConst> sys;
+    std::vector<double> L;
+    std::vector<uint32_t> bucket_off;
+    int kind = -1;
+    double skin = 0.0;
+    std::vector<double> prm_in;      // n*3 (global order)
+    std::vector<uint32_t> rank_in;   // global order
+    std::vector<std::set<uint32_t>> excl;
+    bool have_excl = false, excl_dirty = false;
+    cudaStream_t st = nullptr, st2 = nullptr;
+    std::vector<void*> allocs;
+    void* cell_mem = nullptr;
+    void* nbr_mem = nullptr;
+    void* excl_mem = nullptr;
+    double* staging = nullptr;
+    size_t staging_bytes = 0;
+    double* d_origin = nullptr;
+    StepParams* h_params = nullptr;
+    std::map<uint64_t, GraphEntry> graphs;
+    uint32_t graph_k = 16;
+    bool timing = false;
+    double t_force = 0.0, t_drift = 0.0;
+    uint64_t n_force = 0, n_rebuild = 0;
+    bool pending = false;
+    uint64_t last_launches = 0;
+
+    ~parm_system() {
+        clear_graphs();
+        for (void* p : allocs) cudaFree(p);
+        if (cell_mem) cudaFree(cell_mem);
+        if (nbr_mem) cudaFree(nbr_mem);
+        if (excl_mem) cudaFree(excl_mem);
+        if (staging) cudaFree(staging);
+        if (h_params) cudaFreeHost(h_params);
+        if (st) cudaStreamDestroy(st);
+        if (st2) cudaStreamDestroy(st2);
+    }
+
+    void clear_graphs() {
+        for (auto& kv : graphs) {
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+            if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+            for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
+        }
+        graphs.clear();
+    }
+
+    template <class T>
+    int alloc(T*& p, size_t count) {
+        void* q = nullptr;
+        size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+        CUDA_TRY(cudaMalloc(&q, bytes));
+        CUDA_TRY(cudaMemsetAsync(q, 0, bytes, st));
+        allocs.push_back(q);
+        p = static_cast<T*>(q);
+        return PARM_OK;
+    }
+    int allocv(void*& p, size_t count, size_t elem) {
+        char* q = nullptr;
+        TRY(alloc(q, count * elem));
+        p = q;
+        return PARM_OK;
+    }
+    size_t vbytes() const { return nd == 3 ? 32 : 16; }
+
+    int sync_status() {
+        CUDA_TRY(cudaStreamSynchronize(st));
+        uint32_t stw = 0;
+        CUDA_TRY(cudaMemcpy(&stw, c.status, 4, cudaMemcpyDeviceToHost));
+        if (stw) {
+            CUDA_TRY(cudaMemset(c.status, 0, 4));
+            if (stw & ST_NBR_OVERFLOW)
+                return fail(PARM_ERR_CAPACITY,
+                            "neighbour list capacity exceeded (" + std::to_string(c.maxnb) +
+                                " per atom); raise it with parm_set_nlist_capacity");
+            if (stw & ST_SORT_CAP)
+                return fail(PARM_ERR_CAPACITY, "FP64 path: a neighbour list exceeded 256 entries");
+            if (stw & ST_NONFINITE) return fail(PARM_ERR_RUNTIME, "non-finite atom position");
+            return fail(PARM_ERR_RUNTIME, "device status " + std::to_string(stw));
+        }
+        return PARM_OK;
+    }
+
+    // ---- cell grids (depend on the boxes and on the largest list radius) ----
+    int setup_cells() {
+        double dmax = 0.0;
+        bool any_member = false;
+        for (uint32_t i = 0; i < n; i++) {
+            if (kind < 0 || rank_in[i] == PARM_NOT_MEMBER) continue;
+            any_member = true;
+            const double* p = &prm_in[3 * (size_t)i];
+            double d = (kind == PARM_LJCUT) ? p[1] * p[2] : p[1];
+            dmax = std::max(dmax, d);
+        }
+        const double rl = dmax + skin;
+        bucket_off.assign(nsys + 1, 0);
+        uint32_t total = 0;
+        for (uint32_t s = 0; s < nsys; s++) {
+            SysConst& S = sys[s];
+            for (int d = 0; d < 3; d++) S.nc[d] = 1;
+            if (any_member && rl > 0.0) {
+                for (int d = 0; d < nd; d++) {
+                    double w = rl * (1.0 + 1e-9);
+                    double q = std::floor(S.L[d] / w);
+                    int ncd = q >= 3.0 ? (int)std::min(q, 1024.0) : 1;
+                    S.nc[d] = ncd;
+                }
+                // keep the grid no larger than ~2 cells per atom
+                double cap = std::max(64.0, 2.0 * natoms[s]);
+                while ((double)S.nc[0] * S.nc[1] * S.nc[2] > cap) {
+                    int big = 0;
+                    for (int d = 1; d < nd; d++)
+                        if (S.nc[d] > S.nc[big]) big = d;
+                    S.nc[big] = S.nc[big] * 3 / 4;
+                    if (S.nc[big] < 3) S.nc[big] = 1;
+                }
+            }
+            S.ncell = (uint32_t)(S.nc[0] * S.nc[1] * S.nc[2]);
+            for (int d = 0; d < 3; d++) S.cellw_inv[d] = (float)(S.nc[d] / S.L[d]);
+            S.skin = skin;
+            S.rlist_max = rl;
+            S.cell_off = total;
+            bucket_off[s] = total;
+            total += S.ncell + 1;
+        }
+        bucket_off[nsys] = total;
+        if (cell_mem) cudaFree(cell_mem);
+        cell_mem = nullptr;
+        CUDA_TRY(cudaMalloc(&cell_mem, (size_t)(2 * (size_t)total + 2) * 4));
+        CUDA_TRY(cudaMemsetAsync(cell_mem, 0, (size_t)(2 * (size_t)total + 2) * 4, st));
+        c.cell_count = static_cast<uint32_t*>(cell_mem);
+        c.cell_start = c.cell_count + total + 1;
+        c.nbucket = total;
+        CUDA_TRY(cudaMemcpyAsync(const_cast<SysConst*>(c.sys), sys.data(), sizeof(SysConst) * nsys,
+                                 cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(const_cast<uint32_t*>(c.bucket_off), bucket_off.data(),
+                                 4 * (nsys + 1), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        clear_graphs();
+        return PARM_OK;
+    }
+
+    // (re)allocate the neighbour list; the current lists are kept (a larger
+    // capacity only appends columns), so no rebuild is implied
+    int set_capacity(uint32_t maxnb) {
+        maxnb = std::max<uint32_t>(8, (maxnb + 7) / 8 * 8);
+        void* fresh = nullptr;
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaMalloc(&fresh, (size_t)maxnb * c.nalloc * 4));
+        if (nbr_mem) {
+            uint32_t keep = std::min(maxnb, c.maxnb);
+            CUDA_TRY(cudaMemcpy(fresh, nbr_mem, (size_t)keep * c.nalloc * 4, cudaMemcpyDeviceToDevice));
+            if (maxnb < c.maxnb) {
+                // shrinking: lists longer than the new capacity are rebuilt
+                std::vector<uint32_t> ones(nsys, kind >= 0 ? 1u : 0u);
+                CUDA_TRY(cudaMemcpy(c.force_rb, ones.data(), 4 * nsys, cudaMemcpyHostToDevice));
+            }
+            cudaFree(nbr_mem);
+        }
+        nbr_mem = fresh;
+        c.nbr = static_cast<uint32_t*>(nbr_mem);
+        c.maxnb = maxnb;
+        clear_graphs();
+        return PARM_OK;
+    }
+
+    int request_rebuild_all() {
+        std::vector<uint32_t> ones(nsys, 1u);
+        CUDA_TRY(cudaMemcpy(c.force_rb, ones.data(), 4 * nsys, cudaMemcpyHostToDevice));
+        return PARM_OK;
+    }
+
+    uint32_t estimate_capacity() const {
+        double worst = 8.0;
+        for (uint32_t s = 0; s < nsys; s++) {
+            const SysConst& S = sys[s];
+            double V = S.L[0] * S.L[1] * (nd == 3 ? S.L[2] : 1.0);
+            double rho = natoms[s] / V;
+            double rl = S.rlist_max;
+            double vol = (nd == 3) ? 4.18879020478639 * rl * rl * rl : 3.14159265358979 * rl * rl;
+            worst = std::max(worst, rho * vol);
+        }
+        double est = 1.6 * worst + 24.0;
+        if (est > 4096.0) est = 4096.0;
+        return (uint32_t)std::ceil(est);
+    }
+
+    int upload_exclusions() {
+        if (!excl_dirty) return PARM_OK;
+        excl_dirty = false;
+        if (excl_mem) cudaFree(excl_mem);
+        excl_mem = nullptr;
+        c.excl_off = nullptr;
+        c.excl_list = nullptr;
+        if (!have_excl) return PARM_OK;
+        std::vector<uint32_t> offs(n + 1, 0), lst;
+        for (uint32_t i = 0; i < n; i++) {
+            offs[i] = (uint32_t)lst.size();
+            for (uint32_t j : excl[i]) lst.push_back(j);
+        }
+        offs[n] = (uint32_t)lst.size();
+        CUDA_TRY(cudaMalloc(&excl_mem, 4 * (offs.size() + lst.size() + 1)));
+        uint32_t* p = static_cast<uint32_t*>(excl_mem);
+        CUDA_TRY(cudaMemcpy(p, offs.data(), 4 * offs.size(), cudaMemcpyHostToDevice));
+        if (!lst.empty())
+            CUDA_TRY(cudaMemcpy(p + offs.size(), lst.data(), 4 * lst.size(), cudaMemcpyHostToDevice));
+        c.excl_off = p;
+        c.excl_list = p + offs.size();
+        clear_graphs();
+        return PARM_OK;
+    }
+
+    // resolve the rebuild test left pending by the last time step
+    int flush() {
+        TRY(upload_exclusions());
+        if (!pending) return PARM_OK;
+        pending = false;
+        launch_arm(c, st, 0, 0, 0);
+        launch_rebuild(c, st);
+        CUDA_TRY(cudaGetLastError());
+        return sync_status();
+    }
+
+    int upload_params(const StepParams& p) {
+        *h_params = p;
+        // the step counter lives on the device; copy everything before it
+        CUDA_TRY(cudaMemcpyAsync(c.params, h_params, offsetof(StepParams, step),
+                                 cudaMemcpyHostToDevice, st));
+        return PARM_OK;
+    }
+
+    int build_graph(int mode, uint32_t k, GraphEntry& ge) {
+        ge.k = k;
+        if (timing) {
+            ge.ev.resize(3 * (size_t)k);
+            for (auto& e : ge.ev) CUDA_TRY(cudaEventCreate(&e));
+        }
+        const int dmode = mode == SM_VERLET ? DM_VERLET : (mode == SM_DAMPED ? DM_DAMPED : DM_SOL);
+        const int fmode = mode == SM_VERLET ? FM_VERLET : (mode == SM_DAMPED ? FM_DAMPED : FM_SOL);
+        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (uint32_t step = 0; step < k; step++) {
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t g = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t ndeps = 0;
+            CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+            cudaGraphConditionalHandle h;
+            CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+            launch_arm(c, st, 1, 1, (unsigned long long)h);
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+            // the struct's union has members without default constructors:
+            // build it in zeroed storage
+            alignas(cudaGraphNodeParams) unsigned char cpbuf[sizeof(cudaGraphNodeParams)];
+            std::memset(cpbuf, 0, sizeof(cpbuf));
+            cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cpbuf);
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+            CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                                         cudaStreamSetCaptureDependencies));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            CUDA_TRY(cudaStreamBeginCaptureToGraph(st2, body, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal));
+            launch_rebuild(c, st2);
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaStreamEndCapture(st2, &body));
+            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step], st));
+            launch_drift(c, st, dmode);
+            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step + 1], st));
+            if (prec == PREC_FP64) launch_force64(c, st, fmode);
+            else launch_force32(c, st, fmode);
+            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step + 2], st));
+            CUDA_TRY(cudaGetLastError());
+        }
+        CUDA_TRY(cudaStreamEndCapture(st, &ge.graph));
+        CUDA_TRY(cudaGraphInstantiate(&ge.exec, ge.graph, 0));
+        return PARM_OK;
+    }
+
+    int run_steps(int mode, uint32_t nsteps) {
+        TRY(upload_exclusions());
+        uint32_t w0 = 0;
+        std::vector<uint32_t> which0(nsys), which1(nsys);
+        CUDA_TRY(cudaMemcpyAsync(which0.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost, st));
+        uint32_t done = 0;
+        uint64_t launches = 0;
+        while (done < nsteps) {
+            uint32_t k = std::min(graph_k, nsteps - done);
+            uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)k << 1) | (timing ? 1u : 0u);
+            auto it = graphs.find(key);
+            if (it == graphs.end()) {
+                GraphEntry ge;
+                int r = build_graph(mode, k, ge);
+                if (r != PARM_OK) {
+                    cudaStreamCaptureStatus cs;
+                    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                        cudaGraph_t junk;
+                        cudaStreamEndCapture(st, &junk);
+                        if (junk) cudaGraphDestroy(junk);
+                    }
+                    return r;
+                }
+                it = graphs.emplace(key, ge).first;
+            }
+            CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
+            launches += 3ull * k;
+            if (timing) {
+                CUDA_TRY(cudaStreamSynchronize(st));
+                for (uint32_t q = 0; q < k; q++) {
+                    float a = 0.f, b = 0.f;
+                    CUDA_TRY(cudaEventElapsedTime(&a, it->second.ev[3 * q], it->second.ev[3 * q + 1]));
+                    CUDA_TRY(cudaEventElapsedTime(&b, it->second.ev[3 * q + 1], it->second.ev[3 * q + 2]));
+                    t_drift += a;
+                    t_force += b;
+                }
+                n_force += k;
+            }
+            done += k;
+        }
+        pending = true;
+        TRY(sync_status());
+        CUDA_TRY(cudaMemcpy(which1.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
+        uint64_t rb = 0;
+        for (uint32_t s = 0; s < nsys; s++) rb += (uint64_t)(which1[s] - which0[s]);
+        (void)w0;
+        n_rebuild += rb;
+        uint32_t chains = 0;
+        CUDA_TRY(cudaMemcpy(&chains, c.chains, 4, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemset(c.chains, 0, 4));
+        last_launches = launches + (uint64_t)chains * (c.prec == PREC_FP64 ? 9ull : 8ull);
+        return PARM_OK;
+    }
+
+    int reduce_sys(int ncomp, std::vector<double>& out) {
+        launch_sys_reduce(c, st, ncomp);
+        CUDA_TRY(cudaGetLastError());
+        int nc = ncomp < 0 ? 1 : ncomp;
+        out.resize((size_t)nsys * nc);
+        CUDA_TRY(cudaMemcpyAsync(out.data(), c.sysout, 8 * out.size(), cudaMemcpyDeviceToHost, st));
+        return sync_status();
+    }
+
+    int ensure_staging(size_t bytes) {
+        if (bytes <= staging_bytes) return PARM_OK;
+        if (staging) cudaFree(staging);
+        staging = nullptr;
+        staging_bytes = 0;
+        CUDA_TRY(cudaMalloc(&staging, bytes));
+        staging_bytes = bytes;
+        return PARM_OK;
+    }
+};
+
+// field span inside an Atom record: [lo, hi) in doubles
+static void field_span(uint32_t fields, int nd, uint64_t& lo, uint64_t& hi) {
+    lo = 4 * (uint64_t)nd + 1;
+    hi = 0;
+    const uint64_t offs[5] = {0, (uint64_t)nd, 2 * (uint64_t)nd, 3 * (uint64_t)nd, 4 * (uint64_t)nd};
+    const uint64_t lens[5] = {(uint64_t)nd, (uint64_t)nd, (uint64_t)nd, (uint64_t)nd, 1};
+    for (int b = 0; b < 5; b++) {
+        if (fields & (1u << b)) {
+            lo = std::min(lo, offs[b]);
+            hi = std::max(hi, offs[b] + lens[b]);
+        }
+    }
+}
+
+extern "C" {
+
+const char* parm_last_error(void) { return g_err.c_str(); }
+
+int parm_version(void) { return 100; }
+
+int parm_use_device(int device) {
+    if (device < 0) return fail(PARM_ERR_ARG, "device must be >= 0");
+    CUDA_TRY(cudaSetDevice(device));
+    return PARM_OK;
+}
+
+int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* natoms, int precision) {
+    if (!out) return fail(PARM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (ndim != 2 && ndim != 3) return fail(PARM_ERR_ARG, "ndim must be 2 or 3");
+    if (nsys == 0 || !natoms) return fail(PARM_ERR_ARG, "need at least one system");
+    if (precision != PARM_FP64 && precision != PARM_MIXED) return fail(PARM_ERR_ARG, "bad precision");
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < nsys; s++) total += natoms[s];
+    if (total == 0) return fail(PARM_ERR_ARG, "no atoms");
+    if (total >= (1ull << 31)) return fail(PARM_ERR_ARG, "too many atoms for one handle");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    parm_system* S = new parm_system();
+    S->nd = ndim;
+    S->prec = precision;
+    S->nsys = nsys;
+    S->n = (uint32_t)total;
+    S->natoms.assign(natoms, natoms + nsys);
+    S->off.resize(nsys);
+    uint32_t o = 0;
+    for (uint32_t s = 0; s < nsys; s++) {
+        S->off[s] = o;
+        o += natoms[s];
+    }
+    auto bail = [&](int r) {
+        delete S;
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&S->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->st2, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(PARM_ERR_CUDA, "cudaStreamCreate failed"));
+    DevCtx& c = S->c;
+    c.nd = ndim;
+    c.prec = precision;
+    c.kind = -1;
+    c.nsys = nsys;
+    c.n = S->n;
+    c.nalloc = S->n;
+    const uint32_t n = S->n;
+    const size_t vb = S->vbytes();
+    int r = PARM_OK;
+#define A(expr)          \
+    r = (expr);          \
+    if (r != PARM_OK) return bail(r);
+    A(S->allocv(c.x, n, vb));
+    A(S->allocv(c.v, n, vb));
+    A(S->allocv(c.a, n, vb));
+    A(S->allocv(c.f, n, vb));
+    A(S->allocv(c.lastloc, n, vb));
+    A(S->allocv(c.x2, n, vb));
+    A(S->allocv(c.v2, n, vb));
+    A(S->allocv(c.a2, n, vb));
+    A(S->allocv(c.f2, n, vb));
+    A(S->alloc(c.f32, n));
+    A(S->alloc(c.f32b, n));
+    A(S->alloc(c.m, n));
+    A(S->alloc(c.m2, n));
+    A(S->alloc(c.invm32, n));
+    A(S->alloc(c.invm32b, n));
+    A(S->alloc(c.prm, n));
+    A(S->alloc(c.prm2, n));
+    A(S->alloc(c.prm32, n));
+    A(S->alloc(c.prm32b, n));
+    A(S->alloc(c.diam, n));
+    A(S->alloc(c.diam2, n));
+    A(S->alloc(c.rank, n));
+    A(S->alloc(c.rank2, n));
+    A(S->alloc(c.orig, n));
+    A(S->alloc(c.orig2, n));
+    A(S->alloc(c.slot, n));
+    A(S->alloc(c.atom_sys, n));
+    A(S->alloc(c.nm_rank, n));
+    A(S->alloc(c.bucket, n));
+    A(S->alloc(c.bucket2, n));
+    A(S->alloc(c.cslot, n));
+    A(S->alloc(c.perm, n));
+    A(S->alloc(c.nnb, n));
+    A(S->alloc(c.posA, n));
+    A(S->alloc(c.posB, n));
+    A(S->alloc(c.red, (size_t)n * 12));
+    A(S->alloc(c.flag, nsys));
+    A(S->alloc(c.force_rb, nsys));
+    A(S->alloc(c.top, 2 * (size_t)nsys));
+    A(S->alloc(c.which, nsys));
+    A(S->alloc(c.seed, nsys));
+    A(S->alloc(c.status, 1));
+    A(S->alloc(c.any_flag, 1));
+    A(S->alloc(c.chains, 1));
+    A(S->alloc(c.params, 1));
+    A(S->alloc(c.sysout, (size_t)nsys * 16));
+    A(S->alloc(S->d_origin, (size_t)nsys * 3));
+    {
+        SysConst* dsys = nullptr;
+        A(S->alloc(dsys, nsys));
+        c.sys = dsys;
+        uint32_t* bo = nullptr;
+        A(S->alloc(bo, nsys + 1));
+        c.bucket_off = bo;
+    }
+#undef A
+    if (cudaMallocHost(&S->h_params, sizeof(StepParams)) != cudaSuccess)
+        return bail(fail(PARM_ERR_CUDA, "cudaMallocHost failed"));
+    std::memset(S->h_params, 0, sizeof(StepParams));
+    // identity order, masses 1, unit boxes
+    std::vector<uint32_t> ident(n), sysid(n), nmr(n);
+    for (uint32_t s = 0; s < nsys; s++)
+        for (uint32_t i = 0; i < natoms[s]; i++) {
+            ident[S->off[s] + i] = S->off[s] + i;
+            sysid[S->off[s] + i] = s;
+            nmr[S->off[s] + i] = i;
+        }
+    std::vector<double> ones(n, 1.0);
+    std::vector<float> onesf(n, 1.0f);
+    std::vector<uint32_t> notm(n, PARM_NOT_MEMBER);
+    auto up = [&](void* d, const void* h, size_t bytes) {
+        return cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    cudaStreamSynchronize(S->st);
+    if (!up(c.orig, ident.data(), 4 * (size_t)n) || !up(c.slot, ident.data(), 4 * (size_t)n) ||
+        !up(c.atom_sys, sysid.data(), 4 * (size_t)n) || !up(c.nm_rank, nmr.data(), 4 * (size_t)n) ||
+        !up(c.m, ones.data(), 8 * (size_t)n) || !up(c.invm32, onesf.data(), 4 * (size_t)n) ||
+        !up(c.rank, notm.data(), 4 * (size_t)n))
+        return bail(fail(PARM_ERR_CUDA, "initial upload failed"));
+    S->prm_in.assign(3 * (size_t)n, 0.0);
+    S->rank_in.assign(n, PARM_NOT_MEMBER);
+    S->excl.resize(n);
+    S->L.assign((size_t)nsys * ndim, 1.0);
+    S->sys.resize(nsys);
+    for (uint32_t s = 0; s < nsys; s++) {
+        SysConst& Y = S->sys[s];
+        std::memset(&Y, 0, sizeof(Y));
+        for (int d = 0; d < 3; d++) {
+            Y.L[d] = 1.0;
+            Y.invL[d] = 1.0;
+            Y.halfL[d] = 0.5;
+            Y.Lhi[d] = 1.0f;
+            Y.Llo[d] = 0.0f;
+            Y.invLf[d] = 1.0f;
+        }
+        Y.atom_off = S->off[s];
+        Y.natoms = natoms[s];
+    }
+    r = S->setup_cells();
+    if (r != PARM_OK) return bail(r);
+    r = S->set_capacity(32);
+    if (r != PARM_OK) return bail(r);
+    *out = S;
+    return PARM_OK;
+}
+
+int parm_destroy(parm_system* s) {
+    if (s) {
+        cudaStreamSynchronize(s->st);
+        delete s;
+    }
+    return PARM_OK;
+}
+
+int parm_set_boxes(parm_system* S, const double* L) {
+    if (!S || !L) return fail(PARM_ERR_ARG, "NULL argument");
+    TRY(S->flush());
+    for (uint32_t s = 0; s < S->nsys; s++) {
+        SysConst& Y = S->sys[s];
+        for (int d = 0; d < S->nd; d++) {
+            double l = L[(size_t)s * S->nd + d];
+            if (!(l > 0.0) || !std::isfinite(l)) return fail(PARM_ERR_ARG, "box lengths must be positive");
+            Y.L[d] = l;
+            Y.invL[d] = 1.0 / l;
+            Y.halfL[d] = 0.5 * l;
+            Y.Lhi[d] = (float)l;
+            Y.Llo[d] = (float)(l - (double)Y.Lhi[d]);
+            Y.invLf[d] = (float)(1.0 / l);
+            S->L[(size_t)s * S->nd + d] = l;
+        }
+    }
+    TRY(S->setup_cells());
+    if (S->kind >= 0) {
+        uint32_t need = S->estimate_capacity();
+        if (need > S->c.maxnb) TRY(S->set_capacity(need));
+    }
+    return PARM_OK;
+}
+
+int parm_set_atoms(parm_system* S, const double* atoms, uint64_t stride, uint32_t fields) {
+    if (!S || !atoms) return fail(PARM_ERR_ARG, "NULL argument");
+    if (stride < 4 * (uint64_t)S->nd + 1) return fail(PARM_ERR_ARG, "stride smaller than an Atom record");
+    if (fields & ~31u) return fail(PARM_ERR_ARG, "unknown field bits");
+    if (!fields) return PARM_OK;
+    TRY(S->flush());
+    uint64_t lo, hi;
+    field_span(fields, S->nd, lo, hi);
+    TRY(S->ensure_staging((size_t)S->n * stride * 8));
+    CUDA_TRY(cudaMemcpy2DAsync(S->staging + lo, stride * 8, atoms + lo, stride * 8, (hi - lo) * 8, S->n,
+                               cudaMemcpyHostToDevice, S->st));
+    launch_scatter_in(S->c, S->st, S->staging, stride, fields);
+    CUDA_TRY(cudaGetLastError());
+    return S->sync_status();
+}
+
+int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fields) {
+    if (!S || !atoms) return fail(PARM_ERR_ARG, "NULL argument");
+    if (stride < 4 * (uint64_t)S->nd + 1) return fail(PARM_ERR_ARG, "stride smaller than an Atom record");
+    if (fields & ~31u) return fail(PARM_ERR_ARG, "unknown field bits");
+    if (!fields) return PARM_OK;
+    uint64_t lo, hi;
+    field_span(fields, S->nd, lo, hi);
+    TRY(S->ensure_staging((size_t)S->n * stride * 8));
+    uint64_t covered = 0;
+    for (int b = 0; b < 5; b++)
+        if (fields & (1u << b)) covered += (b == 4) ? 1 : (uint64_t)S->nd;
+    if (covered != hi - lo) {
+        // keep the caller's other fields intact: bring the span over first
+        CUDA_TRY(cudaMemcpy2DAsync(S->staging + lo, stride * 8, atoms + lo, stride * 8, (hi - lo) * 8,
+                                   S->n, cudaMemcpyHostToDevice, S->st));
+    }
+    launch_gather_out(S->c, S->st, S->staging, stride, fields);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpy2DAsync(atoms + lo, stride * 8, S->staging + lo, stride * 8, (hi - lo) * 8, S->n,
+                               cudaMemcpyDeviceToHost, S->st));
+    return S->sync_status();
+}
+
+int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
+                         double skin) {
+    if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
+    if (kind < 0 || kind > 2) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (!(skin >= 0.0) || !std::isfinite(skin)) return fail(PARM_ERR_ARG, "skin must be >= 0");
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    const uint32_t n = S->n;
+    S->kind = kind;
+    S->skin = skin;
+    S->prm_in.assign(params, params + 3 * (size_t)n);
+    S->rank_in.resize(n);
+    for (uint32_t s = 0; s < S->nsys; s++) {
+        std::set<uint32_t> seen;
+        for (uint32_t i = 0; i < S->natoms[s]; i++) {
+            uint32_t g = S->off[s] + i;
+            uint32_t rk = rank ? rank[g] : i;
+            if (rk != PARM_NOT_MEMBER && !seen.insert(rk).second)
+                return fail(PARM_ERR_ARG, "duplicate neighbour-list rank in a system");
+            S->rank_in[g] = rk;
+        }
+    }
+    // per-atom parameter records in the caller's order
+    std::vector<AtomPrm> prm(n);
+    std::vector<float4> prm32(n);
+    std::vector<double> diam(n);
+    std::vector<uint32_t> nmr(n, 0);
+    bool first = true;
+    double e0 = 0, s0 = 0, t0 = 0;
+    uint32_t uni = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_SIG_ONE;
+    for (uint32_t s = 0; s < S->nsys; s++) {
+        uint32_t nm = 0;
+        for (uint32_t i = 0; i < S->natoms[s]; i++) {
+            uint32_t g = S->off[s] + i;
+            const double* p = &params[3 * (size_t)g];
+            AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], 0.0};
+            if (kind == PARM_LJCUT) a.p3 = 1 - 1 / std::pow(a.p2, 6);  // LennardJonesCut ctor
+            prm[g] = a;
+            prm32[g] = make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
+            diam[g] = (kind == PARM_LJCUT) ? a.p1 * a.p2 : a.p1;   // A::max_size()
+            if (S->rank_in[g] == PARM_NOT_MEMBER) {
+                nmr[g] = nm++;
+                continue;
+            }
+            if (!(a.p1 > 0.0) || !(a.p0 >= 0.0)) return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
+            if (first) {
+                e0 = a.p0;
+                s0 = a.p1;
+                t0 = a.p2;
+                first = false;
+            }
+            if (a.p0 != e0) uni &= ~UNI_EPS;
+            if (a.p1 != s0) uni &= ~UNI_SIG;
+            if (a.p2 != t0) uni &= ~UNI_THIRD;
+            if (a.p1 != 1.0) uni &= ~UNI_SIG_ONE;
+        }
+    }
+    if (!(uni & UNI_SIG)) uni &= ~UNI_SIG_ONE;
+    // internal order of the device arrays
+    std::vector<uint32_t> orig(n);
+    CUDA_TRY(cudaMemcpy(orig.data(), S->c.orig, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    std::vector<AtomPrm> prm_k(n);
+    std::vector<float4> prm32_k(n);
+    std::vector<double> diam_k(n);
+    std::vector<uint32_t> rank_k(n);
+    for (uint32_t k = 0; k < n; k++) {
+        uint32_t g = orig[k];
+        prm_k[k] = prm[g];
+        prm32_k[k] = prm32[g];
+        diam_k[k] = diam[g];
+        rank_k[k] = S->rank_in[g];
+    }
+    CUDA_TRY(cudaMemcpy(S->c.prm, prm_k.data(), sizeof(AtomPrm) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->c.prm32, prm32_k.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->c.diam, diam_k.data(), 8 * (size_t)n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->c.rank, rank_k.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->c.nm_rank, nmr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+    S->c.kind = kind;
+    S->c.uniform = uni;
+    launch_posq(S->c, S->st);
+    CUDA_TRY(cudaGetLastError());
+    TRY(S->setup_cells());
+    uint32_t need = S->estimate_capacity();
+    if (need > S->c.maxnb) TRY(S->set_capacity(need));
+    return S->request_rebuild_all();  // ignorechanged = true
+}
+
+int parm_nlist_ignore(parm_system* S, uint32_t a, uint32_t b) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (a >= S->n || b >= S->n) return fail(PARM_ERR_ARG, "atom index out of range");
+    TRY(S->flush());
+    S->excl[a].insert(b);
+    S->excl[b].insert(a);
+    S->have_excl = true;
+    S->excl_dirty = true;
+    // ignorechanged = true for the system(s) involved
+    uint32_t sa = (uint32_t)(std::upper_bound(S->off.begin(), S->off.end(), a) - S->off.begin() - 1);
+    uint32_t sb = (uint32_t)(std::upper_bound(S->off.begin(), S->off.end(), b) - S->off.begin() - 1);
+    uint32_t one = 1;
+    CUDA_TRY(cudaMemcpy(S->c.force_rb + sa, &one, 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->c.force_rb + sb, &one, 4, cudaMemcpyHostToDevice));
+    return PARM_OK;
+}
+
+int parm_nlist_update(parm_system* S, int force, uint8_t* rebuilt) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->flush());
+    if (S->kind < 0) {
+        if (rebuilt) std::memset(rebuilt, 0, S->nsys);
+        return PARM_OK;
+    }
+    if (force) {
+        std::vector<uint32_t> ones(S->nsys, 1u);
+        CUDA_TRY(cudaMemcpyAsync(S->c.force_rb, ones.data(), 4 * S->nsys, cudaMemcpyHostToDevice, S->st));
+    } else {
+        launch_check(S->c, S->st);
+    }
+    launch_arm(S->c, S->st, 0, 0, 0);
+    launch_rebuild(S->c, S->st);
+    CUDA_TRY(cudaGetLastError());
+    TRY(S->sync_status());
+    if (rebuilt) {
+        std::vector<uint32_t> fl(S->nsys);
+        CUDA_TRY(cudaMemcpy(fl.data(), S->c.flag, 4 * S->nsys, cudaMemcpyDeviceToHost));
+        for (uint32_t s = 0; s < S->nsys; s++) rebuilt[s] = fl[s] ? 1 : 0;
+    }
+    return PARM_OK;
+}
+
+int parm_nlist_which(parm_system* S, uint32_t* which) {
+    if (!S || !which) return fail(PARM_ERR_ARG, "NULL argument");
+    TRY(S->flush());
+    CUDA_TRY(cudaMemcpy(which, S->c.which, 4 * S->nsys, cudaMemcpyDeviceToHost));
+    return PARM_OK;
+}
+
+int parm_nlist_numpairs(parm_system* S, uint64_t* numpairs) {
+    if (!S || !numpairs) return fail(PARM_ERR_ARG, "NULL argument");
+    TRY(S->flush());
+    launch_numpairs(S->c, S->st);
+    std::vector<double> out;
+    TRY(S->reduce_sys(1, out));
+    for (uint32_t s = 0; s < S->nsys; s++) numpairs[s] = (uint64_t)(out[s] + 0.5);
+    return PARM_OK;
+}
+
+int parm_nlist_pairs(parm_system* S, uint32_t sys, uint32_t* pairs, uint64_t cap, uint64_t* npairs) {
+    if (!S || !npairs) return fail(PARM_ERR_ARG, "NULL argument");
+    if (sys >= S->nsys) return fail(PARM_ERR_ARG, "system index out of range");
+    TRY(S->flush());
+    const uint32_t o = S->off[sys], na = S->natoms[sys], mx = S->c.maxnb;
+    std::vector<uint32_t> nnb(na), rank(S->n), orig(na), nbr((size_t)na * mx);
+    CUDA_TRY(cudaMemcpy(nnb.data(), S->c.nnb + o, 4 * (size_t)na, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(rank.data(), S->c.rank, 4 * (size_t)S->n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(orig.data(), S->c.orig + o, 4 * (size_t)na, cudaMemcpyDeviceToHost));
+    if (na && mx)
+        CUDA_TRY(cudaMemcpy2D(nbr.data(), 4 * (size_t)na, S->c.nbr + o, 4 * (size_t)S->c.nalloc,
+                              4 * (size_t)na, mx, cudaMemcpyDeviceToHost));
+    struct P {
+        uint32_t r1, r2, a, b;
+    };
+    std::vector<P> v;
+    for (uint32_t i = 0; i < na; i++) {
+        uint32_t ri = rank[o + i];
+        if (ri == PARM_NOT_MEMBER) continue;
+        for (uint32_t k = 0; k < nnb[i]; k++) {
+            uint32_t j = nbr[(size_t)k * na + i];
+            uint32_t rj = rank[j];
+            if (rj < ri) v.push_back({ri, rj, orig[i], orig[j - o]});
+        }
+    }
+    std::sort(v.begin(), v.end(), [](const P& x, const P& y) {
+        return x.r1 != y.r1 ? x.r1 < y.r1 : x.r2 < y.r2;
+    });
+    *npairs = v.size();
+    if (pairs) {
+        uint64_t m = std::min<uint64_t>(cap, v.size());
+        for (uint64_t k = 0; k < m; k++) {
+            pairs[2 * k] = v[k].a;
+            pairs[2 * k + 1] = v[k].b;
+        }
+    }
+    return PARM_OK;
+}
+
+int parm_set_forces(parm_system* S, int constraints_and_a) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->flush());
+    const int mode = constraints_and_a ? FM_FORCES_A : FM_FORCES;
+    if (S->prec == PREC_FP64) launch_force64(S->c, S->st, mode);
+    else launch_force32(S->c, S->st, mode);
+    CUDA_TRY(cudaGetLastError());
+    return S->sync_status();
+}
+
+int parm_evaluate(parm_system* S, int what, double* out) {
+    if (!S || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    if (what < 0 || what > 4) return fail(PARM_ERR_ARG, "unknown quantity");
+    TRY(S->flush());
+    const int ncomp = what == PARM_EVAL_STRESS ? S->nd * S->nd : 1;
+    if (S->kind < 0) {
+        std::fill(out, out + (size_t)S->nsys * ncomp, 0.0);
+        return PARM_OK;
+    }
+    if (S->prec == PREC_FP64) launch_eval64(S->c, S->st, what);
+    else launch_eval32(S->c, S->st, what);
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> v;
+    TRY(S->reduce_sys(ncomp, v));
+    std::copy(v.begin(), v.end(), out);
+    return PARM_OK;
+}
+
+int parm_verlet(parm_system* S, double dt, uint32_t nsteps) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (nsteps == 0) return PARM_OK;
+    StepParams p{};
+    p.dt = dt;
+    p.dt_half = dt / 2;
+    p.dt2_half = dt * dt / 2;
+    TRY(S->upload_params(p));
+    return S->run_steps(SM_VERLET, nsteps);
+}
+
+int parm_damped(parm_system* S, double dt, double damping, uint32_t nsteps) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (!(dt > 0)) return fail(PARM_ERR_ARG, "Collection::CollectionSol: dt >= 0");
+    if (nsteps == 0) return PARM_OK;
+    // CollectionDamped::set_constants (collection.cpp:339-354)
+    double c0, c1, c2;
+    if (damping <= 0.0) {
+        c0 = 1;
+        c1 = 1;
+        c2 = .5;
+    } else {
+        double dampdt = damping * dt;
+        c0 = std::exp(-dampdt);
+        c1 = (-std::expm1(-dampdt)) / dampdt;
+        c2 = (1 - c1) / dampdt;
+    }
+    StepParams p{};
+    p.dt = dt;
+    p.c0 = c0;
+    p.c1dt = c1 * dt;
+    p.c2dtdt = c2 * dt * dt;
+    p.dtc12 = dt * (c1 - c2);
+    p.dtc2 = dt * c2;
+    TRY(S->upload_params(p));
+    return S->run_steps(SM_DAMPED, nsteps);
+}
+
+int parm_sol(parm_system* S, double dt, double damping, double T, uint64_t seed, uint32_t nsteps) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (!(dt > 0)) return fail(PARM_ERR_ARG, "Collection::CollectionSol: dt >= 0");
+    if (nsteps == 0) return PARM_OK;
+    // CollectionSol::set_constants (collection.cpp:230-263) and BivariateGauss::set (vecrand.cpp:48-62)
+    double c0, c1, c2, sigmar, sigmav, corr;
+    const double force_mag = damping;
+    if (force_mag <= 0.0) {
+        c0 = 1;
+        c1 = 1;
+        c2 = .5;
+        sigmar = 0;
+        sigmav = 0;
+        corr = 1;
+    } else {
+        double dampdt = force_mag * dt;
+        c0 = std::exp(-dampdt);
+        c1 = (-std::expm1(-dampdt)) / dampdt;
+        c2 = (1 - c1) / dampdt;
+        if (dampdt > 1e-4)
+            sigmar = std::sqrt((1 / dampdt) * (2 - (-4 * std::expm1(-dampdt) + std::expm1(-2 * dampdt)) / dampdt));
+        else
+            sigmar = std::sqrt(2 * dampdt / 3 - dampdt * dampdt / 2 + 7 * dampdt * dampdt * dampdt / 30);
+        sigmav = std::sqrt(-std::expm1(-2 * dampdt));
+        double exdpdt = (-std::expm1(-dampdt));
+        corr = exdpdt * exdpdt / dampdt / sigmar / sigmav;
+    }
+    if (!(sigmar >= 0) || !(sigmav >= 0) || !(corr >= 0) || !(corr <= 1))
+        return fail(PARM_ERR_ARG, "BivariateGauss::set: invalid constants");
+    StepParams p{};
+    p.dt = dt;
+    p.c0 = c0;
+    p.c1dt = c1 * dt;
+    p.c2dtdt = c2 * dt * dt;
+    p.dtc12 = dt * (c1 - c2);
+    p.dtc2 = dt * c2;
+    p.T = T;
+    p.x11 = sigmar;
+    p.x21 = sigmav * corr;
+    p.x22 = sigmav * std::sqrt(1 - corr * corr);
+    p.noise = damping > 0 ? 1 : 0;
+    std::vector<unsigned long long> seeds(S->nsys);
+    for (uint32_t s = 0; s < S->nsys; s++) seeds[s] = splitmix64(seed + s);
+    CUDA_TRY(cudaMemcpyAsync(S->c.seed, seeds.data(), 8 * S->nsys, cudaMemcpyHostToDevice, S->st));
+    TRY(S->upload_params(p));
+    return S->run_steps(SM_SOL, nsteps);
+}
+
+int parm_kinetic_energy(parm_system* S, const double* origin, double* out) {
+    if (!S || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    if (origin)
+        CUDA_TRY(cudaMemcpyAsync(S->d_origin, origin, 8 * (size_t)S->nsys * S->nd, cudaMemcpyHostToDevice,
+                                 S->st));
+    launch_reduce_atoms(S->c, S->st, AW_KINETIC, origin ? S->d_origin : nullptr);
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> v;
+    TRY(S->reduce_sys(1, v));
+    std::copy(v.begin(), v.end(), out);
+    return PARM_OK;
+}
+
+int parm_momentum(parm_system* S, double* momentum, double* mass) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    launch_reduce_atoms(S->c, S->st, AW_MOMENTUM, nullptr);
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> v;
+    TRY(S->reduce_sys(S->nd + 1, v));
+    for (uint32_t s = 0; s < S->nsys; s++) {
+        for (int d = 0; d < S->nd; d++)
+            if (momentum) momentum[(size_t)s * S->nd + d] = v[(size_t)s * (S->nd + 1) + d];
+        if (mass) mass[s] = v[(size_t)s * (S->nd + 1) + S->nd];
+    }
+    return PARM_OK;
+}
+
+int parm_max_force_sq(parm_system* S, double* out) {
+    if (!S || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    launch_reduce_atoms(S->c, S->st, AW_MAXFORCE, nullptr);
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> v;
+    TRY(S->reduce_sys(-1, v));
+    std::copy(v.begin(), v.end(), out);
+    return PARM_OK;
+}
+
+int parm_get_step(parm_system* S, uint64_t* step) {
+    if (!S || !step) return fail(PARM_ERR_ARG, "NULL argument");
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    CUDA_TRY(cudaMemcpy(step, &S->c.params->step, 8, cudaMemcpyDeviceToHost));
+    return PARM_OK;
+}
+
+int parm_set_step(parm_system* S, uint64_t step) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    CUDA_TRY(cudaMemcpy(&S->c.params->step, &step, 8, cudaMemcpyHostToDevice));
+    return PARM_OK;
+}
+
+int parm_set_nlist_capacity(parm_system* S, uint32_t maxnb) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (maxnb == 0 || maxnb > 65536) return fail(PARM_ERR_ARG, "capacity must be in 1..65536");
+    TRY(S->flush());
+    return S->set_capacity(maxnb);
+}
+
+int parm_get_nlist_capacity(parm_system* S, uint32_t* maxnb) {
+    if (!S || !maxnb) return fail(PARM_ERR_ARG, "NULL argument");
+    *maxnb = S->c.maxnb;
+    return PARM_OK;
+}
+
+int parm_set_graph_steps(parm_system* S, uint32_t k) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (k == 0 || k > 1024) return fail(PARM_ERR_ARG, "steps per graph must be in 1..1024");
+    S->graph_k = k;
+    return PARM_OK;
+}
+
+int parm_timing(parm_system* S, int enable) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    S->timing = enable != 0;
+    S->t_force = S->t_drift = 0.0;
+    S->n_force = 0;
+    S->n_rebuild = 0;
+    return PARM_OK;
+}
+
+int parm_timing_read(parm_system* S, double* force_ms, uint64_t* force_launches, double* drift_ms,
+                     uint64_t* rebuilds) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (force_ms) *force_ms = S->t_force;
+    if (force_launches) *force_launches = S->n_force;
+    if (drift_ms) *drift_ms = S->t_drift;
+    if (rebuilds) *rebuilds = S->n_rebuild;
+    return PARM_OK;
+}
+
+int parm_last_launches(parm_system* S, uint64_t* launches) {
+    if (!S || !launches) return fail(PARM_ERR_ARG, "NULL argument");
+    *launches = S->last_launches;
+    return PARM_OK;
+}
+
+int parm_sync(parm_system* S) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    return S->sync_status();
+}
+
+void* parm_stream(parm_system* S) { return S ? (void*)S->st : nullptr; }
+
+int parm_host_alloc(void** p, uint64_t bytes) {
+    if (!p) return fail(PARM_ERR_ARG, "NULL argument");
+    CUDA_TRY(cudaMallocHost(p, bytes));
+    return PARM_OK;
+}
+
+int parm_host_free(void* p) {
+    CUDA_TRY(cudaFreeHost(p));
+    return PARM_OK;
+}
+
+int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t n) {
+    if (!d || !L || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    if (n == 0) return PARM_OK;
+    double* buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, 24 * (size_t)n));
+    cudaMemcpy(buf, d, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemcpy(buf + n, L, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    launch_remainder_test(buf, buf + n, buf + 2 * (size_t)n, n, 0);
+    cudaError_t e = cudaMemcpy(out, buf + 2 * (size_t)n, 8 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+    return PARM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,315 @@
+// Position/velocity integration, host-layout transfers and per-system
+// reductions.  All FP64 arithmetic here follows the reference's expression
+// order and is compiled with -fmad=false so that it rounds exactly like the
+// reference's unfused CPU code.
+//
+// Reference time-step loops (wackywendell/parm src/collection.cpp):
+//   CollectionVerlet::timestep  442-469  (first loop: drift + half kick)
+//   CollectionDamped::timestep  356-381  (first loop)
+//   CollectionSol::timestep     265-322  (first loop, BivariateGauss noise)
+// The second half of each step (a = f/m and the final velocity update) is
+// fused into the pair-force kernels' epilogue.
+#include "parm_check.cuh"
+
+namespace parm {
+
+__device__ __forceinline__ bool mobile(double m) { return !(m <= 0.0 || isinf(m)); }
+
+__device__ __forceinline__ void posq_split2(double x, float& X, float& xf) {
+    double t = trunc(x * 8.0) * 0.125;
+    X = (float)t;
+    xf = (float)(x - t);
+}
+
+// ---- counter-based Gaussian noise (Philox4x32-10 + Box-Muller) ----
+__device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+        uint32_t n0 = hi1 ^ c[1] ^ k0;
+        uint32_t n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    unsigned long long v = ((unsigned long long)(a >> 5) << 26) | (unsigned long long)(b >> 6);
+    return ((double)v + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ void normals6(unsigned long long seed, unsigned long long step,
+                                         uint32_t atom, double out[6]) {
+#pragma unroll
+    for (uint32_t blk = 0; blk < 3; blk++) {
+        uint32_t c[4] = {atom, (uint32_t)step, (uint32_t)(step >> 32), blk};
+        philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        double u1 = u53(c[0], c[1]);
+        double u2 = u53(c[2], c[3]);
+        double r = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincos(6.283185307179586 * u2, &sn, &cs);
+        out[2 * blk] = r * cs;
+        out[2 * blk + 1] = r * sn;
+    }
+}
+
+template <int ND>
+__device__ __forceinline__ void store_posq(const DevCtx& c, uint32_t i, const double* xs) {
+    float4 A = c.posA[i], B;
+    posq_split2(xs[0], A.x, B.x);
+    posq_split2(xs[1], A.y, B.y);
+    if constexpr (ND == 3) posq_split2(xs[2], A.z, B.z); else { A.z = 0.f; B.z = 0.f; }
+    B.w = 0.f;
+    c.posA[i] = A;
+    c.posB[i] = B;
+}
+
+template <int ND, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_drift(DevCtx c) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    using V = typename DVec<ND>::T;
+    const StepParams& P = *c.params;
+    double m = c.m[i];
+    V xv = static_cast<V*>(c.x)[i];
+    V vv = static_cast<V*>(c.v)[i];
+    V av = static_cast<V*>(c.a)[i];
+    double* x = reinterpret_cast<double*>(&xv);
+    double* v = reinterpret_cast<double*>(&vv);
+    const double* a = reinterpret_cast<const double*>(&av);
+    if (!mobile(m)) {
+#pragma unroll
+        for (int d = 0; d < ND; d++) v[d] = 0.0;
+        static_cast<V*>(c.v)[i] = vv;
+        return;
+    }
+    if constexpr (MODE == DM_VERLET) {
+        // x += v*dt + a*(dt*dt/2); v += a*(dt/2)
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            x[d] = x[d] + (v[d] * P.dt + a[d] * P.dt2_half);
+            v[d] = v[d] + a[d] * P.dt_half;
+        }
+    } else if constexpr (MODE == DM_DAMPED) {
+        // x += v*(c1*dt) + a*(c2*dt*dt); v = v*c0 + a*(dt*(c1-c2))
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            x[d] = x[d] + (v[d] * P.c1dt + a[d] * P.c2dtdt);
+            v[d] = v[d] * P.c0 + a[d] * P.dtc12;
+        }
+    } else {
+        // CollectionSol: x += v*(c1*dt) + a*(c2*dt*dt) + drG*r0;
+        //                v  = v*c0 + a*(dt*(c1-c2)) + dvG*v0
+        double v0 = sqrt(P.T / m);
+        double r0 = P.dt * v0;
+        double g[6] = {0, 0, 0, 0, 0, 0};
+        uint32_t s = c.atom_sys[i];
+        if (P.noise) normals6(c.seed[s], P.step, c.orig[i] - c.sys[s].atom_off, g);
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            double drG = g[d] * P.x11;
+            double dvG = g[d] * P.x21 + g[ND + d] * P.x22;
+            x[d] = x[d] + ((v[d] * P.c1dt + a[d] * P.c2dtdt) + drG * r0);
+            v[d] = (v[d] * P.c0 + a[d] * P.dtc12) + dvG * v0;
+        }
+    }
+    static_cast<V*>(c.x)[i] = xv;
+    static_cast<V*>(c.v)[i] = vv;
+    store_posq<ND>(c, i, x);
+}
+
+void launch_drift(const DevCtx& c, cudaStream_t s, int mode) {
+    unsigned g = grid_for(c.n);
+    if (c.nd == 3) {
+        if (mode == DM_VERLET) k_drift<3, DM_VERLET><<<g, BLOCK, 0, s>>>(c);
+        else if (mode == DM_DAMPED) k_drift<3, DM_DAMPED><<<g, BLOCK, 0, s>>>(c);
+        else k_drift<3, DM_SOL><<<g, BLOCK, 0, s>>>(c);
+    } else {
+        if (mode == DM_VERLET) k_drift<2, DM_VERLET><<<g, BLOCK, 0, s>>>(c);
+        else if (mode == DM_DAMPED) k_drift<2, DM_DAMPED><<<g, BLOCK, 0, s>>>(c);
+        else k_drift<2, DM_SOL><<<g, BLOCK, 0, s>>>(c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host AoS <-> internal SoA.  A record of caller atom o starts at
+// staging + o*stride: x[0..nd), v[nd..2nd), a[2nd..3nd), f[3nd..4nd), m[4nd]
+// (the reference's struct Atom {Vec x, v, a, f; flt m;}).
+// ---------------------------------------------------------------------------
+enum FieldBits : uint32_t { FB_X = 1, FB_V = 2, FB_A = 4, FB_F = 8, FB_M = 16 };
+
+template <int ND>
+__global__ void k_scatter_in(DevCtx c, const double* st, uint64_t stride, uint32_t fields) {
+    uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= c.n) return;
+    using V = typename DVec<ND>::T;
+    uint32_t k = c.slot[o];
+    const double* r = st + (uint64_t)o * stride;
+    auto ld = [&](int off) {
+        V t;
+        double* p = reinterpret_cast<double*>(&t);
+#pragma unroll
+        for (int d = 0; d < (int)(sizeof(V) / 8); d++) p[d] = d < ND ? r[off + d] : 0.0;
+        return t;
+    };
+    if (fields & FB_X) {
+        V xv = ld(0);
+        static_cast<V*>(c.x)[k] = xv;
+        store_posq<ND>(c, k, reinterpret_cast<const double*>(&xv));
+    }
+    if (fields & FB_V) static_cast<V*>(c.v)[k] = ld(ND);
+    if (fields & FB_A) static_cast<V*>(c.a)[k] = ld(2 * ND);
+    if (fields & FB_F) {
+        V fv = ld(3 * ND);
+        static_cast<V*>(c.f)[k] = fv;
+        const double* fp = reinterpret_cast<const double*>(&fv);
+        c.f32[k] = make_float4((float)fp[0], (float)fp[1], ND == 3 ? (float)fp[ND - 1] : 0.f, 0.f);
+    }
+    if (fields & FB_M) {
+        double m = r[4 * ND];
+        c.m[k] = m;
+        c.invm32[k] = mobile(m) ? (float)(1.0 / m) : 0.f;
+    }
+}
+
+template <int ND>
+__global__ void k_gather_out(DevCtx c, double* st, uint64_t stride, uint32_t fields) {
+    uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= c.n) return;
+    using V = typename DVec<ND>::T;
+    uint32_t k = c.slot[o];
+    double* r = st + (uint64_t)o * stride;
+    auto put = [&](int off, const V& t) {
+        const double* p = reinterpret_cast<const double*>(&t);
+#pragma unroll
+        for (int d = 0; d < ND; d++) r[off + d] = p[d];
+    };
+    if (fields & FB_X) put(0, static_cast<const V*>(c.x)[k]);
+    if (fields & FB_V) put(ND, static_cast<const V*>(c.v)[k]);
+    if (fields & FB_A) put(2 * ND, static_cast<const V*>(c.a)[k]);
+    if (fields & FB_F) {
+        if (c.prec == PREC_MIXED) {
+            float4 f = c.f32[k];
+            r[3 * ND] = f.x;
+            r[3 * ND + 1] = f.y;
+            if (ND == 3) r[3 * ND + ND - 1] = f.z;
+        } else {
+            put(3 * ND, static_cast<const V*>(c.f)[k]);
+        }
+    }
+    if (fields & FB_M) r[4 * ND] = c.m[k];
+}
+
+void launch_scatter_in(const DevCtx& c, cudaStream_t s, const double* st, uint64_t stride,
+                       uint32_t fields) {
+    if (c.nd == 3) k_scatter_in<3><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
+    else k_scatter_in<2><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
+}
+
+void launch_gather_out(const DevCtx& c, cudaStream_t s, double* st, uint64_t stride,
+                       uint32_t fields) {
+    if (c.nd == 3) k_gather_out<3><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
+    else k_gather_out<2><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
+}
+
+// ---------------------------------------------------------------------------
+// per-atom reduction inputs (component-major: red[comp * n + i])
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void k_atoms(DevCtx c, int what, const double* origin) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    using V = typename DVec<ND>::T;
+    double m = c.m[i];
+    uint32_t s = c.atom_sys[i];
+    if (what == AW_KINETIC) {
+        // AtomGroup::kinetic_energy (box.cpp:401-411): skip m == 0 or inf
+        double e = 0.0;
+        if (!(m == 0.0 || isinf(m))) {
+            V vv = static_cast<const V*>(c.v)[i];
+            const double* v = reinterpret_cast<const double*>(&vv);
+            double cv[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < ND; d++) cv[d] = v[d] - (origin ? origin[s * ND + d] : 0.0);
+            double dd = cv[0] * cv[0] + cv[1] * cv[1];
+            if constexpr (ND == 3) dd = dd + cv[2] * cv[2];
+            e = m / 2 * dd;
+        }
+        c.red[i] = e;
+    } else if (what == AW_MOMENTUM) {
+        // AtomGroup::momentum / mass (box.cpp:237-258): skip m <= 0 or inf
+        bool ok = mobile(m);
+        V vv = static_cast<const V*>(c.v)[i];
+        const double* v = reinterpret_cast<const double*>(&vv);
+#pragma unroll
+        for (int d = 0; d < ND; d++) c.red[(size_t)d * c.n + i] = ok ? v[d] * m : 0.0;
+        c.red[(size_t)ND * c.n + i] = ok ? m : 0.0;
+    } else {
+        double q = 0.0;
+        if (mobile(m)) {
+            if (c.prec == PREC_MIXED) {
+                float4 f = c.f32[i];
+                q = (double)f.x * f.x + (double)f.y * f.y + (double)f.z * f.z;
+            } else {
+                V fv = static_cast<const V*>(c.f)[i];
+                const double* f = reinterpret_cast<const double*>(&fv);
+                q = f[0] * f[0] + f[1] * f[1];
+                if constexpr (ND == 3) q = q + f[2] * f[2];
+            }
+        }
+        c.red[i] = q;
+    }
+}
+
+void launch_reduce_atoms(const DevCtx& c, cudaStream_t s, int what, const double* origin) {
+    if (c.nd == 3) k_atoms<3><<<grid_for(c.n), BLOCK, 0, s>>>(c, what, origin);
+    else k_atoms<2><<<grid_for(c.n), BLOCK, 0, s>>>(c, what, origin);
+}
+
+// deterministic per-system reduction of red[comp * n + i] over each system's
+// atoms (one CTA per system, fixed striding and tree order).  ncomp < 0 means
+// a single-component maximum.
+__global__ void __launch_bounds__(1024) k_sys_reduce(DevCtx c, int ncomp) {
+    uint32_t s = blockIdx.x;
+    const SysConst& S = c.sys[s];
+    __shared__ double sh[32];
+    const bool is_max = ncomp < 0;
+    const int nc = is_max ? 1 : ncomp;
+    for (int comp = 0; comp < nc; comp++) {
+        const double* r = c.red + (size_t)comp * c.n + S.atom_off;
+        double acc = 0.0;
+        for (uint32_t k = threadIdx.x; k < S.natoms; k += blockDim.x) {
+            double v = r[k];
+            acc = is_max ? fmax(acc, v) : acc + v;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            double o = __shfl_down_sync(0xFFFFFFFFu, acc, off);
+            acc = is_max ? fmax(acc, o) : acc + o;
+        }
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                double o = __shfl_down_sync(0xFFFFFFFFu, v, off);
+                v = is_max ? fmax(v, o) : v + o;
+            }
+            if (threadIdx.x == 0) c.sysout[(size_t)s * nc + comp] = v;
+        }
+        __syncthreads();
+    }
+}
+
+void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp) {
+    k_sys_reduce<<<c.nsys, 1024, 0, s>>>(c, ncomp);
+}
+
+}  // namespace parm

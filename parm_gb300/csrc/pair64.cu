@@ -1,0 +1,327 @@
+// FP64 pair forces, energies, virials and stresses — the drop-in path whose
+// results match the reference CPU code bit for bit.
+//
+// Reference (wackywendell/parm src/interaction.hpp):
+//   NListed<A,P>::set_forces               2165-2175  f_first += F, f_last -= F
+//   NListed<A,P>::energy / pressure / stress 2152-2163, 2247-2291
+//   LennardJonesCut + LennardJonesCutPair   238-281, 967-987
+//   RepulsionPair                           1528-1590
+//   LJRepulsive + LJRepulsePair             119-152, 875-891
+//
+// Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
+// scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
+// ascending j (adding F(k,j)), then neighbours i>k in ascending i
+// (subtracting F(i,k)).  Because the minimum image is an exact odd function
+// and every pair law scales the displacement by a function of |r|^2,
+// -F(i,k) == F(k,i) bit for bit, so gathering F(k, j) over the rank-sorted
+// full list reproduces the reference sums exactly.  Pairs beyond the cut-off
+// (the reference adds Vec::Zero()) are skipped after an FP32 screen.
+//
+// Compiled with -fmad=false.
+#include "parm_check.cuh"
+
+namespace parm {
+
+__device__ __forceinline__ bool mobile64(double m) { return !(m <= 0.0 || isinf(m)); }
+
+struct PairC {
+    double eps, sig, third, m6;
+};
+
+template <int KIND>
+__device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uint32_t uni) {
+    PairC p;
+    // eps = sqrt(e1*e2) (sqrt(e*e) == e exactly, so uniform epsilon skips it)
+    p.eps = (uni & UNI_EPS) ? A.p0 : sqrt(A.p0 * B.p0);
+    p.sig = (uni & UNI_SIG) ? A.p1 : (A.p1 + B.p1) / 2;
+    if constexpr (KIND == KIND_LJCUT) {
+        // cut = max(a1.sigcut, a2.sigcut); its pow(cut, 6) term travels with it
+        bool b_larger = B.p2 > A.p2;
+        p.third = b_larger ? B.p2 : A.p2;
+        p.m6 = b_larger ? B.p3 : A.p3;
+    } else if constexpr (KIND == KIND_REPULSION) {
+        p.third = (uni & UNI_THIRD) ? A.p2 : (A.p2 + B.p2) / 2.0;
+        p.m6 = 0.0;
+    } else {
+        p.third = 0.0;
+        p.m6 = 0.0;
+    }
+    return p;
+}
+
+// pair force scale s (F = r * s); returns false beyond the cut-off
+template <int KIND>
+__device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t uni, double& s) {
+    if constexpr (KIND == KIND_LJCUT) {
+        double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
+        if (rsq > (p.third * p.third)) return false;
+        double rsix = rsq * rsq * rsq;
+        double fmagTimesR = 12 * p.eps / rsix * (1 / rsix - 1);
+        s = fmagTimesR / dsq;
+        return true;
+    } else if constexpr (KIND == KIND_REPULSION) {
+        if (dsq > p.sig * p.sig) return false;
+        double R = sqrt(dsq);
+        double b = 1.0 - (R / p.sig);
+        double pw = (p.third == 2.0) ? b : pow(b, p.third - 1);   // pow(b, 1) == b exactly
+        s = p.eps * pw / p.sig / R;
+        return true;
+    } else {
+        double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
+        if (rsq > 1) return false;
+        double rsix = rsq * rsq * rsq;
+        double fmagTimesR = 12 * p.eps / rsix * (1 / rsix - 1);
+        s = fmagTimesR / dsq;
+        return true;
+    }
+}
+
+template <int KIND>
+__device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32_t uni) {
+    if constexpr (KIND == KIND_LJCUT) {
+        double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
+        if (rsq > (p.third * p.third)) return 0.0;
+        double rsix = rsq * rsq * rsq;
+        double mid = (1 - 1 / rsix);
+        double cut_energy = p.eps * (p.m6 * p.m6 - 1);
+        return p.eps * (mid * mid - 1) - cut_energy;
+    } else if constexpr (KIND == KIND_REPULSION) {
+        if (dsq > p.sig * p.sig) return 0.0;
+        double R = sqrt(dsq);
+        double b = 1.0 - (R / p.sig);
+        double pw = (p.third == 2.0) ? b * b : pow(b, p.third);   // pow(b, 2) == b*b exactly
+        return p.eps * pw / p.third;
+    } else {
+        double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
+        if (rsq > 1) return 0.0;
+        double rsix = rsq * rsq * rsq;
+        double mid = (1 - 1 / rsix);
+        return p.eps * (mid * mid);
+    }
+}
+
+// FP32 screen: true when the pair is certainly beyond the cut-off
+template <int KIND>
+__device__ __forceinline__ bool beyond32(float d2, float sig32i, float sig32j, float th32i,
+                                         float th32j, uint32_t uni) {
+    float sg = (uni & UNI_SIG) ? sig32i : 0.5f * (sig32i + sig32j);
+    float rc;
+    if constexpr (KIND == KIND_LJCUT) rc = sg * fmaxf(th32i, th32j);
+    else rc = sg;
+    return d2 > rc * rc * 1.0002f;
+}
+
+template <int ND>
+__device__ __forceinline__ void load3(const void* p, uint32_t i, double* o) {
+    using V = typename DVec<ND>::T;
+    V t = static_cast<const V*>(p)[i];
+    const double* q = reinterpret_cast<const double*>(&t);
+#pragma unroll
+    for (int d = 0; d < ND; d++) o[d] = q[d];
+}
+
+template <int ND>
+__device__ __forceinline__ void store3(void* p, uint32_t i, const double* o) {
+    using V = typename DVec<ND>::T;
+    V t;
+    double* q = reinterpret_cast<double*>(&t);
+#pragma unroll
+    for (int d = 0; d < (int)(sizeof(V) / 8); d++) q[d] = d < ND ? o[d] : 0.0;
+    static_cast<V*>(p)[i] = t;
+}
+
+template <int ND>
+__device__ __forceinline__ float d2_32(const SysConst& S, const float4& Ai, const float4& Bi,
+                                       const float4& Aj, const float4& Bj) {
+    float dx = disp32(Ai.x, Aj.x, Bi.x, Bj.x, S.Lhi[0], S.Llo[0], S.invLf[0]);
+    float dy = disp32(Ai.y, Aj.y, Bi.y, Bj.y, S.Lhi[1], S.Llo[1], S.invLf[1]);
+    float d2 = dx * dx + dy * dy;
+    if constexpr (ND == 3) {
+        float dz = disp32(Ai.z, Aj.z, Bi.z, Bj.z, S.Lhi[2], S.Llo[2], S.invLf[2]);
+        d2 += dz * dz;
+    }
+    return d2;
+}
+
+template <int ND, int KIND, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < c.n;
+    const uint32_t uni = c.uniform;
+    double f[3] = {0.0, 0.0, 0.0};
+    uint32_t s = 0;
+    bool member = false;
+    if (active) {
+        s = c.atom_sys[i];
+        member = c.rank[i] != NOT_MEMBER;
+    }
+    if (member) {
+        const SysConst& S = c.sys[s];
+        double xi[3] = {0, 0, 0};
+        load3<ND>(c.x, i, xi);
+        const float4 Ai = c.posA[i], Bi = c.posB[i];
+        const AtomPrm Pi = c.prm[i];
+        const float4 Qi = c.prm32[i];
+        const uint32_t nn = c.nnb[i];
+        for (uint32_t k = 0; k < nn; k++) {
+            const uint32_t j = c.nbr[(size_t)k * c.nalloc + i];
+            const float4 Aj = c.posA[j], Bj = c.posB[j];
+            float4 Qj = Qi;
+            if ((uni & (UNI_SIG | UNI_THIRD)) != (UNI_SIG | UNI_THIRD)) Qj = c.prm32[j];
+            if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi.y, Qj.y, Qi.z, Qj.z, uni)) continue;
+            double xj[3] = {0, 0, 0};
+            load3<ND>(c.x, j, xj);
+            double r[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+            double dsq = r[0] * r[0] + r[1] * r[1];
+            if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
+            AtomPrm Pj = Pi;
+            if ((uni & (UNI_EPS | UNI_SIG | UNI_THIRD)) != (UNI_EPS | UNI_SIG | UNI_THIRD)) Pj = c.prm[j];
+            const PairC pc = combine<KIND>(Pi, Pj, uni);
+            double sc;
+            if (!force_scale<KIND>(pc, dsq, uni, sc)) continue;
+#pragma unroll
+            for (int d = 0; d < ND; d++) f[d] = f[d] + r[d] * sc;
+        }
+    }
+    if (active) {
+        const StepParams& P = *c.params;
+        store3<ND>(c.f, i, f);
+        if constexpr (MODE != FM_FORCES) {
+            const double m = c.m[i];
+            double a[3] = {0, 0, 0};
+            if constexpr (MODE == FM_FORCES_A || MODE == FM_DAMPED || MODE == FM_VERLET) {
+                if (mobile64(m)) {
+#pragma unroll
+                    for (int d = 0; d < ND; d++) a[d] = f[d] / m;
+                }
+                store3<ND>(c.a, i, a);
+                if constexpr (MODE != FM_FORCES_A) {
+                    if (mobile64(m)) {
+                        double v[3] = {0, 0, 0};
+                        load3<ND>(c.v, i, v);
+                        const double h = (MODE == FM_VERLET) ? P.dt_half : P.dtc2;
+#pragma unroll
+                        for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * h;
+                        store3<ND>(c.v, i, v);
+                    }
+                }
+            } else {  // FM_SOL: immobile test is m == 0 or inf here (collection.cpp:300-318)
+                double v[3] = {0, 0, 0};
+                if (!(m == 0.0 || isinf(m))) {
+#pragma unroll
+                    for (int d = 0; d < ND; d++) a[d] = f[d] / m;
+                    load3<ND>(c.v, i, v);
+#pragma unroll
+                    for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * P.dtc2;
+                }
+                store3<ND>(c.a, i, a);
+                store3<ND>(c.v, i, v);
+            }
+        }
+    }
+    if constexpr (MODE == FM_VERLET || MODE == FM_DAMPED || MODE == FM_SOL) {
+        double dsq = 0.0;
+        bool valid = false;
+        if (member) {
+            dsq = disp_sq<ND>(static_cast<const typename DVec<ND>::T*>(c.x)[i],
+                              static_cast<const typename DVec<ND>::T*>(c.lastloc)[i]);
+            valid = !(dsq != dsq);
+        }
+        check_accumulate(c, s, valid, dsq);
+    }
+}
+
+// per-atom partial sums over the half list (neighbours of smaller rank), i.e.
+// each reference pair (first = higher rank) exactly once
+template <int ND, int KIND>
+__global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const uint32_t uni = c.uniform;
+    const int ncomp = (what == EV_STRESS) ? ND * ND : 1;
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const uint32_t ri = c.rank[i];
+    if (ri != NOT_MEMBER) {
+        const uint32_t s = c.atom_sys[i];
+        const SysConst& S = c.sys[s];
+        double xi[3] = {0, 0, 0};
+        load3<ND>(c.x, i, xi);
+        const AtomPrm Pi = c.prm[i];
+        const uint32_t nn = c.nnb[i];
+        for (uint32_t k = 0; k < nn; k++) {
+            const uint32_t j = c.nbr[(size_t)k * c.nalloc + i];
+            if (c.rank[j] > ri) continue;
+            double xj[3] = {0, 0, 0};
+            load3<ND>(c.x, j, xj);
+            double r[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+            double dsq = r[0] * r[0] + r[1] * r[1];
+            if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
+            const PairC pc = combine<KIND>(Pi, c.prm[j], uni);
+            if (what == EV_ENERGY || what == EV_CONTACTS || what == EV_OVERLAPS) {
+                double e = pair_energy<KIND>(pc, dsq, uni);
+                if (what == EV_ENERGY) acc[0] = acc[0] + e;
+                else if (what == EV_CONTACTS) acc[0] += (e != 0.0) ? 1.0 : 0.0;
+                else acc[0] += (e > 0.0) ? 1.0 : 0.0;
+            } else {
+                double sc;
+                double fo[3] = {0, 0, 0};
+                if (force_scale<KIND>(pc, dsq, uni, sc)) {
+#pragma unroll
+                    for (int d = 0; d < ND; d++) fo[d] = r[d] * sc;
+                }
+                if (what == EV_VIRIAL) {
+                    double p = r[0] * fo[0] + r[1] * fo[1];
+                    if constexpr (ND == 3) p = p + r[2] * fo[2];
+                    acc[0] = acc[0] + p;
+                } else {
+#pragma unroll
+                    for (int aa = 0; aa < ND; aa++)
+#pragma unroll
+                        for (int bb = 0; bb < ND; bb++) acc[aa * ND + bb] = acc[aa * ND + bb] + r[aa] * fo[bb];
+                }
+            }
+        }
+    }
+    for (int q = 0; q < ncomp; q++) c.red[(size_t)q * c.n + i] = acc[q];
+}
+
+template <int ND, int KIND>
+static void force64_nd_kind(const DevCtx& c, cudaStream_t s, int mode) {
+    unsigned g = grid_for(c.n);
+    switch (mode) {
+        case FM_FORCES: k_force64<ND, KIND, FM_FORCES><<<g, BLOCK, 0, s>>>(c); break;
+        case FM_FORCES_A: k_force64<ND, KIND, FM_FORCES_A><<<g, BLOCK, 0, s>>>(c); break;
+        case FM_VERLET: k_force64<ND, KIND, FM_VERLET><<<g, BLOCK, 0, s>>>(c); break;
+        case FM_DAMPED: k_force64<ND, KIND, FM_DAMPED><<<g, BLOCK, 0, s>>>(c); break;
+        default: k_force64<ND, KIND, FM_SOL><<<g, BLOCK, 0, s>>>(c); break;
+    }
+}
+
+template <int ND>
+static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
+    if (c.kind == KIND_LJCUT) force64_nd_kind<ND, KIND_LJCUT>(c, s, mode);
+    else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
+    else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
+}
+
+void launch_force64(const DevCtx& c, cudaStream_t s, int mode) {
+    if (c.nd == 3) force64_nd<3>(c, s, mode); else force64_nd<2>(c, s, mode);
+}
+
+template <int ND>
+static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
+    unsigned g = grid_for(c.n);
+    if (c.kind == KIND_LJCUT) k_eval64<ND, KIND_LJCUT><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
+    else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
+}
+
+void launch_eval64(const DevCtx& c, cudaStream_t s, int what) {
+    if (c.nd == 3) eval64_nd<3>(c, s, what); else eval64_nd<2>(c, s, what);
+}
+
+}  // namespace parm

@@ -1,0 +1,157 @@
+// Device-side context (plain struct of device pointers, passed by value to
+// kernels) and the host-callable launchers each translation unit provides.
+#pragma once
+#include "parm_internal.cuh"
+
+namespace parm {
+
+// integrator / evaluation modes of the pair-force kernels (the epilogue that
+// runs once an atom's force is complete)
+enum ForceMode : int {
+    FM_FORCES = 0,     // Collection::set_forces(false): write f
+    FM_FORCES_A = 1,   // Collection::set_forces(true):  write f, a = f/m
+    FM_VERLET = 2,     // CollectionVerlet second half: a = f/m; v += a*(dt/2); check
+    FM_DAMPED = 3,     // CollectionDamped second half: a = f/m; v += a*(dt*c2); check
+    FM_SOL = 4,        // CollectionSol second half:    a = f/m; v += a*(dt*c2); check
+};
+
+enum DriftMode : int { DM_VERLET = 0, DM_DAMPED = 1, DM_SOL = 2 };
+
+// scalars of the current integrator call, kept in device memory so cached
+// graphs do not depend on them (all products formed on the host exactly as
+// the reference writes them)
+struct StepParams {
+    double dt;
+    double dt_half;      // dt / 2
+    double dt2_half;     // dt * dt / 2
+    double c0;           // exp(-damping*dt)
+    double c1dt;         // c1 * dt
+    double c2dtdt;       // c2 * dt * dt
+    double dtc12;        // dt * (c1 - c2)
+    double dtc2;         // dt * c2
+    double T;            // desired temperature (CollectionSol)
+    double x11, x21, x22;// BivariateGauss::set outputs
+    int noise;           // damping > 0 in CollectionSol
+    int pad;
+    unsigned long long step;   // Langevin counter, advanced once per step
+};
+
+struct DevCtx {
+    int nd;
+    int prec;
+    int kind;
+    uint32_t nsys;
+    uint32_t n;        // total atoms
+    uint32_t nalloc;   // column stride of the neighbour list (>= n)
+    uint32_t maxnb;    // neighbour capacity per atom
+    uint32_t uniform;  // UniformFlags
+    uint32_t nbucket;  // total buckets (sum over systems of ncell + 1)
+
+    const SysConst* sys;
+    const uint32_t* bucket_off;   // per system: first bucket (cells, then the non-member bucket)
+
+    // per-atom state (internal order)
+    void* x;
+    void* v;
+    void* a;
+    void* f;
+    void* lastloc;
+    float4* f32;          // mixed-path forces
+    double* m;
+    float* invm32;        // mixed path: 1/m in FP32 (0 for immobile atoms)
+    AtomPrm* prm;
+    float4* prm32;        // (sqrt(eps), sigma, third, unused) in FP32
+    double* diam;         // A::max_size()
+    uint32_t* rank;       // NeighborList position, NOT_MEMBER if not added
+    uint32_t* orig;       // caller's atom index (global)
+    uint32_t* slot;       // inverse of orig
+    uint32_t* atom_sys;   // system of each internal slot (constant)
+    uint32_t* nm_rank;    // by orig: rank among the system's non-members
+    float4* posA;         // coarse X (xyz) , w unused
+    float4* posB;         // fine xf (xyz), w unused
+    uint32_t* bucket;     // current bucket of each internal slot
+
+    // rebuild scratch
+    uint32_t* cell_count;
+    uint32_t* cell_start;
+    uint32_t* cslot;
+    uint32_t* perm;       // new slot -> old slot
+    // gather targets for the permutation
+    void* x2; void* v2; void* a2; void* f2;
+    float4* f32b;
+    double* m2; float* invm32b; AtomPrm* prm2; float4* prm32b; double* diam2;
+    uint32_t* rank2; uint32_t* orig2; uint32_t* bucket2;
+
+    // neighbour list
+    uint32_t* nbr;
+    uint32_t* nnb;
+
+    // exclusions (NeighborList::ignore), CSR keyed by caller index
+    const uint32_t* excl_off;   // n + 1 entries, or null when no exclusions
+    const uint32_t* excl_list;
+
+    // per-system control
+    uint32_t* flag;       // rebuild this step
+    uint32_t* force_rb;   // rebuild requested by the host (force / ignorechanged)
+    unsigned long long* top;  // [2*s] largest, [2*s+1] second largest squared displacement (bits)
+    uint32_t* which;      // NeighborList::which()
+    unsigned long long* seed;  // per-system Langevin key
+    uint32_t* status;
+    uint32_t* any_flag;
+    uint32_t* chains;     // rebuild-chain executions (for launch accounting)
+    StepParams* params;
+
+    // reduction scratch
+    double* red;          // per-atom scratch (up to 12 doubles per atom)
+    double* sysout;       // per-system outputs
+};
+
+// ---- launchers (implemented in the .cu files) ----
+// nlist.cu
+void launch_arm(const DevCtx& c, cudaStream_t s, int count_step, int use_cond,
+                unsigned long long handle);
+void launch_rebuild(const DevCtx& c, cudaStream_t s);
+void launch_check(const DevCtx& c, cudaStream_t s);
+void launch_numpairs(const DevCtx& c, cudaStream_t s);   // -> sysout[s] (as double)
+void launch_posq(const DevCtx& c, cudaStream_t s);
+// integrate.cu
+void launch_drift(const DevCtx& c, cudaStream_t s, int mode);
+void launch_scatter_in(const DevCtx& c, cudaStream_t s, const double* staging, uint64_t stride,
+                       uint32_t fields);
+void launch_gather_out(const DevCtx& c, cudaStream_t s, double* staging, uint64_t stride,
+                       uint32_t fields);
+void launch_reduce_atoms(const DevCtx& c, cudaStream_t s, int what, const double* origin);
+void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp);
+// pair64.cu / pair32.cu
+void launch_force64(const DevCtx& c, cudaStream_t s, int mode);
+void launch_force32(const DevCtx& c, cudaStream_t s, int mode);
+void launch_eval64(const DevCtx& c, cudaStream_t s, int what);
+void launch_eval32(const DevCtx& c, cudaStream_t s, int what);
+// debug entry used by the tests of the minimum-image routine
+void launch_remainder_test(const double* d, const double* L, double* out, uint32_t n,
+                           cudaStream_t s);
+
+// what for launch_eval*: writes per-atom partials into c.red, ncomp per atom
+enum EvalWhat : int {
+    EV_ENERGY = 0,     // 1 comp
+    EV_VIRIAL = 1,     // 1 comp  (sum r.f)
+    EV_STRESS = 2,     // nd*nd comps
+    EV_CONTACTS = 3,   // 1 comp (count E != 0)
+    EV_OVERLAPS = 4,   // 1 comp (count E > 0)
+};
+
+// what for launch_reduce_atoms
+enum AtomWhat : int {
+    AW_KINETIC = 0,    // 1 comp, AtomGroup::kinetic_energy(origin)
+    AW_MOMENTUM = 1,   // nd + 1 comps (momentum, mass) over m > 0 finite atoms
+    AW_MAXFORCE = 2,   // 1 comp: max |f|^2 over mobile atoms
+};
+
+constexpr int BLOCK = 256;
+
+inline unsigned grid_for(uint32_t n, int block = BLOCK) {
+    unsigned g = (unsigned)((n + block - 1) / block);
+    return g ? g : 1;
+}
+
+}  // namespace parm

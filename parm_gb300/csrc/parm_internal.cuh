@@ -1,0 +1,121 @@
+// Internal definitions shared by the parm_gb300 CUDA translation units.
+//
+// Device data layout (one context = a batch of `nsys` independent periodic
+// systems; a single simulation is nsys == 1):
+//   * atoms of all systems are concatenated; system s owns the contiguous
+//     range [atom_off[s], atom_off[s] + natoms[s]).
+//   * inside a system the atoms are kept in "cell order": at every
+//     neighbour-list rebuild they are counting-sorted by cell and, inside a
+//     cell, by their original index.  `orig[k]` maps the internal slot k back
+//     to the caller's atom index; `slot[orig]` is the inverse.
+//   * positions, velocities, accelerations, forces and the last-build
+//     positions are FP64 vectors stored as double4 (3D) / double2 (2D), so a
+//     neighbour gather is one aligned 32-byte sector.
+//   * `posq` is the FP32 view of the positions used by the mixed-precision
+//     pair kernel and by the FP32 pre-filters of the FP64 path: a coarse part
+//     X = trunc(x * 8) / 8 (exact in FP32) and a fine part xf = x - X.
+//   * the neighbour list is a full list stored column-major:
+//     nbr[k * nalloc + i] is the k-th neighbour of internal atom i.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace parm {
+
+enum PairKind : int { KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2 };
+enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// status bits (device word, read back by the host after synchronising calls)
+enum StatusBits : uint32_t {
+    ST_NBR_OVERFLOW = 1u << 0,   // an atom had more neighbours than the list capacity
+    ST_NONFINITE = 1u << 1,      // a non-finite position was binned
+    ST_CELL_RANGE = 1u << 2,     // a cell index fell outside its system's grid (bug guard)
+    ST_SORT_CAP = 1u << 3,       // FP64 path: a neighbour list longer than the in-thread sort buffer
+};
+
+constexpr uint32_t NOT_MEMBER = 0xFFFFFFFFu;
+
+struct SysConst {
+    double L[3];
+    double invL[3];
+    double halfL[3];
+    float Lhi[3], Llo[3], invLf[3];
+    double skin;
+    double rlist_max;   // largest (d_i + d_j)/2 + skin
+    int nc[3];          // cells per axis (1 or >= 3)
+    float cellw_inv[3]; // nc / L
+    uint32_t cell_off;  // first cell of this system in the global cell array
+    uint32_t ncell;
+    uint32_t atom_off;
+    uint32_t natoms;
+};
+
+// per-atom FP64 parameters of the pair interaction (kind dependent)
+//   LJCUT:     p0 = epsilon, p1 = sigma, p2 = sigcut, p3 = 1 - 1/pow(sigcut, 6)
+//   REPULSION: p0 = eps,     p1 = sigma, p2 = exponent
+//   LJREPULSE: p0 = epsilon, p1 = sigma
+struct AtomPrm {
+    double p0, p1, p2, p3;
+};
+
+// flags that let the FP64 kernel skip combinations that are exact identities
+enum UniformFlags : uint32_t {
+    UNI_EPS = 1u << 0,     // all members share epsilon -> eps_ij = eps (sqrt(e*e) == e)
+    UNI_SIG = 1u << 1,     // all members share sigma   -> sig_ij = sig
+    UNI_THIRD = 1u << 2,   // all members share sigcut / exponent
+    UNI_SIG_ONE = 1u << 3, // sigma == 1 exactly -> dsq / (sig*sig) == dsq
+};
+
+template <int ND> struct DVec;
+template <> struct DVec<3> { using T = double4; };
+template <> struct DVec<2> { using T = double2; };
+
+// ---------------------------------------------------------------------------
+// Exact IEEE-754 remainder(d, L) (the reference's OriginBox::diff applies
+// remainder() per component on unwrapped coordinates).  The common case is
+// one multiply, one rint and one fma: when n is the true quotient the fma
+// result d - n*L is exactly representable and therefore exact.  A wrong
+// candidate quotient always leaves |r| >= L/2, so the rare branch tries the
+// three candidates and, for a genuine tie, picks the even quotient.  Valid
+// for |d / L| < 2^50 (the candidate quotient is then off by at most one).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double remainder_exact(double d, double L, double invL, double halfL) {
+    double n = rint(d * invL);
+    double r = fma(-n, L, d);
+    if (fabs(r) >= halfL) {
+        double best = r;
+        bool found = false;
+        double tie_n = n;
+#pragma unroll
+        for (int k = -1; k <= 1; k++) {
+            double nk = n + (double)k;
+            double rk = fma(-nk, L, d);
+            if (fabs(rk) < halfL) {
+                best = rk;
+                found = true;
+            } else if (fabs(rk) == halfL) {
+                long long ni = (long long)nk;
+                if ((ni & 1LL) == 0) tie_n = nk;
+            }
+        }
+        if (!found) best = fma(-tie_n, L, d);
+        r = best;
+    }
+    if (r == 0.0) r = copysign(0.0, d);
+    return r;
+}
+
+// FP32 minimum-image displacement from the coarse/fine position split.
+// Xd = Xi - Xj is exact (multiples of 1/8); c = Xd - n*Lhi is exact; the fine
+// parts carry the remaining bits, so the result is within ~1 ulp of the
+// correctly rounded FP64 displacement.
+__device__ __forceinline__ float disp32(float Xi, float Xj, float fi, float fj, float Lhi, float Llo,
+                                       float invL) {
+    float Xd = Xi - Xj;
+    float n = rintf(Xd * invL);
+    float c = fmaf(-n, Lhi, Xd);
+    float fd = fmaf(-n, Llo, fi - fj);
+    return c + fd;
+}
+
+}  // namespace parm

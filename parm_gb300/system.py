@@ -1,0 +1,229 @@
+"""Python view of one parm_gb300 handle (a batch of periodic systems on the GPU).
+
+Arrays crossing this boundary use the reference's per-atom vectors as
+``(natoms, ndim)`` float64 arrays in the caller's atom order; the library
+converts to and from its internal cell-ordered layout on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import capi
+from .capi import check, dptr, u32ptr, u64ptr
+
+
+def _as_f64(a, shape) -> np.ndarray:
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if arr.shape != shape:
+        arr = np.ascontiguousarray(np.broadcast_to(arr, shape))
+    return arr
+
+
+class System:
+    """A GPU handle for ``nsys`` independent periodic systems.
+
+    ``natoms`` is an int (one system) or a sequence of per-system sizes.
+    ``precision`` is ``"fp64"`` (bit-exact with the reference) or ``"mixed"``.
+    """
+
+    def __init__(self, natoms: int | Sequence[int], ndim: int = 3, precision: str = "fp64"):
+        self.lib = capi.load()
+        sizes = [int(natoms)] if np.isscalar(natoms) else [int(s) for s in natoms]
+        self.sizes = np.asarray(sizes, dtype=np.uint32)
+        self.nsys = len(sizes)
+        self.n = int(self.sizes.sum())
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        self.ndim = ndim
+        self.precision = precision
+        prec = {"fp64": capi.FP64, "mixed": capi.MIXED}[precision]
+        h = C.c_void_p()
+        check(self.lib.parm_create(C.byref(h), ndim, self.nsys, u32ptr(self.sizes), prec))
+        self.h = h
+        self.stride = 4 * ndim + 1
+
+    # -- lifetime --
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.parm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- box / atoms --
+    def set_boxes(self, L) -> None:
+        arr = _as_f64(L, (self.nsys, self.ndim))
+        check(self.lib.parm_set_boxes(self.h, dptr(arr)))
+
+    def set_atoms(self, x=None, v=None, a=None, f=None, m=None) -> None:
+        nd = self.ndim
+        buf = np.zeros((self.n, self.stride))
+        fields = 0
+        for bit, off, val in ((capi.X, 0, x), (capi.V, nd, v), (capi.A, 2 * nd, a), (capi.F, 3 * nd, f)):
+            if val is not None:
+                buf[:, off:off + nd] = _as_f64(val, (self.n, nd))
+                fields |= bit
+        if m is not None:
+            buf[:, 4 * nd] = _as_f64(m, (self.n,))
+            fields |= capi.M
+        check(self.lib.parm_set_atoms(self.h, dptr(buf), self.stride, fields))
+
+    def get_atoms(self, fields: int = 31) -> dict:
+        buf = np.zeros((self.n, self.stride))
+        check(self.lib.parm_get_atoms(self.h, dptr(buf), self.stride, fields))
+        nd = self.ndim
+        out = {}
+        for name, bit, off in (("x", capi.X, 0), ("v", capi.V, nd), ("a", capi.A, 2 * nd), ("f", capi.F, 3 * nd)):
+            if fields & bit:
+                out[name] = buf[:, off:off + nd].copy()
+        if fields & capi.M:
+            out["m"] = buf[:, 4 * nd].copy()
+        return out
+
+    # -- interaction / neighbour list --
+    def set_interaction(self, kind: int, params, skin: float, rank=None) -> None:
+        p = _as_f64(params, (self.n, 3))
+        rk = None
+        if rank is not None:
+            rk = np.ascontiguousarray(np.asarray(rank, dtype=np.uint32))
+        check(self.lib.parm_set_interaction(self.h, kind, dptr(p), u32ptr(rk) if rk is not None else None,
+                                            float(skin)))
+
+    def ignore(self, a: int, b: int) -> None:
+        check(self.lib.parm_nlist_ignore(self.h, int(a), int(b)))
+
+    def nlist_update(self, force: bool = True) -> np.ndarray:
+        out = np.zeros(self.nsys, dtype=np.uint8)
+        check(self.lib.parm_nlist_update(self.h, 1 if force else 0, out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out.astype(bool)
+
+    def which(self) -> np.ndarray:
+        out = np.zeros(self.nsys, dtype=np.uint32)
+        check(self.lib.parm_nlist_which(self.h, u32ptr(out)))
+        return out
+
+    def numpairs(self) -> np.ndarray:
+        out = np.zeros(self.nsys, dtype=np.uint64)
+        check(self.lib.parm_nlist_numpairs(self.h, u64ptr(out)))
+        return out
+
+    def pairs(self, sys: int = 0) -> np.ndarray:
+        n = np.zeros(1, dtype=np.uint64)
+        check(self.lib.parm_nlist_pairs(self.h, sys, None, 0, u64ptr(n)))
+        out = np.zeros((int(n[0]), 2), dtype=np.uint32)
+        check(self.lib.parm_nlist_pairs(self.h, sys, u32ptr(out), int(n[0]), u64ptr(n)))
+        return out
+
+    def set_capacity(self, maxnb: int) -> None:
+        check(self.lib.parm_set_nlist_capacity(self.h, int(maxnb)))
+
+    def capacity(self) -> int:
+        v = C.c_uint32()
+        check(self.lib.parm_get_nlist_capacity(self.h, C.byref(v)))
+        return v.value
+
+    # -- forces / quantities --
+    def set_forces(self, constraints_and_a: bool = True) -> None:
+        check(self.lib.parm_set_forces(self.h, 1 if constraints_and_a else 0))
+
+    def evaluate(self, what: int) -> np.ndarray:
+        ncomp = self.ndim * self.ndim if what == capi.EVAL_STRESS else 1
+        out = np.zeros(self.nsys * ncomp)
+        check(self.lib.parm_evaluate(self.h, what, dptr(out)))
+        if what == capi.EVAL_STRESS:
+            return out.reshape(self.nsys, self.ndim, self.ndim)
+        return out
+
+    def energy(self) -> np.ndarray:
+        return self.evaluate(capi.EVAL_ENERGY)
+
+    def virial(self) -> np.ndarray:
+        return self.evaluate(capi.EVAL_VIRIAL)
+
+    def stress(self) -> np.ndarray:
+        return self.evaluate(capi.EVAL_STRESS)
+
+    def contacts(self) -> np.ndarray:
+        return self.evaluate(capi.EVAL_CONTACTS)
+
+    def overlaps(self) -> np.ndarray:
+        return self.evaluate(capi.EVAL_OVERLAPS)
+
+    def kinetic_energy(self, origin=None) -> np.ndarray:
+        out = np.zeros(self.nsys)
+        o = None if origin is None else _as_f64(origin, (self.nsys, self.ndim))
+        check(self.lib.parm_kinetic_energy(self.h, dptr(o) if o is not None else None, dptr(out)))
+        return out
+
+    def momentum(self):
+        mom = np.zeros((self.nsys, self.ndim))
+        mass = np.zeros(self.nsys)
+        check(self.lib.parm_momentum(self.h, dptr(mom), dptr(mass)))
+        return mom, mass
+
+    def max_force_sq(self) -> np.ndarray:
+        out = np.zeros(self.nsys)
+        check(self.lib.parm_max_force_sq(self.h, dptr(out)))
+        return out
+
+    # -- integrators --
+    def verlet(self, dt: float, nsteps: int = 1) -> None:
+        check(self.lib.parm_verlet(self.h, float(dt), int(nsteps)))
+
+    def damped(self, dt: float, damping: float, nsteps: int = 1) -> None:
+        check(self.lib.parm_damped(self.h, float(dt), float(damping), int(nsteps)))
+
+    def sol(self, dt: float, damping: float, T: float, seed: int, nsteps: int = 1) -> None:
+        check(self.lib.parm_sol(self.h, float(dt), float(damping), float(T), int(seed), int(nsteps)))
+
+    def step_counter(self) -> int:
+        v = C.c_uint64()
+        check(self.lib.parm_get_step(self.h, C.byref(v)))
+        return v.value
+
+    def set_step_counter(self, step: int) -> None:
+        check(self.lib.parm_set_step(self.h, int(step)))
+
+    def set_graph_steps(self, k: int) -> None:
+        check(self.lib.parm_set_graph_steps(self.h, int(k)))
+
+    def timing(self, enable: bool) -> None:
+        check(self.lib.parm_timing(self.h, 1 if enable else 0))
+
+    def timing_read(self) -> dict:
+        fm, dm = C.c_double(), C.c_double()
+        fl, rb = C.c_uint64(), C.c_uint64()
+        check(self.lib.parm_timing_read(self.h, C.byref(fm), C.byref(fl), C.byref(dm), C.byref(rb)))
+        return {"force_ms": fm.value, "force_launches": fl.value, "drift_ms": dm.value, "rebuilds": rb.value}
+
+    def last_launches(self) -> int:
+        v = C.c_uint64()
+        check(self.lib.parm_last_launches(self.h, C.byref(v)))
+        return v.value
+
+    def sync(self) -> None:
+        check(self.lib.parm_sync(self.h))
+
+    def stream(self) -> int:
+        return self.lib.parm_stream(self.h) or 0
+
+
+def debug_remainder(d, L) -> np.ndarray:
+    lib = capi.load()
+    d = np.ascontiguousarray(np.asarray(d, dtype=np.float64))
+    L = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), d.shape))
+    out = np.zeros_like(d)
+    check(lib.parm_debug_remainder(dptr(d), dptr(L), dptr(out), d.size))
+    return out

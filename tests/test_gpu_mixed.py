@@ -1,0 +1,97 @@
+"""Mixed-precision path: force/energy error and NVE drift against FP64.
+
+Tolerances (stated by the benchmark specification for the mixed path):
+  max_i |F_i - F_i^FP64| / rms_i |F_i^FP64|  <= 1e-5
+  relative potential-energy error             <= 1e-6
+"""
+import numpy as np
+import pytest
+
+from helpers import force_error, make_gpu, make_oracle
+from parm_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+ENERGY_TOL = 1e-6
+
+
+def _equilibrated_lj(shape, steps=300, seed=12345):
+    """LJ lattice melted with the FP64 GPU path (dt 0.002)."""
+    w = W.lj_lattice(shape=shape, skin_prime=0.3, seed=seed)
+    g = make_gpu(w, "fp64")
+    g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
+    g.verlet(0.002, steps)
+    st = g.get_atoms()
+    w.x, w.v = st["x"], st["v"]
+    return w
+
+
+@pytest.fixture(scope="module")
+def lj32k():
+    return _equilibrated_lj((32, 32, 32))
+
+
+def test_mixed_forces_within_tolerance(lj32k):
+    w = lj32k
+    m = make_gpu(w, "mixed")
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.build_fast()
+    assert np.array_equal(m.pairs(), o.pairs())   # the list test stays FP64-exact
+    m.set_forces(True)
+    o.set_forces(True)
+    F = m.get_atoms()["f"]
+    Fref = o.get_state()["f"]
+    err = force_error(F, Fref)
+    assert err <= FORCE_TOL, err
+    e, eref = m.energy()[0], o.energy()
+    assert abs(e - eref) / abs(eref) <= ENERGY_TOL
+    p, _ = o.pressure()
+    assert abs(m.virial()[0] - p) / abs(p) <= 1e-5
+
+
+@pytest.mark.parametrize("kind,exponent", [(1, 2.0), (1, 2.5), (2, 0.0)])
+def test_mixed_soft_kinds(kind, exponent):
+    w = W.small_random(n=4000, ndim=3, kind=kind, seed=31, phi=0.6 if kind == 1 else 0.4,
+                       exponent=exponent, skin=0.2)
+    if kind == 2:
+        w.params[:, 0] = 1.0
+    m = make_gpu(w, "mixed")
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.nl_update(True)
+    m.set_forces(True)
+    o.set_forces(True)
+    err = force_error(m.get_atoms()["f"], o.get_state()["f"])
+    assert err <= FORCE_TOL, err
+
+
+def test_mixed_2d_disks():
+    w = W.soft_disks(n=4096, phi=0.84)
+    m = make_gpu(w, "mixed")
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.build_fast()
+    m.set_forces(True)
+    o.set_forces(True)
+    err = force_error(m.get_atoms()["f"], o.get_state()["f"])
+    assert err <= FORCE_TOL, err
+
+
+def test_mixed_nve_drift_comparable(lj32k):
+    """NVE energy drift of the mixed path stays within a few times the FP64 path's."""
+    w = lj32k
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = make_gpu(w, prec)
+        g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
+        E = []
+        for _ in range(20):
+            g.verlet(0.002, 50)
+            E.append(g.energy()[0] + g.kinetic_energy()[0])
+        t = np.arange(len(E))
+        slope = np.polyfit(t, E, 1)[0] / 50   # per step
+        out[prec] = abs(slope) * 1e5 / abs(np.mean(E))
+    # drift per 1e5 steps, relative to |E|
+    assert out["mixed"] <= max(5 * out["fp64"], 1e-4), out
