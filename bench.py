@@ -204,7 +204,9 @@ def run_ours(args, rank, world, local_rank):
     n = w.n
     log(f"[rank {rank}] building mixed system, n={n}")
     g = make_system(w, "mixed", local_rank)
-    g.set_graph_steps(50)
+    g.set_graph_steps(args.graph_steps)
+    tpa = g.autotune() if args.tpa == 0 else (g.set_threads_per_atom(args.tpa) or args.tpa)
+    log(f"[rank {rank}] threads per atom: {tpa}")
     g.verlet(DT, args.warmup)
     g.sync()
     e_start = g.energy()[0] + g.kinetic_energy()[0]
@@ -253,7 +255,7 @@ def run_ours(args, rank, world, local_rank):
                          "cutoff_sigma": float(w.params[0, 2]), "precision": "mixed",
                          "parallelism": f"replicas{world}" if world > 1 else "single",
                          "l2": "inputs larger than L2 (state + neighbour lists ~1 GB)",
-                         "steps_per_graph": 50},
+                         "steps_per_graph": args.graph_steps, "threads_per_atom": tpa},
               "clocks": ck,
               "gpu_launches": launches,
               "rebuilds": tr["rebuilds"]}
@@ -264,6 +266,12 @@ def run_ours(args, rank, world, local_rank):
                           "peak_source": f"{peak_kind} hbm_gbs"}
     result["energy_drift_rel"] = {"per_1e5_steps": abs(e_end - e_start) / abs(e_start) * 1e5 / args.steps,
                                   "steps": args.steps}
+
+    if args.only_timed:
+        g.close()
+        if rank == 0:
+            print(json.dumps(result), flush=True)
+        return
 
     # --- FP64 path on the same system, and mixed-vs-FP64 error at one state ---
     st = g.get_atoms(capi.X | capi.V | capi.A)
@@ -305,9 +313,9 @@ def run_ours(args, rank, world, local_rank):
     hp = C.c_void_p()
     capi.check(lib.parm_host_alloc(C.byref(hp), nbytes))
     buf = np.ctypeslib.as_array((C.c_double * (n * stride)).from_address(hp.value)).reshape(n, stride)
-    cur = g.get_atoms(capi.X | capi.V | capi.A)
-    buf[:, 0:3], buf[:, 3:6], buf[:, 6:9] = cur["x"], cur["v"], cur["a"]
-    fields = capi.X | capi.V | capi.A
+    cur = g.get_atoms()
+    buf[:, 0:3], buf[:, 3:6], buf[:, 6:9], buf[:, 9:12], buf[:, 12] = cur["x"], cur["v"], cur["a"], cur["f"], cur["m"]
+    fields = capi.X | capi.V | capi.A | capi.F | capi.M   # whole Atom records, as an AtomVec holds them
     dptr = buf.ctypes.data_as(C.POINTER(C.c_double))
     n_e2e = max(3, min(args.e2e_steps, args.steps))
     for _ in range(2):
@@ -326,9 +334,10 @@ def run_ours(args, rank, world, local_rank):
         t = torch.tensor([t_e2e], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_e2e = float(t.item())
-    result["e2e"] = {"value": world * n * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * 9 * 8,
-                     "d2h_bytes_per_step": n * 9 * 8, "steps": n_e2e,
-                     "api": "parm_set_atoms(x,v,a) + parm_verlet(dt, 1) + parm_get_atoms(x,v,a), pinned host AoS"}
+    result["e2e"] = {"value": world * n * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * stride * 8,
+                     "d2h_bytes_per_step": n * stride * 8, "steps": n_e2e,
+                     "api": "parm_set_atoms + parm_verlet(dt, 1) + parm_get_atoms on whole Atom records "
+                            "{x,v,a,f,m} in pinned host memory"}
     lib.parm_host_free(hp)
     g.close()
 
@@ -355,6 +364,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--graph-steps", type=int, default=50,
+                    help="time steps per CUDA graph launch (0: direct kernel launches, for profilers)")
+    ap.add_argument("--tpa", type=int, default=0,
+                    help="pair-kernel variant (0: autotune; 1/2/4 tiled, 100+t gather)")
+    ap.add_argument("--only-timed", action="store_true",
+                    help="run only the timed mixed-precision region (used for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

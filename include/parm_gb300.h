@@ -146,7 +146,20 @@ int parm_set_step(parm_system* s, uint64_t step);
 int parm_set_nlist_capacity(parm_system* s, uint32_t maxnb);
 int parm_get_nlist_capacity(parm_system* s, uint32_t* maxnb);
 
-/* Steps captured per CUDA graph launch (default 16). */
+/* Variant of the mixed-precision pair kernel: 1, 2 or 4 threads per atom with
+ * neighbour positions staged in shared memory per tile of 64 atoms, or
+ * 100 + t for the plain gather kernel with t = 1, 4, 8, 16 or 32 threads per
+ * atom (default 101).  The FP64 path always uses one thread per atom, so that
+ * each atom's force is summed in the reference's order. */
+int parm_set_threads_per_atom(parm_system* s, uint32_t tpa);
+
+/* Time every variant of the mixed-precision pair kernel on the current
+ * configuration and keep the fastest; *tpa (when not NULL) receives
+ * tiled * 1000 + threads_per_atom * 10 + neighbours_per_iteration.
+ * The state is left unchanged. */
+int parm_autotune(parm_system* s, uint32_t* tpa);
+
+/* Steps captured per CUDA graph launch (default 16; 0 launches kernels directly). */
 int parm_set_graph_steps(parm_system* s, uint32_t k);
 
 /* Kernel timing: when enabled, time-step calls record CUDA events around the

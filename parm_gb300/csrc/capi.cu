@@ -80,6 +80,7 @@ struct parm_system {
     std::vector<void*> allocs;
     void* cell_mem = nullptr;
     void* nbr_mem = nullptr;
+    void* tlst_mem = nullptr;
     void* excl_mem = nullptr;
     double* staging = nullptr;
     size_t staging_bytes = 0;
@@ -98,6 +99,7 @@ struct parm_system {
         for (void* p : allocs) cudaFree(p);
         if (cell_mem) cudaFree(cell_mem);
         if (nbr_mem) cudaFree(nbr_mem);
+        if (tlst_mem) cudaFree(tlst_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
@@ -142,6 +144,12 @@ struct parm_system {
                 return fail(PARM_ERR_CAPACITY,
                             "neighbour list capacity exceeded (" + std::to_string(c.maxnb) +
                                 " per atom); raise it with parm_set_nlist_capacity");
+            if (stw & ST_IMAGE_RANGE)
+                return fail(PARM_ERR_RUNTIME, "an atom moved more than 127 box lengths from its neighbours' "
+                                              "frame (mixed precision)");
+            if (stw & ST_TILE_OVERFLOW)
+                return fail(PARM_ERR_CAPACITY, "a tile of the mixed-precision kernel has more than " +
+                                                   std::to_string(TILE_ECAP) + " distinct neighbours");
             if (stw & ST_SORT_CAP)
                 return fail(PARM_ERR_CAPACITY, "FP64 path: a neighbour list exceeded 256 entries");
             if (stw & ST_NONFINITE) return fail(PARM_ERR_RUNTIME, "non-finite atom position");
@@ -185,7 +193,11 @@ struct parm_system {
                 }
             }
             S.ncell = (uint32_t)(S.nc[0] * S.nc[1] * S.nc[2]);
-            for (int d = 0; d < 3; d++) S.cellw_inv[d] = (float)(S.nc[d] / S.L[d]);
+            for (int d = 0; d < 3; d++) {
+                S.cellw_inv[d] = (float)(S.nc[d] / S.L[d]);
+                S.cellw[d] = S.L[d] / S.nc[d];
+                S.cellw32[d] = (float)S.cellw[d];
+            }
             S.skin = skin;
             S.rlist_max = rl;
             S.cell_off = total;
@@ -193,12 +205,28 @@ struct parm_system {
             total += S.ncell + 1;
         }
         bucket_off[nsys] = total;
+        c.any_wrap = 0;
+        for (uint32_t s2 = 0; s2 < nsys; s2++)
+            for (int d = 0; d < nd; d++)
+                if (sys[s2].nc[d] < 3) c.any_wrap = 1;
         if (cell_mem) cudaFree(cell_mem);
         cell_mem = nullptr;
-        CUDA_TRY(cudaMalloc(&cell_mem, (size_t)(2 * (size_t)total + 2) * 4));
-        CUDA_TRY(cudaMemsetAsync(cell_mem, 0, (size_t)(2 * (size_t)total + 2) * 4, st));
+        const size_t nblk = (total + 4095) / 4096 + 1;
+        const size_t words = 3 * (size_t)total + 2 + 2 * nblk;
+        CUDA_TRY(cudaMalloc(&cell_mem, words * 4));
+        CUDA_TRY(cudaMemsetAsync(cell_mem, 0, words * 4, st));
         c.cell_count = static_cast<uint32_t*>(cell_mem);
         c.cell_start = c.cell_count + total + 1;
+        uint32_t* bsys = c.cell_start + total + 1;
+        c.bucket_sys = bsys;
+        c.scan_aux = bsys + total;
+        {
+            std::vector<uint32_t> hb(total);
+            for (uint32_t s2 = 0; s2 < nsys; s2++)
+                for (uint32_t b = bucket_off[s2]; b < bucket_off[s2 + 1]; b++) hb[b] = s2;
+            CUDA_TRY(cudaMemcpyAsync(bsys, hb.data(), 4 * (size_t)total, cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+        }
         c.nbucket = total;
         CUDA_TRY(cudaMemcpyAsync(const_cast<SysConst*>(c.sys), sys.data(), sizeof(SysConst) * nsys,
                                  cudaMemcpyHostToDevice, st));
@@ -215,10 +243,12 @@ struct parm_system {
         maxnb = std::max<uint32_t>(8, (maxnb + 7) / 8 * 8);
         void* fresh = nullptr;
         CUDA_TRY(cudaStreamSynchronize(st));
-        CUDA_TRY(cudaMalloc(&fresh, (size_t)maxnb * c.nalloc * 4));
+        CUDA_TRY(cudaMalloc(&fresh, (size_t)maxnb * n * 4 + 16));
         if (nbr_mem) {
+            // rows are maxnb long: re-pitch the current lists into the new rows
             uint32_t keep = std::min(maxnb, c.maxnb);
-            CUDA_TRY(cudaMemcpy(fresh, nbr_mem, (size_t)keep * c.nalloc * 4, cudaMemcpyDeviceToDevice));
+            CUDA_TRY(cudaMemcpy2D(fresh, (size_t)maxnb * 4, nbr_mem, (size_t)c.maxnb * 4, (size_t)keep * 4, n,
+                                  cudaMemcpyDeviceToDevice));
             if (maxnb < c.maxnb) {
                 // shrinking: lists longer than the new capacity are rebuilt
                 std::vector<uint32_t> ones(nsys, kind >= 0 ? 1u : 0u);
@@ -228,6 +258,20 @@ struct parm_system {
         }
         nbr_mem = fresh;
         c.nbr = static_cast<uint32_t*>(nbr_mem);
+        if (c.ntile) {
+            // tile lists: [tile][k][atom] with maxnb rows of TILE_ATOMS per tile
+            void* tfresh = nullptr;
+            const size_t tile_new = (size_t)maxnb * TILE_ATOMS * 2;
+            CUDA_TRY(cudaMalloc(&tfresh, tile_new * c.ntile + 16));
+            if (tlst_mem) {
+                const size_t tile_old = (size_t)c.maxnb * TILE_ATOMS * 2;
+                CUDA_TRY(cudaMemcpy2D(tfresh, tile_new, tlst_mem, tile_old, std::min(tile_old, tile_new),
+                                      c.ntile, cudaMemcpyDeviceToDevice));
+                cudaFree(tlst_mem);
+            }
+            tlst_mem = tfresh;
+            c.tile_lst = static_cast<uint16_t*>(tlst_mem);
+        }
         c.maxnb = maxnb;
         clear_graphs();
         return PARM_OK;
@@ -305,7 +349,7 @@ struct parm_system {
             for (auto& e : ge.ev) CUDA_TRY(cudaEventCreate(&e));
         }
         const int dmode = mode == SM_VERLET ? DM_VERLET : (mode == SM_DAMPED ? DM_DAMPED : DM_SOL);
-        const int fmode = mode == SM_VERLET ? FM_VERLET : (mode == SM_DAMPED ? FM_DAMPED : FM_SOL);
+        const int fmode = FM_FORCES;
         CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (uint32_t step = 0; step < k; step++) {
             cudaStreamCaptureStatus cs;
@@ -337,14 +381,16 @@ struct parm_system {
             launch_rebuild(c, st2);
             CUDA_TRY(cudaGetLastError());
             CUDA_TRY(cudaStreamEndCapture(st2, &body));
-            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step], st));
-            launch_drift(c, st, dmode);
-            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step + 1], st));
+            if (timing) CUDA_TRY(cudaEventRecordWithFlags(ge.ev[3 * step], st, cudaEventRecordExternal));
+            launch_drift(c, st, dmode, step > 0);
+            if (timing) CUDA_TRY(cudaEventRecordWithFlags(ge.ev[3 * step + 1], st, cudaEventRecordExternal));
             if (prec == PREC_FP64) launch_force64(c, st, fmode);
             else launch_force32(c, st, fmode);
-            if (timing) CUDA_TRY(cudaEventRecord(ge.ev[3 * step + 2], st));
+            if (timing) CUDA_TRY(cudaEventRecordWithFlags(ge.ev[3 * step + 2], st, cudaEventRecordExternal));
             CUDA_TRY(cudaGetLastError());
         }
+        launch_kick(c, st, dmode);   // second half of the chunk's last step
+        CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaStreamEndCapture(st, &ge.graph));
         CUDA_TRY(cudaGraphInstantiate(&ge.exec, ge.graph, 0));
         return PARM_OK;
@@ -352,11 +398,44 @@ struct parm_system {
 
     int run_steps(int mode, uint32_t nsteps) {
         TRY(upload_exclusions());
-        uint32_t w0 = 0;
         std::vector<uint32_t> which0(nsys), which1(nsys);
         CUDA_TRY(cudaMemcpyAsync(which0.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost, st));
         uint32_t done = 0;
         uint64_t launches = 0;
+        if (graph_k == 0) {
+            // direct launches (no graph): the rebuild chain is always launched
+            // and each of its kernels returns at once for unflagged systems
+            const int dmode = mode == SM_VERLET ? DM_VERLET : (mode == SM_DAMPED ? DM_DAMPED : DM_SOL);
+            const int fmode = FM_FORCES;
+            cudaEvent_t e[3] = {nullptr, nullptr, nullptr};
+            if (timing)
+                for (auto& q : e) CUDA_TRY(cudaEventCreate(&q));
+            for (uint32_t k = 0; k < nsteps; k++) {
+                launch_arm(c, st, 1, 0, 0);
+                launch_rebuild(c, st);
+                if (timing) CUDA_TRY(cudaEventRecord(e[0], st));
+                launch_drift(c, st, dmode, k > 0);
+                if (timing) CUDA_TRY(cudaEventRecord(e[1], st));
+                if (prec == PREC_FP64) launch_force64(c, st, fmode);
+                else launch_force32(c, st, fmode);
+                if (timing) {
+                    CUDA_TRY(cudaEventRecord(e[2], st));
+                    CUDA_TRY(cudaEventSynchronize(e[2]));
+                    float a = 0.f, b = 0.f;
+                    CUDA_TRY(cudaEventElapsedTime(&a, e[0], e[1]));
+                    CUDA_TRY(cudaEventElapsedTime(&b, e[1], e[2]));
+                    t_drift += a;
+                    t_force += b;
+                    n_force += 1;
+                }
+                CUDA_TRY(cudaGetLastError());
+            }
+            launch_kick(c, st, dmode);
+            if (timing)
+                for (auto& q : e) cudaEventDestroy(q);
+            launches = (uint64_t)nsteps * (3 + (prec == PREC_FP64 ? 9 : 8)) + 1;
+            done = nsteps;
+        }
         while (done < nsteps) {
             uint32_t k = std::min(graph_k, nsteps - done);
             uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)k << 1) | (timing ? 1u : 0u);
@@ -376,7 +455,7 @@ struct parm_system {
                 it = graphs.emplace(key, ge).first;
             }
             CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
-            launches += 3ull * k;
+            launches += 3ull * k + 1;
             if (timing) {
                 CUDA_TRY(cudaStreamSynchronize(st));
                 for (uint32_t q = 0; q < k; q++) {
@@ -395,12 +474,11 @@ struct parm_system {
         CUDA_TRY(cudaMemcpy(which1.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
         uint64_t rb = 0;
         for (uint32_t s = 0; s < nsys; s++) rb += (uint64_t)(which1[s] - which0[s]);
-        (void)w0;
         n_rebuild += rb;
         uint32_t chains = 0;
         CUDA_TRY(cudaMemcpy(&chains, c.chains, 4, cudaMemcpyDeviceToHost));
         CUDA_TRY(cudaMemset(c.chains, 0, 4));
-        last_launches = launches + (uint64_t)chains * (c.prec == PREC_FP64 ? 9ull : 8ull);
+        last_launches = graph_k == 0 ? launches : launches + (uint64_t)chains * (c.prec == PREC_FP64 ? 9ull : 8ull);
         return PARM_OK;
     }
 
@@ -487,7 +565,8 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     c.kind = -1;
     c.nsys = nsys;
     c.n = S->n;
-    c.nalloc = S->n;
+    c.tpa = 1;
+    c.unr = 1;
     const uint32_t n = S->n;
     const size_t vb = S->vbytes();
     int r = PARM_OK;
@@ -527,8 +606,8 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     A(S->alloc(c.cslot, n));
     A(S->alloc(c.perm, n));
     A(S->alloc(c.nnb, n));
-    A(S->alloc(c.posA, n));
-    A(S->alloc(c.posB, n));
+    A(S->alloc(c.pos, 2 * (size_t)n));
+    A(S->alloc(c.posw, n));
     A(S->alloc(c.red, (size_t)n * 12));
     A(S->alloc(c.flag, nsys));
     A(S->alloc(c.force_rb, nsys));
@@ -592,6 +671,35 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
         Y.atom_off = S->off[s];
         Y.natoms = natoms[s];
     }
+    if (precision == PARM_MIXED) {
+        std::vector<uint32_t> t0, tn, ts;
+        for (uint32_t s = 0; s < nsys; s++)
+            for (uint32_t a = 0; a < natoms[s]; a += TILE_ATOMS) {
+                t0.push_back(S->off[s] + a);
+                tn.push_back(std::min<uint32_t>(TILE_ATOMS, natoms[s] - a));
+                ts.push_back(s);
+            }
+        const uint32_t nt = (uint32_t)t0.size();
+        uint32_t *d0 = nullptr, *dn = nullptr, *ds = nullptr;
+        r = S->alloc(d0, nt);
+        if (r == PARM_OK) r = S->alloc(dn, nt);
+        if (r == PARM_OK) r = S->alloc(ds, nt);
+        if (r == PARM_OK) r = S->alloc(c.tile_anchor, nt);
+        if (r == PARM_OK) r = S->alloc(c.tile_ne, nt);
+        if (r == PARM_OK) r = S->alloc(c.tile_ent, (size_t)nt * TILE_ECAP);
+        if (r == PARM_OK) r = S->alloc(c.atom_img, n);
+        if (r != PARM_OK) return bail(r);
+        cudaStreamSynchronize(S->st);
+        if (!up(d0, t0.data(), 4 * (size_t)nt) || !up(dn, tn.data(), 4 * (size_t)nt) ||
+            !up(ds, ts.data(), 4 * (size_t)nt))
+            return bail(fail(PARM_ERR_CUDA, "tile upload failed"));
+        c.tile_atom0 = d0;
+        c.tile_natom = dn;
+        c.tile_sys = ds;
+        c.ntile = nt;
+        c.tiled = 0;
+        c.tpa = 1;
+    }
     r = S->setup_cells();
     if (r != PARM_OK) return bail(r);
     r = S->set_capacity(32);
@@ -642,8 +750,13 @@ int parm_set_atoms(parm_system* S, const double* atoms, uint64_t stride, uint32_
     uint64_t lo, hi;
     field_span(fields, S->nd, lo, hi);
     TRY(S->ensure_staging((size_t)S->n * stride * 8));
-    CUDA_TRY(cudaMemcpy2DAsync(S->staging + lo, stride * 8, atoms + lo, stride * 8, (hi - lo) * 8, S->n,
-                               cudaMemcpyHostToDevice, S->st));
+    if (2 * (hi - lo) >= stride) {
+        // one linear copy of the records beats a strided copy of short rows
+        CUDA_TRY(cudaMemcpyAsync(S->staging, atoms, (size_t)S->n * stride * 8, cudaMemcpyHostToDevice, S->st));
+    } else {
+        CUDA_TRY(cudaMemcpy2DAsync(S->staging + lo, stride * 8, atoms + lo, stride * 8, (hi - lo) * 8, S->n,
+                                   cudaMemcpyHostToDevice, S->st));
+    }
     launch_scatter_in(S->c, S->st, S->staging, stride, fields);
     CUDA_TRY(cudaGetLastError());
     return S->sync_status();
@@ -660,15 +773,23 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
     uint64_t covered = 0;
     for (int b = 0; b < 5; b++)
         if (fields & (1u << b)) covered += (b == 4) ? 1 : (uint64_t)S->nd;
-    if (covered != hi - lo) {
-        // keep the caller's other fields intact: bring the span over first
+    const bool linear = 2 * (hi - lo) >= stride;
+    const bool whole = covered == stride;   // every double of each record is written
+    if (linear && !whole) {
+        // keep the caller's other doubles intact: bring the records over first
+        CUDA_TRY(cudaMemcpyAsync(S->staging, atoms, (size_t)S->n * stride * 8, cudaMemcpyHostToDevice, S->st));
+    } else if (!linear && covered != hi - lo) {
         CUDA_TRY(cudaMemcpy2DAsync(S->staging + lo, stride * 8, atoms + lo, stride * 8, (hi - lo) * 8,
                                    S->n, cudaMemcpyHostToDevice, S->st));
     }
     launch_gather_out(S->c, S->st, S->staging, stride, fields);
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaMemcpy2DAsync(atoms + lo, stride * 8, S->staging + lo, stride * 8, (hi - lo) * 8, S->n,
-                               cudaMemcpyDeviceToHost, S->st));
+    if (linear) {
+        CUDA_TRY(cudaMemcpyAsync(atoms, S->staging, (size_t)S->n * stride * 8, cudaMemcpyDeviceToHost, S->st));
+    } else {
+        CUDA_TRY(cudaMemcpy2DAsync(atoms + lo, stride * 8, S->staging + lo, stride * 8, (hi - lo) * 8, S->n,
+                                   cudaMemcpyDeviceToHost, S->st));
+    }
     return S->sync_status();
 }
 
@@ -828,8 +949,7 @@ int parm_nlist_pairs(parm_system* S, uint32_t sys, uint32_t* pairs, uint64_t cap
     CUDA_TRY(cudaMemcpy(rank.data(), S->c.rank, 4 * (size_t)S->n, cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(orig.data(), S->c.orig + o, 4 * (size_t)na, cudaMemcpyDeviceToHost));
     if (na && mx)
-        CUDA_TRY(cudaMemcpy2D(nbr.data(), 4 * (size_t)na, S->c.nbr + o, 4 * (size_t)S->c.nalloc,
-                              4 * (size_t)na, mx, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(nbr.data(), S->c.nbr + (size_t)o * mx, 4 * (size_t)na * mx, cudaMemcpyDeviceToHost));
     struct P {
         uint32_t r1, r2, a, b;
     };
@@ -838,7 +958,7 @@ int parm_nlist_pairs(parm_system* S, uint32_t sys, uint32_t* pairs, uint64_t cap
         uint32_t ri = rank[o + i];
         if (ri == PARM_NOT_MEMBER) continue;
         for (uint32_t k = 0; k < nnb[i]; k++) {
-            uint32_t j = nbr[(size_t)k * na + i];
+            uint32_t j = nbr[(size_t)i * mx + k];
             uint32_t rj = rank[j];
             if (rj < ri) v.push_back({ri, rj, orig[i], orig[j - o]});
         }
@@ -1035,9 +1155,84 @@ int parm_get_nlist_capacity(parm_system* S, uint32_t* maxnb) {
     return PARM_OK;
 }
 
+int parm_set_threads_per_atom(parm_system* S, uint32_t tpa) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    // 1, 2, 4: shared-memory tiled kernel; 101, 104, 108, 116, 132: gather
+    // kernel with 1..32 threads per atom
+    const bool tiled = tpa < 100;
+    if (tiled && S->prec == PREC_MIXED && !S->c.ntile) return fail(PARM_ERR_ARG, "no tiles in this handle");
+    if (tiled && S->prec == PREC_MIXED && !S->c.tiled) {
+        TRY(S->flush());
+        launch_tiles(S->c, S->st, 1);   // tiles for the current lists
+        TRY(S->sync_status());
+    }
+    const uint32_t t = tiled ? tpa : tpa - 100;
+    if (tiled ? !(t == 1 || t == 2 || t == 4) : !(t == 1 || t == 4 || t == 8 || t == 16 || t == 32))
+        return fail(PARM_ERR_ARG, "threads per atom: 1, 2, 4 (tiled) or 101, 104, 108, 116, 132 (gather)");
+    if (S->prec != PREC_MIXED) return PARM_OK;
+    if (S->c.tpa != t || S->c.tiled != (uint32_t)tiled || S->c.unr != 1) {
+        S->c.tpa = t;
+        S->c.tiled = tiled ? 1u : 0u;
+        S->c.unr = 1;
+        S->clear_graphs();
+    }
+    return PARM_OK;
+}
+
+int parm_autotune(parm_system* S, uint32_t* tpa_out) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (S->prec != PREC_MIXED || S->kind < 0) {
+        if (tpa_out) *tpa_out = S->c.tpa;
+        return PARM_OK;
+    }
+    TRY(S->flush());
+    // keep the current forces: the candidates' sums round differently
+    CUDA_TRY(cudaMemcpyAsync(S->c.f32b, S->c.f32, sizeof(float4) * (size_t)S->n, cudaMemcpyDeviceToDevice,
+                             S->st));
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    // (tiled, threads per atom, neighbours per iteration)
+    const uint32_t cands[][3] = {{1, 1, 1}, {1, 2, 1}, {1, 4, 1}, {0, 1, 1}, {0, 1, 2}, {0, 4, 1},
+                                 {0, 8, 1}, {0, 16, 1}};
+    const uint32_t keep = S->c.tpa, keep_u = S->c.unr, keep_t = S->c.tiled;
+    float best = 1e30f;
+    uint32_t pick = keep, pick_u = keep_u, pick_t = keep_t;
+    if (S->c.ntile && !S->c.tiled) launch_tiles(S->c, S->st, 1);
+    for (const auto& cu : cands) {
+        if (cu[0] && !S->c.ntile) continue;
+        S->c.tiled = cu[0];
+        S->c.tpa = cu[1];
+        S->c.unr = cu[2];
+        launch_force32(S->c, S->st, FM_FORCES);   // warm-up
+        CUDA_TRY(cudaEventRecord(e0, S->st));
+        for (int r = 0; r < 3; r++) launch_force32(S->c, S->st, FM_FORCES);
+        CUDA_TRY(cudaEventRecord(e1, S->st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            pick_t = cu[0];
+            pick = cu[1];
+            pick_u = cu[2];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    S->c.tpa = pick;
+    S->c.unr = pick_u;
+    S->c.tiled = pick_t;
+    CUDA_TRY(cudaMemcpyAsync(S->c.f32, S->c.f32b, sizeof(float4) * (size_t)S->n, cudaMemcpyDeviceToDevice,
+                             S->st));
+    if (pick != keep || pick_u != keep_u || pick_t != keep_t) S->clear_graphs();
+    if (tpa_out) *tpa_out = pick_t * 1000 + pick * 10 + pick_u;
+    return S->sync_status();
+}
+
 int parm_set_graph_steps(parm_system* S, uint32_t k) {
     if (!S) return fail(PARM_ERR_ARG, "NULL handle");
-    if (k == 0 || k > 1024) return fail(PARM_ERR_ARG, "steps per graph must be in 1..1024");
+    if (k > 1024) return fail(PARM_ERR_ARG, "steps per graph must be in 0..1024 (0: no graph)");
     S->graph_k = k;
     return PARM_OK;
 }

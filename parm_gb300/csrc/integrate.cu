@@ -7,8 +7,8 @@
 //   CollectionVerlet::timestep  442-469  (first loop: drift + half kick)
 //   CollectionDamped::timestep  356-381  (first loop)
 //   CollectionSol::timestep     265-322  (first loop, BivariateGauss noise)
-// The second half of each step (a = f/m and the final velocity update) is
-// fused into the pair-force kernels' epilogue.
+// The second half of step k (a = f/m and the final velocity update) is fused
+// with the first half of step k+1 in k_kickdrift; a call ends with k_kick.
 #include "parm_check.cuh"
 
 namespace parm {
@@ -61,79 +61,205 @@ __device__ __forceinline__ void normals6(unsigned long long seed, unsigned long 
 
 template <int ND>
 __device__ __forceinline__ void store_posq(const DevCtx& c, uint32_t i, const double* xs) {
-    float4 A = c.posA[i], B;
+    float4 A = c.pos[2 * (size_t)(i)], B;
     posq_split2(xs[0], A.x, B.x);
     posq_split2(xs[1], A.y, B.y);
     if constexpr (ND == 3) posq_split2(xs[2], A.z, B.z); else { A.z = 0.f; B.z = 0.f; }
     B.w = 0.f;
-    c.posA[i] = A;
-    c.posB[i] = B;
+    c.pos[2 * (size_t)(i)] = A;
+    c.pos[2 * (size_t)(i) + 1] = B;
 }
 
-template <int ND, int MODE>
-__global__ void __launch_bounds__(BLOCK) k_drift(DevCtx c) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
-    using V = typename DVec<ND>::T;
+// Second half of the previous step (the reference's loop after set_forces):
+// a = f/m and the final velocity update.  Mobility tests as in the reference:
+// Verlet and Damped skip m <= 0 or inf; Sol tests m == 0 or inf.
+template <int ND, int MODE, bool MIXED>
+__device__ __forceinline__ void kick(const DevCtx& c, uint32_t i, double m, double* a, double* v) {
     const StepParams& P = *c.params;
-    double m = c.m[i];
-    V xv = static_cast<V*>(c.x)[i];
-    V vv = static_cast<V*>(c.v)[i];
-    V av = static_cast<V*>(c.a)[i];
-    double* x = reinterpret_cast<double*>(&xv);
-    double* v = reinterpret_cast<double*>(&vv);
-    const double* a = reinterpret_cast<const double*>(&av);
-    if (!mobile(m)) {
+    double f[3] = {0.0, 0.0, 0.0};
+    float fm[3] = {0.f, 0.f, 0.f};
+    if constexpr (MIXED) {
+        const float4 q = c.f32[i];
+        fm[0] = q.x;
+        fm[1] = q.y;
+        fm[2] = q.z;
+    } else {
+        using V = typename DVec<ND>::T;
+        V fv = static_cast<const V*>(c.f)[i];
+        const double* fp = reinterpret_cast<const double*>(&fv);
 #pragma unroll
-        for (int d = 0; d < ND; d++) v[d] = 0.0;
-        static_cast<V*>(c.v)[i] = vv;
+        for (int d = 0; d < ND; d++) f[d] = fp[d];
+    }
+    const bool sol = (MODE == DM_SOL);
+    const bool has_a = sol ? !(m == 0.0 || isinf(m)) : mobile(m);
+    if (!has_a) {
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            a[d] = 0.0;
+            if (sol) v[d] = 0.0;
+        }
         return;
     }
-    if constexpr (MODE == DM_VERLET) {
-        // x += v*dt + a*(dt*dt/2); v += a*(dt/2)
+    if constexpr (MIXED) {
+        const float im = mobile(m) ? c.invm32[i] : (float)(1.0 / m);
 #pragma unroll
-        for (int d = 0; d < ND; d++) {
-            x[d] = x[d] + (v[d] * P.dt + a[d] * P.dt2_half);
-            v[d] = v[d] + a[d] * P.dt_half;
-        }
-    } else if constexpr (MODE == DM_DAMPED) {
-        // x += v*(c1*dt) + a*(c2*dt*dt); v = v*c0 + a*(dt*(c1-c2))
-#pragma unroll
-        for (int d = 0; d < ND; d++) {
-            x[d] = x[d] + (v[d] * P.c1dt + a[d] * P.c2dtdt);
-            v[d] = v[d] * P.c0 + a[d] * P.dtc12;
-        }
+        for (int d = 0; d < ND; d++) a[d] = (double)(fm[d] * im);
     } else {
-        // CollectionSol: x += v*(c1*dt) + a*(c2*dt*dt) + drG*r0;
-        //                v  = v*c0 + a*(dt*(c1-c2)) + dvG*v0
-        double v0 = sqrt(P.T / m);
-        double r0 = P.dt * v0;
-        double g[6] = {0, 0, 0, 0, 0, 0};
-        uint32_t s = c.atom_sys[i];
-        if (P.noise) normals6(c.seed[s], P.step, c.orig[i] - c.sys[s].atom_off, g);
 #pragma unroll
-        for (int d = 0; d < ND; d++) {
-            double drG = g[d] * P.x11;
-            double dvG = g[d] * P.x21 + g[ND + d] * P.x22;
-            x[d] = x[d] + ((v[d] * P.c1dt + a[d] * P.c2dtdt) + drG * r0);
-            v[d] = (v[d] * P.c0 + a[d] * P.dtc12) + dvG * v0;
-        }
+        for (int d = 0; d < ND; d++) a[d] = f[d] / m;
     }
-    static_cast<V*>(c.x)[i] = xv;
-    static_cast<V*>(c.v)[i] = vv;
-    store_posq<ND>(c, i, x);
+    const double h = (MODE == DM_VERLET) ? P.dt_half : P.dtc2;
+#pragma unroll
+    for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * h;
 }
 
-void launch_drift(const DevCtx& c, cudaStream_t s, int mode) {
+// Fused time-step kernel: [kick of the previous step] + drift of this step +
+// FP32 position view + the neighbour-list displacement test (the reference
+// runs that test at the end of the step; positions do not change after the
+// drift, so testing here sees the same values).
+template <int ND, int MODE, bool KICK, bool MIXED>
+__global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    using V = typename DVec<ND>::T;
+    bool valid = false;
+    double dsq = 0.0;
+    uint32_t s = 0;
+    if (i < c.n) {
+        const StepParams& P = *c.params;
+        s = c.atom_sys[i];
+        const double m = c.m[i];
+        V xv = static_cast<V*>(c.x)[i];
+        V vv = static_cast<V*>(c.v)[i];
+        V av;
+        double* x = reinterpret_cast<double*>(&xv);
+        double* v = reinterpret_cast<double*>(&vv);
+        double* a = reinterpret_cast<double*>(&av);
+        if constexpr (KICK) {
+#pragma unroll
+            for (int d = 0; d < (int)(sizeof(V) / 8); d++) a[d] = 0.0;
+            kick<ND, MODE, MIXED>(c, i, m, a, v);
+        } else {
+            av = static_cast<const V*>(c.a)[i];
+        }
+        const bool mob = mobile(m);
+        if (!mob) {
+#pragma unroll
+            for (int d = 0; d < ND; d++) v[d] = 0.0;
+        } else if constexpr (MODE == DM_VERLET) {
+            // x += v*dt + a*(dt*dt/2); v += a*(dt/2)
+#pragma unroll
+            for (int d = 0; d < ND; d++) {
+                x[d] = x[d] + (v[d] * P.dt + a[d] * P.dt2_half);
+                v[d] = v[d] + a[d] * P.dt_half;
+            }
+        } else if constexpr (MODE == DM_DAMPED) {
+            // x += v*(c1*dt) + a*(c2*dt*dt); v = v*c0 + a*(dt*(c1-c2))
+#pragma unroll
+            for (int d = 0; d < ND; d++) {
+                x[d] = x[d] + (v[d] * P.c1dt + a[d] * P.c2dtdt);
+                v[d] = v[d] * P.c0 + a[d] * P.dtc12;
+            }
+        } else {
+            // CollectionSol: x += v*(c1*dt) + a*(c2*dt*dt) + drG*r0;
+            //                v  = v*c0 + a*(dt*(c1-c2)) + dvG*v0
+            double v0 = sqrt(P.T / m);
+            double r0 = P.dt * v0;
+            double g[6] = {0, 0, 0, 0, 0, 0};
+            if (P.noise) normals6(c.seed[s], P.step, c.orig[i] - c.sys[s].atom_off, g);
+#pragma unroll
+            for (int d = 0; d < ND; d++) {
+                double drG = g[d] * P.x11;
+                double dvG = g[d] * P.x21 + g[ND + d] * P.x22;
+                x[d] = x[d] + ((v[d] * P.c1dt + a[d] * P.c2dtdt) + drG * r0);
+                v[d] = (v[d] * P.c0 + a[d] * P.dtc12) + dvG * v0;
+            }
+        }
+        if (mob) static_cast<V*>(c.x)[i] = xv;
+        static_cast<V*>(c.v)[i] = vv;
+        if (KICK && !MIXED) static_cast<V*>(c.a)[i] = av;
+        if (mob) {
+            // fine part of the FP32 position view against the coarse part fixed
+            // at the last rebuild or upload (x - X is exact in FP64); an atom
+            // that has moved more than 1/4 from its coarse point is re-anchored
+            // (any multiple of 1/8 is a valid coarse point)
+            float4 A = c.pos[2 * (size_t)i];
+            float4 B;
+            B.x = (float)(x[0] - (double)A.x);
+            B.y = (float)(x[1] - (double)A.y);
+            B.z = 0.f;
+            if constexpr (ND == 3) B.z = (float)(x[2] - (double)A.z);
+            B.w = 0.f;
+            if (fabsf(B.x) > 0.25f || fabsf(B.y) > 0.25f || fabsf(B.z) > 0.25f) {
+                posq_split2(x[0], A.x, B.x);
+                posq_split2(x[1], A.y, B.y);
+                if constexpr (ND == 3) posq_split2(x[2], A.z, B.z);
+                c.pos[2 * (size_t)i] = A;
+            }
+            c.pos[2 * (size_t)i + 1] = B;
+        }
+        if (c.rank[i] != NOT_MEMBER) {
+            dsq = disp_sq<ND>(xv, static_cast<const V*>(c.lastloc)[i]);
+            valid = !(dsq != dsq);
+        }
+    }
+    check_accumulate(c, s, valid, dsq);
+}
+
+// final kick of a call, so that the state between calls is the reference's
+template <int ND, int MODE, bool MIXED>
+__global__ void __launch_bounds__(BLOCK) k_kick(DevCtx c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    using V = typename DVec<ND>::T;
+    V vv = static_cast<V*>(c.v)[i];
+    V av;
+    double* a = reinterpret_cast<double*>(&av);
+#pragma unroll
+    for (int d = 0; d < (int)(sizeof(V) / 8); d++) a[d] = 0.0;
+    kick<ND, MODE, MIXED>(c, i, c.m[i], a, reinterpret_cast<double*>(&vv));
+    static_cast<V*>(c.v)[i] = vv;
+    static_cast<V*>(c.a)[i] = av;
+}
+
+template <int ND, int MODE, bool MIXED>
+static void drift_nd(const DevCtx& c, cudaStream_t s, bool with_kick) {
     unsigned g = grid_for(c.n);
+    if (with_kick) k_kickdrift<ND, MODE, true, MIXED><<<g, BLOCK, 0, s>>>(c);
+    else k_kickdrift<ND, MODE, false, MIXED><<<g, BLOCK, 0, s>>>(c);
+}
+
+template <int ND, bool MIXED>
+static void drift_prec(const DevCtx& c, cudaStream_t s, int mode, bool with_kick) {
+    if (mode == DM_VERLET) drift_nd<ND, DM_VERLET, MIXED>(c, s, with_kick);
+    else if (mode == DM_DAMPED) drift_nd<ND, DM_DAMPED, MIXED>(c, s, with_kick);
+    else drift_nd<ND, DM_SOL, MIXED>(c, s, with_kick);
+}
+
+void launch_drift(const DevCtx& c, cudaStream_t s, int mode, bool with_kick) {
     if (c.nd == 3) {
-        if (mode == DM_VERLET) k_drift<3, DM_VERLET><<<g, BLOCK, 0, s>>>(c);
-        else if (mode == DM_DAMPED) k_drift<3, DM_DAMPED><<<g, BLOCK, 0, s>>>(c);
-        else k_drift<3, DM_SOL><<<g, BLOCK, 0, s>>>(c);
+        if (c.prec == PREC_MIXED) drift_prec<3, true>(c, s, mode, with_kick);
+        else drift_prec<3, false>(c, s, mode, with_kick);
     } else {
-        if (mode == DM_VERLET) k_drift<2, DM_VERLET><<<g, BLOCK, 0, s>>>(c);
-        else if (mode == DM_DAMPED) k_drift<2, DM_DAMPED><<<g, BLOCK, 0, s>>>(c);
-        else k_drift<2, DM_SOL><<<g, BLOCK, 0, s>>>(c);
+        if (c.prec == PREC_MIXED) drift_prec<2, true>(c, s, mode, with_kick);
+        else drift_prec<2, false>(c, s, mode, with_kick);
+    }
+}
+
+template <int ND, bool MIXED>
+static void kick_prec(const DevCtx& c, cudaStream_t s, int mode) {
+    unsigned g = grid_for(c.n);
+    if (mode == DM_VERLET) k_kick<ND, DM_VERLET, MIXED><<<g, BLOCK, 0, s>>>(c);
+    else if (mode == DM_DAMPED) k_kick<ND, DM_DAMPED, MIXED><<<g, BLOCK, 0, s>>>(c);
+    else k_kick<ND, DM_SOL, MIXED><<<g, BLOCK, 0, s>>>(c);
+}
+
+void launch_kick(const DevCtx& c, cudaStream_t s, int mode) {
+    if (c.nd == 3) {
+        if (c.prec == PREC_MIXED) kick_prec<3, true>(c, s, mode);
+        else kick_prec<3, false>(c, s, mode);
+    } else {
+        if (c.prec == PREC_MIXED) kick_prec<2, true>(c, s, mode);
+        else kick_prec<2, false>(c, s, mode);
     }
 }
 

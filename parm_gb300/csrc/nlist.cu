@@ -117,48 +117,123 @@ __global__ void k_bin(DevCtx c) {
     c.cslot[i] = slot;
 }
 
-// exclusive scan of one system's cell counts (one CTA per system)
-__global__ void __launch_bounds__(1024) k_scan_cells(DevCtx c) {
-    uint32_t s = blockIdx.x;
-    if (!c.flag[s]) return;
-    const SysConst& S = c.sys[s];
-    const uint32_t b0 = c.bucket_off[s];
-    const uint32_t nb = S.ncell;  // member cells; the non-member bucket starts after them
-    const uint32_t T = blockDim.x;
-    const uint32_t per = (nb + T - 1) / T;
-    const uint32_t lo = threadIdx.x * per;
-    const uint32_t hi = min(lo + per, nb);
-    uint32_t local = 0;
-    for (uint32_t b = lo; b < hi; b++) local += c.cell_count[b0 + b];
-    // block exclusive scan of `local`
-    __shared__ uint32_t wsum[32];
-    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = local;
+// ---------------------------------------------------------------------------
+// Cell offsets: a segmented exclusive scan of the bucket counts over all
+// buckets, one segment per system (its first bucket starts a segment), in
+// three passes (block aggregates, scan of aggregates, final offsets).  Only
+// buckets of flagged systems are written; other systems' counts are stale but
+// never cross a segment boundary.
+// ---------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+struct SegPair {
+    uint32_t f;  // segment starts in this span
+    uint32_t v;  // sum since the last segment start
+};
+
+__device__ __forceinline__ SegPair seg_combine(SegPair a, SegPair b) {
+    return {a.f | b.f, b.f ? b.v : a.v + b.v};
+}
+
+// block-wide inclusive scan of one pair per thread; returns the exclusive
+// carry for this thread and the block aggregate
+__device__ __forceinline__ SegPair seg_block_scan(SegPair x, SegPair& aggregate) {
+    __shared__ SegPair wsum[SCAN_THREADS / 32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    SegPair inc = x;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-        uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-        if (lane >= (uint32_t)off) incl += o;
+        SegPair o;
+        o.f = __shfl_up_sync(0xFFFFFFFFu, inc.f, off);
+        o.v = __shfl_up_sync(0xFFFFFFFFu, inc.v, off);
+        if (lane >= (unsigned)off) inc = seg_combine(o, inc);
     }
-    if (lane == 31) wsum[warp] = incl;
+    if (lane == 31) wsum[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t nw = (T + 31) / 32;
-        uint32_t w = lane < nw ? wsum[lane] : 0u;
-        uint32_t wi = w;
+        SegPair w = lane < SCAN_THREADS / 32 ? wsum[lane] : SegPair{0u, 0u};
+        SegPair wi = w;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
-            if (lane >= (uint32_t)off) wi += o;
+            SegPair o;
+            o.f = __shfl_up_sync(0xFFFFFFFFu, wi.f, off);
+            o.v = __shfl_up_sync(0xFFFFFFFFu, wi.v, off);
+            if (lane >= (unsigned)off) wi = seg_combine(o, wi);
         }
-        wsum[lane] = wi - w;  // exclusive warp offsets
+        if (lane < SCAN_THREADS / 32) wsum[lane] = wi;   // inclusive over warps
     }
     __syncthreads();
-    uint32_t run = S.atom_off + wsum[warp] + (incl - local);
-    for (uint32_t b = lo; b < hi; b++) {
-        c.cell_start[b0 + b] = run;
-        run += c.cell_count[b0 + b];
+    aggregate = wsum[SCAN_THREADS / 32 - 1];
+    // exclusive carry = (inclusive of previous warps) + (inclusive of earlier lanes)
+    SegPair prev_w = warp > 0 ? wsum[warp - 1] : SegPair{0u, 0u};
+    SegPair prev_l;
+    prev_l.f = __shfl_up_sync(0xFFFFFFFFu, inc.f, 1);
+    prev_l.v = __shfl_up_sync(0xFFFFFFFFu, inc.v, 1);
+    if (lane == 0) prev_l = SegPair{0u, 0u};
+    SegPair carry = seg_combine(prev_w, prev_l);
+    __syncthreads();
+    return carry;
+}
+
+__device__ __forceinline__ SegPair bucket_item(const DevCtx& c, uint32_t b) {
+    if (b >= c.nbucket) return {0u, 0u};
+    const uint32_t s = c.bucket_sys[b];
+    return {b == c.bucket_off[s] ? 1u : 0u, c.cell_count[b]};
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_blocks(DevCtx c) {
+    const uint32_t base = blockIdx.x * SCAN_CHUNK + threadIdx.x * SCAN_ITEMS;
+    SegPair t{0u, 0u};
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) t = seg_combine(t, bucket_item(c, base + k));
+    SegPair agg;
+    seg_block_scan(t, agg);
+    if (threadIdx.x == 0) {
+        c.scan_aux[2 * blockIdx.x] = agg.f;
+        c.scan_aux[2 * blockIdx.x + 1] = agg.v;
     }
-    if (threadIdx.x == T - 1) c.cell_start[b0 + nb] = run;  // non-member bucket start
+}
+
+// exclusive segmented scan of the block aggregates (one CTA)
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_aux(DevCtx c, uint32_t nblk) {
+    SegPair run{0u, 0u};
+    for (uint32_t b0 = 0; b0 < nblk; b0 += SCAN_THREADS) {
+        const uint32_t b = b0 + threadIdx.x;
+        SegPair x = b < nblk ? SegPair{c.scan_aux[2 * b], c.scan_aux[2 * b + 1]} : SegPair{0u, 0u};
+        SegPair agg;
+        SegPair carry = seg_block_scan(x, agg);
+        SegPair excl = seg_combine(run, carry);
+        if (b < nblk) {
+            c.scan_aux[2 * b] = excl.f;
+            c.scan_aux[2 * b + 1] = excl.v;
+        }
+        run = seg_combine(run, agg);
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_write(DevCtx c) {
+    const uint32_t base = blockIdx.x * SCAN_CHUNK + threadIdx.x * SCAN_ITEMS;
+    SegPair items[SCAN_ITEMS];
+    SegPair t{0u, 0u};
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        items[k] = bucket_item(c, base + k);
+        t = seg_combine(t, items[k]);
+    }
+    SegPair agg;
+    SegPair carry = seg_block_scan(t, agg);
+    SegPair run = seg_combine(SegPair{c.scan_aux[2 * blockIdx.x], c.scan_aux[2 * blockIdx.x + 1]}, carry);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const uint32_t b = base + k;
+        if (b >= c.nbucket) break;
+        const uint32_t excl = items[k].f ? 0u : run.v;   // exclusive, restarted per system
+        run = seg_combine(run, items[k]);
+        const uint32_t s = c.bucket_sys[b];
+        if (c.flag[s]) c.cell_start[b] = c.sys[s].atom_off + excl;
+    }
 }
 
 __global__ void k_scatter(DevCtx c) {
@@ -170,6 +245,7 @@ __global__ void k_scatter(DevCtx c) {
 }
 
 // deterministic order inside a cell: ascending neighbour-list rank
+constexpr uint32_t CELLSORT_LOCAL = 48;
 __global__ void k_cellsort(DevCtx c) {
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= c.nbucket) return;
@@ -177,7 +253,26 @@ __global__ void k_cellsort(DevCtx c) {
     if (!c.flag[s]) return;
     uint32_t local = b - c.bucket_off[s];
     if (local >= c.sys[s].ncell) return;  // non-member bucket is placed by nm_rank
-    uint32_t lo = c.cell_start[b], hi = c.cell_start[b + 1];
+    const uint32_t lo = c.cell_start[b], hi = c.cell_start[b + 1];
+    const uint32_t cnt = hi - lo;
+    if (cnt < 2) return;
+    if (cnt <= CELLSORT_LOCAL) {
+        uint32_t key[CELLSORT_LOCAL], val[CELLSORT_LOCAL];
+        for (uint32_t k = 0; k < cnt; k++) {
+            const uint32_t v = c.perm[lo + k];
+            const uint32_t rk = c.rank[v];
+            uint32_t p = k;
+            while (p > 0 && key[p - 1] > rk) {
+                key[p] = key[p - 1];
+                val[p] = val[p - 1];
+                p--;
+            }
+            key[p] = rk;
+            val[p] = v;
+        }
+        for (uint32_t k = 0; k < cnt; k++) c.perm[lo + k] = val[k];
+        return;
+    }
     for (uint32_t k = lo + 1; k < hi; k++) {
         uint32_t v = c.perm[k];
         uint32_t key = c.rank[v];
@@ -247,8 +342,23 @@ __global__ void k_copyback(DevCtx c) {
     if constexpr (ND == 3) posq_split(xs[2], A.z, B.z); else { A.z = 0.f; B.z = 0.f; }
     A.w = (float)dk;
     B.w = 0.f;
-    c.posA[k] = A;
-    c.posB[k] = B;
+    c.pos[2 * (size_t)(k)] = A;
+    c.pos[2 * (size_t)(k) + 1] = B;
+    // position relative to the lower corner of its cell, for the list build
+    if (c.rank[k] != NOT_MEMBER) {
+        const SysConst& S = c.sys[s];
+        const uint32_t myb = c.bucket[k] - c.bucket_off[s];
+        const uint32_t ci[3] = {myb % (uint32_t)S.nc[0], (myb / (uint32_t)S.nc[0]) % (uint32_t)S.nc[1],
+                                myb / (uint32_t)(S.nc[0] * S.nc[1])};
+        float pr[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            double t = xs[d] * S.invL[d];
+            double fr = t - floor(t);
+            pr[d] = (float)(fr * S.L[d] - (double)ci[d] * S.cellw[d]);
+        }
+        c.posw[k] = make_float4(pr[0], pr[1], pr[2], (float)dk);
+    }
 }
 
 __device__ __forceinline__ bool is_excluded(const DevCtx& c, uint32_t oi, uint32_t oj) {
@@ -258,88 +368,299 @@ __device__ __forceinline__ bool is_excluded(const DevCtx& c, uint32_t oi, uint32
     return false;
 }
 
-// full neighbour list of every member atom of a flagged system
+// exact reference test: diff(x_i, x_j).norm() < (d_i + d_j)/2 + skin
 template <int ND>
-__global__ void k_build(DevCtx c) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
-    uint32_t s = c.atom_sys[i];
+__device__ __noinline__ bool keep_exact(const DevCtx& c, const SysConst& S, uint32_t i, uint32_t j) {
+    typename DVec<ND>::T xi = ldx<ND>(c.x, i), xj = ldx<ND>(c.x, j);
+    const double* a = reinterpret_cast<const double*>(&xi);
+    const double* bb = reinterpret_cast<const double*>(&xj);
+    double r[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < ND; d++) r[d] = remainder_exact(a[d] - bb[d], S.L[d], S.invL[d], S.halfL[d]);
+    double sq = r[0] * r[0] + r[1] * r[1];
+    if constexpr (ND == 3) sq = sq + r[2] * r[2];
+    double diam = (c.diam[i] + c.diam[j]) / 2;
+    return sqrt(sq) < (diam + S.skin);
+}
+
+// Full neighbour lists of a flagged system's member atoms (row-major:
+// nbr[i * maxnb + k]), one warp per cell with warp-ballot compaction.
+// The candidates of the 3^d stencil cells are numbered consecutively (stencil
+// order, then cell order); the warp takes 32 candidates at a time, one per
+// lane, and tests all of them against each home atom in turn.  The accepted
+// candidates of a home atom are appended in candidate order by a ballot and a
+// population count, so the lists are deterministic and written coalesced.
+// Positions are relative to each cell's lower corner: a candidate in the
+// stencil cell at offset (dx,dy,dz) is displaced by (dx,dy,dz) * cell width in
+// the periodic continuation of the grid (axes with a single cell take a
+// per-pair minimum image instead).  Distances are screened in FP32; candidates
+// within 2e-4 (relative) of the threshold get the exact FP64 reference test.
+constexpr int BUILD_WARPS = 4;
+template <int ND, bool WRAP>
+__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(DevCtx c) {
+    __shared__ float4 home[BUILD_WARPS][32];
+    __shared__ uint32_t pre[BUILD_WARPS][32];
+    __shared__ uint32_t jst[BUILD_WARPS][32];
+    __shared__ float4 soff[BUILD_WARPS][32];
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t b = blockIdx.x * BUILD_WARPS + wib;   // one warp per bucket
+    if (b >= c.nbucket) return;
+    const uint32_t s = c.bucket_sys[b];
     if (!c.flag[s]) return;
-    if (c.rank[i] == NOT_MEMBER) {
-        c.nnb[i] = 0u;
-        return;
-    }
     const SysConst& S = c.sys[s];
     const uint32_t b0 = c.bucket_off[s];
-    const uint32_t myb = c.bucket[i] - b0;
-    int ci[3];
-    ci[0] = (int)(myb % (uint32_t)S.nc[0]);
-    ci[1] = (int)((myb / (uint32_t)S.nc[0]) % (uint32_t)S.nc[1]);
-    ci[2] = (int)(myb / (uint32_t)(S.nc[0] * S.nc[1]));
-    const float4 Ai = c.posA[i], Bi = c.posB[i];
-    const double di = c.diam[i];
-    const float di32 = Ai.w;
-    const float skin32 = (float)S.skin;
-    const uint32_t oi = c.orig[i];
-    const int r0 = S.nc[0] >= 3 ? 1 : 0, r1 = S.nc[1] >= 3 ? 1 : 0;
-    const int r2 = (ND == 3 && S.nc[2] >= 3) ? 1 : 0;
-    uint32_t cnt = 0;
-    for (int dz = -r2; dz <= r2; dz++) {
-        int cz = ci[2] + dz;
-        cz = cz < 0 ? cz + S.nc[2] : (cz >= S.nc[2] ? cz - S.nc[2] : cz);
-        for (int dy = -r1; dy <= r1; dy++) {
-            int cy = ci[1] + dy;
-            cy = cy < 0 ? cy + S.nc[1] : (cy >= S.nc[1] ? cy - S.nc[1] : cy);
-            for (int dx = -r0; dx <= r0; dx++) {
-                int cx = ci[0] + dx;
-                cx = cx < 0 ? cx + S.nc[0] : (cx >= S.nc[0] ? cx - S.nc[0] : cx);
-                uint32_t cb = b0 + (uint32_t)((cz * S.nc[1] + cy) * S.nc[0] + cx);
-                uint32_t js = c.cell_start[cb], je = c.cell_start[cb + 1];
-                for (uint32_t j = js; j < je; j++) {
-                    if (j == i) continue;
-                    const float4 Aj = c.posA[j], Bj = c.posB[j];
-                    float ddx = disp32(Ai.x, Aj.x, Bi.x, Bj.x, S.Lhi[0], S.Llo[0], S.invLf[0]);
-                    float ddy = disp32(Ai.y, Aj.y, Bi.y, Bj.y, S.Lhi[1], S.Llo[1], S.invLf[1]);
-                    float d2 = ddx * ddx + ddy * ddy;
-                    if constexpr (ND == 3) {
-                        float ddz = disp32(Ai.z, Aj.z, Bi.z, Bj.z, S.Lhi[2], S.Llo[2], S.invLf[2]);
-                        d2 += ddz * ddz;
-                    }
-                    float thr = 0.5f * (di32 + Aj.w) + skin32;
-                    float t2 = thr * thr;
-                    bool keep;
-                    if (d2 < t2 * 0.9998f) {
-                        keep = true;
-                    } else if (d2 > t2 * 1.0002f) {
-                        keep = false;
-                    } else {
-                        // exact reference test: diff(x_i, x_j).norm() < (d_i + d_j)/2 + skin
-                        typename DVec<ND>::T xi = ldx<ND>(c.x, i), xj = ldx<ND>(c.x, j);
-                        const double* a = reinterpret_cast<const double*>(&xi);
-                        const double* bb = reinterpret_cast<const double*>(&xj);
-                        double r[3] = {0.0, 0.0, 0.0};
+    const uint32_t myb = b - b0;
+    if (myb >= S.ncell) {
+        // non-member bucket: these atoms have no neighbours
+        for (uint32_t i = c.cell_start[b] + lane; i < S.atom_off + S.natoms; i += 32) c.nnb[i] = 0u;
+        return;
+    }
+    const uint32_t cs = c.cell_start[b], ce = c.cell_start[b + 1];
+    if (cs == ce) return;
+    const int nc0 = S.nc[0], nc1 = S.nc[1], nc2 = S.nc[2];
+    const int ci0 = (int)(myb % (uint32_t)nc0);
+    const int ci1 = (int)((myb / (uint32_t)nc0) % (uint32_t)nc1);
+    const int ci2 = (int)(myb / (uint32_t)(nc0 * nc1));
+    const int r0 = nc0 >= 3 ? 1 : 0, r1 = nc1 >= 3 ? 1 : 0;
+    const int r2 = (ND == 3 && nc2 >= 3) ? 1 : 0;
+    const int w0 = 2 * r0 + 1, w1 = 2 * r1 + 1, w2 = 2 * r2 + 1;
+    const uint32_t nst = (uint32_t)(w0 * w1 * w2);
+    // stencil table: lane t describes stencil cell t
+    uint32_t cntl = 0;
+    if (lane < nst) {
+        const int dx = (int)(lane % (uint32_t)w0) - r0;
+        const int dy = (int)((lane / (uint32_t)w0) % (uint32_t)w1) - r1;
+        const int dz = (int)(lane / (uint32_t)(w0 * w1)) - r2;
+        int cx = ci0 + dx, cy = ci1 + dy, cz = ci2 + dz;
+        cx = cx < 0 ? cx + nc0 : (cx >= nc0 ? cx - nc0 : cx);
+        cy = cy < 0 ? cy + nc1 : (cy >= nc1 ? cy - nc1 : cy);
+        cz = cz < 0 ? cz + nc2 : (cz >= nc2 ? cz - nc2 : cz);
+        const uint32_t cb = b0 + (uint32_t)((cz * nc1 + cy) * nc0 + cx);
+        const uint32_t js = c.cell_start[cb];
+        cntl = c.cell_start[cb + 1] - js;
+        jst[wib][lane] = js;
+        soff[wib][lane] = make_float4((float)dx * S.cellw32[0], (float)dy * S.cellw32[1],
+                                      (float)dz * S.cellw32[2], 0.f);
+    }
+    uint32_t incl = cntl;
 #pragma unroll
-                        for (int d = 0; d < ND; d++)
-                            r[d] = remainder_exact(a[d] - bb[d], S.L[d], S.invL[d], S.halfL[d]);
-                        double sq = r[0] * r[0] + r[1] * r[1];
-                        if constexpr (ND == 3) sq = sq + r[2] * r[2];
-                        double diam = (di + c.diam[j]) / 2;
-                        keep = sqrt(sq) < (diam + S.skin);
-                    }
-                    if (keep && is_excluded(c, oi, c.orig[j])) keep = false;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    pre[wib][lane] = incl - cntl;
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    __syncwarp();
+
+    // per-pair minimum image only along axes with a single cell (WRAP kernels)
+    const bool wrap0 = WRAP && r0 == 0, wrap1 = WRAP && r1 == 0, wrap2 = WRAP && (ND == 3) && r2 == 0;
+    const float kShift = 12582912.0f;
+    const float skin32 = (float)S.skin;
+    const bool uni_thr = (c.uniform & UNI_SIG) && (c.uniform & UNI_THIRD);
+    const uint32_t maxnb = c.maxnb;
+    for (uint32_t hb = cs; hb < ce; hb += 32) {
+        const uint32_t mh = min(32u, ce - hb);
+        if (lane < mh) home[wib][lane] = c.posw[hb + lane];
+        uint32_t mycnt = 0;   // neighbours found so far for home atom hb + lane
+        __syncwarp();
+        const float4 H0 = home[wib][0];
+        const float t2u = (H0.w + skin32) * (H0.w + skin32);
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t q = base + lane;
+            const bool valid = q < total;
+            uint32_t j = 0xFFFFFFFFu;
+            float4 Q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                uint32_t st = 0;
+#pragma unroll 1
+                for (uint32_t k = 1; k < nst; k++)
+                    if (pre[wib][k] <= q) st = k;
+                j = jst[wib][st] + (q - pre[wib][st]);
+                const float4 R = c.posw[j];
+                const float4 O = soff[wib][st];
+                Q = make_float4(R.x + O.x, R.y + O.y, R.z + O.z, R.w);
+            }
+            for (uint32_t h = 0; h < mh; h++) {
+                const float4 P = home[wib][h];
+                float d0 = P.x - Q.x, d1 = P.y - Q.y, d2c = 0.f;
+                if (wrap0) d0 = __fmaf_rn(-__fsub_rn(__fmaf_rn(d0, S.invLf[0], kShift), kShift), S.Lhi[0], d0);
+                if (wrap1) d1 = __fmaf_rn(-__fsub_rn(__fmaf_rn(d1, S.invLf[1], kShift), kShift), S.Lhi[1], d1);
+                if constexpr (ND == 3) {
+                    d2c = P.z - Q.z;
+                    if (wrap2) d2c = __fmaf_rn(-__fsub_rn(__fmaf_rn(d2c, S.invLf[2], kShift), kShift), S.Lhi[2], d2c);
+                }
+                const float rr = d0 * d0 + d1 * d1 + d2c * d2c;
+                float t2 = t2u;
+                if (!uni_thr) {
+                    const float thr = 0.5f * (P.w + Q.w) + skin32;
+                    t2 = thr * thr;
+                }
+                const uint32_t i = hb + h;
+                bool keep = valid && rr < t2 * 0.9998f && j != i;
+                const bool band = valid && !keep && rr <= t2 * 1.0002f && j != i;
+                if (__any_sync(0xFFFFFFFFu, band)) {   // rare: exact reference test
+                    if (band) keep = keep_exact<ND>(c, S, i, j);
+                }
+                if (c.excl_off) {
+                    if (keep && is_excluded(c, c.orig[i], c.orig[j])) keep = false;
+                }
+                const uint32_t mask = __ballot_sync(0xFFFFFFFFu, keep);
+                if (mask) {
+                    const uint32_t ch = __shfl_sync(0xFFFFFFFFu, mycnt, h);
                     if (keep) {
-                        if (cnt < c.maxnb) c.nbr[(size_t)cnt * c.nalloc + i] = j;
-                        cnt++;
+                        const uint32_t pos = ch + __popc(mask & ((1u << lane) - 1u));
+                        if (pos < maxnb) c.nbr[(size_t)i * maxnb + pos] = j;
                     }
+                    if (lane == h) mycnt += __popc(mask);
                 }
             }
         }
+        if (lane < mh) {
+            if (mycnt > maxnb) {
+                atomicOr(c.status, ST_NBR_OVERFLOW);
+                mycnt = maxnb;
+            }
+            c.nnb[hb + lane] = mycnt;
+        }
+        __syncwarp();
     }
-    if (cnt > c.maxnb) {
-        atomicOr(c.status, ST_NBR_OVERFLOW);
-        cnt = c.maxnb;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory tiles for the mixed-precision pair kernel (built after the
+// lists).  A tile is TILE_ATOMS consecutive atoms of one system.  Its frame
+// origin is the coarse position A0 of its first atom; atom i sits in the frame
+// at X_i - m_i L (m_i rounds (X_i - A0)/L), and its neighbour j, whose pair
+// image is n_ij = round((X_i - X_j)/L), at X_j + (n_ij - m_i) L.  The tile's
+// entries are its distinct (j, n_ij - m_i) pairs (deduplicated through a
+// shared-memory hash table) and the tile lists hold 16-bit entry numbers.
+// Images are stored as 8-bit signed numbers per axis.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t img_code(int a, int b, int c) {
+    return (uint32_t)(a + 128) | ((uint32_t)(b + 128) << 8) | ((uint32_t)(c + 128) << 16);
+}
+
+__device__ __forceinline__ float round_ratio(float num, float inv) {
+    const float kShift = 12582912.0f;
+    return __fsub_rn(__fmaf_rn(num, inv, kShift), kShift);
+}
+
+__device__ __forceinline__ uint32_t hash_slot(unsigned long long key) {
+    return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 52) & (TILE_HASH - 1);
+}
+
+constexpr unsigned long long HASH_EMPTY = ~0ull;
+
+template <int ND>
+__global__ void __launch_bounds__(TILE_ATOMS) k_tile(DevCtx c, int all) {
+    __shared__ unsigned long long hkey[TILE_HASH];
+    __shared__ uint16_t hidx[TILE_HASH];
+    __shared__ uint32_t wsum[TILE_ATOMS / 32];
+    const uint32_t t = blockIdx.x;
+    if (t >= c.ntile) return;
+    const uint32_t s = c.tile_sys[t];
+    if (!all && !c.flag[s]) return;
+    const SysConst& S = c.sys[s];
+    const uint32_t a0 = c.tile_atom0[t], na = c.tile_natom[t];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t q = tid; q < TILE_HASH; q += blockDim.x) hkey[q] = HASH_EMPTY;
+    const float4 A0 = c.pos[2 * (size_t)a0];
+    __syncthreads();
+    const uint32_t i = a0 + tid;
+    const bool act = tid < na && c.rank[i] != NOT_MEMBER;
+    int m[3] = {0, 0, 0};
+    uint32_t nn = 0;
+    bool bad = false;
+    float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) {
+        Ai = c.pos[2 * (size_t)i];
+        m[0] = (int)round_ratio(Ai.x - A0.x, S.invLf[0]);
+        m[1] = (int)round_ratio(Ai.y - A0.y, S.invLf[1]);
+        if (ND == 3) m[2] = (int)round_ratio(Ai.z - A0.z, S.invLf[2]);
+        nn = c.nnb[i];
+        for (uint32_t k = 0; k < nn; k++) {
+            const uint32_t j = c.nbr[(size_t)i * c.maxnb + k];
+            const float4 Aj = c.pos[2 * (size_t)j];
+            int im[3] = {0, 0, 0};
+            im[0] = (int)round_ratio(Ai.x - Aj.x, S.invLf[0]) - m[0];
+            im[1] = (int)round_ratio(Ai.y - Aj.y, S.invLf[1]) - m[1];
+            if (ND == 3) im[2] = (int)round_ratio(Ai.z - Aj.z, S.invLf[2]) - m[2];
+            if (im[0] < -127 || im[0] > 127 || im[1] < -127 || im[1] > 127 || im[2] < -127 || im[2] > 127)
+                bad = true;
+            const unsigned long long key = ((unsigned long long)j << 24) | img_code(im[0], im[1], im[2]);
+            uint32_t slot = hash_slot(key);
+            bool placed = false;
+            for (uint32_t p = 0; p < TILE_HASH; p++) {   // bounded linear probing
+                const unsigned long long old = atomicCAS(&hkey[slot], HASH_EMPTY, key);
+                if (old == HASH_EMPTY || old == key) {
+                    placed = true;
+                    break;
+                }
+                slot = (slot + 1) & (TILE_HASH - 1);
+            }
+            if (!placed) bad = true;
+        }
+        if (m[0] < -127 || m[0] > 127 || m[1] < -127 || m[1] > 127 || m[2] < -127 || m[2] > 127) bad = true;
+        c.atom_img[i] = img_code(m[0], m[1], m[2]);
     }
-    c.nnb[i] = cnt;
+    if (bad) atomicOr(c.status, ST_IMAGE_RANGE | ST_TILE_OVERFLOW);
+    __syncthreads();
+    // compact the occupied slots into entry numbers (block exclusive scan)
+    constexpr uint32_t PER = TILE_HASH / TILE_ATOMS;
+    uint32_t cnt = 0;
+    for (uint32_t q = 0; q < PER; q++) cnt += hkey[tid * PER + q] != HASH_EMPTY;
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t base = incl - cnt;
+    for (uint32_t w = 0; w < warp; w++) base += wsum[w];
+    uint32_t total = 0;
+    for (uint32_t w = 0; w < TILE_ATOMS / 32; w++) total += wsum[w];
+    for (uint32_t q = 0; q < PER; q++) {
+        const uint32_t slot = tid * PER + q;
+        const unsigned long long key = hkey[slot];
+        if (key == HASH_EMPTY) continue;
+        if (base < TILE_ECAP) c.tile_ent[(size_t)t * TILE_ECAP + base] = key;
+        hidx[slot] = (uint16_t)min(base, (uint32_t)TILE_ECAP - 1u);
+        base++;
+    }
+    if (tid == 0) {
+        c.tile_ne[t] = min(total, (uint32_t)TILE_ECAP);
+        c.tile_anchor[t] = A0;
+        if (total > TILE_ECAP) atomicOr(c.status, ST_TILE_OVERFLOW);
+    }
+    __syncthreads();
+    // tile lists: entry number of every (atom, neighbour)
+    if (act) {
+        uint16_t* lst = c.tile_lst + (size_t)t * c.maxnb * TILE_ATOMS + tid;
+        for (uint32_t k = 0; k < nn; k++) {
+            const uint32_t j = c.nbr[(size_t)i * c.maxnb + k];
+            const float4 Aj = c.pos[2 * (size_t)j];
+            int im[3] = {0, 0, 0};
+            im[0] = (int)round_ratio(Ai.x - Aj.x, S.invLf[0]) - m[0];
+            im[1] = (int)round_ratio(Ai.y - Aj.y, S.invLf[1]) - m[1];
+            if (ND == 3) im[2] = (int)round_ratio(Ai.z - Aj.z, S.invLf[2]) - m[2];
+            const unsigned long long key = ((unsigned long long)j << 24) | img_code(im[0], im[1], im[2]);
+            uint32_t slot = hash_slot(key);
+            uint16_t e = 0;
+            for (uint32_t p = 0; p < TILE_HASH; p++) {
+                const unsigned long long kk = hkey[slot];
+                if (kk == key) {
+                    e = hidx[slot];
+                    break;
+                }
+                if (kk == HASH_EMPTY) break;
+                slot = (slot + 1) & (TILE_HASH - 1);
+            }
+            lst[(size_t)k * TILE_ATOMS] = e;
+        }
+    }
 }
 
 // FP64 path: order each list by neighbour-list rank, which reproduces the
@@ -361,7 +682,7 @@ __global__ void k_sort_lists(DevCtx c) {
     }
     uint32_t m = cnt;
     for (uint32_t k = 0; k < m; k++) {
-        uint32_t j = c.nbr[(size_t)k * c.nalloc + i];
+        uint32_t j = c.nbr[(size_t)i * c.maxnb + k];
         uint32_t rk = c.rank[j];
         uint32_t p = k;
         while (p > 0 && key[p - 1] > rk) {
@@ -372,7 +693,7 @@ __global__ void k_sort_lists(DevCtx c) {
         key[p] = rk;
         val[p] = j;
     }
-    for (uint32_t k = 0; k < m; k++) c.nbr[(size_t)k * c.nalloc + i] = val[k];
+    for (uint32_t k = 0; k < m; k++) c.nbr[(size_t)i * c.maxnb + k] = val[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -403,7 +724,7 @@ __global__ void k_count_half(DevCtx c) {
     if (ri != NOT_MEMBER) {
         uint32_t nn = c.nnb[i];
         for (uint32_t k = 0; k < nn; k++)
-            if (c.rank[c.nbr[(size_t)k * c.nalloc + i]] < ri) cnt++;
+            if (c.rank[c.nbr[(size_t)i * c.maxnb + k]] < ri) cnt++;
     }
     c.red[i] = (double)cnt;
 }
@@ -421,11 +742,13 @@ __global__ void k_posq(DevCtx c) {
     if constexpr (ND == 3) posq_split(xs[2], A.z, B.z); else { A.z = 0.f; B.z = 0.f; }
     A.w = (float)c.diam[k];
     B.w = 0.f;
-    c.posA[k] = A;
-    c.posB[k] = B;
+    c.pos[2 * (size_t)(k)] = A;
+    c.pos[2 * (size_t)(k) + 1] = B;
 }
 
 // ---------------------------------------------------------------------------
+void launch_tiles(const DevCtx& c, cudaStream_t s, int all);
+
 void launch_arm(const DevCtx& c, cudaStream_t s, int count_step, int use_cond,
                 unsigned long long handle) {
     k_arm<<<1, 1024, 0, s>>>(c, count_step, use_cond, (cudaGraphConditionalHandle)handle);
@@ -435,19 +758,33 @@ void launch_rebuild(const DevCtx& c, cudaStream_t s) {
     unsigned ga = grid_for(c.n);
     k_zero_cells<<<c.nsys, 256, 0, s>>>(c);
     if (c.nd == 3) k_bin<3><<<ga, BLOCK, 0, s>>>(c); else k_bin<2><<<ga, BLOCK, 0, s>>>(c);
-    k_scan_cells<<<c.nsys, 1024, 0, s>>>(c);
+    const uint32_t nblk = (c.nbucket + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    k_scan_blocks<<<nblk, SCAN_THREADS, 0, s>>>(c);
+    k_scan_aux<<<1, SCAN_THREADS, 0, s>>>(c, nblk);
+    k_scan_write<<<nblk, SCAN_THREADS, 0, s>>>(c);
     k_scatter<<<ga, BLOCK, 0, s>>>(c);
     k_cellsort<<<grid_for(c.nbucket), BLOCK, 0, s>>>(c);
     if (c.nd == 3) {
         k_gather<3><<<ga, BLOCK, 0, s>>>(c);
         k_copyback<3><<<ga, BLOCK, 0, s>>>(c);
-        k_build<3><<<ga, BLOCK, 0, s>>>(c);
+        if (c.any_wrap) k_build<3, true><<<(c.nbucket + BUILD_WARPS - 1) / BUILD_WARPS, BUILD_WARPS * 32, 0, s>>>(c);
+        else k_build<3, false><<<(c.nbucket + BUILD_WARPS - 1) / BUILD_WARPS, BUILD_WARPS * 32, 0, s>>>(c);
     } else {
         k_gather<2><<<ga, BLOCK, 0, s>>>(c);
         k_copyback<2><<<ga, BLOCK, 0, s>>>(c);
-        k_build<2><<<ga, BLOCK, 0, s>>>(c);
+        if (c.any_wrap) k_build<2, true><<<(c.nbucket + BUILD_WARPS - 1) / BUILD_WARPS, BUILD_WARPS * 32, 0, s>>>(c);
+        else k_build<2, false><<<(c.nbucket + BUILD_WARPS - 1) / BUILD_WARPS, BUILD_WARPS * 32, 0, s>>>(c);
     }
-    if (c.prec == PREC_FP64) k_sort_lists<<<grid_for(c.n, 128), 128, 0, s>>>(c);
+    if (c.prec == PREC_FP64) {
+        k_sort_lists<<<grid_for(c.n, 128), 128, 0, s>>>(c);
+    } else if (c.ntile && c.tiled) {
+        launch_tiles(c, s, 0);
+    }
+}
+
+void launch_tiles(const DevCtx& c, cudaStream_t s, int all) {
+    if (c.nd == 3) k_tile<3><<<c.ntile, TILE_ATOMS, 0, s>>>(c, all);
+    else k_tile<2><<<c.ntile, TILE_ATOMS, 0, s>>>(c, all);
 }
 
 void launch_check(const DevCtx& c, cudaStream_t s) {

@@ -159,13 +159,15 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
         const SysConst& S = c.sys[s];
         double xi[3] = {0, 0, 0};
         load3<ND>(c.x, i, xi);
-        const float4 Ai = c.posA[i], Bi = c.posB[i];
+        const float4 Ai = c.pos[2 * (size_t)(i)], Bi = c.pos[2 * (size_t)(i) + 1];
         const AtomPrm Pi = c.prm[i];
         const float4 Qi = c.prm32[i];
         const uint32_t nn = c.nnb[i];
+        const uint32_t* nb = c.nbr + (size_t)i * c.maxnb;
         for (uint32_t k = 0; k < nn; k++) {
-            const uint32_t j = c.nbr[(size_t)k * c.nalloc + i];
-            const float4 Aj = c.posA[j], Bj = c.posB[j];
+            const uint32_t j = __ldg(nb + k);
+            float4 Aj, Bj;
+            ld_pos(c.pos, j, Aj, Bj);
             float4 Qj = Qi;
             if ((uni & (UNI_SIG | UNI_THIRD)) != (UNI_SIG | UNI_THIRD)) Qj = c.prm32[j];
             if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi.y, Qj.y, Qi.z, Qj.z, uni)) continue;
@@ -186,50 +188,17 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
         }
     }
     if (active) {
-        const StepParams& P = *c.params;
         store3<ND>(c.f, i, f);
-        if constexpr (MODE != FM_FORCES) {
+        if constexpr (MODE == FM_FORCES_A) {
+            // Collection::set_forces(true): a = f/m, zero for m <= 0 or inf
             const double m = c.m[i];
             double a[3] = {0, 0, 0};
-            if constexpr (MODE == FM_FORCES_A || MODE == FM_DAMPED || MODE == FM_VERLET) {
-                if (mobile64(m)) {
+            if (mobile64(m)) {
 #pragma unroll
-                    for (int d = 0; d < ND; d++) a[d] = f[d] / m;
-                }
-                store3<ND>(c.a, i, a);
-                if constexpr (MODE != FM_FORCES_A) {
-                    if (mobile64(m)) {
-                        double v[3] = {0, 0, 0};
-                        load3<ND>(c.v, i, v);
-                        const double h = (MODE == FM_VERLET) ? P.dt_half : P.dtc2;
-#pragma unroll
-                        for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * h;
-                        store3<ND>(c.v, i, v);
-                    }
-                }
-            } else {  // FM_SOL: immobile test is m == 0 or inf here (collection.cpp:300-318)
-                double v[3] = {0, 0, 0};
-                if (!(m == 0.0 || isinf(m))) {
-#pragma unroll
-                    for (int d = 0; d < ND; d++) a[d] = f[d] / m;
-                    load3<ND>(c.v, i, v);
-#pragma unroll
-                    for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * P.dtc2;
-                }
-                store3<ND>(c.a, i, a);
-                store3<ND>(c.v, i, v);
+                for (int d = 0; d < ND; d++) a[d] = f[d] / m;
             }
+            store3<ND>(c.a, i, a);
         }
-    }
-    if constexpr (MODE == FM_VERLET || MODE == FM_DAMPED || MODE == FM_SOL) {
-        double dsq = 0.0;
-        bool valid = false;
-        if (member) {
-            dsq = disp_sq<ND>(static_cast<const typename DVec<ND>::T*>(c.x)[i],
-                              static_cast<const typename DVec<ND>::T*>(c.lastloc)[i]);
-            valid = !(dsq != dsq);
-        }
-        check_accumulate(c, s, valid, dsq);
     }
 }
 
@@ -251,7 +220,7 @@ __global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
         const AtomPrm Pi = c.prm[i];
         const uint32_t nn = c.nnb[i];
         for (uint32_t k = 0; k < nn; k++) {
-            const uint32_t j = c.nbr[(size_t)k * c.nalloc + i];
+            const uint32_t j = c.nbr[(size_t)i * c.maxnb + k];
             if (c.rank[j] > ri) continue;
             double xj[3] = {0, 0, 0};
             load3<ND>(c.x, j, xj);
@@ -292,13 +261,8 @@ __global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
 template <int ND, int KIND>
 static void force64_nd_kind(const DevCtx& c, cudaStream_t s, int mode) {
     unsigned g = grid_for(c.n);
-    switch (mode) {
-        case FM_FORCES: k_force64<ND, KIND, FM_FORCES><<<g, BLOCK, 0, s>>>(c); break;
-        case FM_FORCES_A: k_force64<ND, KIND, FM_FORCES_A><<<g, BLOCK, 0, s>>>(c); break;
-        case FM_VERLET: k_force64<ND, KIND, FM_VERLET><<<g, BLOCK, 0, s>>>(c); break;
-        case FM_DAMPED: k_force64<ND, KIND, FM_DAMPED><<<g, BLOCK, 0, s>>>(c); break;
-        default: k_force64<ND, KIND, FM_SOL><<<g, BLOCK, 0, s>>>(c); break;
-    }
+    if (mode == FM_FORCES_A) k_force64<ND, KIND, FM_FORCES_A><<<g, BLOCK, 0, s>>>(c);
+    else k_force64<ND, KIND, FM_FORCES><<<g, BLOCK, 0, s>>>(c);
 }
 
 template <int ND>

@@ -40,7 +40,6 @@ __device__ __forceinline__ void check_accumulate(const DevCtx& c, uint32_t sys_i
                                                  double dsq) {
     __shared__ unsigned long long s1[BLOCK / 32], s2[BLOCK / 32];
     __shared__ uint32_t ssys[BLOCK / 32];
-    __shared__ int suniform;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     unsigned long long v1 = (valid && dsq > 0.0) ? (unsigned long long)__double_as_longlong(dsq) : 0ull;
     unsigned long long v2 = 0ull;
@@ -50,7 +49,6 @@ __device__ __forceinline__ void check_accumulate(const DevCtx& c, uint32_t sys_i
     uint32_t wsys = 0xFFFFFFFFu;
     if (vmask) wsys = __shfl_sync(0xFFFFFFFFu, sid, __ffs(vmask) - 1);
     bool same = __all_sync(0xFFFFFFFFu, !valid || sid == wsys);
-    if (threadIdx.x == 0) suniform = 1;
     __syncthreads();
     if (same) {
 #pragma unroll

@@ -8,11 +8,8 @@ namespace parm {
 // integrator / evaluation modes of the pair-force kernels (the epilogue that
 // runs once an atom's force is complete)
 enum ForceMode : int {
-    FM_FORCES = 0,     // Collection::set_forces(false): write f
+    FM_FORCES = 0,     // Collection::set_forces(false) and time steps: write f
     FM_FORCES_A = 1,   // Collection::set_forces(true):  write f, a = f/m
-    FM_VERLET = 2,     // CollectionVerlet second half: a = f/m; v += a*(dt/2); check
-    FM_DAMPED = 3,     // CollectionDamped second half: a = f/m; v += a*(dt*c2); check
-    FM_SOL = 4,        // CollectionSol second half:    a = f/m; v += a*(dt*c2); check
 };
 
 enum DriftMode : int { DM_VERLET = 0, DM_DAMPED = 1, DM_SOL = 2 };
@@ -42,10 +39,13 @@ struct DevCtx {
     int kind;
     uint32_t nsys;
     uint32_t n;        // total atoms
-    uint32_t nalloc;   // column stride of the neighbour list (>= n)
+    uint32_t tpa;      // threads per atom of the mixed-precision pair kernel (1..32)
+    uint32_t unr;      // neighbours per thread and iteration in that kernel (1, 2, 4)
+    uint32_t tiled;    // use the shared-memory tiled variant (lists via tiles)
     uint32_t maxnb;    // neighbour capacity per atom
     uint32_t uniform;  // UniformFlags
     uint32_t nbucket;  // total buckets (sum over systems of ncell + 1)
+    uint32_t any_wrap; // some system has an axis with a single cell (per-pair minimum image)
 
     const SysConst* sys;
     const uint32_t* bucket_off;   // per system: first bucket (cells, then the non-member bucket)
@@ -67,13 +67,17 @@ struct DevCtx {
     uint32_t* slot;       // inverse of orig
     uint32_t* atom_sys;   // system of each internal slot (constant)
     uint32_t* nm_rank;    // by orig: rank among the system's non-members
-    float4* posA;         // coarse X (xyz) , w unused
-    float4* posB;         // fine xf (xyz), w unused
+    float4* pos;          // FP32 position view, interleaved per atom:
+                          //   pos[2i]   = (coarse X xyz, FP32 list diameter)
+                          //   pos[2i+1] = (fine xf xyz, 0)
     uint32_t* bucket;     // current bucket of each internal slot
+    float4* posw;         // rebuild only: position relative to its cell's lower corner (FP32), w = list diameter
 
     // rebuild scratch
     uint32_t* cell_count;
-    uint32_t* cell_start;
+    uint32_t* cell_start;   // start of every bucket; the bucket after a system's cells holds its non-members
+    const uint32_t* bucket_sys;  // system of each bucket
+    uint32_t* scan_aux;     // per scan block: (segment flag, sum)
     uint32_t* cslot;
     uint32_t* perm;       // new slot -> old slot
     // gather targets for the permutation
@@ -85,6 +89,19 @@ struct DevCtx {
     // neighbour list
     uint32_t* nbr;
     uint32_t* nnb;
+
+    // shared-memory tiles of the mixed-precision pair kernel: TILE_ATOMS
+    // consecutive atoms of one system; entries are the tile's distinct
+    // (neighbour, periodic image) pairs, the tile lists index them (16 bit)
+    uint32_t ntile;
+    const uint32_t* tile_atom0;   // first atom of each tile
+    const uint32_t* tile_natom;   // atoms in each tile (<= TILE_ATOMS)
+    const uint32_t* tile_sys;     // system of each tile
+    float4* tile_anchor;          // frame origin (a coarse position, multiple of 1/8)
+    uint32_t* tile_ne;            // entries per tile
+    unsigned long long* tile_ent; // [t * TILE_ECAP + e]: (neighbour << 12) | image code
+    uint16_t* tile_lst;           // [t * maxnb * TILE_ATOMS + k * TILE_ATOMS + a]
+    uint32_t* atom_img;           // image of each atom in its tile's frame (4-bit signed per axis)
 
     // exclusions (NeighborList::ignore), CSR keyed by caller index
     const uint32_t* excl_off;   // n + 1 entries, or null when no exclusions
@@ -112,10 +129,12 @@ void launch_arm(const DevCtx& c, cudaStream_t s, int count_step, int use_cond,
                 unsigned long long handle);
 void launch_rebuild(const DevCtx& c, cudaStream_t s);
 void launch_check(const DevCtx& c, cudaStream_t s);
+void launch_tiles(const DevCtx& c, cudaStream_t s, int all);   // tiles of every system when all != 0
 void launch_numpairs(const DevCtx& c, cudaStream_t s);   // -> sysout[s] (as double)
 void launch_posq(const DevCtx& c, cudaStream_t s);
 // integrate.cu
-void launch_drift(const DevCtx& c, cudaStream_t s, int mode);
+void launch_drift(const DevCtx& c, cudaStream_t s, int mode, bool with_kick);
+void launch_kick(const DevCtx& c, cudaStream_t s, int mode);
 void launch_scatter_in(const DevCtx& c, cudaStream_t s, const double* staging, uint64_t stride,
                        uint32_t fields);
 void launch_gather_out(const DevCtx& c, cudaStream_t s, double* staging, uint64_t stride,
@@ -148,6 +167,9 @@ enum AtomWhat : int {
 };
 
 constexpr int BLOCK = 256;
+constexpr int TILE_ATOMS = 64;
+constexpr int TILE_ECAP = 1024;
+constexpr int TILE_HASH = 4096;
 
 inline unsigned grid_for(uint32_t n, int block = BLOCK) {
     unsigned g = (unsigned)((n + block - 1) / block);

@@ -14,8 +14,8 @@
 //   * `posq` is the FP32 view of the positions used by the mixed-precision
 //     pair kernel and by the FP32 pre-filters of the FP64 path: a coarse part
 //     X = trunc(x * 8) / 8 (exact in FP32) and a fine part xf = x - X.
-//   * the neighbour list is a full list stored column-major:
-//     nbr[k * nalloc + i] is the k-th neighbour of internal atom i.
+//   * the neighbour list is a full list stored row-major:
+//     nbr[i * maxnb + k] is the k-th neighbour of internal atom i.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -31,6 +31,8 @@ enum StatusBits : uint32_t {
     ST_NONFINITE = 1u << 1,      // a non-finite position was binned
     ST_CELL_RANGE = 1u << 2,     // a cell index fell outside its system's grid (bug guard)
     ST_SORT_CAP = 1u << 3,       // FP64 path: a neighbour list longer than the in-thread sort buffer
+    ST_TILE_OVERFLOW = 1u << 4,  // a tile had more distinct neighbours than its capacity
+    ST_IMAGE_RANGE = 1u << 5,    // an atom is more than 7 box lengths from its tile frame
 };
 
 constexpr uint32_t NOT_MEMBER = 0xFFFFFFFFu;
@@ -44,6 +46,8 @@ struct SysConst {
     double rlist_max;   // largest (d_i + d_j)/2 + skin
     int nc[3];          // cells per axis (1 or >= 3)
     float cellw_inv[3]; // nc / L
+    double cellw[3];    // L / nc
+    float cellw32[3];   // L / nc in FP32
     uint32_t cell_off;  // first cell of this system in the global cell array
     uint32_t ncell;
     uint32_t atom_off;
@@ -108,14 +112,27 @@ __device__ __forceinline__ double remainder_exact(double d, double L, double inv
 // FP32 minimum-image displacement from the coarse/fine position split.
 // Xd = Xi - Xj is exact (multiples of 1/8); c = Xd - n*Lhi is exact; the fine
 // parts carry the remaining bits, so the result is within ~1 ulp of the
-// correctly rounded FP64 displacement.
+// correctly rounded FP64 displacement.  n = round(Xd / L) uses the 1.5*2^23
+// shift (exact round-to-nearest for |Xd/L| < 2^22) instead of a rounding
+// instruction, keeping the whole routine on the FMA pipe.
 __device__ __forceinline__ float disp32(float Xi, float Xj, float fi, float fj, float Lhi, float Llo,
                                        float invL) {
+    const float kShift = 12582912.0f;   // 1.5 * 2^23
     float Xd = Xi - Xj;
-    float n = rintf(Xd * invL);
-    float c = fmaf(-n, Lhi, Xd);
-    float fd = fmaf(-n, Llo, fi - fj);
+    float n = __fsub_rn(__fmaf_rn(Xd, invL, kShift), kShift);
+    float c = __fmaf_rn(-n, Lhi, Xd);
+    float fd = __fmaf_rn(-n, Llo, fi - fj);
     return c + fd;
+}
+
+// One neighbour's FP32 position record (coarse X, fine xf: 32 bytes, 32-byte
+// aligned) in a single 256-bit read-only load, so a gather touches its sector
+// once instead of twice.
+__device__ __forceinline__ void ld_pos(const float4* pos, uint32_t j, float4& A, float4& B) {
+    const float* q = reinterpret_cast<const float*>(pos) + 8 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(A.x), "=f"(A.y), "=f"(A.z), "=f"(A.w), "=f"(B.x), "=f"(B.y), "=f"(B.z), "=f"(B.w)
+        : "l"(q));
 }
 
 }  // namespace parm

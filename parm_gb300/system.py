@@ -199,6 +199,14 @@ class System:
     def set_graph_steps(self, k: int) -> None:
         check(self.lib.parm_set_graph_steps(self.h, int(k)))
 
+    def set_threads_per_atom(self, tpa: int) -> None:
+        check(self.lib.parm_set_threads_per_atom(self.h, int(tpa)))
+
+    def autotune(self) -> int:
+        v = C.c_uint32()
+        check(self.lib.parm_autotune(self.h, C.byref(v)))
+        return v.value
+
     def timing(self, enable: bool) -> None:
         check(self.lib.parm_timing(self.h, 1 if enable else 0))
 

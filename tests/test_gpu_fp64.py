@@ -185,3 +185,35 @@ def test_large_lattice_pairs_and_forces():
     g.set_forces(True)
     o.set_forces(True)
     assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+
+
+@pytest.mark.parametrize("graph_steps", [0, 1, 7])
+def test_launch_modes_identical(graph_steps):
+    """Direct launches (profiling mode) and any graph size give the reference trajectory."""
+    w = W.lj_lattice(shape=(8, 8, 8), seed=99)
+    g = make_gpu(w)
+    g.set_graph_steps(graph_steps)
+    o = make_oracle(w)
+    g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
+    o.initialize()
+    g.verlet(0.002, 150)
+    o.verlet(0.002, 150)
+    st, ref = g.get_atoms(), o.get_state()
+    for k in ("x", "v", "a", "f"):
+        assert np.array_equal(st[k], ref[k]), k
+    assert g.which()[0] == o.which() > 2
+
+
+def test_partial_field_transfers_keep_other_fields():
+    """parm_get_atoms writes only the requested fields of the caller's records."""
+    from parm_gb300 import capi
+    import ctypes as C
+    w = W.small_random(n=100, ndim=3, kind=1, seed=50)
+    g = make_gpu(w)
+    rec = np.full((w.n, 13), 7.0)
+    capi.check(g.lib.parm_get_atoms(g.h, rec.ctypes.data_as(C.POINTER(C.c_double)), 13, capi.X))
+    assert np.array_equal(rec[:, 0:3], w.x) and np.all(rec[:, 3:] == 7.0)
+    rec2 = np.full((w.n, 20), 5.0)
+    capi.check(g.lib.parm_get_atoms(g.h, rec2.ctypes.data_as(C.POINTER(C.c_double)), 20, capi.V | capi.M))
+    assert np.array_equal(rec2[:, 3:6], w.v) and np.array_equal(rec2[:, 12], w.m)
+    assert np.all(rec2[:, 0:3] == 5.0) and np.all(rec2[:, 6:12] == 5.0) and np.all(rec2[:, 13:] == 5.0)

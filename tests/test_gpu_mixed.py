@@ -51,12 +51,23 @@ def test_mixed_forces_within_tolerance(lj32k):
     assert abs(m.virial()[0] - p) / abs(p) <= 1e-5
 
 
-@pytest.mark.parametrize("kind,exponent", [(1, 2.0), (1, 2.5), (2, 0.0)])
-def test_mixed_soft_kinds(kind, exponent):
-    w = W.small_random(n=4000, ndim=3, kind=kind, seed=31, phi=0.6 if kind == 1 else 0.4,
-                       exponent=exponent, skin=0.2)
-    if kind == 2:
-        w.params[:, 0] = 1.0
+@pytest.mark.parametrize("exponent", [2.0, 2.5])
+def test_mixed_soft_spheres(exponent):
+    """Random overlapping soft spheres (the packings' starting state)."""
+    w = W.small_random(n=4000, ndim=3, kind=1, seed=31, phi=0.6, exponent=exponent, skin=0.2)
+    m = make_gpu(w, "mixed")
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.nl_update(True)
+    m.set_forces(True)
+    o.set_forces(True)
+    err = force_error(m.get_atoms()["f"], o.get_state()["f"])
+    assert err <= FORCE_TOL, err
+
+
+def test_mixed_wca_fluid():
+    """WCA fluid at the replicas' densities (lattice start, as in the Langevin workload)."""
+    w = W.wca_replicas(nrep=1, nmin=8000, nmax=8000, rho_lo=0.9, rho_hi=0.9, seed=32)
     m = make_gpu(w, "mixed")
     o = make_oracle(w)
     m.nlist_update(True)
@@ -95,3 +106,29 @@ def test_mixed_nve_drift_comparable(lj32k):
         out[prec] = abs(slope) * 1e5 / abs(np.mean(E))
     # drift per 1e5 steps, relative to |E|
     assert out["mixed"] <= max(5 * out["fp64"], 1e-4), out
+
+
+@pytest.mark.parametrize("tpa", [1, 2, 4, 101, 104, 108, 116, 132])
+def test_mixed_threads_per_atom(lj32k, tpa):
+    """Every threads-per-atom variant of the mixed kernel meets the force tolerance."""
+    w = lj32k
+    m = make_gpu(w, "mixed")
+    m.set_threads_per_atom(tpa)
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.build_fast()
+    m.set_forces(True)
+    o.set_forces(True)
+    assert force_error(m.get_atoms()["f"], o.get_state()["f"]) <= FORCE_TOL
+
+
+def test_autotune_leaves_state_unchanged(lj32k):
+    m = make_gpu(lj32k, "mixed")
+    m.nlist_update(False); m.set_forces(True); m.nlist_update(False)
+    m.verlet(0.002, 5)
+    before = m.get_atoms()
+    tpa = m.autotune()
+    assert tpa // 1000 in (0, 1) and (tpa % 1000) // 10 in (1, 2, 4, 8, 16, 32) and tpa % 10 in (1, 2, 4)
+    after = m.get_atoms()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
