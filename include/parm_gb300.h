@@ -180,6 +180,22 @@ void* parm_stream(parm_system* s);
 int parm_host_alloc(void** p, uint64_t bytes);
 int parm_host_free(void* p);
 
+/* AtomGroup::kinetic_energy of Atom records that the caller already holds in
+ * device memory (stride doubles per record, as for parm_set_atoms), without
+ * allocating anything: for callers that cannot allocate device memory (code
+ * running during CUDA graph capture, frameworks whose pool owns every device
+ * buffer, loops that must not enter the driver's allocator).  No counterpart
+ * in the reference.  `atoms` and `out` (one double) are device pointers,
+ * `origin` a host pointer to ndim doubles or NULL, `stream` a cudaStream_t
+ * (NULL: the legacy default stream).  The call is asynchronous on `stream`.
+ * At most 262144 atoms per call: the per-atom scratch is a static 2 MiB
+ * device array that every GPU loading the library holds until exit.  The
+ * first call on a device looks up that array's address, so make it before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race with each other. */
+int parm_kinetic_energy_noalloc(const double* atoms, uint64_t stride, uint32_t natoms, int ndim,
+                                const double* origin, double* out, void* stream);
+
 /* Evaluate the library's minimum-image routine remainder(d[i], L[i]) on the
  * GPU (test hook for the exact IEEE remainder used by OriginBox::diff). */
 int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t n);

@@ -38,6 +38,7 @@ CUDA_UNITS = {
     "pair64.cu": ["-fmad=false"],
     "pair32.cu": [],
     "capi.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
 }
 HOST_UNITS = ["parm_host.cpp"]
 

@@ -78,6 +78,8 @@ SIGNATURES = {
     "parm_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
     "parm_host_free": (C.c_int, [C.c_void_p]),
     "parm_debug_remainder": (C.c_int, [_dp, _dp, _dp, C.c_uint32]),
+    "parm_kinetic_energy_noalloc": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, _dp, C.c_void_p,
+                                              C.c_void_p]),
 }
 
 _lib = None

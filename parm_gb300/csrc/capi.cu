@@ -62,6 +62,11 @@ struct GraphEntry {
 enum StepMode { SM_VERLET = 0, SM_DAMPED = 1, SM_SOL = 2 };
 }  // namespace
 
+namespace parm {
+// records an error for parm_last_error() from other translation units
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace parm
+
 struct parm_system {
     DevCtx c{};
     int nd = 3, prec = 0;

@@ -123,6 +123,9 @@ struct DevCtx {
     double* sysout;       // per-system outputs
 };
 
+// capi.cu: store the error text returned by parm_last_error(); returns code
+int set_error(int code, const char* msg);
+
 // ---- launchers (implemented in the .cu files) ----
 // nlist.cu
 void launch_arm(const DevCtx& c, cudaStream_t s, int count_step, int use_cond,
