@@ -25,5 +25,26 @@ def build() -> Path:
     return OUT
 
 
+REFBUILD = HERE / "refbuild"
+REF_OUT = HERE / "_ref"
+REF_SRC = Path("/root/reference/src")
+
+
+def build_ref(ref_src: Path = REF_SRC) -> Path | None:
+    """Compile the reference's own sources into oracle/_ref (fixture drivers).
+
+    Only possible where the reference sources are present; returns None
+    elsewhere.  The drivers regenerate tests/golden/*.npz; no test runs them.
+    """
+    if not (ref_src / "collection.cpp").exists():
+        return None
+    r = subprocess.run(["make", "-C", str(REFBUILD), f"REF={ref_src}", f"OUT={REF_OUT}", "-j2"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + r.stdout + r.stderr)
+    return REF_OUT
+
+
 if __name__ == "__main__":
     print(build())
+    print(build_ref())

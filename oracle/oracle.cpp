@@ -6,13 +6,16 @@
 // smoke check and bench.py's CPU-baseline leg load this library.
 //
 // Parity status: pinned.  The fixtures under tests/golden/ are produced by the
-// reference's own sources (src/box.cpp, src/trackers.cpp, src/collection.cpp,
-// src/vecrand.cpp and the NListed templates of src/interaction.hpp) compiled
-// against a small restatement of the Eigen/Boost subset they use
-// (oracle/refbuild/), and tests/test_oracle_golden.py checks this file
-// against them.  The Langevin noise stream is the project's counter-based
-// generator (the reference draws from Boost's mt19937, which cannot be
-// reproduced), so Langevin parity with the reference is statistical.
+// reference's own sources (src/vecrand.cpp, src/box.cpp, src/trackers.cpp,
+// src/collection.cpp and the NListed templates of src/interaction.hpp)
+// compiled as they are against a restatement of the Eigen/Boost subset they
+// use (oracle/refbuild/shim, recipe oracle/refbuild/Makefile, generator
+// tests/golden/make_golden.py), and tests/test_oracle_golden.py checks this
+// file against them bit for bit: pair lists, forces, energies, stresses and
+// Verlet / damped / Langevin (T = 0) trajectories up to 1000 steps.
+// Not pinned: Eigen's own arithmetic (the restatement fixes its reduction
+// order) and the Langevin noise stream (the reference draws from Boost's
+// mt19937; here a counter-based generator), whose parity is statistical.
 //
 // Evaluation-order facts taken from the reference (all FP64, no FMA; build
 // with -ffp-contract=off):

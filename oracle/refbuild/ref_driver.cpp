@@ -1,0 +1,128 @@
+// Fixture driver: runs the reference's own classes (built from its sources
+// by oracle/refbuild/Makefile) on an input deck and prints every quantity the
+// parity tests compare, with 17 significant digits.  Test infrastructure.
+//
+// Input (whitespace separated): kind integrator nsteps dt damping T skin
+//   L[NDIM]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2
+//   norder order[norder]   nign (a b)[nign]   nout out_steps[nout]
+// kind: 0 NListed<EpsSigCutAtom,LennardJonesCutPair>, 1 <EpsSigExpAtom,RepulsionPair>,
+//       2 <EpsSigAtom,LJRepulsePair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0)
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <string>
+
+#include "collection.hpp"
+#include "interaction.hpp"
+
+// numbers are read with strtod so that "inf" and "nan" parse like any value
+static double rd() {
+    std::string t;
+    if (!(std::cin >> t)) {
+        std::fprintf(stderr, "ref_driver: truncated input\n");
+        std::exit(2);
+    }
+    return std::strtod(t.c_str(), nullptr);
+}
+static unsigned rdu() { return (unsigned)rd(); }
+
+static void pvec(const Vec& v) {
+    for (int d = 0; d < NDIM; d++) std::printf(" %.17g", v[d]);
+}
+
+template <class A>
+A make_atom(AtomID id, int kind, const double* p);
+template <>
+EpsSigCutAtom make_atom<EpsSigCutAtom>(AtomID id, int, const double* p) {
+    return EpsSigCutAtom(id, p[0], p[1], p[2]);
+}
+template <>
+EpsSigExpAtom make_atom<EpsSigExpAtom>(AtomID id, int, const double* p) {
+    return EpsSigExpAtom(id, p[0], p[1], p[2]);
+}
+template <>
+EpsSigAtom make_atom<EpsSigAtom>(AtomID id, int, const double* p) {
+    return EpsSigAtom(id, p[0], p[1]);
+}
+
+template <class A, class P>
+int run(int kind, int integ, int nsteps, double dt, double damping, double T, double skin) {
+    Vec L;
+    for (int d = 0; d < NDIM; d++) L[d] = rd();
+    unsigned N = rdu();
+    std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * 3);
+    for (unsigned i = 0; i < N; i++) {
+        for (int d = 0; d < NDIM; d++) xs[i * NDIM + d] = rd();
+        for (int d = 0; d < NDIM; d++) vs[i * NDIM + d] = rd();
+        ms[i] = rd();
+        for (int k = 0; k < 3; k++) ps[3 * i + k] = rd();
+    }
+    std::vector<unsigned> order(rdu());
+    for (auto& o : order) o = rdu();
+    std::vector<unsigned> ign(2 * rdu());
+    for (auto& q : ign) q = rdu();
+    std::vector<int> outs(rdu());
+    for (auto& q : outs) q = (int)rd();
+
+    boost::shared_ptr<OriginBox> obox(new OriginBox(L));
+    boost::shared_ptr<AtomVec> atoms(new AtomVec(ms));
+    for (unsigned i = 0; i < N; i++) {
+        for (int d = 0; d < NDIM; d++) {
+            (*atoms)[i].x[d] = xs[i * NDIM + d];
+            (*atoms)[i].v[d] = vs[i * NDIM + d];
+        }
+    }
+    boost::shared_ptr<NListed<A, P> > inter(new NListed<A, P>(obox, atoms, skin));
+    boost::shared_ptr<NeighborList> nl = inter->neighbor_list();
+    for (unsigned i : order) inter->add(make_atom<A>(atoms->get_id(i), kind, &ps[3 * i]));
+    for (size_t q = 0; q < ign.size() / 2; q++) nl->ignore(atoms->get_id(ign[2 * q]), atoms->get_id(ign[2 * q + 1]));
+    nl->update_list(true);
+    std::printf("PAIRS %u\n", nl->numpairs());
+    for (unsigned k = 0; k < nl->numpairs(); k++) {
+        IDPair pr = nl->get(k);
+        std::printf("%u %u\n", pr.first().n(), pr.last().n());
+    }
+
+    std::vector<boost::shared_ptr<Interaction> > is(1, inter);
+    std::vector<boost::shared_ptr<StateTracker> > ts(1, nl);
+    boost::shared_ptr<Collection> col;
+    if (integ == 0) col.reset(new CollectionVerlet(obox, atoms, dt, is, ts));
+    else if (integ == 1) col.reset(new CollectionDamped(obox, atoms, dt, damping, is, ts));
+    else col.reset(new CollectionSol(obox, atoms, dt, damping, T, is, ts));
+
+    Matrix st = inter->stress(*obox);
+    std::printf("INIT %.17g %.17g %llu %llu %u\n", inter->energy(*obox), inter->pressure(*obox),
+                inter->contacts(*obox), inter->overlaps(*obox), nl->which());
+    for (int a = 0; a < NDIM; a++)
+        for (int b = 0; b < NDIM; b++) std::printf(" %.17g", st(a, b));
+    std::printf("\n");
+    for (unsigned i = 0; i < N; i++) {
+        pvec((*atoms)[i].f);
+        pvec((*atoms)[i].a);
+        std::printf("\n");
+    }
+    int step = 0;
+    for (int target : outs) {
+        while (step < target && step < nsteps) {
+            col->timestep();
+            step++;
+        }
+        std::printf("STEP %d %u %.17g %.17g\n", step, nl->which(), inter->energy(*obox), atoms->kinetic_energy());
+        for (unsigned i = 0; i < N; i++) {
+            pvec((*atoms)[i].x);
+            pvec((*atoms)[i].v);
+            pvec((*atoms)[i].a);
+            pvec((*atoms)[i].f);
+            std::printf("\n");
+        }
+    }
+    return 0;
+}
+
+int main() {
+    int kind = (int)rd(), integ = (int)rd(), nsteps = (int)rd();
+    double dt = rd(), damping = rd(), T = rd(), skin = rd();
+    if (kind == 0) return run<EpsSigCutAtom, LennardJonesCutPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 1) return run<EpsSigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);
+    return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
+}

@@ -1,0 +1,221 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+The reference's own sources (vecrand.cpp, box.cpp, trackers.cpp,
+collection.cpp and the headers they include) are compiled where they lie by
+``oracle/refbuild/Makefile`` against a restatement of the Eigen/Boost subset
+they use (``oracle/refbuild/shim``), together with ``ref_driver.cpp``, which
+drives ``OriginBox``, ``AtomVec``, ``NListed<A,P>``, ``NeighborList`` and
+``CollectionVerlet`` / ``CollectionDamped`` / ``CollectionSol`` exactly as a
+reference program does.  Each case below is a seeded input deck; the driver's
+output (pair list, initial forces, energies, stresses, trajectories) is
+stored with the deck in ``<case>.npz``.
+
+Run from the repository root (needs the reference sources)::
+
+    python tests/golden/make_golden.py [--ref-src /path/to/parm/src]
+
+Positions and velocities come from numpy's seeded generators, so the decks
+are reproducible; the reference's own random streams (Boost.Random) are not
+used: Langevin cases run at T = 0, where the noise term vanishes.
+"""
+from __future__ import annotations
+
+import argparse
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+REFBUILD = ROOT / "oracle" / "refbuild"
+REFOUT = ROOT / "oracle" / "_ref"
+
+VERLET, DAMPED, SOL = 0, 1, 2
+LJCUT, REPULSION, LJREPULSE = 0, 1, 2
+SIG_PRIME = 2.0 ** (-1.0 / 6.0)
+
+
+def _deck(c: dict) -> str:
+    nd = c["L"].shape[0]
+    out = [f"{c['kind']} {c['integ']} {c['nsteps']} {c['dt']!r} {c['damping']!r} {c['T']!r} {c['skin']!r}",
+           " ".join(repr(float(q)) for q in c["L"]), str(len(c["m"]))]
+    for i in range(len(c["m"])):
+        vals = list(c["x"][i]) + list(c["v"][i]) + [c["m"][i]] + list(c["params"][i])
+        out.append(" ".join(repr(float(q)) for q in vals))
+    out.append(f"{len(c['order'])} " + " ".join(str(int(q)) for q in c["order"]))
+    ig = c["ignores"].reshape(-1)
+    out.append(f"{len(ig) // 2} " + " ".join(str(int(q)) for q in ig))
+    out.append(f"{len(c['out_steps'])} " + " ".join(str(int(q)) for q in c["out_steps"]))
+    assert nd in (2, 3)
+    return "\n".join(out) + "\n"
+
+
+def _parse(text: str, n: int, nd: int) -> dict:
+    lines = text.splitlines()
+    pos = 0
+
+    def nxt():
+        nonlocal pos
+        pos += 1
+        return lines[pos - 1].split()
+
+    h = nxt()
+    assert h[0] == "PAIRS"
+    k = int(h[1])
+    pairs = np.array([[int(t) for t in nxt()] for _ in range(k)], dtype=np.uint32).reshape(k, 2)
+    h = nxt()
+    assert h[0] == "INIT"
+    init = np.array([float(h[1]), float(h[2])])
+    counts = np.array([int(h[3]), int(h[4]), int(h[5])], dtype=np.int64)
+    stress = np.array([float(t) for t in nxt()]).reshape(nd, nd)
+    fa = np.array([[float(t) for t in nxt()] for _ in range(n)]).reshape(n, 2 * nd)
+    steps, which, energy, ke, st = [], [], [], [], []
+    while pos < len(lines):
+        h = nxt()
+        assert h[0] == "STEP"
+        steps.append(int(h[1]))
+        which.append(int(h[2]))
+        energy.append(float(h[3]))
+        ke.append(float(h[4]))
+        st.append(np.array([[float(t) for t in nxt()] for _ in range(n)]).reshape(n, 4 * nd))
+    st = np.array(st).reshape(len(steps), n, 4 * nd)
+    return {"pairs": pairs, "init": init, "init_counts": counts, "stress": stress,
+            "f0": fa[:, :nd], "a0": fa[:, nd:], "steps": np.array(steps, dtype=np.int64),
+            "which_steps": np.array(which, dtype=np.int64), "energy_steps": np.array(energy),
+            "ke_steps": np.array(ke), "x_steps": st[:, :, 0:nd], "v_steps": st[:, :, nd:2 * nd],
+            "a_steps": st[:, :, 2 * nd:3 * nd], "f_steps": st[:, :, 3 * nd:4 * nd]}
+
+
+def _case(name, kind, integ, nsteps, dt, L, x, v, m, params, skin, out_steps, damping=0.0, T=0.0,
+          order=None, ignores=None):
+    n = len(m)
+    return {"name": name, "kind": kind, "integ": integ, "nsteps": nsteps, "dt": float(dt),
+            "damping": float(damping), "T": float(T), "skin": float(skin),
+            "L": np.asarray(L, dtype=np.float64), "x": np.asarray(x, dtype=np.float64),
+            "v": np.asarray(v, dtype=np.float64), "m": np.asarray(m, dtype=np.float64),
+            "params": np.asarray(params, dtype=np.float64).reshape(n, 3),
+            "order": np.arange(n, dtype=np.int64) if order is None else np.asarray(order, dtype=np.int64),
+            "ignores": np.zeros((0, 2), np.int64) if ignores is None else np.asarray(ignores, np.int64),
+            "out_steps": np.asarray(out_steps, dtype=np.int64)}
+
+
+def lj_lattice_deck(shape, seed, T=1.0):
+    """Config-0 style: simple-cubic lattice at rho' = 0.8, +-0.05 sigma' jitter."""
+    rng = np.random.default_rng(seed)
+    rho = 0.8 / SIG_PRIME ** 3
+    a = (1.0 / rho) ** (1.0 / 3.0)
+    g = np.stack(np.meshgrid(*[np.arange(s) for s in shape], indexing="ij"), -1).reshape(-1, len(shape))
+    x = (g + 0.5) * a + rng.uniform(-0.05 * SIG_PRIME, 0.05 * SIG_PRIME, size=g.shape)
+    v = rng.normal(0.0, np.sqrt(T), size=g.shape)
+    v -= v.mean(axis=0)
+    L = np.array(shape, dtype=np.float64) * a
+    return L, x, v
+
+
+def cases() -> list[dict]:
+    out = []
+    cut = 2.5 * SIG_PRIME
+    # 1. LJ, 1000 atoms, the plain FP64 configuration: 1000 Verlet steps
+    L, x, v = lj_lattice_deck((10, 10, 10), 12345)
+    n = len(x)
+    out.append(_case("lj1000_verlet", LJCUT, VERLET, 1000, 0.001, L, x, v, np.ones(n),
+                     np.tile([1.0, 1.0, cut], (n, 1)), 0.4 * SIG_PRIME, [1, 10, 100, 1000]))
+    # 2. the 12-atom Hertzian fixture of pyparm/tests.py (PairedCollectionTest,
+    #    RandomHertzianVerletTest): legacy numpy stream seeded 131
+    N = 12
+    sig = np.array([1.0] * (N // 2) + [1.4] * (N - N // 2))
+    Lh = float((np.sum((sig / 2) ** 3) * 4 / 3 * np.pi / 0.3) ** (1 / 3))
+    rs = np.random.RandomState(131)
+    xs, vs = [], []
+    for s in sig:
+        xs.append(rs.uniform(0.0, Lh, size=(3,)))
+        vs.append(rs.normal(size=(3,)) / s ** 3)
+        rs.normal(size=(3,))   # the fixture also draws a force it never uses
+    out.append(_case("hertz12_verlet", REPULSION, VERLET, 2000, 0.01, [Lh] * 3, xs, vs, sig ** 3,
+                     np.stack([np.full(N, 1.2), sig, np.full(N, 2.0)], 1), 0.4, [1, 10, 100, 1000, 2000]))
+    # 3. 3D soft spheres, exponent 2.5, damped minimisation steps
+    rng = np.random.default_rng(7)
+    n = 200
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lc = (np.sum(np.pi * sig ** 3 / 6) / 0.64) ** (1 / 3)
+    out.append(_case("spheres200_damped", REPULSION, DAMPED, 300, 0.01, [Lc] * 3,
+                     rng.uniform(0, Lc, (n, 3)), np.zeros((n, 3)), np.ones(n),
+                     np.stack([np.ones(n), sig, np.full(n, 2.5)], 1), 0.1, [1, 10, 100, 300], damping=0.5))
+    # 4. 2D harmonic disks at phi = 0.84, damped
+    rng = np.random.default_rng(8)
+    n = 256
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Ld = np.sqrt(np.sum(np.pi * sig ** 2 / 4) / 0.84)
+    out.append(_case("disks256_damped", REPULSION, DAMPED, 300, 0.01, [Ld, Ld],
+                     rng.uniform(0, Ld, (n, 2)), np.zeros((n, 2)), np.ones(n),
+                     np.stack([np.ones(n), sig, np.full(n, 2.0)], 1), 0.1, [1, 10, 100, 300], damping=1.0))
+    # 5. WCA fluid under CollectionSol at T = 0 (the noise term vanishes)
+    L, x, v = lj_lattice_deck((6, 6, 6), 99)
+    n = len(x)
+    out.append(_case("wca216_sol", LJREPULSE, SOL, 300, 0.001, L, x, v, np.ones(n),
+                     np.tile([1.0, 1.0, 0.0], (n, 1)), 0.3, [1, 10, 100, 300], damping=1.0))
+    # 6. 2D LJ, Verlet
+    L, x, v = lj_lattice_deck((20, 20), 5)
+    n = len(x)
+    L = L * (0.8 / SIG_PRIME ** 3) ** (1 / 3) / (0.8 / SIG_PRIME ** 2) ** (1 / 2)   # rho' = 0.8 in 2D
+    x = x * L[0] / (20 * (1.0 / (0.8 / SIG_PRIME ** 3)) ** (1 / 3))
+    out.append(_case("lj400_2d_verlet", LJCUT, VERLET, 300, 0.002, L, x, v, np.ones(n),
+                     np.tile([1.0, 1.0, cut], (n, 1)), 0.3, [1, 10, 100, 300]))
+    # 7. bidisperse LJ with shuffled insertion order, non-member atoms,
+    #    exclusions, immobile atoms (mass 0 and inf)
+    rng = np.random.default_rng(21)
+    L, x, v = lj_lattice_deck((8, 8, 8), 21)
+    n = len(x)
+    eps = rng.choice([0.8, 1.2], n)
+    sg = rng.choice([1.0, 1.2], n)
+    order = rng.permutation(n)[: n - 7]
+    ign = np.array([[order[0], order[1]], [order[5], order[2]], [3, 4], [10, 11]])
+    m = np.ones(n)
+    m[order[3]] = 0.0
+    m[order[4]] = np.inf
+    out.append(_case("ljmix512_order_excl", LJCUT, VERLET, 200, 0.001, L, x, v, m,
+                     np.stack([eps, sg, 2.5 * sg], 1), 0.3, [1, 10, 100, 200], order=order, ignores=ign))
+    # 8. boundary cases: atoms exactly at +-L/2 and beyond the box, a pair
+    #    separated by exactly cut + skin (the list test is a strict '<')
+    rng = np.random.default_rng(33)
+    n = 64
+    Lb = np.array([8.0, 8.0, 8.0])
+    x = rng.uniform(-4.0, 4.0, (n, 3))
+    x[0] = [4.0, -4.0, 0.5]
+    x[1] = [-4.0, 4.0, 26.5]          # unwrapped: 26.5 = 2.5 + 3 L
+    x[2] = [1.0, 1.0, 1.0]
+    x[3] = [1.0 + 2.5, 1.0, 1.0]      # |x3 - x2| = 2.0 + 0.5 exactly
+    x[4] = [-3.0, -3.0, -3.0]
+    x[5] = [-3.0, -3.0, -3.0 + 2.5 - 2.0 ** -40]
+    params = np.tile([1.0, 2.0, 2.0], (n, 1))     # cut = sigma = 2.0, list radius 2.5
+    out.append(_case("edges64_pairs", REPULSION, VERLET, 50, 0.005, Lb, x, rng.normal(0, 0.3, (n, 3)),
+                     np.ones(n), params, 0.5, [1, 20, 50]))
+    return out
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-src", default="/root/reference/src")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args(argv)
+    subprocess.run(["make", "-C", str(REFBUILD), f"REF={a.ref_src}", f"OUT={REFOUT}", "-j2"], check=True)
+    for c in cases():
+        if a.only and c["name"] != a.only:
+            continue
+        nd = c["L"].shape[0]
+        exe = REFOUT / f"ref_driver{nd}d"
+        r = subprocess.run([str(exe)], input=_deck(c), capture_output=True, text=True, check=True)
+        res = _parse(r.stdout, len(c["m"]), nd)
+        arrays = {k: v for k, v in c.items() if k != "name"}
+        arrays.update(res)
+        arrays = {k: (np.asarray(v) if not isinstance(v, np.ndarray) else v) for k, v in arrays.items()}
+        np.savez_compressed(HERE / f"{c['name']}.npz", **arrays)
+        print(f"{c['name']}: n={len(c['m'])} pairs={len(res['pairs'])} E0={res['init'][0]!r} "
+              f"which={res['which_steps'].tolist()}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

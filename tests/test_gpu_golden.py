@@ -1,0 +1,78 @@
+"""FP64 GPU path against the reference's own outputs (golden fixtures).
+
+Same decks as tests/test_oracle_golden.py, run through the C ABI: the pair
+list (order included), forces, accelerations and Verlet / damped / Langevin
+(T = 0) trajectories must equal the reference's bit for bit.  Two documented
+exceptions: pair laws with a non-integer exponent call the device ``pow``,
+which may differ from the host's by an ulp, so those cases are held to
+1e-12 relative (scaled by the largest entry of the array); and energies,
+pressures and stresses are parallel sums, held to 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+from golden_cases import DAMPED, VERLET, load, names
+
+pytestmark = pytest.mark.gpu
+
+CASES = names()
+RTOL = 1e-12
+
+
+def _close(got, want, exact, what):
+    if exact:
+        np.testing.assert_array_equal(got, want, err_msg=what)
+    else:
+        scale = max(float(np.abs(want).max()), 1e-300)
+        err = float(np.abs(got - want).max()) / scale
+        assert err <= RTOL, f"{what}: relative error {err:.3e}"
+
+
+def _gpu(d):
+    from parm_gb300 import System
+    n, nd = d["n"], d["ndim"]
+    s = System([n], ndim=nd, precision="fp64")
+    s.set_boxes(d["L"][None, :])
+    s.set_atoms(x=d["x"], v=d["v"], a=np.zeros((n, nd)), f=np.zeros((n, nd)), m=d["m"])
+    rank = np.full(n, 0xFFFFFFFF, dtype=np.uint32)
+    rank[d["order"]] = np.arange(len(d["order"]), dtype=np.uint32)
+    s.set_interaction(d["kind"], d["params"], d["skin"], rank=rank)
+    for a, b in d["ignores"]:
+        s.ignore(int(a), int(b))
+    return s
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_fp64_matches_reference(name):
+    d = load(name)
+    exact = not (d["kind"] == 1 and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
+    s = _gpu(d)
+    s.nlist_update(True)
+    np.testing.assert_array_equal(s.pairs(), d["pairs"])
+    s.set_forces(True)
+    st = s.get_atoms()
+    _close(st["f"], d["f0"], exact, "initial forces")
+    _close(st["a"], d["a0"], exact, "initial accelerations")
+    assert s.energy()[0] == pytest.approx(d["init"][0], rel=RTOL, abs=1e-13)
+    assert s.virial()[0] == pytest.approx(d["init"][1], rel=RTOL, abs=1e-13)
+    np.testing.assert_allclose(s.stress()[0], d["stress"], rtol=RTOL, atol=1e-13 * np.abs(d["stress"]).max())
+    assert s.contacts()[0] == d["init_counts"][0]
+    assert s.overlaps()[0] == d["init_counts"][1]
+    assert s.which()[0] == d["init_counts"][2]
+    done = 0
+    for i, step in enumerate(d["steps"]):
+        k = int(step) - done
+        if d["integ"] == VERLET:
+            s.verlet(d["dt"], k)
+        elif d["integ"] == DAMPED:
+            s.damped(d["dt"], d["damping"], k)
+        else:
+            s.sol(d["dt"], d["damping"], 0.0, seed=1, nsteps=k)
+        done = int(step)
+        st = s.get_atoms()
+        for key in ("x", "v", "a", "f"):
+            _close(st[key], d[f"{key}_steps"][i], exact, f"{key} at step {step}")
+        assert s.which()[0] == d["which_steps"][i], f"rebuilds at step {step}"
+        assert s.energy()[0] == pytest.approx(d["energy_steps"][i], rel=RTOL, abs=1e-13)
+        assert s.kinetic_energy()[0] == pytest.approx(d["ke_steps"][i], rel=RTOL, abs=1e-13)
+    s.close()
