@@ -146,17 +146,23 @@ int parm_set_step(parm_system* s, uint64_t step);
 int parm_set_nlist_capacity(parm_system* s, uint32_t maxnb);
 int parm_get_nlist_capacity(parm_system* s, uint32_t* maxnb);
 
-/* Variant of the mixed-precision pair kernel: 1, 2 or 4 threads per atom with
- * neighbour positions staged in shared memory per tile of 64 atoms, or
- * 100 + t for the plain gather kernel with t = 1, 4, 8, 16 or 32 threads per
- * atom (default 101).  The FP64 path always uses one thread per atom, so that
- * each atom's force is summed in the reference's order. */
+/* Variant of the mixed-precision pair kernel and list build:
+ *   200      cell blocks: the neighbourhood of a block of cells is staged in
+ *            shared memory (16-byte records) and the lists hold 16-bit local
+ *            indices (default wherever every system has >= 3 cells per axis);
+ *   1, 2, 4  threads per atom with neighbour positions staged per tile of 64 atoms;
+ *   100 + t  plain gather kernel with t = 1, 4, 8, 16 or 32 threads per atom.
+ * Switching converts the current lists (same pairs, same order).  The FP64
+ * path always uses one thread per atom, so that each atom's force is summed
+ * in the reference's order. */
 int parm_set_threads_per_atom(parm_system* s, uint32_t tpa);
+/* The variant in use, in the codes of parm_set_threads_per_atom. */
+int parm_get_threads_per_atom(parm_system* s, uint32_t* tpa);
 
 /* Time every variant of the mixed-precision pair kernel on the current
- * configuration and keep the fastest; *tpa (when not NULL) receives
- * tiled * 1000 + threads_per_atom * 10 + neighbours_per_iteration.
- * The state is left unchanged. */
+ * configuration and keep the fastest; *tpa (when not NULL) receives 2000 for
+ * the cell-block kernel, else tiled * 1000 + threads_per_atom * 10 +
+ * neighbours_per_iteration.  The state is left unchanged. */
 int parm_autotune(parm_system* s, uint32_t* tpa);
 
 /* Steps captured per CUDA graph launch (default 16; 0 launches kernels directly). */
@@ -199,6 +205,11 @@ int parm_kinetic_energy_noalloc(const double* atoms, uint64_t stride, uint32_t n
 /* Evaluate the library's minimum-image routine remainder(d[i], L[i]) on the
  * GPU (test hook for the exact IEEE remainder used by OriginBox::diff). */
 int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t n);
+
+/* Test hook: atoms staged in shared memory per cell block (the rest of a
+ * block's neighbourhood is read from global memory); 0 restores the size
+ * chosen from the density.  Results do not depend on it. */
+int parm_debug_stage_cap(parm_system* s, uint32_t cap);
 
 #ifdef __cplusplus
 }

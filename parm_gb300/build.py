@@ -37,6 +37,7 @@ CUDA_UNITS = {
     "integrate.cu": ["-fmad=false"],
     "pair64.cu": ["-fmad=false"],
     "pair32.cu": [],
+    "staged.cu": [],
     "capi.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
 }

@@ -98,6 +98,14 @@ struct parm_system {
     uint64_t n_force = 0, n_rebuild = 0;
     bool pending = false;
     uint64_t last_launches = 0;
+    // cell-block kernels of the mixed path (staged.cu)
+    void* blk_mem = nullptr;
+    void* nbr16_mem = nullptr;
+    bool want_staged = true;     // prefer them when the grids allow
+    bool stg_ok = false;         // the current grids allow them
+    bool stg_pending = false;    // grids changed under staged lists: switch back once every system rebuilt
+    std::vector<uint32_t> stg_mark;   // which() of each system when the grids changed
+    uint32_t stage_cap_override = 0;  // test hook (parm_debug_stage_cap)
 
     ~parm_system() {
         clear_graphs();
@@ -105,6 +113,8 @@ struct parm_system {
         if (cell_mem) cudaFree(cell_mem);
         if (nbr_mem) cudaFree(nbr_mem);
         if (tlst_mem) cudaFree(tlst_mem);
+        if (blk_mem) cudaFree(blk_mem);
+        if (nbr16_mem) cudaFree(nbr16_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
@@ -175,6 +185,9 @@ struct parm_system {
             dmax = std::max(dmax, d);
         }
         const double rl = dmax + skin;
+        std::vector<int> oldnc;
+        for (uint32_t s = 0; s < nsys; s++)
+            for (int d = 0; d < 3; d++) oldnc.push_back(sys[s].nc[d]);
         bucket_off.assign(nsys + 1, 0);
         uint32_t total = 0;
         for (uint32_t s = 0; s < nsys; s++) {
@@ -202,6 +215,9 @@ struct parm_system {
                 S.cellw_inv[d] = (float)(S.nc[d] / S.L[d]);
                 S.cellw[d] = S.L[d] / S.nc[d];
                 S.cellw32[d] = (float)S.cellw[d];
+                const double l8 = std::rint(S.L[d] * 8.0) * 0.125;
+                S.L8[d] = (float)l8;
+                S.Lr8[d] = (float)(S.L[d] - l8);
             }
             S.skin = skin;
             S.rlist_max = rl;
@@ -214,6 +230,28 @@ struct parm_system {
         for (uint32_t s2 = 0; s2 < nsys; s2++)
             for (int d = 0; d < nd; d++)
                 if (sys[s2].nc[d] < 3) c.any_wrap = 1;
+        std::vector<int> newnc;
+        for (uint32_t s2 = 0; s2 < nsys; s2++)
+            for (int d = 0; d < 3; d++) newnc.push_back(sys[s2].nc[d]);
+        if (cell_mem && newnc == oldnc) {
+            // same grids: the cell arrays (and staged lists) stay valid
+            CUDA_TRY(cudaMemcpyAsync(const_cast<SysConst*>(c.sys), sys.data(), sizeof(SysConst) * nsys,
+                                     cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            clear_graphs();
+            return plan_blocks();
+        }
+        if (c.staged) {
+            // the staged lists index the old grids: keep them as row-major lists
+            // until every system has been rebuilt on the new grids
+            launch_expand_stg(c, st);
+            CUDA_TRY(cudaGetLastError());
+            TRY(sync_status());
+            c.staged = 0;
+            stg_pending = true;
+            stg_mark.assign(nsys, 0);
+            CUDA_TRY(cudaMemcpy(stg_mark.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
+        }
         if (cell_mem) cudaFree(cell_mem);
         cell_mem = nullptr;
         const size_t nblk = (total + 4095) / 4096 + 1;
@@ -239,6 +277,96 @@ struct parm_system {
                                  4 * (nsys + 1), cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         clear_graphs();
+        return plan_blocks();
+    }
+
+    // Cell blocks of the mixed path (staged.cu): blocks of Kx x Ky cells of
+    // one z layer holding about 100 atoms; usable when every system has at
+    // least 3 cells per axis and the block frames fit the 9-bit coarse
+    // fields (+-32 length units around the block centre).  Sets stg_ok and, when the blocks are not usable, c.staged = 0.
+    int plan_blocks() {
+        stg_ok = false;
+        if (prec != PREC_MIXED || kind < 0) {
+            c.staged = 0;
+            return PARM_OK;
+        }
+        std::vector<uint4> bl;
+        double worst = 0.0;
+        bool ok = true;
+        const double margin = 2.0 * skin + 1.0;
+        for (uint32_t s = 0; s < nsys && ok; s++) {
+            const SysConst& S = sys[s];
+            for (int d = 0; d < nd; d++)
+                if (S.nc[d] < 3) ok = false;
+            if (!ok) break;
+            const double a = std::max(1e-3, (double)natoms[s] / S.ncell);
+            const int cells = std::max(1, (int)std::lround(0.8 * STG_THREADS_HOST / a));
+            const int ky = std::max(1, std::min({(int)std::lround(std::sqrt(cells / 2.0)), STG_KY_MAX, S.nc[1] - 2}));
+            const int kx = std::max(1, std::min({(int)std::lround((double)cells / ky), STG_KX_MAX, S.nc[0] - 2}));
+            const int nbx = (S.nc[0] + kx - 1) / kx, nby = (S.nc[1] + ky - 1) / ky;
+            const double wx = std::ceil((double)S.nc[0] / nbx), wy = std::ceil((double)S.nc[1] / nby);
+            const double ex = (0.5 * wx + 1.0) * S.cellw[0] + margin;
+            const double ey = (0.5 * wy + 1.0) * S.cellw[1] + margin;
+            const double ez = nd == 3 ? 1.5 * S.cellw[2] + margin : 0.0;
+            if (ex >= 31.0 || ey >= 31.0 || ez >= 31.0) ok = false;   // 9-bit coarse fields (+-32)
+            worst = std::max(worst, a * (wx + 2) * (wy + 2) * (nd == 3 ? 3 : 1));
+            const int nzl = nd == 3 ? S.nc[2] : 1;
+            for (int z = 0; z < nzl; z++)
+                for (int by = 0; by < nby; by++)
+                    for (int bx = 0; bx < nbx; bx++) {
+                        const uint32_t x0 = (uint32_t)(bx * S.nc[0] / nbx), x1 = (uint32_t)((bx + 1) * S.nc[0] / nbx);
+                        const uint32_t y0 = (uint32_t)(by * S.nc[1] / nby), y1 = (uint32_t)((by + 1) * S.nc[1] / nby);
+                        bl.push_back(make_uint4(s, x0 | (x1 << 16), y0 | (y1 << 16), (uint32_t)z));
+                    }
+        }
+        if (!ok || worst > 20000.0 || bl.empty()) {
+            c.staged = 0;
+            return PARM_OK;
+        }
+        if (blk_mem) cudaFree(blk_mem);
+        blk_mem = nullptr;
+        CUDA_TRY(cudaMalloc(&blk_mem, sizeof(uint4) * bl.size()));
+        CUDA_TRY(cudaMemcpy(blk_mem, bl.data(), sizeof(uint4) * bl.size(), cudaMemcpyHostToDevice));
+        c.blk = static_cast<const uint4*>(blk_mem);
+        c.nblk = (uint32_t)bl.size();
+        c.stg_cap = (uint32_t)std::min(4096.0, std::ceil((1.5 * worst + 64.0) / 32.0) * 32.0);
+        if (stage_cap_override) c.stg_cap = stage_cap_override;
+        const bool uni_eps = c.uniform & UNI_EPS, uni_sig = c.uniform & UNI_SIG, uni_th = c.uniform & UNI_THIRD;
+        c.stg_prm = (uni_eps && uni_sig && uni_th) ? 0u : ((uni_eps && uni_th) ? 1u : 2u);
+        c.stg_dia = (uni_sig && (kind != PARM_LJCUT || uni_th)) ? 0u : 1u;
+        static bool limits_set[256] = {};
+        int dev = 0;
+        CUDA_TRY(cudaGetDevice(&dev));
+        if (dev >= 0 && dev < 256 && !limits_set[dev]) {
+            const int e = stg_set_smem_limits();
+            if (e != 0) return fail(PARM_ERR_CUDA, "raising the shared-memory limit of the cell-block kernels failed");
+            limits_set[dev] = true;
+        }
+        stg_ok = true;
+        return PARM_OK;
+    }
+
+    // back to the cell-block kernels once every system has been rebuilt on
+    // the current grids (their row-major lists then convert exactly)
+    int maybe_restage() {
+        if (!stg_pending || !want_staged || !stg_ok || c.staged) return PARM_OK;
+        std::vector<uint32_t> w(nsys);
+        CUDA_TRY(cudaMemcpy(w.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
+        for (uint32_t s = 0; s < nsys; s++)
+            if (w[s] == stg_mark[s]) return PARM_OK;
+        launch_compress_stg(c, st);
+        CUDA_TRY(cudaGetLastError());
+        c.staged = 1;
+        stg_pending = false;
+        clear_graphs();
+        return sync_status();
+    }
+
+    // row-major lists for the kernels that read them (evaluation, pair listing)
+    int rowmajor() {
+        if (!c.staged) return PARM_OK;
+        launch_expand_stg(c, st);
+        CUDA_TRY(cudaGetLastError());
         return PARM_OK;
     }
 
@@ -247,6 +375,7 @@ struct parm_system {
     int set_capacity(uint32_t maxnb) {
         maxnb = std::max<uint32_t>(8, (maxnb + 7) / 8 * 8);
         void* fresh = nullptr;
+        if (c.staged && nbr_mem) launch_expand_stg(c, st);   // the staged layout depends on maxnb
         CUDA_TRY(cudaStreamSynchronize(st));
         CUDA_TRY(cudaMalloc(&fresh, (size_t)maxnb * n * 4 + 16));
         if (nbr_mem) {
@@ -278,6 +407,17 @@ struct parm_system {
             c.tile_lst = static_cast<uint16_t*>(tlst_mem);
         }
         c.maxnb = maxnb;
+        if (prec == PREC_MIXED) {
+            if (nbr16_mem) cudaFree(nbr16_mem);
+            nbr16_mem = nullptr;
+            CUDA_TRY(cudaMalloc(&nbr16_mem, (size_t)maxnb * n * 2 + 16));
+            c.nbr16 = static_cast<uint16_t*>(nbr16_mem);
+            if (c.staged) {
+                launch_compress_stg(c, st);
+                CUDA_TRY(cudaGetLastError());
+                TRY(sync_status());
+            }
+        }
         clear_graphs();
         return PARM_OK;
     }
@@ -336,7 +476,8 @@ struct parm_system {
         launch_arm(c, st, 0, 0, 0);
         launch_rebuild(c, st);
         CUDA_TRY(cudaGetLastError());
-        return sync_status();
+        TRY(sync_status());
+        return maybe_restage();
     }
 
     int upload_params(const StepParams& p) {
@@ -438,7 +579,7 @@ struct parm_system {
             launch_kick(c, st, dmode);
             if (timing)
                 for (auto& q : e) cudaEventDestroy(q);
-            launches = (uint64_t)nsteps * (3 + (prec == PREC_FP64 ? 9 : 8)) + 1;
+            launches = (uint64_t)nsteps * (3 + chain_len()) + 1;
             done = nsteps;
         }
         while (done < nsteps) {
@@ -483,8 +624,14 @@ struct parm_system {
         uint32_t chains = 0;
         CUDA_TRY(cudaMemcpy(&chains, c.chains, 4, cudaMemcpyDeviceToHost));
         CUDA_TRY(cudaMemset(c.chains, 0, 4));
-        last_launches = graph_k == 0 ? launches : launches + (uint64_t)chains * (c.prec == PREC_FP64 ? 9ull : 8ull);
-        return PARM_OK;
+        last_launches = graph_k == 0 ? launches : launches + (uint64_t)chains * chain_len();
+        return maybe_restage();
+    }
+
+    // kernels in one rebuild chain (launch_rebuild)
+    uint64_t chain_len() const {
+        if (c.prec == PREC_FP64) return 11;
+        return (!c.staged && c.ntile && c.tiled) ? 11 : 10;
     }
 
     int reduce_sys(int ncomp, std::vector<double>& out) {
@@ -624,6 +771,33 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     A(S->alloc(c.chains, 1));
     A(S->alloc(c.params, 1));
     A(S->alloc(c.sysout, (size_t)nsys * 16));
+    {
+        // reduction chunks: consecutive atoms of one system, at least one per system
+        std::vector<uint4> ch;
+        std::vector<uint32_t> sc(nsys + 1);
+        for (uint32_t s = 0; s < nsys; s++) {
+            sc[s] = (uint32_t)ch.size();
+            uint32_t a = 0;
+            do {
+                const uint32_t cnt = std::min<uint32_t>(RED_CHUNK, natoms[s] - a);
+                ch.push_back(make_uint4(s, S->off[s] + a, cnt, 0u));
+                a += cnt;
+            } while (a < natoms[s]);
+        }
+        sc[nsys] = (uint32_t)ch.size();
+        uint4* dch = nullptr;
+        uint32_t* dsc = nullptr;
+        A(S->alloc(dch, ch.size()));
+        A(S->alloc(dsc, sc.size()));
+        A(S->alloc(c.part, ch.size() * 12));
+        cudaStreamSynchronize(S->st);
+        if (cudaMemcpy(dch, ch.data(), sizeof(uint4) * ch.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dsc, sc.data(), 4 * sc.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(PARM_ERR_CUDA, "reduction chunk upload failed"));
+        c.chunk = dch;
+        c.sys_chunk = dsc;
+        c.nchunk = (uint32_t)ch.size();
+    }
     A(S->alloc(S->d_origin, (size_t)nsys * 3));
     {
         SysConst* dsys = nullptr;
@@ -882,6 +1056,11 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     TRY(S->setup_cells());
     uint32_t need = S->estimate_capacity();
     if (need > S->c.maxnb) TRY(S->set_capacity(need));
+    // every list is rebuilt next (ignorechanged), in the preferred format
+    const uint32_t was = S->c.staged;
+    S->c.staged = (S->stg_ok && S->want_staged) ? 1u : 0u;
+    S->stg_pending = false;
+    if (S->c.staged != was) S->clear_graphs();
     return S->request_rebuild_all();  // ignorechanged = true
 }
 
@@ -919,6 +1098,7 @@ int parm_nlist_update(parm_system* S, int force, uint8_t* rebuilt) {
     launch_rebuild(S->c, S->st);
     CUDA_TRY(cudaGetLastError());
     TRY(S->sync_status());
+    TRY(S->maybe_restage());
     if (rebuilt) {
         std::vector<uint32_t> fl(S->nsys);
         CUDA_TRY(cudaMemcpy(fl.data(), S->c.flag, 4 * S->nsys, cudaMemcpyDeviceToHost));
@@ -937,6 +1117,7 @@ int parm_nlist_which(parm_system* S, uint32_t* which) {
 int parm_nlist_numpairs(parm_system* S, uint64_t* numpairs) {
     if (!S || !numpairs) return fail(PARM_ERR_ARG, "NULL argument");
     TRY(S->flush());
+    TRY(S->rowmajor());
     launch_numpairs(S->c, S->st);
     std::vector<double> out;
     TRY(S->reduce_sys(1, out));
@@ -948,6 +1129,7 @@ int parm_nlist_pairs(parm_system* S, uint32_t sys, uint32_t* pairs, uint64_t cap
     if (!S || !npairs) return fail(PARM_ERR_ARG, "NULL argument");
     if (sys >= S->nsys) return fail(PARM_ERR_ARG, "system index out of range");
     TRY(S->flush());
+    TRY(S->rowmajor());
     const uint32_t o = S->off[sys], na = S->natoms[sys], mx = S->c.maxnb;
     std::vector<uint32_t> nnb(na), rank(S->n), orig(na), nbr((size_t)na * mx);
     CUDA_TRY(cudaMemcpy(nnb.data(), S->c.nnb + o, 4 * (size_t)na, cudaMemcpyDeviceToHost));
@@ -1002,7 +1184,10 @@ int parm_evaluate(parm_system* S, int what, double* out) {
         return PARM_OK;
     }
     if (S->prec == PREC_FP64) launch_eval64(S->c, S->st, what);
-    else launch_eval32(S->c, S->st, what);
+    else {
+        TRY(S->rowmajor());
+        launch_eval32(S->c, S->st, what);
+    }
     CUDA_TRY(cudaGetLastError());
     std::vector<double> v;
     TRY(S->reduce_sys(ncomp, v));
@@ -1160,27 +1345,73 @@ int parm_get_nlist_capacity(parm_system* S, uint32_t* maxnb) {
     return PARM_OK;
 }
 
+// switch the mixed path between the cell-block kernels and the gather /
+// tiled kernels, converting the current lists (same pairs)
+static int set_staged(parm_system* S, bool on) {
+    if (on == (S->c.staged != 0)) return PARM_OK;
+    if (on) {
+        if (!S->stg_ok) return fail(PARM_ERR_ARG, "the cell-block kernel needs >= 3 cells per axis in every system");
+        if (S->stg_pending) return PARM_OK;   // switches after the next rebuild of every system
+        launch_compress_stg(S->c, S->st);
+        S->c.staged = 1;
+    } else {
+        launch_expand_stg(S->c, S->st);
+        S->c.staged = 0;
+    }
+    CUDA_TRY(cudaGetLastError());
+    S->clear_graphs();
+    return S->sync_status();
+}
+
 int parm_set_threads_per_atom(parm_system* S, uint32_t tpa) {
     if (!S) return fail(PARM_ERR_ARG, "NULL handle");
-    // 1, 2, 4: shared-memory tiled kernel; 101, 104, 108, 116, 132: gather
-    // kernel with 1..32 threads per atom
+    // 200: cell-block kernel (shared-memory staging); 1, 2, 4: tiled kernel;
+    // 101, 104, 108, 116, 132: gather kernel with 1..32 threads per atom
+    if (tpa == 200) {
+        if (S->prec != PREC_MIXED) return PARM_OK;
+        TRY(S->flush());
+        S->want_staged = true;
+        return set_staged(S, true);
+    }
     const bool tiled = tpa < 100;
     if (tiled && S->prec == PREC_MIXED && !S->c.ntile) return fail(PARM_ERR_ARG, "no tiles in this handle");
-    if (tiled && S->prec == PREC_MIXED && !S->c.tiled) {
-        TRY(S->flush());
+    const uint32_t t = tiled ? tpa : tpa - 100;
+    if (tiled ? !(t == 1 || t == 2 || t == 4) : !(t == 1 || t == 4 || t == 8 || t == 16 || t == 32))
+        return fail(PARM_ERR_ARG, "threads per atom: 200 (cell blocks), 1, 2, 4 (tiled) or 101, 104, 108, 116, "
+                                  "132 (gather)");
+    if (S->prec != PREC_MIXED) return PARM_OK;
+    TRY(S->flush());
+    S->want_staged = false;
+    S->stg_pending = false;
+    TRY(set_staged(S, false));
+    if (tiled && !S->c.tiled) {
         launch_tiles(S->c, S->st, 1);   // tiles for the current lists
         TRY(S->sync_status());
     }
-    const uint32_t t = tiled ? tpa : tpa - 100;
-    if (tiled ? !(t == 1 || t == 2 || t == 4) : !(t == 1 || t == 4 || t == 8 || t == 16 || t == 32))
-        return fail(PARM_ERR_ARG, "threads per atom: 1, 2, 4 (tiled) or 101, 104, 108, 116, 132 (gather)");
-    if (S->prec != PREC_MIXED) return PARM_OK;
     if (S->c.tpa != t || S->c.tiled != (uint32_t)tiled || S->c.unr != 1) {
         S->c.tpa = t;
         S->c.tiled = tiled ? 1u : 0u;
         S->c.unr = 1;
         S->clear_graphs();
     }
+    return PARM_OK;
+}
+
+int parm_get_threads_per_atom(parm_system* S, uint32_t* tpa) {
+    if (!S || !tpa) return fail(PARM_ERR_ARG, "NULL argument");
+    if (S->prec != PREC_MIXED) *tpa = 101;
+    else if (S->c.staged) *tpa = 200;
+    else *tpa = S->c.tiled ? S->c.tpa : 100 + S->c.tpa;
+    return PARM_OK;
+}
+
+int parm_debug_stage_cap(parm_system* S, uint32_t cap) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (cap > 4096) return fail(PARM_ERR_ARG, "stage capacity above 4096 atoms");
+    TRY(S->flush());
+    S->stage_cap_override = cap;
+    TRY(S->plan_blocks());
+    S->clear_graphs();
     return PARM_OK;
 }
 
@@ -1197,16 +1428,36 @@ int parm_autotune(parm_system* S, uint32_t* tpa_out) {
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
-    // (tiled, threads per atom, neighbours per iteration)
-    const uint32_t cands[][3] = {{1, 1, 1}, {1, 2, 1}, {1, 4, 1}, {0, 1, 1}, {0, 1, 2}, {0, 4, 1},
-                                 {0, 8, 1}, {0, 16, 1}};
-    const uint32_t keep = S->c.tpa, keep_u = S->c.unr, keep_t = S->c.tiled;
+    // (kind: 2 cell blocks, 1 tiled, 0 gather; threads per atom; neighbours per iteration)
+    const uint32_t cands[][3] = {{2, 1, 1}, {1, 1, 1}, {1, 2, 1}, {1, 4, 1}, {0, 1, 1}, {0, 1, 2},
+                                 {0, 4, 1}, {0, 8, 1}, {0, 16, 1}};
+    const uint32_t keep = S->c.tpa, keep_u = S->c.unr, keep_t = S->c.staged ? 2u : S->c.tiled;
+    const bool can_stage = S->stg_ok && !S->stg_pending;
+    // both list formats for the comparison
+    if (S->c.staged) {
+        launch_expand_stg(S->c, S->st);
+    } else if (can_stage) {
+        launch_compress_stg(S->c, S->st);
+    }
+    CUDA_TRY(cudaGetLastError());
     float best = 1e30f;
     uint32_t pick = keep, pick_u = keep_u, pick_t = keep_t;
-    if (S->c.ntile && !S->c.tiled) launch_tiles(S->c, S->st, 1);
+    // the tiled variants rebuild their tiles at every list rebuild: charge
+    // that cost, spread over an assumed 10 steps between rebuilds
+    float tile_ms = 0.f;
+    if (S->c.ntile) {
+        launch_tiles(S->c, S->st, 1);
+        CUDA_TRY(cudaEventRecord(e0, S->st));
+        launch_tiles(S->c, S->st, 1);
+        CUDA_TRY(cudaEventRecord(e1, S->st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        CUDA_TRY(cudaEventElapsedTime(&tile_ms, e0, e1));
+    }
     for (const auto& cu : cands) {
-        if (cu[0] && !S->c.ntile) continue;
-        S->c.tiled = cu[0];
+        if (cu[0] == 2 && !can_stage) continue;
+        if (cu[0] == 1 && !S->c.ntile) continue;
+        S->c.staged = cu[0] == 2 ? 1u : 0u;
+        S->c.tiled = cu[0] == 1 ? 1u : 0u;
         S->c.tpa = cu[1];
         S->c.unr = cu[2];
         launch_force32(S->c, S->st, FM_FORCES);   // warm-up
@@ -1216,6 +1467,7 @@ int parm_autotune(parm_system* S, uint32_t* tpa_out) {
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0.f;
         CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        ms = ms / 3.f + (cu[0] == 1 ? tile_ms / 10.f : 0.f);
         if (ms < best) {
             best = ms;
             pick_t = cu[0];
@@ -1225,13 +1477,15 @@ int parm_autotune(parm_system* S, uint32_t* tpa_out) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    S->c.staged = pick_t == 2 ? 1u : 0u;
+    S->c.tiled = pick_t == 1 ? 1u : 0u;
     S->c.tpa = pick;
     S->c.unr = pick_u;
-    S->c.tiled = pick_t;
+    S->want_staged = pick_t == 2;
     CUDA_TRY(cudaMemcpyAsync(S->c.f32, S->c.f32b, sizeof(float4) * (size_t)S->n, cudaMemcpyDeviceToDevice,
                              S->st));
     if (pick != keep || pick_u != keep_u || pick_t != keep_t) S->clear_graphs();
-    if (tpa_out) *tpa_out = pick_t * 1000 + pick * 10 + pick_u;
+    if (tpa_out) *tpa_out = pick_t == 2 ? 2000u : pick_t * 1000 + pick * 10 + pick_u;
     return S->sync_status();
 }
 

@@ -110,7 +110,7 @@ __device__ __forceinline__ void kick(const DevCtx& c, uint32_t i, double m, doub
     }
     const double h = (MODE == DM_VERLET) ? P.dt_half : P.dtc2;
 #pragma unroll
-    for (int d = 0; d < ND; d++) v[d] = v[d] + a[d] * h;
+    for (int d = 0; d < ND; d++) v[d] = MIXED ? __fma_rn(a[d], h, v[d]) : v[d] + a[d] * h;
 }
 
 // Fused time-step kernel: [kick of the previous step] + drift of this step +
@@ -145,6 +145,17 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
         if (!mob) {
 #pragma unroll
             for (int d = 0; d < ND; d++) v[d] = 0.0;
+        } else if constexpr (MIXED && MODE != DM_SOL) {
+            // the mixed path contracts the same FP64 updates into fused
+            // multiply-adds (half the FP64 operations; it is not bit-exact)
+            const double cv = MODE == DM_VERLET ? P.dt : P.c1dt;
+            const double ca = MODE == DM_VERLET ? P.dt2_half : P.c2dtdt;
+#pragma unroll
+            for (int d = 0; d < ND; d++) {
+                x[d] = __fma_rn(v[d], cv, __fma_rn(a[d], ca, x[d]));
+                v[d] = MODE == DM_VERLET ? __fma_rn(a[d], P.dt_half, v[d])
+                                         : __fma_rn(a[d], P.dtc12, v[d] * P.c0);
+            }
         } else if constexpr (MODE == DM_VERLET) {
             // x += v*dt + a*(dt*dt/2); v += a*(dt/2)
 #pragma unroll
@@ -198,7 +209,18 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
             c.pos[2 * (size_t)i + 1] = B;
         }
         if (c.rank[i] != NOT_MEMBER) {
-            dsq = disp_sq<ND>(xv, static_cast<const V*>(c.lastloc)[i]);
+            const V l = static_cast<const V*>(c.lastloc)[i];
+            if constexpr (MIXED) {
+                const double* lp = reinterpret_cast<const double*>(&l);
+                const double d0 = x[0] - lp[0], d1 = x[1] - lp[1];
+                dsq = __fma_rn(d1, d1, d0 * d0);
+                if constexpr (ND == 3) {
+                    const double d2 = x[2] - lp[2];
+                    dsq = __fma_rn(d2, d2, dsq);
+                }
+            } else {
+                dsq = disp_sq<ND>(xv, l);
+            }
             valid = !(dsq != dsq);
         }
     }
@@ -398,44 +420,72 @@ void launch_reduce_atoms(const DevCtx& c, cudaStream_t s, int what, const double
     else k_atoms<2><<<grid_for(c.n), BLOCK, 0, s>>>(c, what, origin);
 }
 
-// deterministic per-system reduction of red[comp * n + i] over each system's
-// atoms (one CTA per system, fixed striding and tree order).  ncomp < 0 means
-// a single-component maximum.
-__global__ void __launch_bounds__(1024) k_sys_reduce(DevCtx c, int ncomp) {
-    uint32_t s = blockIdx.x;
-    const SysConst& S = c.sys[s];
+// Deterministic per-system reduction of red[comp * n + i] over each system's
+// atoms in two passes with a fixed order: every chunk of up to RED_CHUNK
+// consecutive atoms of one system is reduced by one CTA (fixed striding and
+// tree), then one CTA per system reduces its chunks in chunk order.  ncomp < 0
+// means a single-component maximum.
+template <int NT>
+__device__ __forceinline__ double block_reduce(double acc, bool is_max, double* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_down_sync(0xFFFFFFFFu, acc, off);
+        acc = is_max ? fmax(acc, o) : acc + o;
+    }
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    double v = 0.0;
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < NT / 32 ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double o = __shfl_down_sync(0xFFFFFFFFu, v, off);
+            v = is_max ? fmax(v, o) : v + o;
+        }
+    }
+    __syncthreads();
+    return v;   // valid in thread 0
+}
+
+constexpr int RED_THREADS = 256;
+
+__global__ void __launch_bounds__(RED_THREADS) k_red_chunks(DevCtx c, int ncomp) {
     __shared__ double sh[32];
+    const uint4 ch = c.chunk[blockIdx.x];   // (system, first atom, atoms, -)
     const bool is_max = ncomp < 0;
     const int nc = is_max ? 1 : ncomp;
     for (int comp = 0; comp < nc; comp++) {
-        const double* r = c.red + (size_t)comp * c.n + S.atom_off;
+        const double* r = c.red + (size_t)comp * c.n + ch.y;
         double acc = 0.0;
-        for (uint32_t k = threadIdx.x; k < S.natoms; k += blockDim.x) {
-            double v = r[k];
+        for (uint32_t k = threadIdx.x; k < ch.z; k += RED_THREADS) {
+            const double v = r[k];
             acc = is_max ? fmax(acc, v) : acc + v;
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            double o = __shfl_down_sync(0xFFFFFFFFu, acc, off);
-            acc = is_max ? fmax(acc, o) : acc + o;
+        acc = block_reduce<RED_THREADS>(acc, is_max, sh);
+        if (threadIdx.x == 0) c.part[(size_t)blockIdx.x * nc + comp] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_sys_reduce(DevCtx c, int ncomp) {
+    __shared__ double sh[32];
+    const uint32_t s = blockIdx.x;
+    const bool is_max = ncomp < 0;
+    const int nc = is_max ? 1 : ncomp;
+    const uint32_t k0 = c.sys_chunk[s], k1 = c.sys_chunk[s + 1];
+    for (int comp = 0; comp < nc; comp++) {
+        double acc = 0.0;
+        for (uint32_t k = k0 + threadIdx.x; k < k1; k += RED_THREADS) {
+            const double v = c.part[(size_t)k * nc + comp];
+            acc = is_max ? fmax(acc, v) : acc + v;
         }
-        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            double v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                double o = __shfl_down_sync(0xFFFFFFFFu, v, off);
-                v = is_max ? fmax(v, o) : v + o;
-            }
-            if (threadIdx.x == 0) c.sysout[(size_t)s * nc + comp] = v;
-        }
-        __syncthreads();
+        acc = block_reduce<RED_THREADS>(acc, is_max, sh);
+        if (threadIdx.x == 0) c.sysout[(size_t)s * nc + comp] = acc;
     }
 }
 
 void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp) {
-    k_sys_reduce<<<c.nsys, 1024, 0, s>>>(c, ncomp);
+    k_red_chunks<<<c.nchunk, RED_THREADS, 0, s>>>(c, ncomp);
+    k_sys_reduce<<<c.nsys, RED_THREADS, 0, s>>>(c, ncomp);
 }
 
 }  // namespace parm

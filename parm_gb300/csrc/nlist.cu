@@ -764,6 +764,17 @@ void launch_rebuild(const DevCtx& c, cudaStream_t s) {
     k_scan_write<<<nblk, SCAN_THREADS, 0, s>>>(c);
     k_scatter<<<ga, BLOCK, 0, s>>>(c);
     k_cellsort<<<grid_for(c.nbucket), BLOCK, 0, s>>>(c);
+    if (c.staged) {
+        if (c.nd == 3) {
+            k_gather<3><<<ga, BLOCK, 0, s>>>(c);
+            k_copyback<3><<<ga, BLOCK, 0, s>>>(c);
+        } else {
+            k_gather<2><<<ga, BLOCK, 0, s>>>(c);
+            k_copyback<2><<<ga, BLOCK, 0, s>>>(c);
+        }
+        launch_build_stg(c, s);
+        return;
+    }
     if (c.nd == 3) {
         k_gather<3><<<ga, BLOCK, 0, s>>>(c);
         k_copyback<3><<<ga, BLOCK, 0, s>>>(c);

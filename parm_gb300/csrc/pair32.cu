@@ -13,18 +13,11 @@
 #include <algorithm>
 
 #include "parm_check.cuh"
+#include "parm_pair32.cuh"
 
 namespace parm {
 
 __device__ __forceinline__ bool mobile32(double m) { return !(m <= 0.0 || isinf(m)); }
-
-// The reference's truncated LJ force jumps by ~0.044 eps/sigma at the cut-off
-// (LennardJonesCut::forces, src/interaction.hpp:263-271: zero for
-// rsq > cut^2).  A pair whose FP32 rsq lies within 4e-6 (relative) of cut^2 is
-// therefore classified with the exact FP64 test of the reference, so the set
-// of interacting pairs is identical to the FP64 path's.  (RepulsionPair and
-// LJRepulsive forces vanish continuously at their cut-offs.)
-constexpr float CUT_BAND = 4e-6f;
 
 __device__ __noinline__ bool lj_beyond_exact(const DevCtx& c, const SysConst& S, uint32_t i, uint32_t j,
                                              int nd) {
@@ -43,52 +36,6 @@ __device__ __noinline__ bool lj_beyond_exact(const DevCtx& c, const SysConst& S,
     double cut = B.p2 > A.p2 ? B.p2 : A.p2;
     double rsq = __ddiv_rn(dsq, __dmul_rn(sig, sig));
     return rsq > __dmul_rn(cut, cut);
-}
-
-// FP32 pair law; returns the force scale s (F = r * s), 0 beyond the cut-off.
-// isig2 = 1/sigma_ij^2; e12 = 12*eps_ij (LJ kinds) or eps_ij (repulsion).
-template <int KIND>
-__device__ __forceinline__ float scale32(float d2, float e12, float sig, float isig2, float third,
-                                         bool& near_cut) {
-    near_cut = false;
-    if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
-        const float rsq = d2 * isig2;
-        const float cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
-        if constexpr (KIND == KIND_LJCUT) near_cut = fabsf(rsq - cut2) <= CUT_BAND * cut2;
-        const float ir = __fdividef(1.0f, rsq);
-        const float ir3 = ir * ir * ir;   // 1 / rsix
-        const float sc = e12 * ir3 * (ir3 - 1.0f) * ir * isig2;   // fmagTimesR / dsq
-        return rsq > cut2 ? 0.0f : sc;
-    } else {
-        if (d2 > sig * sig) return 0.0f;
-        const float R = sqrtf(d2);
-        const float isig = __fdividef(1.0f, sig);
-        const float b = 1.0f - R * isig;
-        float pw;
-        if (third == 2.0f) pw = b;
-        else if (third == 2.5f) pw = b * sqrtf(b);
-        else pw = powf(b, third - 1.0f);
-        return e12 * pw * isig * __fdividef(1.0f, R);
-    }
-}
-
-template <int KIND>
-__device__ __forceinline__ float energy32(float d2, float eps, float sig, float third, float m6) {
-    if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
-        float rsq = d2 / (sig * sig);
-        float cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
-        if (rsq > cut2) return 0.0f;
-        float ir3 = 1.0f / (rsq * rsq * rsq);
-        float mid = 1.0f - ir3;
-        if constexpr (KIND == KIND_LJCUT) return eps * (mid * mid - 1.0f) - eps * (m6 * m6 - 1.0f);
-        else return eps * (mid * mid);
-    } else {
-        if (d2 > sig * sig) return 0.0f;
-        float R = sqrtf(d2);
-        float b = 1.0f - R / sig;
-        float pw = (third == 2.0f) ? b * b : powf(b, third);
-        return eps * pw / third;
-    }
 }
 
 template <int ND>
@@ -496,7 +443,9 @@ static void force32_nd(const DevCtx& c, cudaStream_t s, int mode) {
 }
 
 void launch_force32(const DevCtx& c, cudaStream_t s, int mode) {
-    if (c.nd == 3) force32_nd<3>(c, s, mode); else force32_nd<2>(c, s, mode);
+    if (c.staged) launch_force_stg(c, s, mode);
+    else if (c.nd == 3) force32_nd<3>(c, s, mode);
+    else force32_nd<2>(c, s, mode);
 }
 
 template <int ND>

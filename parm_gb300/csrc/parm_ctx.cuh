@@ -103,6 +103,16 @@ struct DevCtx {
     uint16_t* tile_lst;           // [t * maxnb * TILE_ATOMS + k * TILE_ATOMS + a]
     uint32_t* atom_img;           // image of each atom in its tile's frame (4-bit signed per axis)
 
+    // cell-block kernels of the mixed path (staged.cu): blocks of Kx x Ky
+    // cells whose neighbourhood is staged in shared memory; 16-bit lists
+    uint32_t staged;      // use them (every system has >= 3 cells per axis)
+    uint32_t nblk;        // blocks over all systems
+    uint32_t stg_cap;     // atoms staged in shared memory per block
+    uint32_t stg_prm;     // force kernel: 0 uniform parameters, 1 per-atom sigma, 2 all per atom
+    uint32_t stg_dia;     // list build: per-atom list diameters
+    const uint4* blk;     // per block: (system, x0 | x1 << 16, y0 | y1 << 16, z)
+    uint16_t* nbr16;      // staged lists (layout in staged.cu)
+
     // exclusions (NeighborList::ignore), CSR keyed by caller index
     const uint32_t* excl_off;   // n + 1 entries, or null when no exclusions
     const uint32_t* excl_list;
@@ -121,6 +131,10 @@ struct DevCtx {
     // reduction scratch
     double* red;          // per-atom scratch (up to 12 doubles per atom)
     double* sysout;       // per-system outputs
+    uint32_t nchunk;      // reduction chunks (up to RED_CHUNK atoms of one system)
+    const uint4* chunk;   // (system, first atom, atoms, 0)
+    const uint32_t* sys_chunk;   // first chunk of each system (nsys + 1)
+    double* part;         // per-chunk partials (up to 12 per chunk)
 };
 
 // capi.cu: store the error text returned by parm_last_error(); returns code
@@ -149,6 +163,12 @@ void launch_force64(const DevCtx& c, cudaStream_t s, int mode);
 void launch_force32(const DevCtx& c, cudaStream_t s, int mode);
 void launch_eval64(const DevCtx& c, cudaStream_t s, int what);
 void launch_eval32(const DevCtx& c, cudaStream_t s, int what);
+// staged.cu (mixed path, cell blocks)
+void launch_build_stg(const DevCtx& c, cudaStream_t s);
+void launch_force_stg(const DevCtx& c, cudaStream_t s, int mode);
+void launch_expand_stg(const DevCtx& c, cudaStream_t s);     // staged lists -> nbr (row-major)
+void launch_compress_stg(const DevCtx& c, cudaStream_t s);   // nbr (row-major) -> staged lists
+int stg_set_smem_limits();   // cudaError_t of raising the kernels' shared-memory limits
 // debug entry used by the tests of the minimum-image routine
 void launch_remainder_test(const double* d, const double* L, double* out, uint32_t n,
                            cudaStream_t s);
@@ -170,9 +190,16 @@ enum AtomWhat : int {
 };
 
 constexpr int BLOCK = 256;
+constexpr uint32_t RED_CHUNK = 4096;   // atoms per reduction chunk
 constexpr int TILE_ATOMS = 64;
 constexpr int TILE_ECAP = 1024;
 constexpr int TILE_HASH = 4096;
+// cell blocks: at most STG_KY_MAX cell rows along y per block
+constexpr int STG_KY_MAX = 6;
+constexpr int STG_ROWS_MAX = 3 * (STG_KY_MAX + 2);
+constexpr int STG_PIECES_MAX = 3 * STG_ROWS_MAX;
+constexpr int STG_KX_MAX = 32;
+constexpr int STG_THREADS_HOST = 128;   // threads per block of the cell-block kernels
 
 inline unsigned grid_for(uint32_t n, int block = BLOCK) {
     unsigned g = (unsigned)((n + block - 1) / block);

@@ -42,6 +42,7 @@ struct SysConst {
     double invL[3];
     double halfL[3];
     float Lhi[3], Llo[3], invLf[3];
+    float L8[3], Lr8[3];   // L rounded to the 1/8 grid (exact in FP32) and L - L8
     double skin;
     double rlist_max;   // largest (d_i + d_j)/2 + skin
     int nc[3];          // cells per axis (1 or >= 3)

@@ -1,0 +1,820 @@
+// Mixed-precision cell-block kernels: list build, pair forces and list
+// expansion with the neighbourhood of a block of cells staged in shared memory.
+//
+// Reference behaviour (wackywendell/parm): NeighborList::update_list
+// (src/trackers.cpp:19-85) keeps every pair with
+// |diff(x_i, x_j)| < (d_i + d_j)/2 + skin; NListed::set_forces
+// (src/interaction.hpp:2165-2175) adds the pair force of every listed pair.
+// The pair set here is the reference's exactly (FP32 screening, exact FP64
+// test near the threshold); forces are FP32 sums, as in pair32.cu.
+//
+// Blocks.  A system whose cell grid has at least 3 cells along every axis is
+// cut into blocks of Kx x Ky cells of one z layer (x fastest, the order of
+// the cells in memory).  The block's neighbourhood is made of "rows": the
+// cells x0-1 .. x1 of the y rows y0-1 .. y1 in the z layers z-1, z, z+1
+// (2D: no z).  Each row is three "pieces" (left cell, the block's own cells,
+// right cell), each a contiguous range of atoms in memory with one periodic
+// image; pieces are numbered row by row and their atoms get consecutive local
+// indices.  Kx <= nx - 2 and Ky <= ny - 2, so no atom appears twice in a
+// block's neighbourhood.
+//
+// Staged record (16 bytes) of atom j in the frame of block origin C (a point
+// of the 1/8 grid): the image n of j that lies next to its piece is
+// n = round((P - X_j) / L) (P: the piece's unwrapped centre); the coarse part
+// q = 8 * (X_j + n L8 - C) is an exact integer in [-256, 255] (L8: L rounded
+// to the 1/8 grid), stored as q + 256 in three 10-bit slots of one word; the
+// fine part xf_j + n (L - L8) is FP32.  A pair displacement is then
+// 0.125 * (q_i - q_j) + (f_i - f_j): the coarse difference is exact and only
+// the fine parts round, the accuracy of the coarse/fine split of the gather
+// kernel.  One 32-bit subtraction (W_i + 512 per slot) - W_j forms the three
+// biased differences at once (each in [1, 1023], so no borrow crosses a
+// slot), and OR-ing a slot into the mantissa of 1.5 * 2^20 (ulp 1/8) turns it
+// into 1.5 * 2^20 + (q_i - q_j + 512) / 8 exactly.
+//
+// The list build only screens candidates, so it stages plain FP32 positions
+// relative to C (0.125 q + f, one rounding); pairs within 2e-5 (relative, on
+// r^2) of the threshold are decided by the exact FP64 test.
+//
+// Lists.  Entries are 16-bit local indices.  The home atoms of a block are the
+// atoms of its own pieces in the z = 0 layer (one contiguous range of memory
+// per home row).  For a home row starting at atom s0 with H atoms, entry k of
+// home atom s0 + h lives at u16 offset s0 * maxnb + (k / 2) * 2H + 2h + k % 2,
+// so a warp reads the entries of 32 consecutive atoms as one coalesced line of
+// 32-bit words (two entries each).
+#include "parm_check.cuh"
+#include "parm_pair32.cuh"
+
+namespace parm {
+
+constexpr int STG_THREADS = STG_THREADS_HOST;
+constexpr float STG_BAND = 2e-5f;   // relative band on r^2 decided by the exact FP64 test
+constexpr float CUT_BAND_S = 4e-6f; // LJ cut-off band (see pair32.cu)
+
+struct StgTable {
+    uint32_t g0[STG_PIECES_MAX];        // first atom of each piece
+    uint32_t cnt[STG_PIECES_MAX];       // atoms in each piece
+    uint32_t off[STG_PIECES_MAX + 1];   // local index of the first atom of each piece
+    float P[STG_PIECES_MAX][3];         // unwrapped centre of each piece
+    uint32_t rowbase[STG_ROWS_MAX];     // bucket of cell x = 0 of each row
+    uint32_t hoff[STG_KY_MAX + 1];      // home atoms before each home row
+    float C[3];                         // block frame origin (1/8 grid)
+    uint32_t nrow, npiece, total, nhome, nyr;
+    int x0, x1, y0, y1, z;
+};
+
+__device__ __forceinline__ int wrap_idx(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// fill the block table (all threads; ends with a barrier)
+template <int ND>
+__device__ void stg_setup(const DevCtx& c, const SysConst& S, const uint4& bd, StgTable& T) {
+    const int x0 = (int)(bd.y & 0xFFFFu), x1 = (int)(bd.y >> 16);
+    const int y0 = (int)(bd.z & 0xFFFFu), y1 = (int)(bd.z >> 16);
+    const int z = (int)bd.w;
+    const int nyr = y1 - y0 + 2;
+    const int nrow = (ND == 3 ? 3 : 1) * nyr;
+    const uint32_t b0 = c.bucket_off[bd.x];
+    const int nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
+    for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+        const int dz = (ND == 3) ? r / nyr - 1 : 0;
+        const int yy = y0 - 1 + r % nyr;
+        const int cy = wrap_idx(yy, ny), cz = (ND == 3) ? wrap_idx(z + dz, nz) : 0;
+        const uint32_t rb = b0 + (uint32_t)((cz * ny + cy) * nx);
+        T.rowbase[r] = rb;
+        const float py = ((float)yy + 0.5f) * S.cellw32[1];
+        const float pz = (ND == 3) ? ((float)(z + dz) + 0.5f) * S.cellw32[2] : 0.f;
+        const uint32_t cl = (uint32_t)wrap_idx(x0 - 1, nx), cr = (uint32_t)wrap_idx(x1, nx);
+        const uint32_t gl = c.cell_start[rb + cl], gm = c.cell_start[rb + (uint32_t)x0],
+                       gr = c.cell_start[rb + cr];
+        T.g0[3 * r] = gl;
+        T.cnt[3 * r] = c.cell_start[rb + cl + 1] - gl;
+        T.g0[3 * r + 1] = gm;
+        T.cnt[3 * r + 1] = c.cell_start[rb + (uint32_t)x1] - gm;
+        T.g0[3 * r + 2] = gr;
+        T.cnt[3 * r + 2] = c.cell_start[rb + cr + 1] - gr;
+        const float px[3] = {((float)x0 - 0.5f) * S.cellw32[0], 0.5f * (float)(x0 + x1) * S.cellw32[0],
+                             ((float)x1 + 0.5f) * S.cellw32[0]};
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            T.P[3 * r + p][0] = px[p];
+            T.P[3 * r + p][1] = py;
+            T.P[3 * r + p][2] = pz;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int p = 0; p < 3 * nrow; p++) {
+            T.off[p] = acc;
+            acc += T.cnt[p];
+        }
+        T.off[3 * nrow] = acc;
+        T.total = acc;
+        T.nrow = (uint32_t)nrow;
+        T.npiece = (uint32_t)(3 * nrow);
+        T.nyr = (uint32_t)nyr;
+        T.x0 = x0; T.x1 = x1; T.y0 = y0; T.y1 = y1; T.z = z;
+        const int hbase = (ND == 3) ? nyr : 0;   // first home row (z layer 0, y = y0)
+        uint32_t h = 0;
+        for (int hr = 0; hr < y1 - y0; hr++) {
+            T.hoff[hr] = h;
+            h += T.cnt[3 * (hbase + hr + 1) + 1];
+        }
+        T.hoff[y1 - y0] = h;
+        T.nhome = h;
+        // frame origin: the block's centre rounded to the 1/8 grid
+        const double cx = 0.5 * (double)(x0 + x1) * S.cellw[0];
+        const double cy = 0.5 * (double)(y0 + y1) * S.cellw[1];
+        const double cz = (ND == 3) ? ((double)z + 0.5) * S.cellw[2] : 0.0;
+        T.C[0] = (float)(rint(cx * 8.0) * 0.125);
+        T.C[1] = (float)(rint(cy * 8.0) * 0.125);
+        T.C[2] = (float)(rint(cz * 8.0) * 0.125);
+    }
+    __syncthreads();
+}
+
+// the staged record of atom j seen from piece centre P
+template <int ND>
+__device__ __forceinline__ float4 stg_record(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                             uint32_t j, const float* P) {
+    const float kShift = 12582912.0f;
+    float4 A, B;
+    ld_pos(c.pos, j, A, B);
+    const float X[3] = {A.x, A.y, A.z}, F[3] = {B.x, B.y, B.z};
+    float fo[3] = {0.f, 0.f, 0.f};
+    uint32_t packed = 0;
+    bool bad = false;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        const float n = __fsub_rn(__fmaf_rn(P[d] - X[d], S.invLf[d], kShift), kShift);
+        const float u = __fmaf_rn(n, S.L8[d], __fsub_rn(X[d], T.C[d]));   // exact
+        fo[d] = __fmaf_rn(n, S.Lr8[d], F[d]);
+        int q = __float2int_rn(u * 8.0f);
+        bad |= !(fabsf(X[d]) < 1048576.0f) || q < -256 || q > 255;
+        q = q < -256 ? -256 : (q > 255 ? 255 : q);
+        packed |= (uint32_t)(q + 256) << (10 * d);
+    }
+    if (bad) atomicOr(c.status, ST_IMAGE_RANGE);
+    return make_float4(fo[0], fo[1], fo[2], __uint_as_float(packed));
+}
+
+// piece of local index q (binary search over the offsets)
+__device__ __forceinline__ uint32_t stg_piece(const StgTable& T, uint32_t q) {
+    uint32_t lo = 0, hi = T.npiece;   // off[lo] <= q < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.off[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t stg_global(const StgTable& T, uint32_t q) {
+    const uint32_t p = stg_piece(T, q);
+    return T.g0[p] + (q - T.off[p]);
+}
+
+// a local index that does not belong to the block (inconsistent lists) is
+// reported and replaced by the home atom itself, whose pair term is zero
+__device__ __forceinline__ uint32_t stg_check(const DevCtx& c, const StgTable& T, uint32_t q, uint32_t qi) {
+    if (q < T.total) return q;
+    atomicOr(c.status, ST_TILE_OVERFLOW);
+    return qi;
+}
+
+// record of local index q: shared memory, or rebuilt from global memory when
+// the neighbourhood is larger than the staging capacity
+template <int ND>
+__device__ __forceinline__ float4 stg_get(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                          const float4* srec, uint32_t cap, uint32_t q) {
+    if (q < cap) return srec[q];
+    const uint32_t p = stg_piece(T, q);
+    return stg_record<ND>(c, S, T, T.g0[p] + (q - T.off[p]), T.P[p]);
+}
+
+constexpr uint32_t STG_GUARD = 256u | (256u << 10) | (256u << 20);   // + 256 per slot
+constexpr uint32_t STG_MANT = 0x49C00000u;                           // 1.5 * 2^20, ulp 1/8
+constexpr float STG_K = 1572864.0f + 64.0f;                          // 1.5 * 2^20 + 512 / 8
+
+// W_i + 512 per slot (the home atom's side of the packed subtraction)
+__device__ __forceinline__ uint32_t stg_wi(const float4& ri) { return __float_as_uint(ri.w) + 2u * STG_GUARD; }
+
+// displacement x_i - x_j from two packed records
+template <int ND>
+__device__ __forceinline__ void stg_disp(uint32_t wi, const float4& ri, const float4& rj, float* r) {
+    const uint32_t D = wi - __float_as_uint(rj.w);
+    r[0] = (__uint_as_float((D & 0x3FFu) | STG_MANT) - STG_K) + (ri.x - rj.x);
+    r[1] = (__uint_as_float(((D >> 10) & 0x3FFu) | STG_MANT) - STG_K) + (ri.y - rj.y);
+    if constexpr (ND == 3) r[2] = (__uint_as_float((D >> 20) | STG_MANT) - STG_K) + (ri.z - rj.z);
+    else r[2] = 0.f;
+}
+
+// plain FP32 position relative to the block origin (list screening)
+__device__ __forceinline__ float4 stg_plain(const float4& rec, float w) {
+    const uint32_t W = __float_as_uint(rec.w);
+    const float qx = (float)((int)(W & 0x3FFu) - 256), qy = (float)((int)((W >> 10) & 0x3FFu) - 256),
+                qz = (float)((int)(W >> 20) - 256);
+    return make_float4(fmaf(qx, 0.125f, rec.x), fmaf(qy, 0.125f, rec.y), fmaf(qz, 0.125f, rec.z), w);
+}
+
+// warp-per-piece staging of the first `cap` local indices; EXTRA: 0 nothing,
+// 1 one float per atom (sigma), 2 the FP32 pair parameters; `plain`: FP32
+// positions with the list diameter in w instead of packed records
+template <int ND, int EXTRA>
+__device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec, void* sext,
+                         uint32_t cap, int ext_sigma, bool plain = false) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t p = warp; p < T.npiece; p += nw) {
+        const uint32_t o = T.off[p], n = T.cnt[p], g = T.g0[p];
+        if (o >= cap) break;
+        const float P[3] = {T.P[p][0], T.P[p][1], T.P[p][2]};
+        for (uint32_t t = lane; t < n; t += 32) {
+            const uint32_t q = o + t;
+            if (q >= cap) break;
+            const float4 rec = stg_record<ND>(c, S, T, g + t, P);
+            if (plain) {
+                srec[q] = stg_plain(rec, c.pos[2 * (size_t)(g + t)].w);
+                continue;
+            }
+            srec[q] = rec;
+            if constexpr (EXTRA == 1) {
+                // list diameter (build) or sigma (forces)
+                static_cast<float*>(sext)[q] = ext_sigma ? c.prm32[g + t].y : c.pos[2 * (size_t)(g + t)].w;
+            } else if constexpr (EXTRA == 2) {
+                static_cast<float4*>(sext)[q] = c.prm32[g + t];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// home atom h -> (home row, global atom, local index, cell x)
+struct HomeAtom {
+    uint32_t hr, i, qi, s0, H, hs;
+    int cx;
+};
+
+template <int ND, bool CELL = true>
+__device__ __forceinline__ HomeAtom stg_home(const DevCtx& c, const StgTable& T, uint32_t h) {
+    HomeAtom a;
+    uint32_t hr = 0;
+    while (h >= T.hoff[hr + 1]) hr++;
+    const uint32_t r = (ND == 3 ? T.nyr : 0u) + hr + 1u;
+    const uint32_t p = 3u * r + 1u;
+    a.hr = hr;
+    a.hs = h - T.hoff[hr];
+    a.s0 = T.g0[p];
+    a.H = T.cnt[p];
+    a.i = a.s0 + a.hs;
+    a.qi = T.off[p] + a.hs;
+    a.cx = T.x0;
+    if constexpr (CELL) {
+        a.cx = (int)(c.bucket[a.i] - T.rowbase[r]);
+        if (a.cx < T.x0 || a.cx >= T.x1) {   // never for lists of the current grid
+            atomicOr(c.status, ST_CELL_RANGE);
+            a.cx = T.x0;
+        }
+    }
+    return a;
+}
+
+// local candidate range of a home atom in stencil row r
+__device__ __forceinline__ void stg_range(const DevCtx& c, const StgTable& T, uint32_t r, int cx,
+                                          uint32_t& lo, uint32_t& hi) {
+    const uint32_t pm = 3u * r + 1u;
+    lo = (cx == T.x0) ? T.off[pm - 1] : T.off[pm] + (c.cell_start[T.rowbase[r] + (uint32_t)(cx - 1)] - T.g0[pm]);
+    hi = (cx == T.x1 - 1) ? T.off[pm + 1] + T.cnt[pm + 1]   // through the right piece
+                          : T.off[pm] + (c.cell_start[T.rowbase[r] + (uint32_t)(cx + 2)] - T.g0[pm]);
+}
+
+__device__ __forceinline__ size_t stg_entry16(const HomeAtom& a, uint32_t maxnb, uint32_t k) {
+    return (size_t)a.s0 * maxnb + (size_t)(k >> 1) * 2u * a.H + 2u * a.hs + (k & 1u);
+}
+
+// exact reference list test, explicit round-to-nearest FP64 operations:
+// diff(x_i, x_j).norm() < (d_i + d_j)/2 + skin
+template <int ND>
+__device__ __noinline__ bool keep_exact_rn(const DevCtx& c, const SysConst& S, uint32_t i, uint32_t j) {
+    const double* a = reinterpret_cast<const double*>(c.x) + (size_t)i * (ND == 3 ? 4 : 2);
+    const double* b = reinterpret_cast<const double*>(c.x) + (size_t)j * (ND == 3 ? 4 : 2);
+    double sq[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        const double r = remainder_exact(__dsub_rn(a[d], b[d]), S.L[d], S.invL[d], S.halfL[d]);
+        sq[d] = __dmul_rn(r, r);
+    }
+    double s2 = __dadd_rn(sq[0], sq[1]);
+    if constexpr (ND == 3) s2 = __dadd_rn(s2, sq[2]);
+    const double diam = __dmul_rn(__dadd_rn(c.diam[i], c.diam[j]), 0.5);
+    return __dsqrt_rn(s2) < __dadd_rn(diam, S.skin);
+}
+
+__device__ __forceinline__ bool is_excluded_s(const DevCtx& c, uint32_t oi, uint32_t oj) {
+    for (uint32_t e = c.excl_off[oi]; e < c.excl_off[oi + 1]; e++)
+        if (c.excl_list[e] == oj) return true;
+    return false;
+}
+
+// exact LJ cut-off classification (as lj_beyond_exact in pair32.cu)
+__device__ __noinline__ bool lj_beyond_exact_s(const DevCtx& c, const SysConst& S, uint32_t i, uint32_t j,
+                                               int nd) {
+    const double* xi = reinterpret_cast<const double*>(c.x) + (size_t)i * (nd == 3 ? 4 : 2);
+    const double* xj = reinterpret_cast<const double*>(c.x) + (size_t)j * (nd == 3 ? 4 : 2);
+    double sq[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < nd; d++) {
+        double r = remainder_exact(__dsub_rn(xi[d], xj[d]), S.L[d], S.invL[d], S.halfL[d]);
+        sq[d] = __dmul_rn(r, r);
+    }
+    double dsq = __dadd_rn(sq[0], sq[1]);
+    if (nd == 3) dsq = __dadd_rn(dsq, sq[2]);
+    const AtomPrm A = c.prm[i], B = c.prm[j];
+    const double sig = __dmul_rn(__dadd_rn(A.p1, B.p1), 0.5);
+    const double cut = B.p2 > A.p2 ? B.p2 : A.p2;
+    const double rsq = __ddiv_rn(dsq, __dmul_rn(sig, sig));
+    return rsq > __dmul_rn(cut, cut);
+}
+
+// non-member atoms of a system (no neighbours, zero force)
+__device__ void stg_nonmembers(const DevCtx& c, uint32_t s, int zero_a) {
+    const SysConst& S = c.sys[s];
+    const uint32_t b = c.bucket_off[s] + S.ncell;
+    const uint32_t hi = S.atom_off + S.natoms;
+    const uint32_t lo = max(c.cell_start[b], S.atom_off);
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        c.nnb[i] = 0u;
+        c.f32[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (zero_a) {
+            double* a = static_cast<double*>(c.a) + (size_t)i * (c.nd == 3 ? 4 : 2);
+            for (int d = 0; d < c.nd; d++) a[d] = 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// list build: one CTA per block, one thread per home atom
+// ---------------------------------------------------------------------------
+template <int ND>
+__device__ __forceinline__ float4 stg_get_plain(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                                const float4* sp, uint32_t cap, uint32_t q) {
+    if (q < cap) return sp[q];
+    const uint32_t p = stg_piece(T, q);
+    const uint32_t j = T.g0[p] + (q - T.off[p]);
+    return stg_plain(stg_record<ND>(c, S, T, j, T.P[p]), c.pos[2 * (size_t)j].w);
+}
+
+template <int ND, int DIA, bool FULL>
+__device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                           const float4* sp, uint32_t cap, const HomeAtom& a) {
+    const uint32_t maxnb = c.maxnb;
+    uint16_t* out = c.nbr16;
+    const float skin32 = (float)S.skin;
+    const float4 P = FULL ? sp[a.qi] : stg_get_plain<ND>(c, S, T, sp, cap, a.qi);
+    const float tu = P.w + skin32;
+    const float hiu = tu * tu * (1.0f + STG_BAND), lou = tu * tu * (1.0f - STG_BAND);
+    const uint32_t oi = c.excl_off ? c.orig[a.i] : 0u;
+    uint32_t k = 0;
+#pragma unroll 1
+    for (int dz = 0; dz < (ND == 3 ? 3 : 1); dz++) {
+#pragma unroll 1
+        for (int dy = 0; dy < 3; dy++) {
+            const uint32_t r = (uint32_t)dz * T.nyr + a.hr + (uint32_t)dy;
+            uint32_t lo, hi;
+            stg_range(c, T, r, a.cx, lo, hi);
+#pragma unroll 4
+            for (uint32_t q = lo; q < hi; q++) {
+                const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
+                const float dx = P.x - Q.x, dyv = P.y - Q.y;
+                float rr = fmaf(dyv, dyv, dx * dx);
+                if constexpr (ND == 3) {
+                    const float dzv = P.z - Q.z;
+                    rr = fmaf(dzv, dzv, rr);
+                }
+                float hi2 = hiu, lo2 = lou;
+                if constexpr (DIA) {
+                    const float thr = 0.5f * (P.w + Q.w) + skin32;
+                    hi2 = thr * thr * (1.0f + STG_BAND);
+                    lo2 = thr * thr * (1.0f - STG_BAND);
+                }
+                if (rr > hi2 || q == a.qi) continue;
+                bool keep = rr < lo2;
+                uint32_t j = 0xFFFFFFFFu;
+                if (!keep) {   // rare: the exact reference test
+                    j = stg_global(T, q);
+                    keep = keep_exact_rn<ND>(c, S, a.i, j);
+                }
+                if (keep && c.excl_off) {
+                    if (j == 0xFFFFFFFFu) j = stg_global(T, q);
+                    keep = !is_excluded_s(c, oi, c.orig[j]);
+                }
+                if (!keep) continue;
+                if (k < maxnb) out[stg_entry16(a, maxnb, k)] = (uint16_t)q;
+                k++;
+            }
+        }
+    }
+    if (k > maxnb) {
+        atomicOr(c.status, ST_NBR_OVERFLOW);
+        k = maxnb;
+    }
+    c.nnb[a.i] = k;
+}
+
+template <int ND, int DIA>
+__global__ void __launch_bounds__(STG_THREADS) k_build_stg(DevCtx c) {
+    extern __shared__ float4 smem_b[];
+    __shared__ StgTable T;
+    if (blockIdx.x >= c.nblk) {
+        const uint32_t s = blockIdx.x - c.nblk;
+        if (c.flag[s]) stg_nonmembers(c, s, 0);
+        return;
+    }
+    const uint4 bd = c.blk[blockIdx.x];
+    if (!c.flag[bd.x]) return;
+    const SysConst& S = c.sys[bd.x];
+    stg_setup<ND>(c, S, bd, T);
+    if (T.total > 0xFFFFu) {   // more than 65535 atoms around one block
+        if (threadIdx.x == 0) atomicOr(c.status, ST_TILE_OVERFLOW);
+        return;
+    }
+    const uint32_t cap = c.stg_cap;
+    stg_load<ND, 0>(c, S, T, smem_b, nullptr, cap, 0, true);
+    const bool full = T.total <= cap;
+    for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
+        const HomeAtom a = stg_home<ND>(c, T, h);
+        if (full) build_home<ND, DIA, true>(c, S, T, smem_b, cap, a);
+        else build_home<ND, DIA, false>(c, S, T, smem_b, cap, a);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair forces: one CTA per block, one thread per home atom.  PRM: 0 uniform
+// parameters, 1 per-atom sigma (epsilon and exponent / cut-off uniform),
+// 2 per-atom (sqrt(eps), sigma, third).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// pair-law constants of one pair type
+template <int KIND>
+struct Law {
+    float e12, isig2, sig, third, C, cut2, band;
+    __device__ __forceinline__ void set(float e12_, float sig_, float isig2_, float third_) {
+        e12 = e12_;
+        sig = sig_;
+        isig2 = isig2_;
+        third = third_;
+        C = e12 * isig2;
+        cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
+        band = CUT_BAND_S * cut2;
+    }
+    // force scale s (F_i += r * s); `inb`: LJ pair within the cut-off band
+    __device__ __forceinline__ float scale(float d2, bool& inb) const {
+        if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
+            const float rsq = d2 * isig2;
+            const float ir = rcp_approx(rsq);
+            const float ir2 = ir * ir;
+            const float ir4 = ir2 * ir2;
+            const float ir3 = ir2 * ir;
+            const float t = C * ir4;
+            const float sc = fmaf(t, ir3, -t);   // 12 eps / sigma^2 * ir^4 (ir^3 - 1)
+            const float dd = rsq - cut2;
+            if constexpr (KIND == KIND_LJCUT) {
+                inb = fabsf(dd) <= band;
+                return (dd > 0.0f && !inb) ? 0.0f : sc;
+            } else {
+                inb = false;
+                return dd > 0.0f ? 0.0f : sc;
+            }
+        } else {
+            bool nc;
+            inb = false;
+            return scale32<KIND>(d2, e12, sig, isig2, third, nc);
+        }
+    }
+};
+
+// per-home-atom data loaded from global memory before the pair loop (issued
+// ahead of the staging barrier for a thread's first home atom)
+struct HomePre {
+    uint32_t nn, w0, w1;
+    float4 Qi;   // (sqrt(eps), sigma, third, m6)
+    const uint32_t* row;
+};
+
+__device__ __forceinline__ HomePre home_pre(const DevCtx& c, const HomeAtom& a) {
+    HomePre p;
+    p.nn = c.nnb[a.i];
+    p.Qi = c.prm32[a.i];
+    p.row = reinterpret_cast<const uint32_t*>(c.nbr16) + ((size_t)a.s0 * c.maxnb >> 1) + a.hs;
+    p.w0 = __ldg(p.row);       // entries of the first two words (read even when
+    p.w1 = __ldg(p.row + a.H); // the list is shorter: they lie inside its region)
+    return p;
+}
+
+template <int ND, int KIND, int PRM, bool FULL>
+__device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                           const float4* srec, const void* sext, uint32_t cap,
+                                           const HomeAtom& a, const HomePre& pre, const Law<KIND>& law0,
+                                           float* f, bool& any_band) {
+    const float4 ri = FULL ? srec[a.qi] : stg_get<ND>(c, S, T, srec, cap, a.qi);
+    const uint32_t wi = stg_wi(ri);
+    const float* ssig = static_cast<const float*>(sext);
+    const float4* sprm = static_cast<const float4*>(sext);
+    const float4 Qi = pre.Qi;
+    const uint32_t nn = pre.nn;
+    const uint32_t H = a.H;
+    const uint32_t* row = pre.row;
+    const uint32_t qmax = T.total - 1u;
+    auto pair = [&](uint32_t q) {
+        float4 rj;
+        if (FULL) {
+            q = min(q, qmax);
+            rj = srec[q];
+        } else {
+            q = stg_check(c, T, q, a.qi);
+            if (q == a.qi) return;
+            rj = stg_get<ND>(c, S, T, srec, cap, q);
+        }
+        float r[3];
+        stg_disp<ND>(wi, ri, rj, r);
+        float d2 = fmaf(r[1], r[1], r[0] * r[0]);
+        if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
+        Law<KIND> law = law0;
+        if constexpr (PRM == 1) {
+            const float sj = (FULL || q < cap) ? ssig[q] : c.prm32[stg_global(T, q)].y;
+            const float sg = 0.5f * (Qi.y + sj);
+            law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
+        } else if constexpr (PRM == 2) {
+            const float4 Qj = (FULL || q < cap) ? sprm[q] : c.prm32[stg_global(T, q)];
+            const float eps = Qi.x * Qj.x;
+            const float sg = 0.5f * (Qi.y + Qj.y);
+            law.set((KIND == KIND_REPULSION) ? eps : 12.0f * eps, sg, rcp_approx(sg * sg),
+                    (KIND == KIND_LJCUT) ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z));
+        }
+        bool inb;
+        const float sc = law.scale(d2, inb);
+        any_band |= inb;
+#pragma unroll
+        for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sc, f[d]);
+    };
+    const uint32_t nw = nn >> 1;   // words holding two entries
+    uint32_t p = 0;
+    if (nw >= 2) {
+        uint32_t w0 = pre.w0, w1 = pre.w1;
+#pragma unroll 1
+        for (; p + 3 < nw; p += 2) {
+            const uint32_t n0 = __ldg(row + (size_t)(p + 2) * H), n1 = __ldg(row + (size_t)(p + 3) * H);
+            pair(w0 & 0xFFFFu);
+            pair(w0 >> 16);
+            pair(w1 & 0xFFFFu);
+            pair(w1 >> 16);
+            w0 = n0;
+            w1 = n1;
+        }
+        pair(w0 & 0xFFFFu);
+        pair(w0 >> 16);
+        pair(w1 & 0xFFFFu);
+        pair(w1 >> 16);
+        p += 2;
+    }
+    if (p < nw) {
+        const uint32_t w = p == 0 ? pre.w0 : __ldg(row + (size_t)p * H);
+        pair(w & 0xFFFFu);
+        pair(w >> 16);
+    }
+    if (nn & 1u) pair((nw == 0 ? pre.w0 : (nw == 1 ? pre.w1 : __ldg(row + (size_t)nw * H))) & 0xFFFFu);
+    if constexpr (KIND == KIND_LJCUT) {
+        if (any_band) {
+            // rare: remove band pairs that the exact FP64 test puts beyond the cut-off
+            for (uint32_t k = 0; k < nn; k++) {
+                const uint32_t w = __ldg(row + (size_t)(k >> 1) * H);
+                const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
+                if (q == a.qi) continue;
+                const float4 rj = stg_get<ND>(c, S, T, srec, cap, q);
+                float r[3];
+                stg_disp<ND>(wi, ri, rj, r);
+                float d2 = fmaf(r[1], r[1], r[0] * r[0]);
+                if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
+                Law<KIND> law = law0;
+                if constexpr (PRM == 1) {
+                    const float sj = q < cap ? ssig[q] : c.prm32[stg_global(T, q)].y;
+                    const float sg = 0.5f * (Qi.y + sj);
+                    law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
+                } else if constexpr (PRM == 2) {
+                    const float4 Qj = q < cap ? sprm[q] : c.prm32[stg_global(T, q)];
+                    const float sg = 0.5f * (Qi.y + Qj.y);
+                    law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
+                }
+                bool inb;
+                const float sc = law.scale(d2, inb);
+                if (!inb) continue;
+                if (!lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND)) continue;
+#pragma unroll
+                for (int d = 0; d < ND; d++) f[d] = fmaf(-r[d], sc, f[d]);
+            }
+        }
+    }
+}
+
+template <int ND, int KIND, int MODE, int PRM>
+__global__ void __launch_bounds__(STG_THREADS) k_force_stg(DevCtx c) {
+    extern __shared__ float4 smem_f[];
+    __shared__ StgTable T;
+    if (blockIdx.x >= c.nblk) {
+        stg_nonmembers(c, blockIdx.x - c.nblk, MODE == FM_FORCES_A);
+        return;
+    }
+    const uint4 bd = c.blk[blockIdx.x];
+    const SysConst& S = c.sys[bd.x];
+    stg_setup<ND>(c, S, bd, T);
+    const uint32_t cap = c.stg_cap;
+    float4* srec = smem_f;
+    void* sext = smem_f + cap;
+    // the first home atom's global data is requested before the staging
+    // barrier, so its latency overlaps with the staging loads
+    HomeAtom a0{};
+    HomePre p0{};
+    const bool has0 = threadIdx.x < T.nhome;
+    if (has0) {
+        a0 = stg_home<ND, false>(c, T, threadIdx.x);
+        p0 = home_pre(c, a0);
+    }
+    stg_load<ND, PRM>(c, S, T, srec, sext, cap, 1);
+    const bool full = T.total <= cap;
+    for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
+        const HomeAtom a = h == threadIdx.x ? a0 : stg_home<ND, false>(c, T, h);
+        const HomePre pre = h == threadIdx.x ? p0 : home_pre(c, a);
+        const float4 Qi = pre.Qi;
+        Law<KIND> law;
+        law.set((KIND == KIND_REPULSION) ? Qi.x * Qi.x : 12.0f * Qi.x * Qi.x, Qi.y, rcp_approx(Qi.y * Qi.y),
+                Qi.z);
+        float f[3] = {0.f, 0.f, 0.f};
+        bool any_band = false;
+        if (full) force_home<ND, KIND, PRM, true>(c, S, T, srec, sext, cap, a, pre, law, f, any_band);
+        else force_home<ND, KIND, PRM, false>(c, S, T, srec, sext, cap, a, pre, law, f, any_band);
+        c.f32[a.i] = make_float4(f[0], f[1], f[2], 0.f);
+        if constexpr (MODE == FM_FORCES_A) {
+            using V = typename DVec<ND>::T;
+            V av;
+            double* ad = reinterpret_cast<double*>(&av);
+#pragma unroll
+            for (int d = 0; d < (int)(sizeof(V) / 8); d++) ad[d] = 0.0;
+            const double m = c.m[a.i];
+            if (!(m <= 0.0 || isinf(m))) {
+                const float im = c.invm32[a.i];
+#pragma unroll
+                for (int d = 0; d < ND; d++) ad[d] = (double)(f[d] * im);
+            }
+            static_cast<V*>(c.a)[a.i] = av;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// expansion of the staged lists into the row-major global-index lists used by
+// the evaluation kernels and the pair listing (same pairs, same order)
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(STG_THREADS) k_expand_stg(DevCtx c) {
+    __shared__ StgTable T;
+    if (blockIdx.x >= c.nblk) return;
+    const uint4 bd = c.blk[blockIdx.x];
+    const SysConst& S = c.sys[bd.x];
+    stg_setup<ND>(c, S, bd, T);
+    const uint32_t maxnb = c.maxnb;
+    for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
+        const HomeAtom a = stg_home<ND>(c, T, h);
+        const uint32_t nn = c.nnb[a.i];
+        for (uint32_t k = 0; k < nn; k++)
+            c.nbr[(size_t)a.i * maxnb + k] = stg_global(T, stg_check(c, T, c.nbr16[stg_entry16(a, maxnb, k)], a.qi));
+    }
+}
+
+// the inverse: row-major lists (global indices, built on the same cell grid)
+// -> staged lists; every neighbour lies in one of the home atom's stencil rows
+template <int ND>
+__global__ void __launch_bounds__(STG_THREADS) k_compress_stg(DevCtx c) {
+    __shared__ StgTable T;
+    if (blockIdx.x >= c.nblk) return;
+    const uint4 bd = c.blk[blockIdx.x];
+    const SysConst& S = c.sys[bd.x];
+    stg_setup<ND>(c, S, bd, T);
+    const uint32_t maxnb = c.maxnb;
+    for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
+        const HomeAtom a = stg_home<ND>(c, T, h);
+        const uint32_t nn = c.nnb[a.i];
+        for (uint32_t k = 0; k < nn; k++) {
+            const uint32_t j = c.nbr[(size_t)a.i * maxnb + k];
+            uint32_t q = 0xFFFFFFFFu;
+            for (uint32_t p = 0; p < T.npiece; p++)
+                if (j - T.g0[p] < T.cnt[p]) {
+                    q = T.off[p] + (j - T.g0[p]);
+                    break;
+                }
+            if (q > 0xFFFFu) {
+                atomicOr(c.status, ST_TILE_OVERFLOW);
+                q = a.qi;
+            }
+            c.nbr16[stg_entry16(a, maxnb, k)] = (uint16_t)q;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+size_t stg_smem_build(const DevCtx& c) { return (size_t)c.stg_cap * sizeof(float4); }
+size_t stg_smem_force(const DevCtx& c) {
+    const size_t ext = c.stg_prm == 1 ? sizeof(float) : (c.stg_prm == 2 ? sizeof(float4) : 0);
+    return (size_t)c.stg_cap * (sizeof(float4) + ext);
+}
+
+template <class K>
+static void set_smem(K kern, size_t bytes) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int ND, int KIND, int MODE>
+static void limits_prm(size_t sm) {
+    set_smem(k_force_stg<ND, KIND, MODE, 0>, sm);
+    set_smem(k_force_stg<ND, KIND, MODE, 1>, sm);
+    set_smem(k_force_stg<ND, KIND, MODE, 2>, sm);
+}
+template <int ND, int KIND>
+static void limits_kind(size_t sm) {
+    limits_prm<ND, KIND, FM_FORCES>(sm);
+    limits_prm<ND, KIND, FM_FORCES_A>(sm);
+}
+template <int ND>
+static void limits_nd(size_t build, size_t force) {
+    set_smem(k_build_stg<ND, 0>, build);
+    set_smem(k_build_stg<ND, 1>, build);
+    limits_kind<ND, KIND_LJCUT>(force);
+    limits_kind<ND, KIND_REPULSION>(force);
+    limits_kind<ND, KIND_LJREPULSE>(force);
+}
+
+// dynamic shared memory limit of every cell-block kernel, raised once to
+// the largest stage (4096 atoms of 16 + 16 bytes); called outside stream
+// capture.  A limit is an upper bound only: occupancy follows each launch's
+// own size.
+int stg_set_smem_limits() {
+    const size_t most = 4096 * (sizeof(float4) + sizeof(float4));
+    limits_nd<3>(most, most);
+    limits_nd<2>(most, most);
+    return (int)cudaGetLastError();
+}
+
+void launch_build_stg(const DevCtx& c, cudaStream_t s) {
+    const size_t sm = stg_smem_build(c);
+    const unsigned g = c.nblk + c.nsys;
+    if (c.nd == 3) {
+        if (c.stg_dia) { k_build_stg<3, 1><<<g, STG_THREADS, sm, s>>>(c); }
+        else { k_build_stg<3, 0><<<g, STG_THREADS, sm, s>>>(c); }
+    } else {
+        if (c.stg_dia) { k_build_stg<2, 1><<<g, STG_THREADS, sm, s>>>(c); }
+        else { k_build_stg<2, 0><<<g, STG_THREADS, sm, s>>>(c); }
+    }
+}
+
+template <int ND, int KIND, int MODE>
+static void force_stg_prm(const DevCtx& c, cudaStream_t s) {
+    const size_t sm = stg_smem_force(c);
+    const unsigned g = c.nblk + c.nsys;
+    switch (c.stg_prm) {
+        case 0: k_force_stg<ND, KIND, MODE, 0><<<g, STG_THREADS, sm, s>>>(c); break;
+        case 1: k_force_stg<ND, KIND, MODE, 1><<<g, STG_THREADS, sm, s>>>(c); break;
+        default: k_force_stg<ND, KIND, MODE, 2><<<g, STG_THREADS, sm, s>>>(c); break;
+    }
+}
+
+template <int ND, int KIND>
+static void force_stg_mode(const DevCtx& c, cudaStream_t s, int mode) {
+    if (mode == FM_FORCES_A) force_stg_prm<ND, KIND, FM_FORCES_A>(c, s);
+    else force_stg_prm<ND, KIND, FM_FORCES>(c, s);
+}
+
+template <int ND>
+static void force_stg_kind(const DevCtx& c, cudaStream_t s, int mode) {
+    switch (c.kind) {
+        case KIND_LJCUT: force_stg_mode<ND, KIND_LJCUT>(c, s, mode); break;
+        case KIND_REPULSION: force_stg_mode<ND, KIND_REPULSION>(c, s, mode); break;
+        default: force_stg_mode<ND, KIND_LJREPULSE>(c, s, mode); break;
+    }
+}
+
+void launch_force_stg(const DevCtx& c, cudaStream_t s, int mode) {
+    if (c.nd == 3) force_stg_kind<3>(c, s, mode);
+    else force_stg_kind<2>(c, s, mode);
+}
+
+void launch_expand_stg(const DevCtx& c, cudaStream_t s) {
+    if (c.nd == 3) k_expand_stg<3><<<c.nblk, STG_THREADS, 0, s>>>(c);
+    else k_expand_stg<2><<<c.nblk, STG_THREADS, 0, s>>>(c);
+}
+
+void launch_compress_stg(const DevCtx& c, cudaStream_t s) {
+    if (c.nd == 3) k_compress_stg<3><<<c.nblk, STG_THREADS, 0, s>>>(c);
+    else k_compress_stg<2><<<c.nblk, STG_THREADS, 0, s>>>(c);
+}
+
+}  // namespace parm

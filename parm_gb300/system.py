@@ -202,6 +202,14 @@ class System:
     def set_threads_per_atom(self, tpa: int) -> None:
         check(self.lib.parm_set_threads_per_atom(self.h, int(tpa)))
 
+    def threads_per_atom(self) -> int:
+        v = C.c_uint32(0)
+        check(self.lib.parm_get_threads_per_atom(self.h, C.byref(v)))
+        return int(v.value)
+
+    def debug_stage_cap(self, cap: int) -> None:
+        check(self.lib.parm_debug_stage_cap(self.h, int(cap)))
+
     def autotune(self) -> int:
         v = C.c_uint32()
         check(self.lib.parm_autotune(self.h, C.byref(v)))
