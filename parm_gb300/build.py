@@ -2,9 +2,10 @@
 
 * ``parm_gb300/_lib/libparm_gb300.so`` — the CUDA kernels and the C ABI
   declared in ``include/parm_gb300.h`` (sm_103a only).
-* ``parm_gb300/_lib/libparm_host.so`` — the C++ host API that mirrors the
-  reference's classes (Box, AtomVec, NeighborList, NListed, Collection...) on
-  top of the C ABI.
+* ``parm_gb300/_lib/libparm_host.so`` (3D) and ``libparm_host2d.so`` (2D) —
+  the C++ host API of ``parm_gb300/host/`` that mirrors the reference's
+  classes (Box, AtomVec, NeighborList, NListed, Collection...) on top of the
+  C ABI.
 
 Each translation unit is compiled by its own nvcc/g++ process in parallel.
 The FP64 translation units use ``-fmad=false`` so that no multiply-add is
@@ -42,6 +43,8 @@ CUDA_UNITS = {
     "noalloc.cu": ["-fmad=false"],
 }
 HOST_UNITS = ["parm_host.cpp"]
+# the host API is built once per dimension, like the reference (-DVEC3D / -DVEC2D)
+HOST_LIBS = {"libparm_host.so": [], "libparm_host2d.so": ["-DVEC2D"]}
 
 
 def nvcc() -> str:
@@ -83,17 +86,19 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         objs.append(obj)
         if _stale(obj, [src, *headers, Path(__file__)]):
             tasks.append([nv, *ARCH, *NVCC_COMMON, *extra, "-c", str(src), "-o", str(obj)])
-    host_objs = []
+    host_objs = {}
     host_headers = sorted(HOST.glob("*.hpp")) + [INCLUDE / "parm_gb300.h"]
-    for unit in HOST_UNITS:
-        src = HOST / unit
-        if not src.exists():
-            continue
-        obj = BUILD / (unit + ".o")
-        host_objs.append(obj)
-        if _stale(obj, [src, *host_headers, Path(__file__)]):
-            tasks.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}",
-                          f"-I{HOST}", "-c", str(src), "-o", str(obj)])
+    for libname, defs in HOST_LIBS.items():
+        host_objs[libname] = []
+        for unit in HOST_UNITS:
+            src = HOST / unit
+            if not src.exists():
+                continue
+            obj = BUILD / (unit + ("".join(defs) + ".o"))
+            host_objs[libname].append(obj)
+            if _stale(obj, [src, *host_headers, Path(__file__)]):
+                tasks.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *defs, f"-I{INCLUDE}",
+                              f"-I{HOST}", "-c", str(src), "-o", str(obj)])
     with cf.ThreadPoolExecutor(jobs) as ex:
         for cmd in tasks:
             if verbose:
@@ -106,10 +111,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
             cudalib = cuda_home() / "lib"
         _run([nv, *ARCH, "-shared", "-o", str(lib), *map(str, objs), f"-L{cudalib}", "-lcudart",
               "-Xlinker", f"-rpath={cudalib}"])
-    if host_objs:
-        hlib = LIB / "libparm_host.so"
-        if _stale(hlib, host_objs + [lib]):
-            _run(["g++", "-shared", "-o", str(hlib), *map(str, host_objs), f"-L{LIB}", "-lparm_gb300",
+    for libname, objs_h in host_objs.items():
+        if not objs_h:
+            continue
+        hlib = LIB / libname
+        if _stale(hlib, objs_h + [lib]):
+            _run(["g++", "-shared", "-o", str(hlib), *map(str, objs_h), f"-L{LIB}", "-lparm_gb300",
                   "-Wl,-rpath,$ORIGIN"])
     return lib
 

@@ -1,0 +1,119 @@
+// parm_gb300 host API: time-step loops with the interface of the reference's
+// src/collection.hpp (wackywendell/parm), run on the GPU.
+//
+// A Collection here drives one GPU handle: its interactions and trackers are
+// the NListed interaction and NeighborList of one AtomVec (constraints and
+// other interactions are outside this library and rejected).  timestep()
+// uploads the Atom records, runs one step of the reference's algorithm on the
+// GPU and downloads the records, so code that reads or edits atoms[i]
+// between steps behaves as with the reference; timesteps(n) runs n steps with
+// one upload and one download.
+#ifndef PARM_GB300_COLLECTION_HPP
+#define PARM_GB300_COLLECTION_HPP
+
+#include <vector>
+
+#include "interaction.hpp"
+
+//! Constraints are not part of this library; the type exists so that
+//! constructor signatures match the reference's.
+class Constraint {
+   public:
+    virtual ~Constraint() {}
+};
+
+//! Base of the time-step loops (src/collection.hpp:15-150, src/collection.cpp:1-180).
+class Collection {
+   protected:
+    sptr<Box> box;
+    sptr<AtomVec> atoms;
+    std::vector<sptr<Interaction>> interactions;
+    std::vector<sptr<StateTracker>> trackers;
+    sptr<GpuLink> link;
+    void attach();
+    GpuLink& gpu();
+
+   public:
+    Collection(sptr<Box> box, sptr<AtomVec> atoms,
+               std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+               std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+               std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>(),
+               bool should_initialize = true);
+    virtual ~Collection() {}
+
+    //! update_trackers(); set_forces(true); update_trackers() (src/collection.cpp:13-19)
+    void initialize();
+    void update_trackers();
+    virtual void set_forces(bool constraints_and_a = true);
+    virtual flt set_forces_get_pressure(bool constraints_and_a = true);
+    virtual void timestep() = 0;
+    //! n time steps with one upload and one download of the Atom records
+    virtual void timesteps(uint n);
+
+    flt potential_energy();
+    flt energy();
+    virtual flt kinetic_energy() { return atoms->kinetic_energy(); }
+    flt degrees_of_freedom();
+    virtual flt temp(bool minuscomv = true);
+    virtual flt pressure();
+    Vec com_velocity() { return atoms->com_velocity(); }
+    void reset_com_velocity() { atoms->reset_com_velocity(); }
+    void scale_velocities(flt scaleby);
+    void scale_velocities_to_temp(flt T, bool minuscomv = true);
+    void scale_velocities_to_energy(flt E);
+
+    virtual void add_interaction(sptr<Interaction> inter);
+    virtual void add_tracker(sptr<StateTracker> track);
+};
+
+//! Velocity Verlet (src/collection.hpp:755-790, src/collection.cpp:442-469).
+class CollectionVerlet : public Collection {
+   protected:
+    flt dt;
+
+   public:
+    CollectionVerlet(sptr<Box> box, sptr<AtomVec> atoms, const flt dt,
+                     std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+                     std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+                     std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>())
+        : Collection(box, atoms, is, ts, cs), dt(dt) {}
+    void timestep() override { timesteps(1); }
+    void timesteps(uint n) override;
+    void set_dt(flt newdt) { dt = newdt; }
+};
+
+//! Damped velocity Verlet (src/collection.hpp:254-300, src/collection.cpp:324-381).
+class CollectionDamped : public Collection {
+   protected:
+    flt dt, damping;
+
+   public:
+    CollectionDamped(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
+                     std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+                     std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+                     std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>());
+    void timestep() override { timesteps(1); }
+    void timesteps(uint n) override;
+};
+
+//! Langevin dynamics (src/collection.hpp:205-250, src/collection.cpp:230-322).
+//! The noise comes from a counter-based generator (one stream per handle,
+//! keyed from the seeded host engine), not from the reference's Boost stream.
+class CollectionSol : public Collection {
+   protected:
+    flt dt, damping, desT;
+    unsigned long long key;
+
+   public:
+    CollectionSol(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
+                  const flt desired_temperature,
+                  std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+                  std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+                  std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>());
+    void timestep() override { timesteps(1); }
+    void timesteps(uint n) override;
+    void set_damping(flt d) { damping = d; }
+    void set_temperature(flt T) { desT = T; }
+};
+
+#endif

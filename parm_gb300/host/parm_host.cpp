@@ -1,0 +1,416 @@
+// parm_gb300 host API implementation: the reference's C++ classes
+// (wackywendell/parm src/box.*, src/trackers.*, src/interaction.hpp,
+// src/collection.*) on top of the C ABI of include/parm_gb300.h.
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "collection.hpp"
+
+// ---------------------------------------------------------------------------
+// random numbers (std::mt19937; the reference's vecrand.cpp uses Boost's)
+std::mt19937& parm_random_engine() {
+    static std::mt19937 eng(5489u);
+    return eng;
+}
+flt rand01() { return std::uniform_real_distribution<flt>(0.0, 1.0)(parm_random_engine()); }
+Vec rand_vec() {
+    std::normal_distribution<flt> g(0.0, 1.0);
+    Vec v;
+    for (int d = 0; d < NDIM; d++) v[d] = g(parm_random_engine());
+    return v;
+}
+Vec rand_vec_boxed() {
+    Vec v;
+    for (int d = 0; d < NDIM; d++) v[d] = rand01();
+    return v;
+}
+unsigned int seed(unsigned int n) {
+    parm_random_engine().seed(n);
+    return n;
+}
+unsigned int seed() { return seed(static_cast<unsigned int>(time(nullptr))); }
+
+// ---------------------------------------------------------------------------
+// AtomGroup (src/box.cpp:237-258, 395-415)
+flt AtomGroup::mass() const {
+    flt m = 0;
+    for (uint i = 0; i < size(); i++) {
+        const Atom& a = (*this)[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        m += a.m;
+    }
+    return m;
+}
+
+Vec AtomGroup::momentum() const {
+    Vec tot = Vec::Zero();
+    for (uint i = 0; i < size(); i++) {
+        const Atom& a = (*this)[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        tot += a.v * a.m;
+    }
+    return tot;
+}
+
+flt AtomGroup::kinetic_energy(const Vec originvelocity) const {
+    flt totE = 0;
+    for (uint i = 0; i < size(); i++) {
+        const Atom& a = (*this)[i];
+        if (a.m == 0 || std::isinf(a.m)) continue;
+        const Vec curv = a.v - originvelocity;
+        totE += a.m / 2 * curv.dot(curv);
+    }
+    return totE;
+}
+
+void AtomGroup::add_velocity(Vec v) {
+    for (uint i = 0; i < size(); i++) (*this)[i].v += v;
+}
+
+void AtomGroup::reset_forces() {
+    for (uint i = 0; i < size(); i++) (*this)[i].f = Vec::Zero();
+}
+
+void AtomGroup::randomize_velocities(flt T) {
+    for (uint i = 0; i < size(); i++) {
+        Atom& a = (*this)[i];
+        a.v = rand_vec() * std::sqrt(T / a.m);
+    }
+}
+
+flt OriginBox::resize(flt factor, AtomGroup& atoms) {
+    boxsize *= factor;
+    for (uint i = 0; i < atoms.size(); i++) atoms[i].x *= factor;
+    return V();
+}
+
+flt OriginBox::resize_to(Vec newsize, AtomGroup& atoms) {
+    const Vec scale = newsize.cwiseQuotient(boxsize);
+    boxsize = newsize;
+    for (uint i = 0; i < atoms.size(); i++) atoms[i].x = atoms[i].x.cwiseProduct(scale);
+    return V();
+}
+
+// ---------------------------------------------------------------------------
+// GPU handles
+static int g_precision = -1;
+
+void parm_host_set_precision(int precision) { g_precision = precision; }
+
+int parm_host_precision() {
+    if (g_precision < 0) {
+        const char* e = std::getenv("PARM_PRECISION");
+        g_precision = (e && std::strcmp(e, "mixed") == 0) ? PARM_MIXED : PARM_FP64;
+    }
+    return g_precision;
+}
+
+void parm_host_check(int rc, const char* what) {
+    if (rc != PARM_OK) throw std::runtime_error(std::string(what) + ": " + parm_last_error());
+}
+
+GpuLink::GpuLink(sptr<Box> box, sptr<AtomVec> atoms, flt skin) : bx(box), atomv(atoms), skin_(skin) {
+    if (!std::dynamic_pointer_cast<OriginBox>(bx))
+        throw std::invalid_argument("parm_gb300: the GPU path supports periodic OriginBox boxes");
+    params.assign(3 * (size_t)atomv->size(), 0.0);
+    rank.assign(atomv->size(), PARM_NOT_MEMBER);
+}
+
+GpuLink::~GpuLink() {
+    if (h) parm_destroy(h);
+}
+
+void GpuLink::add(uint atom, int k, const double p[3]) {
+    if (atom >= atomv->size()) throw std::out_of_range("NListed::add: atom not in this AtomVec");
+    if (kind >= 0 && k != kind) throw std::invalid_argument("NListed::add: one pair law per interaction");
+    if (rank[atom] != PARM_NOT_MEMBER) throw std::invalid_argument("NListed::add: atom added twice");
+    kind = k;
+    for (int q = 0; q < 3; q++) params[3 * (size_t)atom + q] = p[q];
+    rank[atom] = nmembers++;
+    interaction_dirty = true;
+}
+
+void GpuLink::ignore(uint a, uint b) { pending_ignores.emplace_back(a, b); }
+
+void GpuLink::push() {
+    if (!h) {
+        uint32_t n = atomv->size();
+        parm_host_check(parm_create(&h, NDIM, 1, &n, parm_host_precision()), "parm_create");
+    }
+    OriginBox& ob = *std::dynamic_pointer_cast<OriginBox>(bx);
+    const Vec L = ob.box_shape();
+    std::vector<double> lv(L.data(), L.data() + NDIM);
+    if (lv != lastbox) {
+        parm_host_check(parm_set_boxes(h, lv.data()), "parm_set_boxes");
+        lastbox = lv;
+    }
+    if (interaction_dirty && kind >= 0) {
+        parm_host_check(parm_set_interaction(h, kind, params.data(), rank.data(), skin_), "parm_set_interaction");
+        interaction_dirty = false;
+    }
+    for (auto& pr : pending_ignores) parm_host_check(parm_nlist_ignore(h, pr.first, pr.second), "parm_nlist_ignore");
+    pending_ignores.clear();
+    parm_host_check(parm_set_atoms(h, atomv->records(), 4 * NDIM + 1, PARM_X | PARM_V | PARM_A | PARM_F | PARM_M),
+                    "parm_set_atoms");
+}
+
+void GpuLink::pull() {
+    parm_host_check(parm_get_atoms(h, atomv->records(), 4 * NDIM + 1, PARM_X | PARM_V | PARM_A | PARM_F | PARM_M),
+                    "parm_get_atoms");
+}
+
+// ---------------------------------------------------------------------------
+// NeighborList
+NeighborList::NeighborList(sptr<Box> box, sptr<AtomVec> atoms, const flt skin)
+    : link(new GpuLink(box, atoms, skin)) {}
+
+bool NeighborList::update_list(bool force) {
+    link->push();
+    link->touch();
+    uint8_t rebuilt = 0;
+    parm_host_check(parm_nlist_update(link->handle(), force ? 1 : 0, &rebuilt), "parm_nlist_update");
+    return rebuilt != 0;
+}
+
+uint NeighborList::which() {
+    link->push();
+    uint32_t w = 0;
+    parm_host_check(parm_nlist_which(link->handle(), &w), "parm_nlist_which");
+    return w;
+}
+
+uint NeighborList::numpairs() {
+    link->push();
+    uint64_t np = 0;
+    parm_host_check(parm_nlist_numpairs(link->handle(), &np), "parm_nlist_numpairs");
+    return (uint)np;
+}
+
+const std::vector<IDPair>& NeighborList::pairs() {
+    if (cache_epoch == link->epoch()) return cache;
+    link->push();
+    uint64_t np = 0;
+    parm_host_check(parm_nlist_pairs(link->handle(), 0, nullptr, 0, &np), "parm_nlist_pairs");
+    std::vector<uint32_t> p(2 * np);
+    parm_host_check(parm_nlist_pairs(link->handle(), 0, p.data(), np, &np), "parm_nlist_pairs");
+    cache.clear();
+    cache.reserve(np);
+    AtomVec& av = *link->atoms();
+    for (uint64_t k = 0; k < np; k++) cache.emplace_back(av.get_id(p[2 * k]), av.get_id(p[2 * k + 1]));
+    cache_epoch = link->epoch();
+    return cache;
+}
+
+// ---------------------------------------------------------------------------
+// interaction quantities
+flt gpu_evaluate(GpuLink& link, int what) {
+    link.push();
+    double v = 0.0;
+    parm_host_check(parm_evaluate(link.handle(), what, &v), "parm_evaluate");
+    return v;
+}
+
+Matrix gpu_stress(GpuLink& link) {
+    link.push();
+    double v[NDIM * NDIM];
+    parm_host_check(parm_evaluate(link.handle(), PARM_EVAL_STRESS, v), "parm_evaluate");
+    Matrix m;
+    for (int a = 0; a < NDIM; a++)
+        for (int b = 0; b < NDIM; b++) m(a, b) = v[a * NDIM + b];
+    return m;
+}
+
+void gpu_add_forces(GpuLink& link) {
+    AtomVec& av = *link.atoms();
+    std::vector<Vec> f0(av.size());
+    bool nonzero = false;
+    for (uint i = 0; i < av.size(); i++) {
+        f0[i] = av[i].f;
+        nonzero |= f0[i] != Vec::Zero();
+    }
+    link.push();
+    link.touch();
+    parm_host_check(parm_set_forces(link.handle(), 0), "parm_set_forces");
+    link.pull();
+    if (nonzero)
+        for (uint i = 0; i < av.size(); i++) av[i].f = f0[i] + av[i].f;
+}
+
+// ---------------------------------------------------------------------------
+// Collection
+Collection::Collection(sptr<Box> box, sptr<AtomVec> atoms, std::vector<sptr<Interaction>> is,
+                       std::vector<sptr<StateTracker>> ts, std::vector<sptr<Constraint>> cs, bool should_initialize)
+    : box(box), atoms(atoms), interactions(is), trackers(ts) {
+    if (!cs.empty()) throw std::invalid_argument("parm_gb300: constraints are not supported on the GPU path");
+    attach();
+    if (should_initialize) initialize();
+}
+
+void Collection::attach() {
+    sptr<GpuLink> found;
+    for (auto& it : interactions) {
+        sptr<GpuLink> l = it->gpu();
+        if (found && l != found) throw std::invalid_argument("parm_gb300: one NListed interaction per Collection");
+        found = l;
+    }
+    for (auto& t : trackers) {
+        auto nl = std::dynamic_pointer_cast<NeighborList>(t);
+        if (!nl) throw std::invalid_argument("parm_gb300: trackers must be NeighborList objects");
+        if (found && nl->gpu() != found)
+            throw std::invalid_argument("parm_gb300: the tracker must be the interaction's NeighborList");
+        found = nl->gpu();
+    }
+    if (found && found->atoms() != atoms)
+        throw std::invalid_argument("parm_gb300: the interaction was built on another AtomVec");
+    link = found;
+}
+
+GpuLink& Collection::gpu() {
+    if (!link) throw std::logic_error("parm_gb300: the Collection has no NListed interaction");
+    return *link;
+}
+
+void Collection::update_trackers() {
+    for (auto& t : trackers) t->update(*box);
+}
+
+void Collection::initialize() {
+    update_trackers();
+    set_forces(true);
+    update_trackers();
+}
+
+void Collection::set_forces(bool constraints_and_a) {
+    if (!link || interactions.empty()) {
+        // no interaction: zero forces, a = f/m (src/collection.cpp:159-179)
+        atoms->reset_forces();
+        if (constraints_and_a)
+            for (uint i = 0; i < atoms->size(); i++) (*atoms)[i].a = Vec::Zero();
+        return;
+    }
+    link->push();
+    link->touch();
+    parm_host_check(parm_set_forces(link->handle(), constraints_and_a ? 1 : 0), "parm_set_forces");
+    link->pull();
+}
+
+flt Collection::set_forces_get_pressure(bool constraints_and_a) {
+    set_forces(constraints_and_a);
+    flt p = 0;
+    for (auto& it : interactions) p += it->pressure(*box);
+    return p;
+}
+
+void Collection::timesteps(uint n) {
+    for (uint k = 0; k < n; k++) timestep();
+}
+
+flt Collection::potential_energy() {
+    flt E = 0;
+    for (auto& it : interactions) E += it->energy(*box);
+    return E;
+}
+
+flt Collection::energy() { return potential_energy() + kinetic_energy(); }
+
+flt Collection::degrees_of_freedom() {
+    int ndof = 0;
+    for (uint i = 0; i < atoms->size(); i++) {
+        const Atom& a = (*atoms)[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        ndof += NDIM;
+    }
+    return ndof;
+}
+
+flt Collection::temp(bool minuscomv) {
+    Vec v = Vec::Zero();
+    if (minuscomv) v = com_velocity();
+    int ndof = (int)degrees_of_freedom();
+    if (minuscomv) ndof -= NDIM;
+    return atoms->kinetic_energy(v) * 2 / ndof;
+}
+
+flt Collection::pressure() {
+    const flt V = box->V();
+    flt E = 2.0 * kinetic_energy();
+    for (auto& it : interactions) E += it->pressure(*box);
+    return E / V / flt(NDIM);
+}
+
+void Collection::scale_velocities(flt scaleby) {
+    for (uint i = 0; i < atoms->size(); i++) {
+        Atom& a = (*atoms)[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        a.v *= scaleby;
+    }
+}
+
+void Collection::scale_velocities_to_temp(flt T, bool minuscomv) {
+    const flt t = temp(minuscomv);
+    scale_velocities(std::sqrt(T / t));
+}
+
+void Collection::scale_velocities_to_energy(flt E) {
+    const flt E0 = energy();
+    const flt k0 = kinetic_energy();
+    const flt goalkinetic = k0 + (E - E0);
+    scale_velocities(std::sqrt(goalkinetic / k0));
+}
+
+void Collection::add_interaction(sptr<Interaction> inter) {
+    interactions.push_back(inter);
+    attach();
+    update_trackers();
+}
+
+void Collection::add_tracker(sptr<StateTracker> track) {
+    trackers.push_back(track);
+    attach();
+    update_trackers();
+}
+
+void CollectionVerlet::timesteps(uint n) {
+    if (!n) return;
+    GpuLink& g = gpu();
+    g.push();
+    g.touch();
+    parm_host_check(parm_verlet(g.handle(), dt, n), "parm_verlet");
+    g.pull();
+}
+
+CollectionDamped::CollectionDamped(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
+                                   std::vector<sptr<Interaction>> is, std::vector<sptr<StateTracker>> ts,
+                                   std::vector<sptr<Constraint>> cs)
+    : Collection(box, atoms, is, ts, cs, false), dt(dt), damping(damping) {
+    initialize();
+}
+
+void CollectionDamped::timesteps(uint n) {
+    if (!n) return;
+    GpuLink& g = gpu();
+    g.push();
+    g.touch();
+    parm_host_check(parm_damped(g.handle(), dt, damping, n), "parm_damped");
+    g.pull();
+}
+
+CollectionSol::CollectionSol(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
+                             const flt desired_temperature, std::vector<sptr<Interaction>> is,
+                             std::vector<sptr<StateTracker>> ts, std::vector<sptr<Constraint>> cs)
+    : Collection(box, atoms, is, ts, cs, false), dt(dt), damping(damping), desT(desired_temperature) {
+    if (dt <= 0) throw std::invalid_argument("Collection::CollectionSol: dt >= 0");
+    key = ((unsigned long long)parm_random_engine()() << 32) | parm_random_engine()();
+    initialize();
+}
+
+void CollectionSol::timesteps(uint n) {
+    if (!n) return;
+    GpuLink& g = gpu();
+    g.push();
+    g.touch();
+    parm_host_check(parm_sol(g.handle(), dt, damping, desT, key, n), "parm_sol");
+    g.pull();
+}

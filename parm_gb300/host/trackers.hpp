@@ -1,0 +1,111 @@
+// parm_gb300 host API: the neighbour list with the interface of the
+// reference's src/trackers.hpp (wackywendell/parm), backed by the GPU.
+//
+// One GPU handle (parm_system, include/parm_gb300.h) serves one AtomVec and
+// the one NListed interaction and NeighborList built on it.  `GpuLink` holds
+// that handle and the host-side description of the interaction, and moves
+// the Atom records between host and GPU around every GPU operation.
+#ifndef PARM_GB300_TRACKERS_HPP
+#define PARM_GB300_TRACKERS_HPP
+
+#include <set>
+#include <utility>
+#include <vector>
+
+#include "box.hpp"
+#include "parm_gb300.h"
+
+//! Precision of GPU handles created from now on: PARM_FP64 (default, the
+//! reference's results) or PARM_MIXED.  The environment variable
+//! PARM_PRECISION=mixed sets the default.
+void parm_host_set_precision(int precision);
+int parm_host_precision();
+
+//! Throws std::runtime_error with parm_last_error() when rc != PARM_OK.
+void parm_host_check(int rc, const char* what);
+
+class GpuLink {
+   public:
+    GpuLink(sptr<Box> box, sptr<AtomVec> atoms, flt skin);
+    ~GpuLink();
+    GpuLink(const GpuLink&) = delete;
+    GpuLink& operator=(const GpuLink&) = delete;
+
+    //! NListed::add: per-atom parameters (kind: PARM_LJCUT, ...) and the
+    //! atom's position in the neighbour list (insertion order)
+    void add(uint atom, int kind, const double p[3]);
+    void ignore(uint a, uint b);
+    //! upload box, interaction and Atom records (create the handle if needed)
+    void push();
+    //! download the Atom records
+    void pull();
+    parm_system* handle() { return h; }
+    sptr<Box> box() { return bx; }
+    sptr<AtomVec> atoms() { return atomv; }
+    uint members() const { return nmembers; }
+    flt skin() const { return skin_; }
+    //! advanced by every operation that may change the pair list
+    unsigned long long epoch() const { return epoch_; }
+    void touch() { epoch_++; }
+
+   private:
+    sptr<Box> bx;
+    sptr<AtomVec> atomv;
+    flt skin_;
+    parm_system* h = nullptr;
+    int kind = -1;
+    std::vector<double> params;
+    std::vector<uint32_t> rank;
+    uint nmembers = 0;
+    bool interaction_dirty = false;
+    std::vector<std::pair<uint, uint>> pending_ignores;
+    std::vector<double> lastbox;
+    unsigned long long epoch_ = 0;
+};
+
+//! Something to update before or after each time step (src/trackers.hpp:9-16).
+class StateTracker {
+   public:
+    virtual void update(Box& box) = 0;
+    virtual ~StateTracker() {}
+};
+
+//! A pair of atoms of the neighbour list.
+class IDPair {
+   protected:
+    AtomID a1, a2;
+
+   public:
+    IDPair() {}
+    IDPair(AtomID a, AtomID b) : a1(a), a2(b) {}
+    AtomID first() const { return a1; }
+    AtomID last() const { return a2; }
+};
+
+//! Verlet neighbour list with displacement-triggered rebuild
+//! (src/trackers.hpp:133-215, src/trackers.cpp:19-85).
+class NeighborList : public StateTracker {
+   public:
+    NeighborList(sptr<Box> box, sptr<AtomVec> atoms, const flt skin);
+    explicit NeighborList(sptr<GpuLink> link) : link(link) {}
+    void update(Box& newbox) override { update_list(false); }
+    //! rebuild if forced or if the two largest displacements sum to >= skin;
+    //! returns whether a rebuild happened
+    bool update_list(bool force = true);
+    uint which();
+    uint numpairs();
+    void ignore(AtomID a, AtomID b) { link->ignore(a.n(), b.n()); }
+    uint size() const { return link->members(); }
+    flt skin() const { return link->skin(); }
+    //! the current pairs in the reference's order
+    const std::vector<IDPair>& pairs();
+    IDPair get(uint i) { return pairs().at(i); }
+    sptr<GpuLink> gpu() { return link; }
+
+   private:
+    sptr<GpuLink> link;
+    std::vector<IDPair> cache;
+    unsigned long long cache_epoch = ~0ull;
+};
+
+#endif

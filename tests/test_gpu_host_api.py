@@ -1,0 +1,67 @@
+"""The C++ host API on the GPU reproduces the reference's own outputs.
+
+oracle/refbuild/ref_driver.cpp drives OriginBox, AtomVec, NListed,
+NeighborList and CollectionVerlet / CollectionDamped / CollectionSol exactly
+as a reference program does.  Built against the reference it produced the
+golden fixtures; built unchanged against parm_gb300/host (FP64 GPU path) it
+must print the same numbers: bit for bit, except that pair laws with a
+non-integer exponent (device pow) are held to 1e-12 relative.
+"""
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden_cases import load, names
+from host_api import DECK_DRIVER, compile_program
+
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+import make_golden as MG  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def drivers(tmp_path_factory, built_lib):
+    d = tmp_path_factory.mktemp("host_api")
+    out = {}
+    for nd in (3, 2):
+        r = compile_program(DECK_DRIVER, d / f"drv{nd}", ndim=nd)
+        assert r.returncode == 0, r.stderr[-3000:]
+        out[nd] = d / f"drv{nd}"
+    return out
+
+
+def _close(got, want, exact, what):
+    if exact:
+        np.testing.assert_array_equal(got, want, err_msg=what)
+    else:
+        scale = max(float(np.abs(want).max()), 1e-300)
+        assert float(np.abs(got - want).max()) / scale <= 1e-12, what
+
+
+@pytest.mark.parametrize("name", names())
+def test_host_api_matches_reference(drivers, name):
+    d = load(name)
+    case = {k: d[k] for k in ("kind", "integ", "nsteps", "dt", "damping", "T", "skin", "L", "x", "v", "m",
+                              "params", "order", "ignores", "out_steps")}
+    deck = MG._deck(case)
+    r = subprocess.run([str(drivers[d["ndim"]])], input=deck, capture_output=True, text=True, timeout=600,
+                       env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = MG._parse(r.stdout, d["n"], d["ndim"])
+    exact = not (d["kind"] == 1 and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
+    np.testing.assert_array_equal(got["pairs"], d["pairs"])
+    np.testing.assert_array_equal(got["init_counts"], d["init_counts"])
+    np.testing.assert_allclose(got["init"], d["init"], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(got["stress"], d["stress"], rtol=1e-12, atol=1e-13 * np.abs(d["stress"]).max())
+    _close(got["f0"], d["f0"], exact, "initial forces")
+    _close(got["a0"], d["a0"], exact, "initial accelerations")
+    np.testing.assert_array_equal(got["steps"], d["steps"])
+    np.testing.assert_array_equal(got["which_steps"], d["which_steps"])
+    for key in ("x", "v", "a", "f"):
+        _close(got[f"{key}_steps"], d[f"{key}_steps"], exact, key)
+    np.testing.assert_allclose(got["energy_steps"], d["energy_steps"], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(got["ke_steps"], d["ke_steps"], rtol=1e-12, atol=1e-13)

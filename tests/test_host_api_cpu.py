@@ -1,0 +1,29 @@
+"""The C++ host API compiles the programs written against the reference.
+
+The deck driver of the golden fixtures (oracle/refbuild/ref_driver.cpp) is
+one source that builds against the reference's own headers and, unchanged,
+against parm_gb300/host; the reference's example program src/bin/LJatoms.cpp
+does too where the reference sources are present.  (Running them needs a GPU:
+tests/test_gpu_host_api.py.)
+"""
+from pathlib import Path
+
+import pytest
+
+from host_api import DECK_DRIVER, compile_program
+
+REF_LJATOMS = Path("/root/reference/src/bin/LJatoms.cpp")
+
+
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_deck_driver_builds_against_host_api(tmp_path, built_lib, ndim):
+    r = compile_program(DECK_DRIVER, tmp_path / f"drv{ndim}", ndim=ndim)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert (tmp_path / f"drv{ndim}").exists()
+
+
+def test_reference_ljatoms_compiles_against_host_api(tmp_path, built_lib):
+    if not REF_LJATOMS.exists():
+        pytest.skip("reference sources not present")
+    r = compile_program(REF_LJATOMS, tmp_path / "lj.o", link=False)
+    assert r.returncode == 0, r.stderr[-3000:]
