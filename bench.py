@@ -52,13 +52,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles():
-    """dram bytes per launch of the force kernel from the committed ncu summary (if any)."""
-    p = ROOT / "profiles" / "force32_lj1m_traffic.txt"
+def traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch of `kernel` on this workload from its committed ncu summary."""
+    p = ROOT / "profiles" / f"{kernel}_lj1m.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch_1M:"):
+        if line.startswith("dram_bytes_per_launch:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -168,22 +168,57 @@ def cpu_baseline_sample(w, max_steps=3):
             "rebuild_s_16k": tb, "rebuild_s_extrapolated": t_rebuild_1m}
 
 
-def run_reference(args, rank):
+def _replica_steps(job):
+    """One host thread: time `steps` oracle steps of an independent replica (spawned process)."""
+    seed, steps = job
+    import numpy as np_
+    from oracle.oracle import Oracle
     from parm_gb300 import workloads as W
-    w = W.lj_lattice(shape=SHAPE, skin_prime=0.3)
-    s = cpu_baseline_sample(w, max_steps=max(1, min(args.steps, 5)))
-    sample = (f"oracle port of the reference step on the full {w.n}-atom system, 1 host thread: "
-              f"{s['steps']} CollectionVerlet steps without a list rebuild in {s['seconds']:.1f} s; the "
-              f"reference's O(N^2) rebuild measured {s['rebuild_s_16k']:.2f} s at 16384 atoms, "
-              f"extrapolated {s['rebuild_s_extrapolated']:.0f} s at {w.n} atoms (not included)")
-    out = {"metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": s["steps"],
-           "warmup": 0, "ms_per_step": 1000 * s["seconds"] / s["steps"], "higher_is_better": True,
+    w = W.lj_lattice(shape=SHAPE, skin_prime=0.3, seed=seed)
+    o = Oracle(w.n, 3)
+    o.set_box(w.L[0])
+    o.set_state(x=w.x, v=w.v, a=np_.zeros_like(w.x), f=np_.zeros_like(w.x), m=w.m)
+    o.set_interaction(w.kind, w.params, w.skin)
+    o.build_fast()
+    o.set_forces(True)
+    t0 = time.perf_counter()
+    o.verlet(DT, steps)
+    return w.n * steps, time.perf_counter() - t0, t0
+
+
+def run_reference(args, rank):
+    """The reference's CPU step (the oracle port, bit-exact with it) on every host thread.
+
+    Each host thread runs an independent replica of the 1M-atom system (the
+    reference step is single-threaded); value = all replicas' atom-steps over
+    the wall time from the first start to the last finish.
+    """
+    import multiprocessing as mp
+    from oracle.build import build as build_oracle
+    build_oracle()
+    ncpu = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    nrep = max(1, min(ncpu, 64))
+    steps = max(1, min(args.steps, 3))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(nrep) as pool:
+        res = pool.map(_replica_steps, [(12345 + r, steps) for r in range(nrep)])
+    total = sum(r[0] for r in res)
+    wall = max(r[2] + r[1] for r in res) - min(r[2] for r in res)
+    value = total / wall
+    n = res[0][0] // steps
+    sample = (f"oracle port of the reference step (bit-exact with the reference's compiled sources), "
+              f"{nrep} independent {n}-atom replicas, one per host thread, {steps} CollectionVerlet steps "
+              f"each without a list rebuild ({wall:.1f} s wall); the reference's O(N^2) list rebuild "
+              f"(~1.8e4 s per rebuild at this size, extrapolated from 16384 atoms) is excluded")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+           "warmup": 0, "ms_per_step": 1000 * wall / steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference",
-           "config": {"workload": f"lj_nve_{w.n}_atoms", "n_atoms": w.n, "dt": DT,
-                      "skin_sigma": w.skin, "lattice": list(SHAPE)},
-           "cpu_baseline": {"value": s["value"], "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
-           "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": {"workload": f"lj_nve_{n}_atoms", "n_atoms": n, "dt": DT,
+                      "skin_sigma": 0.3 * 2.0 ** (-1.0 / 6.0), "lattice": list(SHAPE),
+                      "replicas": nrep},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": nrep, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -239,13 +274,19 @@ def run_ours(args, rank, world, local_rank):
     npairs = int(g.numpairs()[0])
 
     # --- roofline of the dominant kernel (the mixed pair-force kernel) ---
+    # algorithmic bytes per atom and launch: the atom's FP32 position record
+    # (32 B, each read once), its pair parameters (16 B) and list length (4 B),
+    # its list entries (2 B each for the cell-block kernel, 4 B for the
+    # gather kernel) and its force (16 B written)
     force_ms = tr["force_ms"] / max(1, tr["force_launches"])
     nnb = 2.0 * npairs / n   # full-list entries per atom
-    bytes_per_atom = 232.0 + 4.0 * nnb
+    staged = tpa == 2000 or tpa == 200
+    kernel = "k_force_stg" if staged else "k_force32"
+    bytes_per_atom = 32.0 + 16.0 + 4.0 + 16.0 + (2.0 if staged else 4.0) * nnb
     algo_bytes = n * bytes_per_atom
     achieved = algo_bytes / (force_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = traffic_from_profiles()
+    traffic = traffic_from_profiles(kernel)
 
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -261,9 +302,11 @@ def run_ours(args, rank, world, local_rank):
               "rebuilds": tr["rebuilds"]}
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic,
-                          "kernel": "k_force32 (pair forces + kick + rebuild test)",
-                          "algorithmic_bytes_per_atom": bytes_per_atom, "force_ms_per_launch": force_ms,
-                          "peak_source": f"{peak_kind} hbm_gbs"}
+                          "kernel": f"{kernel} (mixed-precision pair forces)",
+                          "algorithmic_bytes_per_atom": bytes_per_atom,
+                          "algorithmic_bytes_per_launch": algo_bytes, "force_ms_per_launch": force_ms,
+                          "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                          else "fallback 6800 GB/s"}
     result["energy_drift_rel"] = {"per_1e5_steps": abs(e_end - e_start) / abs(e_start) * 1e5 / args.steps,
                                   "steps": args.steps}
 
