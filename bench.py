@@ -41,6 +41,21 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def max_over_ranks(value: float, dist=None, device: str = "cpu") -> float:
+    """Largest `value` over all ranks (the slowest replica sets the job time)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(atoms_per_rank: int, steps: int, ms_max: float, world: int) -> float:
+    """Whole-job atom-timesteps/s: every rank advances its own replica (weak scaling)."""
+    return world * atoms_per_rank * steps / (ms_max / 1000.0)
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -265,12 +280,10 @@ def run_ours(args, rank, world, local_rank):
     tr = g.timing_read()
     g.timing(False)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     e_end = g.energy()[0] + g.kinetic_energy()[0]
-    value = world * n * args.steps / (ms / 1000.0)
+    value = job_throughput(n, args.steps, ms, world)
     npairs = int(g.numpairs()[0])
 
     # --- roofline of the dominant kernel (the mixed pair-force kernel) ---
@@ -374,9 +387,7 @@ def run_ours(args, rank, world, local_rank):
         capi.check(lib.parm_get_atoms(g.h, dptr, stride, fields))
     t_e2e = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+        t_e2e = max_over_ranks(t_e2e, dist, "cuda")
     result["e2e"] = {"value": world * n * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * stride * 8,
                      "d2h_bytes_per_step": n * stride * 8, "steps": n_e2e,
                      "api": "parm_set_atoms + parm_verlet(dt, 1) + parm_get_atoms on whole Atom records "

@@ -137,6 +137,14 @@ int parm_momentum(parm_system* s, double* momentum, double* mass);
 /* max over mobile atoms of |f|^2, per system (minimisation convergence). */
 int parm_max_force_sq(parm_system* s, double* out);
 
+/* Freeze systems of a batch: time steps and force evaluations skip the
+ * systems whose active[s] is 0 (their atoms, forces and neighbour lists stay
+ * as they are; a rebuild test that was due waits until they are stepped
+ * again).  All systems start active.  No counterpart in the reference, which
+ * runs one system per Collection: this lets a batched minimisation stop the
+ * systems that have converged. */
+int parm_set_active(parm_system* s, const uint8_t* active);
+
 /* Langevin step counter (advanced once per parm_sol step; the counter used
  * by a step is the value after the advance). */
 int parm_get_step(parm_system* s, uint64_t* step);

@@ -71,6 +71,7 @@ SIGNATURES = {
     "parm_set_threads_per_atom": (C.c_int, [_h, C.c_uint32]),
     "parm_autotune": (C.c_int, [_h, _u32p]),
     "parm_get_threads_per_atom": (C.c_int, [_h, _u32p]),
+    "parm_set_active": (C.c_int, [_h, C.POINTER(C.c_uint8)]),
     "parm_debug_stage_cap": (C.c_int, [_h, C.c_uint32]),
     "parm_timing": (C.c_int, [_h, C.c_int]),
     "parm_timing_read": (C.c_int, [_h, _dp, _u64p, _dp, _u64p]),

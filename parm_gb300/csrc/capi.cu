@@ -761,6 +761,15 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     A(S->alloc(c.pos, 2 * (size_t)n));
     A(S->alloc(c.posw, n));
     A(S->alloc(c.red, (size_t)n * 12));
+    {
+        uint32_t* act = nullptr;
+        A(S->alloc(act, nsys));
+        std::vector<uint32_t> ones(nsys, 1u);
+        cudaStreamSynchronize(S->st);
+        if (cudaMemcpy(act, ones.data(), 4 * (size_t)nsys, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(PARM_ERR_CUDA, "initial upload failed"));
+        c.active = act;
+    }
     A(S->alloc(c.flag, nsys));
     A(S->alloc(c.force_rb, nsys));
     A(S->alloc(c.top, 2 * (size_t)nsys));
@@ -1395,6 +1404,16 @@ int parm_set_threads_per_atom(parm_system* S, uint32_t tpa) {
         S->clear_graphs();
     }
     return PARM_OK;
+}
+
+int parm_set_active(parm_system* S, const uint8_t* active) {
+    if (!S || !active) return fail(PARM_ERR_ARG, "NULL argument");
+    TRY(S->flush());
+    std::vector<uint32_t> a(S->nsys);
+    for (uint32_t s = 0; s < S->nsys; s++) a[s] = active[s] ? 1u : 0u;
+    CUDA_TRY(cudaMemcpyAsync(const_cast<uint32_t*>(S->c.active), a.data(), 4 * (size_t)S->nsys,
+                             cudaMemcpyHostToDevice, S->st));
+    return S->sync_status();
 }
 
 int parm_get_threads_per_atom(parm_system* S, uint32_t* tpa) {

@@ -123,10 +123,9 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
     using V = typename DVec<ND>::T;
     bool valid = false;
     double dsq = 0.0;
-    uint32_t s = 0;
-    if (i < c.n) {
+    uint32_t s = i < c.n ? c.atom_sys[i] : 0u;
+    if (i < c.n && c.active[s]) {
         const StepParams& P = *c.params;
-        s = c.atom_sys[i];
         const double m = c.m[i];
         V xv = static_cast<V*>(c.x)[i];
         V vv = static_cast<V*>(c.v)[i];
@@ -231,7 +230,7 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
 template <int ND, int MODE, bool MIXED>
 __global__ void __launch_bounds__(BLOCK) k_kick(DevCtx c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    if (i >= c.n || !c.active[c.atom_sys[i]]) return;
     using V = typename DVec<ND>::T;
     V vv = static_cast<V*>(c.v)[i];
     V av;

@@ -48,6 +48,12 @@ __global__ void k_arm(DevCtx c, int count_step, int use_cond, cudaGraphCondition
     __syncthreads();
     int any = 0;
     for (uint32_t s = threadIdx.x; s < c.nsys; s += blockDim.x) {
+        if (count_step && !c.active[s]) {
+            // frozen system: no rebuild in time steps; its pending test
+            // (displacements, forced rebuild) waits until it is stepped again
+            c.flag[s] = 0u;
+            continue;
+        }
         double t1 = __longlong_as_double((long long)c.top[2 * (size_t)s]);
         double t2 = __longlong_as_double((long long)c.top[2 * (size_t)s + 1]);
         // reference: bigdist + biggestdist >= skin, evaluated only once some atom moved

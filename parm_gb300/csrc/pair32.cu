@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(BLOCK) k_force32(DevCtx c) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = gt / TPA;
     const uint32_t sub = gt % TPA;
-    const bool active = i < c.n;
+    const bool active = i < c.n && c.active[c.atom_sys[i]];
     const uint32_t uni = c.uniform;
     float f[3] = {0.f, 0.f, 0.f};
     bool member = false;
@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(TILE_ATOMS * TPA) k_force32t(DevCtx c) {
     const uint32_t t = blockIdx.x;
     const uint32_t tid = threadIdx.x;
     const uint32_t s = c.tile_sys[t];
+    if (!c.active[s]) return;   // frozen system: forces unchanged
     const SysConst& S = c.sys[s];
     const uint32_t ne = c.tile_ne[t];
     const float4 A0 = c.tile_anchor[t];

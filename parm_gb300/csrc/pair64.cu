@@ -146,7 +146,7 @@ __device__ __forceinline__ float d2_32(const SysConst& S, const float4& Ai, cons
 template <int ND, int KIND, int MODE>
 __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < c.n;
+    const bool active = i < c.n && c.active[c.atom_sys[i]];
     const uint32_t uni = c.uniform;
     double f[3] = {0.0, 0.0, 0.0};
     uint32_t s = 0;

@@ -118,6 +118,7 @@ struct DevCtx {
     const uint32_t* excl_list;
 
     // per-system control
+    const uint32_t* active;  // per system: 0 = frozen (time steps and force launches skip it)
     uint32_t* flag;       // rebuild this step
     uint32_t* force_rb;   // rebuild requested by the host (force / ignorechanged)
     unsigned long long* top;  // [2*s] largest, [2*s+1] second largest squared displacement (bits)

@@ -622,10 +622,11 @@ __global__ void __launch_bounds__(STG_THREADS) k_force_stg(DevCtx c) {
     extern __shared__ float4 smem_f[];
     __shared__ StgTable T;
     if (blockIdx.x >= c.nblk) {
-        stg_nonmembers(c, blockIdx.x - c.nblk, MODE == FM_FORCES_A);
+        if (c.active[blockIdx.x - c.nblk]) stg_nonmembers(c, blockIdx.x - c.nblk, MODE == FM_FORCES_A);
         return;
     }
     const uint4 bd = c.blk[blockIdx.x];
+    if (!c.active[bd.x]) return;   // frozen system: forces unchanged
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
     const uint32_t cap = c.stg_cap;

@@ -202,6 +202,11 @@ class System:
     def set_threads_per_atom(self, tpa: int) -> None:
         check(self.lib.parm_set_threads_per_atom(self.h, int(tpa)))
 
+    def set_active(self, active) -> None:
+        """Freeze (False) or step (True) each system of the batch."""
+        a = np.ascontiguousarray(np.asarray(active, dtype=np.uint8).reshape(self.nsys))
+        check(self.lib.parm_set_active(self.h, a.ctypes.data_as(C.POINTER(C.c_uint8))))
+
     def threads_per_atom(self) -> int:
         v = C.c_uint32(0)
         check(self.lib.parm_get_threads_per_atom(self.h, C.byref(v)))

@@ -61,3 +61,30 @@ def test_batched_wca_sol_mixed():
     m.sol(0.001, 1.0, 1.0, 5, 50)
     st = m.get_atoms()
     assert np.all(np.isfinite(st["x"]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_frozen_systems_keep_their_state(precision):
+    """parm_set_active: frozen systems do not move; the others step as if alone."""
+    w = W.packings(nsys=4, nmin=200, nmax=500, exponent=2.0, seed=44, skin=0.15)
+    g = make_gpu(w, precision)
+    g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
+    g.damped(0.01, 1.0, 10)
+    frozen = g.get_atoms()
+    g.set_active([True, False, True, True])
+    g.damped(0.01, 1.0, 25)
+    st = g.get_atoms()
+    off = np.cumsum([0] + w.sizes)
+    sl = slice(off[1], off[2])
+    for k in ("x", "v", "a", "f"):
+        assert np.array_equal(st[k][sl], frozen[k][sl]), k
+    g.set_active([True] * 4)
+    if precision == "fp64":
+        # the systems that kept stepping equal their own 35-step runs
+        for s in (0, 2, 3):
+            o = make_oracle(w, sys=s)
+            o.initialize()
+            o.damped(0.01, 1.0, 35)
+            ref = o.get_state()
+            for k in ("x", "v"):
+                assert np.array_equal(st[k][off[s]:off[s + 1]], ref[k]), (s, k)
