@@ -410,6 +410,202 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(result), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# further workloads (not the headline line): batched packings, Langevin
+# replicas and the 2D disk minimisation; each prints its own JSON line
+# ---------------------------------------------------------------------------
+def _sync_time(g):
+    g.sync()
+    return time.perf_counter()
+
+
+def _minimise(g, dt, damping, tol, max_steps, chunk, active=None):
+    """Damped steps until every system's max |F| < tol; converged systems are frozen."""
+    nsys = g.nsys
+    act = np.ones(nsys, bool) if active is None else active.copy()
+    steps = np.zeros(nsys, dtype=np.int64)
+    done = 0
+    while done < max_steps and act.any():
+        g.set_active(act)
+        g.damped(dt, damping, chunk)
+        steps[act] += chunk
+        done += chunk
+        fmax = np.sqrt(g.max_force_sq())
+        act &= ~(fmax < tol)
+    g.set_active(np.ones(nsys, bool))
+    return steps, np.sqrt(g.max_force_sq())
+
+
+def _phase_state(g):
+    st = g.get_atoms()
+    return st["x"], st["v"]
+
+
+def run_packings(args):
+    """Batched 3D packings: mixed-precision bulk minimisation, FP64 finish."""
+    from parm_gb300 import workloads as W
+    nsys = args.nsys or 4096
+    w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=0.1)
+    dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
+    cap32, cap64, chunk = args.min_steps, args.min_steps // 4, 200
+    log(f"packings: {nsys} systems, {w.n} atoms")
+    g = make_system(w, "mixed", 0)
+    g.set_graph_steps(50)
+    tpa = g.autotune()
+    log(f"packings: kernel {tpa}")
+    t0 = _sync_time(g)
+    s32, f32 = _minimise(g, dt, damping, tol32, cap32, chunk)
+    x, v = _phase_state(g)
+    w64 = W.Workload(w.name, 3, w.sizes, w.L, x, np.zeros_like(v), w.m, w.kind, w.params, w.skin)
+    g64 = make_system(w64, "fp64", 0)
+    g64.set_graph_steps(50)
+    t1 = _sync_time(g64)
+    s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
+    t2 = _sync_time(g64)
+    E = g64.energy()
+    conv = f64 < tol64
+    # FP64-only minimisation of a sample of systems for the energy error
+    ns = min(nsys, args.sample_sys)
+    sizes = w.sizes[:ns]
+    nat = int(sum(sizes))
+    wr = W.Workload(w.name, 3, sizes, w.L[:ns], w.x[:nat], w.v[:nat], w.m[:nat], w.kind, w.params[:nat], w.skin)
+    gr = make_system(wr, "fp64", 0)
+    gr.set_graph_steps(50)
+    sr, fr = _minimise(gr, dt, damping, tol64, cap32 + cap64, chunk)
+    Er = gr.energy()
+    both = conv[:ns] & (fr < tol64)
+    rel = np.abs(E[:ns] - Er) / np.maximum(np.abs(Er), 1e-300)
+    # one system per launch: the same protocol, one handle per system, for a few systems
+    nsingle = min(nsys, args.single_sys)
+    t_single = 0.0
+    for s in range(nsingle):
+        o = int(sum(w.sizes[:s]))
+        ws = W.Workload(w.name, 3, [w.sizes[s]], w.L[s:s + 1], w.x[o:o + w.sizes[s]], w.v[o:o + w.sizes[s]],
+                        w.m[o:o + w.sizes[s]], w.kind, w.params[o:o + w.sizes[s]], w.skin)
+        gs = make_system(ws, "mixed", 0)
+        gs.set_graph_steps(50)
+        ta = _sync_time(gs)
+        _minimise(gs, dt, damping, tol32, cap32, chunk)
+        xs, vs = _phase_state(gs)
+        ws64 = W.Workload(w.name, 3, [w.sizes[s]], w.L[s:s + 1], xs, np.zeros_like(vs), ws.m, w.kind, ws.params, w.skin)
+        gs64 = make_system(ws64, "fp64", 0)
+        gs64.set_graph_steps(50)
+        tb = _sync_time(gs64)
+        _minimise(gs64, dt, damping, tol64, cap64, chunk)
+        tc = _sync_time(gs64)
+        t_single += (tb - ta) + (tc - tb)
+        gs.close(); gs64.close()
+    wall = (t1 - t0) + (t2 - t1)
+    value = float(conv.sum()) / wall
+    single_rate = nsingle / t_single if t_single > 0 else None
+    out = {"metric": "packings/s (batched 3D soft-sphere minimisation, mixed bulk + FP64 finish)",
+           "value": value, "unit": "packings/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
+           "config": {"workload": f"packings_{nsys}_systems", "systems": nsys, "atoms": w.n,
+                      "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "integrator":
+                      "CollectionDamped", "dt": dt, "damping": damping, "tol_mixed": tol32, "tol_fp64": tol64,
+                      "max_steps_mixed": cap32, "max_steps_fp64": cap64, "kernel": tpa},
+           "converged": int(conv.sum()), "wall_s": wall, "mixed_s": t1 - t0, "fp64_s": t2 - t1,
+           "steps_mixed_median": float(np.median(s32)), "steps_fp64_median": float(np.median(s64)),
+           "energy_rel_err_vs_fp64": {"systems": int(both.sum()), "median": float(np.median(rel[both])) if both.any() else None,
+                                      "max": float(rel[both].max()) if both.any() else None},
+           "one_system_per_launch": {"systems": nsingle, "packings_per_s": single_rate,
+                                     "batched_speedup": value / single_rate if single_rate else None}}
+    print(json.dumps(out), flush=True)
+
+
+def _msd(x, x0, sizes):
+    d = ((x - x0) ** 2).sum(1)
+    off = np.cumsum([0] + list(sizes))
+    return np.array([d[off[s]:off[s + 1]].mean() for s in range(len(sizes))])
+
+
+def run_replicas(args):
+    """Batched WCA Langevin replicas: mixed vs FP64 on MSD and potential energy."""
+    from parm_gb300 import workloads as W
+    nrep = args.nsys or 512
+    w = W.wca_replicas(nrep=nrep, nmin=256, nmax=32768, rho_lo=0.5, rho_hi=0.9, seed=4)
+    dt, damping, T, seed = 0.001, 1.0, 1.0, 20261204
+    steps, chunk = args.steps, 1000
+    steps64 = min(steps, args.fp64_steps)
+    res = {}
+    for prec, nst in (("mixed", steps), ("fp64", steps64)):
+        g = make_system(w, prec, 0)
+        g.set_graph_steps(50)
+        if prec == "mixed":
+            res["kernel"] = g.autotune()
+        x0 = g.get_atoms(1)["x"]
+        msd, pe, tt = [], [], 0.0
+        done = 0
+        while done < nst:
+            k = min(chunk, nst - done)
+            ta = _sync_time(g)
+            g.sol(dt, damping, T, seed, k)
+            tt += _sync_time(g) - ta
+            done += k
+            msd.append(_msd(g.get_atoms(1)["x"], x0, w.sizes))
+            pe.append(g.energy() / np.array(w.sizes))
+        res[prec] = {"atom_steps_per_s": w.n * nst / tt, "steps": nst, "seconds": tt,
+                     "msd": np.array(msd), "pe": np.array(pe)}
+        g.close()
+    k = len(res["fp64"]["msd"])
+    m32, m64 = res["mixed"]["msd"][:k], res["fp64"]["msd"][:k]
+    p32, p64 = res["mixed"]["pe"][:k], res["fp64"]["pe"][:k]
+    msd_rel = np.abs(m32.mean(1) - m64.mean(1)) / m64.mean(1)
+    spread = m64.std(1) / np.sqrt(nrep) / m64.mean(1)
+    out = {"metric": "atom-timesteps/s (batched WCA Langevin replicas), mixed vs FP64 on MSD and PE",
+           "value": res["mixed"]["atom_steps_per_s"], "unit": "atom-timesteps/s", "n_gpus": 1,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)",
+           "data": "synthetic",
+           "config": {"workload": f"wca_replicas_{nrep}", "replicas": nrep, "atoms": w.n, "n_range": [256, 32768],
+                      "rho_range": [0.5, 0.9], "T": T, "damping": damping, "dt": dt, "steps": steps,
+                      "fp64_steps": steps64, "kernel": res["kernel"]},
+           "fp64_value": res["fp64"]["atom_steps_per_s"],
+           "mixed_vs_fp64": res["mixed"]["atom_steps_per_s"] / res["fp64"]["atom_steps_per_s"],
+           "msd_batch_mean_rel_diff": [float(q) for q in msd_rel],
+           "msd_rel_standard_error": [float(q) for q in spread],
+           "pe_per_atom_rel_diff": float(np.abs(p32.mean() - p64.mean()) / abs(p64.mean())),
+           "pe_per_atom_max_replica_rel_diff": float((np.abs(p32[-1] - p64[-1]) / np.abs(p64[-1])).max())}
+    print(json.dumps(out), flush=True)
+
+
+def run_disks(args):
+    """2D bidisperse harmonic disks: mixed bulk minimisation, FP64 finish, vs FP64 alone."""
+    from parm_gb300 import workloads as W
+    w = W.soft_disks(n=65536, phi=0.84, exponent=2.0, seed=2, skin=0.1)
+    dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
+    cap, chunk = args.min_steps, 500
+    g = make_system(w, "mixed", 0)
+    g.set_graph_steps(50)
+    tpa = g.autotune()
+    t0 = _sync_time(g)
+    s32, f32 = _minimise(g, dt, damping, tol32, cap, chunk)
+    x, v = _phase_state(g)
+    w64 = W.Workload(w.name, 2, w.sizes, w.L, x, np.zeros_like(v), w.m, w.kind, w.params, w.skin)
+    g64 = make_system(w64, "fp64", 0)
+    g64.set_graph_steps(50)
+    t1 = _sync_time(g64)
+    s64, f64 = _minimise(g64, dt, damping, tol64, cap, chunk)
+    t2 = _sync_time(g64)
+    E = float(g64.energy()[0])
+    gr = make_system(w, "fp64", 0)
+    gr.set_graph_steps(50)
+    t3 = _sync_time(gr)
+    sr, fr = _minimise(gr, dt, damping, tol64, 2 * cap, chunk)
+    t4 = _sync_time(gr)
+    Er = float(gr.energy()[0])
+    out = {"metric": "seconds to minimise 65536 2D disks to max|F| < 1e-12 (mixed bulk + FP64 finish)",
+           "value": t2 - t0, "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "strong",
+           "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
+           "config": {"workload": "disks2d_65536", "phi": 0.84, "exponent": 2.0, "dt": dt, "damping": damping,
+                      "tol_mixed": tol32, "tol_fp64": tol64, "max_steps": cap, "kernel": tpa},
+           "steps_mixed": int(s32[0]), "steps_fp64": int(s64[0]), "max_force": float(f64[0]),
+           "energy": E, "fp64_alone": {"seconds": t4 - t3, "steps": int(sr[0]), "max_force": float(fr[0]),
+                                       "energy": Er},
+           "energy_rel_diff": abs(E - Er) / max(abs(Er), 1e-300)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,6 +620,13 @@ def main():
                     help="pair-kernel variant (0: autotune; 1/2/4 tiled, 100+t gather)")
     ap.add_argument("--only-timed", action="store_true",
                     help="run only the timed mixed-precision region (used for profiler captures)")
+    ap.add_argument("--workload", default="lj1m", choices=["lj1m", "packings", "replicas", "disks"],
+                    help="lj1m: the headline line; the others print their own line")
+    ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workloads")
+    ap.add_argument("--min-steps", type=int, default=20000, help="step cap of each minimisation phase")
+    ap.add_argument("--fp64-steps", type=int, default=2000, help="FP64 steps of the replica comparison")
+    ap.add_argument("--sample-sys", type=int, default=64, help="packings minimised by FP64 alone")
+    ap.add_argument("--single-sys", type=int, default=16, help="packings run one system per launch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -434,6 +637,11 @@ def main():
         if rank != 0:
             return
         run_reference(args, rank)
+        return
+    if args.workload != "lj1m":
+        import torch
+        torch.cuda.set_device(local_rank)
+        {"packings": run_packings, "replicas": run_replicas, "disks": run_disks}[args.workload](args)
         return
     run_ours(args, rank, world, local_rank)
 

@@ -32,7 +32,9 @@ __device__ __forceinline__ float scale32(float d2, float e12, float sig, float i
         if (d2 > sig * sig) return 0.0f;
         const float R = sqrtf(d2);
         const float isig = __fdividef(1.0f, sig);
-        const float b = 1.0f - R * isig;
+        // R <= sigma here, but the approximate reciprocal can leave 1 - R/sigma
+        // a rounding below zero, where b^1.5 or pow would be NaN
+        const float b = fmaxf(1.0f - R * isig, 0.0f);
         float pw;
         if (third == 2.0f) pw = b;
         else if (third == 2.5f) pw = b * sqrtf(b);
@@ -54,7 +56,7 @@ __device__ __forceinline__ float energy32(float d2, float eps, float sig, float 
     } else {
         if (d2 > sig * sig) return 0.0f;
         float R = sqrtf(d2);
-        float b = 1.0f - R / sig;
+        float b = fmaxf(1.0f - R / sig, 0.0f);
         float pw = (third == 2.0f) ? b * b : powf(b, third);
         return eps * pw / third;
     }

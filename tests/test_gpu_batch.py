@@ -88,3 +88,24 @@ def test_frozen_systems_keep_their_state(precision):
             ref = o.get_state()
             for k in ("x", "v"):
                 assert np.array_equal(st[k][off[s]:off[s + 1]], ref[k]), (s, k)
+
+
+@pytest.mark.parametrize("tpa", [200, 1, 2, 4, 101, 104])
+def test_batched_soft_spheres_every_kernel(tpa):
+    """Small uneven systems (3 cells per axis at N = 64), exponent 2.5, every mixed kernel variant."""
+    w = W.packings(nsys=24, nmin=64, nmax=1200, exponent=2.5, seed=45, skin=0.1)
+    m = make_gpu(w, "mixed")
+    m.set_threads_per_atom(tpa)
+    m.nlist_update(True)
+    m.set_forces(True)
+    F = m.get_atoms()["f"]
+    off = np.cumsum([0] + w.sizes)
+    for s in range(len(w.sizes)):
+        o = make_oracle(w, sys=s)
+        o.nl_update(True)
+        o.set_forces(True)
+        err = force_error(F[off[s]:off[s + 1]], o.get_state()["f"])
+        assert err <= 1e-5, (s, w.sizes[s], err)
+    m.damped(0.01, 1.0, 300)
+    st = m.get_atoms()
+    assert np.isfinite(st["x"]).all() and np.isfinite(st["f"]).all()
