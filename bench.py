@@ -142,6 +142,20 @@ def make_system(w, precision, device):
     return s
 
 
+def host_cpu() -> str:
+    """Core model and count of this host (for the CPU baseline's description)."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return f"{model or 'unknown CPU'}, {os.cpu_count()} logical cores"
+
+
 def cpu_baseline_sample(w, max_steps=3):
     """Time the oracle (a single-threaded restatement of the reference step) on the same system.
 
@@ -222,7 +236,7 @@ def run_reference(args, rank):
     value = total / wall
     n = res[0][0] // steps
     sample = (f"oracle port of the reference step (bit-exact with the reference's compiled sources), "
-              f"{nrep} independent {n}-atom replicas, one per host thread, {steps} CollectionVerlet steps "
+              f"{nrep} independent {n}-atom replicas, one per host thread of {host_cpu()}, {steps} CollectionVerlet steps "
               f"each without a list rebuild ({wall:.1f} s wall); the reference's O(N^2) list rebuild "
               f"(~1.8e4 s per rebuild at this size, extrapolated from 16384 atoms) is excluded")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
@@ -287,15 +301,15 @@ def run_ours(args, rank, world, local_rank):
     npairs = int(g.numpairs()[0])
 
     # --- roofline of the dominant kernel (the mixed pair-force kernel) ---
-    # algorithmic bytes per atom and launch: the atom's FP32 position record
-    # (32 B, each read once), its pair parameters (16 B) and list length (4 B),
-    # its list entries (2 B each for the cell-block kernel, 4 B for the
-    # gather kernel) and its force (16 B written)
+    # algorithmic bytes per atom-timestep of the mixed step (fused, list
+    # reused): x and v in FP64 read and written (96 B), the FP32 force/
+    # acceleration read and written (24 B) and 4 B per half-list pair; one
+    # launch of the force kernel advances every atom by one step
     force_ms = tr["force_ms"] / max(1, tr["force_launches"])
-    nnb = 2.0 * npairs / n   # full-list entries per atom
+    n_half = npairs / n
     staged = tpa == 2000 or tpa == 200
     kernel = "k_force_stg" if staged else "k_force32"
-    bytes_per_atom = 32.0 + 16.0 + 4.0 + 16.0 + (2.0 if staged else 4.0) * nnb
+    bytes_per_atom = 96.0 + 24.0 + 4.0 * n_half
     algo_bytes = n * bytes_per_atom
     achieved = algo_bytes / (force_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
@@ -316,7 +330,8 @@ def run_ours(args, rank, world, local_rank):
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic,
                           "kernel": f"{kernel} (mixed-precision pair forces)",
-                          "algorithmic_bytes_per_atom": bytes_per_atom,
+                          "algorithmic_bytes_per_atom": bytes_per_atom, "half_list_pairs_per_atom": n_half,
+                          "step_achieved_gbs": bytes_per_atom * value / 1e9,
                           "algorithmic_bytes_per_launch": algo_bytes, "force_ms_per_launch": force_ms,
                           "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
                           else "fallback 6800 GB/s"}
@@ -401,7 +416,7 @@ def run_ours(args, rank, world, local_rank):
         result["cpu_baseline"] = {
             "value": s["value"], "unit": UNIT, "cores": 1, "kind": "port",
             "sample": (f"oracle port, {s['steps']} CollectionVerlet steps of the same {n}-atom system on one "
-                       f"host thread ({s['seconds']:.1f} s), list installed by the cell-list construction "
+                       f"host thread of {host_cpu()} ({s['seconds']:.1f} s), list installed by the cell-list construction "
                        f"(untimed); reference O(N^2) rebuild: {s['rebuild_s_16k']:.2f} s at 16384 atoms, "
                        f"~{s['rebuild_s_extrapolated']:.0f} s extrapolated to {n} (excluded)")}
     if dist:
@@ -442,75 +457,81 @@ def _phase_state(g):
 
 
 def run_packings(args):
-    """Batched 3D packings: mixed-precision bulk minimisation, FP64 finish."""
+    """Batched 3D packings: damped minimisation, mixed-precision bulk then FP64 finish.
+
+    A packing is one minimisation with a fixed step budget (the systems near
+    jamming converge too slowly for a max|F| criterion to bound the run):
+    S damped steps in mixed precision, then S/10 in FP64; systems whose
+    max |F| falls below the tolerance of a phase stop early (frozen).
+    Reported: packings/s of the batch, the same protocol run one system per
+    handle and launch (speed-up), and the final-energy error against a pure
+    FP64 minimisation with the same total budget on a sample of systems.
+    """
     from parm_gb300 import workloads as W
     nsys = args.nsys or 4096
     w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=0.1)
     dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
-    cap32, cap64, chunk = args.min_steps, args.min_steps // 4, 200
+    cap32, cap64, chunk = args.min_steps, max(args.min_steps // 10, 200), 200
     log(f"packings: {nsys} systems, {w.n} atoms")
-    g = make_system(w, "mixed", 0)
-    g.set_graph_steps(50)
-    tpa = g.autotune()
-    log(f"packings: kernel {tpa}")
-    t0 = _sync_time(g)
-    s32, f32 = _minimise(g, dt, damping, tol32, cap32, chunk)
-    x, v = _phase_state(g)
-    w64 = W.Workload(w.name, 3, w.sizes, w.L, x, np.zeros_like(v), w.m, w.kind, w.params, w.skin)
-    g64 = make_system(w64, "fp64", 0)
-    g64.set_graph_steps(50)
-    t1 = _sync_time(g64)
-    s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
-    t2 = _sync_time(g64)
-    E = g64.energy()
-    conv = f64 < tol64
-    # FP64-only minimisation of a sample of systems for the energy error
+
+    def protocol(ws):
+        g = make_system(ws, "mixed", 0)
+        g.set_graph_steps(50)
+        kern = g.autotune()
+        ta = _sync_time(g)
+        s32, f32 = _minimise(g, dt, damping, tol32, cap32, chunk)
+        x, v = _phase_state(g)
+        g.close()
+        w64 = W.Workload(ws.name, 3, ws.sizes, ws.L, x, np.zeros_like(v), ws.m, ws.kind, ws.params, ws.skin)
+        g64 = make_system(w64, "fp64", 0)
+        g64.set_graph_steps(50)
+        tb = _sync_time(g64)
+        s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
+        tc = _sync_time(g64)
+        E = g64.energy()
+        g64.close()
+        return {"kernel": kern, "t32": tb - ta, "t64": tc - tb, "f32": f32, "f64": f64, "E": E,
+                "s32": s32, "s64": s64}
+
+    def sub(lo, hi):
+        o0, o1 = int(sum(w.sizes[:lo])), int(sum(w.sizes[:hi]))
+        return W.Workload(w.name, 3, w.sizes[lo:hi], w.L[lo:hi], w.x[o0:o1], w.v[o0:o1], w.m[o0:o1], w.kind,
+                          w.params[o0:o1], w.skin)
+
+    r = protocol(w)
+    wall = r["t32"] + r["t64"]
+    value = nsys / wall
+    # pure FP64 minimisation of a sample, same total budget
     ns = min(nsys, args.sample_sys)
-    sizes = w.sizes[:ns]
-    nat = int(sum(sizes))
-    wr = W.Workload(w.name, 3, sizes, w.L[:ns], w.x[:nat], w.v[:nat], w.m[:nat], w.kind, w.params[:nat], w.skin)
-    gr = make_system(wr, "fp64", 0)
+    gr = make_system(sub(0, ns), "fp64", 0)
     gr.set_graph_steps(50)
-    sr, fr = _minimise(gr, dt, damping, tol64, cap32 + cap64, chunk)
+    _minimise(gr, dt, damping, tol64, cap32 + cap64, chunk)
     Er = gr.energy()
-    both = conv[:ns] & (fr < tol64)
-    rel = np.abs(E[:ns] - Er) / np.maximum(np.abs(Er), 1e-300)
-    # one system per launch: the same protocol, one handle per system, for a few systems
+    gr.close()
+    rel = np.abs(r["E"][:ns] - Er) / np.maximum(np.abs(Er), 1e-300)
+    # one system per handle and launch sequence, same protocol
     nsingle = min(nsys, args.single_sys)
     t_single = 0.0
-    for s in range(nsingle):
-        o = int(sum(w.sizes[:s]))
-        ws = W.Workload(w.name, 3, [w.sizes[s]], w.L[s:s + 1], w.x[o:o + w.sizes[s]], w.v[o:o + w.sizes[s]],
-                        w.m[o:o + w.sizes[s]], w.kind, w.params[o:o + w.sizes[s]], w.skin)
-        gs = make_system(ws, "mixed", 0)
-        gs.set_graph_steps(50)
-        ta = _sync_time(gs)
-        _minimise(gs, dt, damping, tol32, cap32, chunk)
-        xs, vs = _phase_state(gs)
-        ws64 = W.Workload(w.name, 3, [w.sizes[s]], w.L[s:s + 1], xs, np.zeros_like(vs), ws.m, w.kind, ws.params, w.skin)
-        gs64 = make_system(ws64, "fp64", 0)
-        gs64.set_graph_steps(50)
-        tb = _sync_time(gs64)
-        _minimise(gs64, dt, damping, tol64, cap64, chunk)
-        tc = _sync_time(gs64)
-        t_single += (tb - ta) + (tc - tb)
-        gs.close(); gs64.close()
-    wall = (t1 - t0) + (t2 - t1)
-    value = float(conv.sum()) / wall
-    single_rate = nsingle / t_single if t_single > 0 else None
-    out = {"metric": "packings/s (batched 3D soft-sphere minimisation, mixed bulk + FP64 finish)",
+    for q in range(nsingle):
+        rs = protocol(sub(q, q + 1))
+        t_single += rs["t32"] + rs["t64"]
+    single_rate = nsingle / t_single
+    out = {"metric": "packings/s (batched 3D soft-sphere damped minimisation, mixed bulk + FP64 finish)",
            "value": value, "unit": "packings/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
            "config": {"workload": f"packings_{nsys}_systems", "systems": nsys, "atoms": w.n,
-                      "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "integrator":
-                      "CollectionDamped", "dt": dt, "damping": damping, "tol_mixed": tol32, "tol_fp64": tol64,
-                      "max_steps_mixed": cap32, "max_steps_fp64": cap64, "kernel": tpa},
-           "converged": int(conv.sum()), "wall_s": wall, "mixed_s": t1 - t0, "fp64_s": t2 - t1,
-           "steps_mixed_median": float(np.median(s32)), "steps_fp64_median": float(np.median(s64)),
-           "energy_rel_err_vs_fp64": {"systems": int(both.sum()), "median": float(np.median(rel[both])) if both.any() else None,
-                                      "max": float(rel[both].max()) if both.any() else None},
+                      "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5,
+                      "integrator": "CollectionDamped", "dt": dt, "damping": damping,
+                      "steps_mixed": cap32, "steps_fp64": cap64, "tol_mixed": tol32, "tol_fp64": tol64,
+                      "kernel": r["kernel"]},
+           "wall_s": wall, "mixed_s": r["t32"], "fp64_s": r["t64"],
+           "mixed_atom_steps_per_s": float((r["s32"] * np.array(w.sizes)).sum() / r["t32"]),
+           "fp64_atom_steps_per_s": float((r["s64"] * np.array(w.sizes)).sum() / r["t64"]),
+           "converged_fp64_tol": int((r["f64"] < tol64).sum()),
+           "max_force_median": {"after_mixed": float(np.median(r["f32"])), "after_fp64": float(np.median(r["f64"]))},
+           "energy_rel_err_vs_fp64": {"systems": ns, "median": float(np.median(rel)), "max": float(rel.max())},
            "one_system_per_launch": {"systems": nsingle, "packings_per_s": single_rate,
-                                     "batched_speedup": value / single_rate if single_rate else None}}
+                                     "batched_speedup": value / single_rate}}
     print(json.dumps(out), flush=True)
 
 
@@ -575,6 +596,7 @@ def run_disks(args):
     w = W.soft_disks(n=65536, phi=0.84, exponent=2.0, seed=2, skin=0.1)
     dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
     cap, chunk = args.min_steps, 500
+    cap64 = max(cap // 10, chunk)
     g = make_system(w, "mixed", 0)
     g.set_graph_steps(50)
     tpa = g.autotune()
@@ -585,20 +607,20 @@ def run_disks(args):
     g64 = make_system(w64, "fp64", 0)
     g64.set_graph_steps(50)
     t1 = _sync_time(g64)
-    s64, f64 = _minimise(g64, dt, damping, tol64, cap, chunk)
+    s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
     t2 = _sync_time(g64)
     E = float(g64.energy()[0])
     gr = make_system(w, "fp64", 0)
     gr.set_graph_steps(50)
     t3 = _sync_time(gr)
-    sr, fr = _minimise(gr, dt, damping, tol64, 2 * cap, chunk)
+    sr, fr = _minimise(gr, dt, damping, tol64, cap + cap64, chunk)
     t4 = _sync_time(gr)
     Er = float(gr.energy()[0])
-    out = {"metric": "seconds to minimise 65536 2D disks to max|F| < 1e-12 (mixed bulk + FP64 finish)",
+    out = {"metric": "seconds for the 65536-disk 2D damped minimisation (mixed bulk + FP64 finish, fixed budget)",
            "value": t2 - t0, "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "strong",
            "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
            "config": {"workload": "disks2d_65536", "phi": 0.84, "exponent": 2.0, "dt": dt, "damping": damping,
-                      "tol_mixed": tol32, "tol_fp64": tol64, "max_steps": cap, "kernel": tpa},
+                      "tol_mixed": tol32, "tol_fp64": tol64, "steps_mixed": cap, "steps_fp64": cap64, "kernel": tpa},
            "steps_mixed": int(s32[0]), "steps_fp64": int(s64[0]), "max_force": float(f64[0]),
            "energy": E, "fp64_alone": {"seconds": t4 - t3, "steps": int(sr[0]), "max_force": float(fr[0]),
                                        "energy": Er},
