@@ -281,7 +281,7 @@ struct parm_system {
     }
 
     // Cell blocks of the mixed path (staged.cu): blocks of Kx x Ky cells of
-    // one z layer holding about 100 atoms; usable when every system has at
+    // one z layer holding about 180 atoms; usable when every system has at
     // least 3 cells per axis and the block frames fit the 9-bit coarse
     // fields (+-32 length units around the block centre).  Sets stg_ok and, when the blocks are not usable, c.staged = 0.
     int plan_blocks() {
@@ -300,7 +300,8 @@ struct parm_system {
                 if (S.nc[d] < 3) ok = false;
             if (!ok) break;
             const double a = std::max(1e-3, (double)natoms[s] / S.ncell);
-            const int cells = std::max(1, (int)std::lround(0.8 * STG_THREADS_HOST / a));
+            // about 0.7 home atoms per thread: the fullest blocks still fit one pass
+            const int cells = std::max(1, (int)std::lround(0.7 * STG_THREADS_HOST / a));
             const int ky = std::max(1, std::min({(int)std::lround(std::sqrt(cells / 2.0)), STG_KY_MAX, S.nc[1] - 2}));
             const int kx = std::max(1, std::min({(int)std::lround((double)cells / ky), STG_KX_MAX, S.nc[0] - 2}));
             const int nbx = (S.nc[0] + kx - 1) / kx, nby = (S.nc[1] + ky - 1) / ky;

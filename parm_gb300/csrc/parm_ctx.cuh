@@ -200,7 +200,7 @@ constexpr int STG_KY_MAX = 6;
 constexpr int STG_ROWS_MAX = 3 * (STG_KY_MAX + 2);
 constexpr int STG_PIECES_MAX = 3 * STG_ROWS_MAX;
 constexpr int STG_KX_MAX = 32;
-constexpr int STG_THREADS_HOST = 128;   // threads per block of the cell-block kernels
+constexpr int STG_THREADS_HOST = 256;   // threads per block of the cell-block kernels
 
 inline unsigned grid_for(uint32_t n, int block = BLOCK) {
     unsigned g = (unsigned)((n + block - 1) / block);

@@ -72,73 +72,90 @@ __device__ void stg_setup(const DevCtx& c, const SysConst& S, const uint4& bd, S
     const int z = (int)bd.w;
     const int nyr = y1 - y0 + 2;
     const int nrow = (ND == 3 ? 3 : 1) * nyr;
+    const int npiece = 3 * nrow;
     const uint32_t b0 = c.bucket_off[bd.x];
     const int nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
-    for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+    // one thread per piece (row r = t / 3, part t % 3: left cell, the block's
+    // cells, right cell)
+    for (int t = threadIdx.x; t < npiece; t += blockDim.x) {
+        const int r = t / 3, part = t % 3;
         const int dz = (ND == 3) ? r / nyr - 1 : 0;
         const int yy = y0 - 1 + r % nyr;
         const int cy = wrap_idx(yy, ny), cz = (ND == 3) ? wrap_idx(z + dz, nz) : 0;
         const uint32_t rb = b0 + (uint32_t)((cz * ny + cy) * nx);
-        T.rowbase[r] = rb;
-        const float py = ((float)yy + 0.5f) * S.cellw32[1];
-        const float pz = (ND == 3) ? ((float)(z + dz) + 0.5f) * S.cellw32[2] : 0.f;
-        const uint32_t cl = (uint32_t)wrap_idx(x0 - 1, nx), cr = (uint32_t)wrap_idx(x1, nx);
-        const uint32_t gl = c.cell_start[rb + cl], gm = c.cell_start[rb + (uint32_t)x0],
-                       gr = c.cell_start[rb + cr];
-        T.g0[3 * r] = gl;
-        T.cnt[3 * r] = c.cell_start[rb + cl + 1] - gl;
-        T.g0[3 * r + 1] = gm;
-        T.cnt[3 * r + 1] = c.cell_start[rb + (uint32_t)x1] - gm;
-        T.g0[3 * r + 2] = gr;
-        T.cnt[3 * r + 2] = c.cell_start[rb + cr + 1] - gr;
-        const float px[3] = {((float)x0 - 0.5f) * S.cellw32[0], 0.5f * (float)(x0 + x1) * S.cellw32[0],
-                             ((float)x1 + 0.5f) * S.cellw32[0]};
-#pragma unroll
-        for (int p = 0; p < 3; p++) {
-            T.P[3 * r + p][0] = px[p];
-            T.P[3 * r + p][1] = py;
-            T.P[3 * r + p][2] = pz;
+        if (part == 0) T.rowbase[r] = rb;
+        uint32_t lo, hi;
+        float px;
+        if (part == 0) {
+            lo = rb + (uint32_t)wrap_idx(x0 - 1, nx);
+            hi = lo + 1;
+            px = ((float)x0 - 0.5f) * S.cellw32[0];
+        } else if (part == 1) {
+            lo = rb + (uint32_t)x0;
+            hi = rb + (uint32_t)x1;
+            px = 0.5f * (float)(x0 + x1) * S.cellw32[0];
+        } else {
+            lo = rb + (uint32_t)wrap_idx(x1, nx);
+            hi = lo + 1;
+            px = ((float)x1 + 0.5f) * S.cellw32[0];
         }
+        const uint32_t g = c.cell_start[lo];
+        T.g0[t] = g;
+        T.cnt[t] = c.cell_start[hi] - g;
+        T.P[t][0] = px;
+        T.P[t][1] = ((float)yy + 0.5f) * S.cellw32[1];
+        T.P[t][2] = (ND == 3) ? ((float)(z + dz) + 0.5f) * S.cellw32[2] : 0.f;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int p = 0; p < 3 * nrow; p++) {
-            T.off[p] = acc;
-            acc += T.cnt[p];
+    if (threadIdx.x < 32) {
+        // exclusive scan of the piece sizes, 32 pieces per pass
+        const uint32_t lane = threadIdx.x;
+        uint32_t carry = 0;
+        for (int base = 0; base < npiece; base += 32) {
+            const int p = base + (int)lane;
+            const uint32_t v = p < npiece ? T.cnt[p] : 0u;
+            uint32_t inc = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                if (lane >= (uint32_t)o) inc += u;
+            }
+            if (p < npiece) T.off[p] = carry + inc - v;
+            carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
         }
-        T.off[3 * nrow] = acc;
-        T.total = acc;
-        T.nrow = (uint32_t)nrow;
-        T.npiece = (uint32_t)(3 * nrow);
-        T.nyr = (uint32_t)nyr;
-        T.x0 = x0; T.x1 = x1; T.y0 = y0; T.y1 = y1; T.z = z;
-        const int hbase = (ND == 3) ? nyr : 0;   // first home row (z layer 0, y = y0)
-        uint32_t h = 0;
-        for (int hr = 0; hr < y1 - y0; hr++) {
-            T.hoff[hr] = h;
-            h += T.cnt[3 * (hbase + hr + 1) + 1];
+        if (lane == 0) {
+            T.off[npiece] = carry;
+            T.total = carry;
+            T.nrow = (uint32_t)nrow;
+            T.npiece = (uint32_t)npiece;
+            T.nyr = (uint32_t)nyr;
+            T.x0 = x0; T.x1 = x1; T.y0 = y0; T.y1 = y1; T.z = z;
+            const int hbase = (ND == 3) ? nyr : 0;   // first home row (z layer 0, y = y0)
+            uint32_t h = 0;
+            for (int hr = 0; hr < y1 - y0; hr++) {
+                T.hoff[hr] = h;
+                h += T.cnt[3 * (hbase + hr + 1) + 1];
+            }
+            T.hoff[y1 - y0] = h;
+            T.nhome = h;
+            // frame origin: the block's centre rounded to the 1/8 grid
+            const double cx = 0.5 * (double)(x0 + x1) * S.cellw[0];
+            const double cy = 0.5 * (double)(y0 + y1) * S.cellw[1];
+            const double cz = (ND == 3) ? ((double)z + 0.5) * S.cellw[2] : 0.0;
+            T.C[0] = (float)(rint(cx * 8.0) * 0.125);
+            T.C[1] = (float)(rint(cy * 8.0) * 0.125);
+            T.C[2] = (float)(rint(cz * 8.0) * 0.125);
         }
-        T.hoff[y1 - y0] = h;
-        T.nhome = h;
-        // frame origin: the block's centre rounded to the 1/8 grid
-        const double cx = 0.5 * (double)(x0 + x1) * S.cellw[0];
-        const double cy = 0.5 * (double)(y0 + y1) * S.cellw[1];
-        const double cz = (ND == 3) ? ((double)z + 0.5) * S.cellw[2] : 0.0;
-        T.C[0] = (float)(rint(cx * 8.0) * 0.125);
-        T.C[1] = (float)(rint(cy * 8.0) * 0.125);
-        T.C[2] = (float)(rint(cz * 8.0) * 0.125);
     }
     __syncthreads();
 }
 
-// the staged record of atom j seen from piece centre P
+// the staged record of an atom, from its position view (A: coarse, B: fine),
+// seen from piece centre P
 template <int ND>
-__device__ __forceinline__ float4 stg_record(const DevCtx& c, const SysConst& S, const StgTable& T,
-                                             uint32_t j, const float* P) {
+__device__ __forceinline__ float4 stg_convert(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                              const float4& A, const float4& B, const float* P) {
     const float kShift = 12582912.0f;
-    float4 A, B;
-    ld_pos(c.pos, j, A, B);
     const float X[3] = {A.x, A.y, A.z}, F[3] = {B.x, B.y, B.z};
     float fo[3] = {0.f, 0.f, 0.f};
     uint32_t packed = 0;
@@ -155,6 +172,14 @@ __device__ __forceinline__ float4 stg_record(const DevCtx& c, const SysConst& S,
     }
     if (bad) atomicOr(c.status, ST_IMAGE_RANGE);
     return make_float4(fo[0], fo[1], fo[2], __uint_as_float(packed));
+}
+
+template <int ND>
+__device__ __forceinline__ float4 stg_record(const DevCtx& c, const SysConst& S, const StgTable& T,
+                                             uint32_t j, const float* P) {
+    float4 A, B;
+    ld_pos(c.pos, j, A, B);
+    return stg_convert<ND>(c, S, T, A, B, P);
 }
 
 // piece of local index q (binary search over the offsets)
@@ -219,27 +244,58 @@ __device__ __forceinline__ float4 stg_plain(const float4& rec, float w) {
 // 1 one float per atom (sigma), 2 the FP32 pair parameters; `plain`: FP32
 // positions with the list diameter in w instead of packed records
 template <int ND, int EXTRA>
+__device__ __forceinline__ void stg_store(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec,
+                                          void* sext, uint32_t q, uint32_t p, const float4& A, const float4& B,
+                                          const float4& X, bool plain) {
+    const float P[3] = {T.P[p][0], T.P[p][1], T.P[p][2]};
+    const float4 rec = stg_convert<ND>(c, S, T, A, B, P);
+    if (plain) {
+        srec[q] = stg_plain(rec, A.w);   // A.w: the list diameter
+        return;
+    }
+    srec[q] = rec;
+    if constexpr (EXTRA == 1) static_cast<float*>(sext)[q] = X.y;   // sigma
+    else if constexpr (EXTRA == 2) static_cast<float4*>(sext)[q] = X;
+}
+
+// Warp-per-piece staging of the first `cap` local indices.  Each warp takes
+// two pieces at a time and each lane issues the loads of up to four atoms
+// (two per piece) before converting any, so that their latencies overlap.
+template <int ND, int EXTRA>
 __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec, void* sext,
                          uint32_t cap, int ext_sigma, bool plain = false) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (uint32_t p = warp; p < T.npiece; p += nw) {
-        const uint32_t o = T.off[p], n = T.cnt[p], g = T.g0[p];
-        if (o >= cap) break;
-        const float P[3] = {T.P[p][0], T.P[p][1], T.P[p][2]};
-        for (uint32_t t = lane; t < n; t += 32) {
-            const uint32_t q = o + t;
-            if (q >= cap) break;
-            const float4 rec = stg_record<ND>(c, S, T, g + t, P);
-            if (plain) {
-                srec[q] = stg_plain(rec, c.pos[2 * (size_t)(g + t)].w);
-                continue;
+    for (uint32_t p0 = warp; p0 < T.npiece; p0 += 2 * nw) {
+        float4 A[4], B[4], X[4];
+        uint32_t q[4], pc[4];
+        bool ok[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t p = p0 + (k >> 1) * nw;
+            const uint32_t t = lane + 32u * (k & 1);
+            pc[k] = p;
+            ok[k] = p < T.npiece && t < T.cnt[p] && T.off[p] + t < cap;
+            q[k] = ok[k] ? T.off[p] + t : 0u;
+            if (ok[k]) {
+                const uint32_t j = T.g0[p] + t;
+                ld_pos(c.pos, j, A[k], B[k]);
+                if constexpr (EXTRA != 0) X[k] = __ldg(&c.prm32[j]);
             }
-            srec[q] = rec;
-            if constexpr (EXTRA == 1) {
-                // list diameter (build) or sigma (forces)
-                static_cast<float*>(sext)[q] = ext_sigma ? c.prm32[g + t].y : c.pos[2 * (size_t)(g + t)].w;
-            } else if constexpr (EXTRA == 2) {
-                static_cast<float4*>(sext)[q] = c.prm32[g + t];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (ok[k]) stg_store<ND, EXTRA>(c, S, T, srec, sext, q[k], pc[k], A[k], B[k], X[k], plain);
+        // pieces longer than 64 atoms (large blocks of sparse systems)
+#pragma unroll 1
+        for (int k = 0; k < 2; k++) {
+            const uint32_t p = p0 + k * nw;
+            if (p >= T.npiece) break;
+            for (uint32_t t = lane + 64u; t < T.cnt[p] && T.off[p] + t < cap; t += 32u) {
+                const uint32_t j = T.g0[p] + t;
+                float4 a, b, x = make_float4(0.f, 0.f, 0.f, 0.f);
+                ld_pos(c.pos, j, a, b);
+                if constexpr (EXTRA != 0) x = __ldg(&c.prm32[j]);
+                stg_store<ND, EXTRA>(c, S, T, srec, sext, T.off[p] + t, p, a, b, x, plain);
             }
         }
     }
@@ -357,7 +413,9 @@ __device__ __forceinline__ float4 stg_get_plain(const DevCtx& c, const SysConst&
     if (q < cap) return sp[q];
     const uint32_t p = stg_piece(T, q);
     const uint32_t j = T.g0[p] + (q - T.off[p]);
-    return stg_plain(stg_record<ND>(c, S, T, j, T.P[p]), c.pos[2 * (size_t)j].w);
+    float4 A, B;
+    ld_pos(c.pos, j, A, B);
+    return stg_plain(stg_convert<ND>(c, S, T, A, B, T.P[p]), A.w);
 }
 
 template <int ND, int DIA, bool FULL>
@@ -468,27 +526,29 @@ struct Law {
         cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
         band = CUT_BAND_S * cut2;
     }
-    // force scale s (F_i += r * s); `inb`: LJ pair within the cut-off band
-    __device__ __forceinline__ float scale(float d2, bool& inb) const {
+    // LJ kinds: the force scale s (F_i += r * s) ignoring the cut-off, and
+    // dd = r^2/sigma^2 - cut^2
+    __device__ __forceinline__ float lj_raw(float d2, float& dd) const {
+        const float rsq = d2 * isig2;
+        const float ir = rcp_approx(rsq);
+        const float ir2 = ir * ir;
+        const float ir4 = ir2 * ir2;
+        const float ir3 = ir2 * ir;
+        const float t = C * ir4;
+        dd = rsq - cut2;
+        return fmaf(t, ir3, -t);   // 12 eps / sigma^2 * ir^4 (ir^3 - 1)
+    }
+    // force scale s (F_i += r * s), zero beyond the FP32 cut-off test; for
+    // LJCUT, `dmin` tracks min(|dd| - band): a pair with |dd| <= band is
+    // settled afterwards by the exact FP64 test
+    __device__ __forceinline__ float scale(float d2, float& dmin) const {
         if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
-            const float rsq = d2 * isig2;
-            const float ir = rcp_approx(rsq);
-            const float ir2 = ir * ir;
-            const float ir4 = ir2 * ir2;
-            const float ir3 = ir2 * ir;
-            const float t = C * ir4;
-            const float sc = fmaf(t, ir3, -t);   // 12 eps / sigma^2 * ir^4 (ir^3 - 1)
-            const float dd = rsq - cut2;
-            if constexpr (KIND == KIND_LJCUT) {
-                inb = fabsf(dd) <= band;
-                return (dd > 0.0f && !inb) ? 0.0f : sc;
-            } else {
-                inb = false;
-                return dd > 0.0f ? 0.0f : sc;
-            }
+            float dd;
+            const float sc = lj_raw(d2, dd);
+            if constexpr (KIND == KIND_LJCUT) dmin = fminf(dmin, fabsf(dd) - band);
+            return dd > 0.0f ? 0.0f : sc;
         } else {
             bool nc;
-            inb = false;
             return scale32<KIND>(d2, e12, sig, isig2, third, nc);
         }
     }
@@ -516,7 +576,8 @@ template <int ND, int KIND, int PRM, bool FULL>
 __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, const StgTable& T,
                                            const float4* srec, const void* sext, uint32_t cap,
                                            const HomeAtom& a, const HomePre& pre, const Law<KIND>& law0,
-                                           float* f, bool& any_band) {
+                                           float* f) {
+    float dmin = 1.0f;   // min over pairs of |rsq - cut^2| - band (LJCUT)
     const float4 ri = FULL ? srec[a.qi] : stg_get<ND>(c, S, T, srec, cap, a.qi);
     const uint32_t wi = stg_wi(ri);
     const float* ssig = static_cast<const float*>(sext);
@@ -552,9 +613,7 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
             law.set((KIND == KIND_REPULSION) ? eps : 12.0f * eps, sg, rcp_approx(sg * sg),
                     (KIND == KIND_LJCUT) ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z));
         }
-        bool inb;
-        const float sc = law.scale(d2, inb);
-        any_band |= inb;
+        const float sc = law.scale(d2, dmin);
 #pragma unroll
         for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sc, f[d]);
     };
@@ -585,8 +644,9 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
     }
     if (nn & 1u) pair((nw == 0 ? pre.w0 : (nw == 1 ? pre.w1 : __ldg(row + (size_t)nw * H))) & 0xFFFFu);
     if constexpr (KIND == KIND_LJCUT) {
-        if (any_band) {
-            // rare: remove band pairs that the exact FP64 test puts beyond the cut-off
+        if (dmin <= 0.0f) {
+            // rare: settle the pairs within the band by the exact FP64 test
+            // (add those the FP32 test cut, remove those it kept wrongly)
             for (uint32_t k = 0; k < nn; k++) {
                 const uint32_t w = __ldg(row + (size_t)(k >> 1) * H);
                 const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
@@ -606,19 +666,21 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
                     const float sg = 0.5f * (Qi.y + Qj.y);
                     law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
                 }
-                bool inb;
-                const float sc = law.scale(d2, inb);
-                if (!inb) continue;
-                if (!lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND)) continue;
+                float dd;
+                const float sc = law.lj_raw(d2, dd);
+                if (fabsf(dd) > law.band) continue;
+                const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
+                if (beyond == (dd > 0.0f)) continue;   // the FP32 test agreed
+                const float sg = beyond ? -sc : sc;
 #pragma unroll
-                for (int d = 0; d < ND; d++) f[d] = fmaf(-r[d], sc, f[d]);
+                for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sg, f[d]);
             }
         }
     }
 }
 
 template <int ND, int KIND, int MODE, int PRM>
-__global__ void __launch_bounds__(STG_THREADS) k_force_stg(DevCtx c) {
+__global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
     extern __shared__ float4 smem_f[];
     __shared__ StgTable T;
     if (blockIdx.x >= c.nblk) {
@@ -651,9 +713,8 @@ __global__ void __launch_bounds__(STG_THREADS) k_force_stg(DevCtx c) {
         law.set((KIND == KIND_REPULSION) ? Qi.x * Qi.x : 12.0f * Qi.x * Qi.x, Qi.y, rcp_approx(Qi.y * Qi.y),
                 Qi.z);
         float f[3] = {0.f, 0.f, 0.f};
-        bool any_band = false;
-        if (full) force_home<ND, KIND, PRM, true>(c, S, T, srec, sext, cap, a, pre, law, f, any_band);
-        else force_home<ND, KIND, PRM, false>(c, S, T, srec, sext, cap, a, pre, law, f, any_band);
+        if (full) force_home<ND, KIND, PRM, true>(c, S, T, srec, sext, cap, a, pre, law, f);
+        else force_home<ND, KIND, PRM, false>(c, S, T, srec, sext, cap, a, pre, law, f);
         c.f32[a.i] = make_float4(f[0], f[1], f[2], 0.f);
         if constexpr (MODE == FM_FORCES_A) {
             using V = typename DVec<ND>::T;
