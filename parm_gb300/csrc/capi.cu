@@ -781,6 +781,10 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     A(S->alloc(c.chains, 1));
     A(S->alloc(c.params, 1));
     A(S->alloc(c.sysout, (size_t)nsys * 16));
+    if (precision == PARM_MIXED) {
+        A(S->alloc(c.bandn, 1));
+        A(S->alloc(c.bandq, n));
+    }
     {
         // reduction chunks: consecutive atoms of one system, at least one per system
         std::vector<uint4> ch;

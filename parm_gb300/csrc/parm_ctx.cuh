@@ -112,6 +112,8 @@ struct DevCtx {
     uint32_t stg_dia;     // list build: per-atom list diameters
     const uint4* blk;     // per block: (system, x0 | x1 << 16, y0 | y1 << 16, z)
     uint16_t* nbr16;      // staged lists (layout in staged.cu)
+    uint32_t* bandn;      // home atoms with a pair in the LJ cut-off band (this force launch)
+    uint2* bandq;         // their (block, home index), up to n entries
 
     // exclusions (NeighborList::ignore), CSR keyed by caller index
     const uint32_t* excl_off;   // n + 1 entries, or null when no exclusions

@@ -436,35 +436,60 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
             const uint32_t r = (uint32_t)dz * T.nyr + a.hr + (uint32_t)dy;
             uint32_t lo, hi;
             stg_range(c, T, r, a.cx, lo, hi);
-#pragma unroll 4
-            for (uint32_t q = lo; q < hi; q++) {
-                const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
-                const float dx = P.x - Q.x, dyv = P.y - Q.y;
-                float rr = fmaf(dyv, dyv, dx * dx);
-                if constexpr (ND == 3) {
-                    const float dzv = P.z - Q.z;
-                    rr = fmaf(dzv, dzv, rr);
+            // 32 candidates at a time: a branch-free screening pass sets one
+            // bit per candidate within the widened threshold, then the set
+            // bits (the ~15 % that are kept) are settled and written in order
+#pragma unroll 1
+            for (uint32_t base = lo; base < hi; base += 32u) {
+                const uint32_t m = min(32u, hi - base);
+                uint32_t mask = 0u;
+#pragma unroll 8
+                for (uint32_t u = 0; u < m; u++) {
+                    const uint32_t q = base + u;
+                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
+                    const float dx = P.x - Q.x, dyv = P.y - Q.y;
+                    float rr = fmaf(dyv, dyv, dx * dx);
+                    if constexpr (ND == 3) {
+                        const float dzv = P.z - Q.z;
+                        rr = fmaf(dzv, dzv, rr);
+                    }
+                    float hi2 = hiu;
+                    if constexpr (DIA) {
+                        const float thr = 0.5f * (P.w + Q.w) + skin32;
+                        hi2 = thr * thr * (1.0f + STG_BAND);
+                    }
+                    mask |= (rr <= hi2 && q != a.qi) ? (1u << u) : 0u;
                 }
-                float hi2 = hiu, lo2 = lou;
-                if constexpr (DIA) {
-                    const float thr = 0.5f * (P.w + Q.w) + skin32;
-                    hi2 = thr * thr * (1.0f + STG_BAND);
-                    lo2 = thr * thr * (1.0f - STG_BAND);
+                while (mask) {
+                    const uint32_t u = (uint32_t)__ffs(mask) - 1u;
+                    mask &= mask - 1u;
+                    const uint32_t q = base + u;
+                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
+                    const float dx = P.x - Q.x, dyv = P.y - Q.y;
+                    float rr = fmaf(dyv, dyv, dx * dx);
+                    if constexpr (ND == 3) {
+                        const float dzv = P.z - Q.z;
+                        rr = fmaf(dzv, dzv, rr);
+                    }
+                    float lo2 = lou;
+                    if constexpr (DIA) {
+                        const float thr = 0.5f * (P.w + Q.w) + skin32;
+                        lo2 = thr * thr * (1.0f - STG_BAND);
+                    }
+                    bool keep = rr < lo2;
+                    uint32_t j = 0xFFFFFFFFu;
+                    if (!keep) {   // rare: the exact reference test
+                        j = stg_global(T, q);
+                        keep = keep_exact_rn<ND>(c, S, a.i, j);
+                    }
+                    if (keep && c.excl_off) {
+                        if (j == 0xFFFFFFFFu) j = stg_global(T, q);
+                        keep = !is_excluded_s(c, oi, c.orig[j]);
+                    }
+                    if (!keep) continue;
+                    if (k < maxnb) out[stg_entry16(a, maxnb, k)] = (uint16_t)q;
+                    k++;
                 }
-                if (rr > hi2 || q == a.qi) continue;
-                bool keep = rr < lo2;
-                uint32_t j = 0xFFFFFFFFu;
-                if (!keep) {   // rare: the exact reference test
-                    j = stg_global(T, q);
-                    keep = keep_exact_rn<ND>(c, S, a.i, j);
-                }
-                if (keep && c.excl_off) {
-                    if (j == 0xFFFFFFFFu) j = stg_global(T, q);
-                    keep = !is_excluded_s(c, oi, c.orig[j]);
-                }
-                if (!keep) continue;
-                if (k < maxnb) out[stg_entry16(a, maxnb, k)] = (uint16_t)q;
-                k++;
             }
         }
     }
@@ -511,6 +536,38 @@ __device__ __forceinline__ float rcp_approx(float x) {
     float y;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// packed pairs of FP32 values (Blackwell's f32x2 add / mul / fma: two lanes
+// of work per instruction)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
 }
 
 // pair-law constants of one pair type
@@ -572,11 +629,62 @@ __device__ __forceinline__ HomePre home_pre(const DevCtx& c, const HomeAtom& a) 
     return p;
 }
 
+// rare: settle the pairs within the LJ cut-off band by the exact FP64 test
+// (add those the FP32 test cut, remove those it kept wrongly); kept out of
+// line so that the pair loop keeps its registers
+template <int ND, int KIND, int PRM>
+__device__ __forceinline__ float3 band_fix(const DevCtx& c, const SysConst& S, const StgTable& T, const float4* srec,
+                                        const void* sext, uint32_t cap, uint32_t ai, uint32_t aqi, uint32_t H,
+                                        float rx, float ry, float rz, uint32_t wi, float qx, float qy, float qz,
+                                        float e12, float isig2, float third, const uint32_t* row, uint32_t nn,
+                                        float fx, float fy, float fz) {
+    float f[3] = {fx, fy, fz};
+    const float4 ri = make_float4(rx, ry, rz, __uint_as_float(wi));
+    const float4 Qi = make_float4(qx, qy, qz, 0.f);
+    Law<KIND> law0;
+    law0.set(e12, Qi.y, isig2, third);
+    HomeAtom a;
+    a.i = ai;
+    a.qi = aqi;
+    a.H = H;
+    const float* ssig = static_cast<const float*>(sext);
+    const float4* sprm = static_cast<const float4*>(sext);
+    for (uint32_t k = 0; k < nn; k++) {
+        const uint32_t w = __ldg(row + (size_t)(k >> 1) * H);
+        const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
+        if (q == a.qi) continue;
+        const float4 rj = stg_get<ND>(c, S, T, srec, cap, q);
+        float r[3];
+        stg_disp<ND>(wi, ri, rj, r);
+        float d2 = fmaf(r[1], r[1], r[0] * r[0]);
+        if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
+        Law<KIND> law = law0;
+        if constexpr (PRM == 1) {
+            const float sj = q < cap ? ssig[q] : c.prm32[stg_global(T, q)].y;
+            const float sg = 0.5f * (Qi.y + sj);
+            law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
+        } else if constexpr (PRM == 2) {
+            const float4 Qj = q < cap ? sprm[q] : c.prm32[stg_global(T, q)];
+            const float sg = 0.5f * (Qi.y + Qj.y);
+            law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
+        }
+        float dd;
+        const float sc = law.lj_raw(d2, dd);
+        if (fabsf(dd) > law.band) continue;
+        const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
+        if (beyond == (dd > 0.0f)) continue;   // the FP32 test agreed
+        const float sg = beyond ? -sc : sc;
+#pragma unroll
+        for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sg, f[d]);
+    }
+    return make_float3(f[0], f[1], f[2]);
+}
+
 template <int ND, int KIND, int PRM, bool FULL>
 __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, const StgTable& T,
                                            const float4* srec, const void* sext, uint32_t cap,
                                            const HomeAtom& a, const HomePre& pre, const Law<KIND>& law0,
-                                           float* f) {
+                                           float* f, uint32_t hidx) {
     float dmin = 1.0f;   // min over pairs of |rsq - cut^2| - band (LJCUT)
     const float4 ri = FULL ? srec[a.qi] : stg_get<ND>(c, S, T, srec, cap, a.qi);
     const uint32_t wi = stg_wi(ri);
@@ -619,7 +727,72 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
     };
     const uint32_t nw = nn >> 1;   // words holding two entries
     uint32_t p = 0;
-    if (nw >= 2) {
+    if constexpr (FULL && PRM == 0 && (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE)) {
+        // the two entries of each list word together, in packed FP32 pairs:
+        // even entries accumulate in the low half, odd ones in the high half
+        const f32x2 K2 = pk2(STG_K, STG_K), is2 = pk2(law0.isig2, law0.isig2), C2 = pk2(law0.C, law0.C);
+        f32x2 fx = pk2(0.f, 0.f), fy = fx, fz = fx;
+        auto pair2 = [&](uint32_t w) {
+            const uint32_t q0 = min(w & 0xFFFFu, qmax), q1 = min(w >> 16, qmax);
+            const float4 ra = srec[q0], rb = srec[q1];
+            const uint32_t D0 = wi - __float_as_uint(ra.w), D1 = wi - __float_as_uint(rb.w);
+            const f32x2 rx = add2(sub2(pk2(__uint_as_float((D0 & 0x3FFu) | STG_MANT),
+                                           __uint_as_float((D1 & 0x3FFu) | STG_MANT)), K2),
+                                  pk2(ri.x - ra.x, ri.x - rb.x));
+            const f32x2 ry = add2(sub2(pk2(__uint_as_float(((D0 >> 10) & 0x3FFu) | STG_MANT),
+                                           __uint_as_float(((D1 >> 10) & 0x3FFu) | STG_MANT)), K2),
+                                  pk2(ri.y - ra.y, ri.y - rb.y));
+            f32x2 d2 = fma2(ry, ry, mul2(rx, rx));
+            f32x2 rz = pk2(0.f, 0.f);
+            if constexpr (ND == 3) {
+                rz = add2(sub2(pk2(__uint_as_float((D0 >> 20) | STG_MANT), __uint_as_float((D1 >> 20) | STG_MANT)),
+                               K2),
+                          pk2(ri.z - ra.z, ri.z - rb.z));
+                d2 = fma2(rz, rz, d2);
+            }
+            float r0, r1;
+            upk2(mul2(d2, is2), r0, r1);
+            const f32x2 ir = pk2(rcp_approx(r0), rcp_approx(r1));
+            const f32x2 ir2 = mul2(ir, ir);
+            const f32x2 ir4 = mul2(ir2, ir2);
+            const f32x2 ir3 = mul2(ir2, ir);
+            const f32x2 t = mul2(C2, ir4);
+            float s0, s1;
+            upk2(sub2(mul2(t, ir3), t), s0, s1);   // 12 eps / sigma^2 * ir^4 (ir^3 - 1)
+            const float dd0 = r0 - law0.cut2, dd1 = r1 - law0.cut2;
+            if constexpr (KIND == KIND_LJCUT) dmin = fminf(dmin, fminf(fabsf(dd0), fabsf(dd1)) - law0.band);
+            const f32x2 sc = pk2(dd0 > 0.0f ? 0.0f : s0, dd1 > 0.0f ? 0.0f : s1);
+            fx = fma2(rx, sc, fx);
+            fy = fma2(ry, sc, fy);
+            if constexpr (ND == 3) fz = fma2(rz, sc, fz);
+        };
+        if (nw >= 2) {
+            uint32_t w0 = pre.w0, w1 = pre.w1;
+#pragma unroll 1
+            for (; p + 3 < nw; p += 2) {
+                const uint32_t n0 = __ldg(row + (size_t)(p + 2) * H), n1 = __ldg(row + (size_t)(p + 3) * H);
+                pair2(w0);
+                pair2(w1);
+                w0 = n0;
+                w1 = n1;
+            }
+            pair2(w0);
+            pair2(w1);
+            p += 2;
+        }
+        if (p < nw) pair2(p == 0 ? pre.w0 : __ldg(row + (size_t)p * H));
+        float a0, a1;
+        upk2(fx, a0, a1);
+        f[0] = a0 + a1;
+        upk2(fy, a0, a1);
+        f[1] = a0 + a1;
+        if constexpr (ND == 3) {
+            upk2(fz, a0, a1);
+            f[2] = a0 + a1;
+        }
+        p = nw;
+    }
+    if (nw >= 2 && p == 0) {
         uint32_t w0 = pre.w0, w1 = pre.w1;
 #pragma unroll 1
         for (; p + 3 < nw; p += 2) {
@@ -644,37 +817,12 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
     }
     if (nn & 1u) pair((nw == 0 ? pre.w0 : (nw == 1 ? pre.w1 : __ldg(row + (size_t)nw * H))) & 0xFFFFu);
     if constexpr (KIND == KIND_LJCUT) {
+        // rare: a pair within the cut-off band; k_band_stg settles it by the
+        // exact FP64 test after this kernel (kept out of this loop so that the
+        // loop keeps its registers)
         if (dmin <= 0.0f) {
-            // rare: settle the pairs within the band by the exact FP64 test
-            // (add those the FP32 test cut, remove those it kept wrongly)
-            for (uint32_t k = 0; k < nn; k++) {
-                const uint32_t w = __ldg(row + (size_t)(k >> 1) * H);
-                const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
-                if (q == a.qi) continue;
-                const float4 rj = stg_get<ND>(c, S, T, srec, cap, q);
-                float r[3];
-                stg_disp<ND>(wi, ri, rj, r);
-                float d2 = fmaf(r[1], r[1], r[0] * r[0]);
-                if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
-                Law<KIND> law = law0;
-                if constexpr (PRM == 1) {
-                    const float sj = q < cap ? ssig[q] : c.prm32[stg_global(T, q)].y;
-                    const float sg = 0.5f * (Qi.y + sj);
-                    law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
-                } else if constexpr (PRM == 2) {
-                    const float4 Qj = q < cap ? sprm[q] : c.prm32[stg_global(T, q)];
-                    const float sg = 0.5f * (Qi.y + Qj.y);
-                    law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
-                }
-                float dd;
-                const float sc = law.lj_raw(d2, dd);
-                if (fabsf(dd) > law.band) continue;
-                const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
-                if (beyond == (dd > 0.0f)) continue;   // the FP32 test agreed
-                const float sg = beyond ? -sc : sc;
-#pragma unroll
-                for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sg, f[d]);
-            }
+            const uint32_t k = atomicAdd(c.bandn, 1u);
+            if (k < c.n) c.bandq[k] = make_uint2(blockIdx.x, hidx);
         }
     }
 }
@@ -713,8 +861,8 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
         law.set((KIND == KIND_REPULSION) ? Qi.x * Qi.x : 12.0f * Qi.x * Qi.x, Qi.y, rcp_approx(Qi.y * Qi.y),
                 Qi.z);
         float f[3] = {0.f, 0.f, 0.f};
-        if (full) force_home<ND, KIND, PRM, true>(c, S, T, srec, sext, cap, a, pre, law, f);
-        else force_home<ND, KIND, PRM, false>(c, S, T, srec, sext, cap, a, pre, law, f);
+        if (full) force_home<ND, KIND, PRM, true>(c, S, T, srec, sext, cap, a, pre, law, f, h);
+        else force_home<ND, KIND, PRM, false>(c, S, T, srec, sext, cap, a, pre, law, f, h);
         c.f32[a.i] = make_float4(f[0], f[1], f[2], 0.f);
         if constexpr (MODE == FM_FORCES_A) {
             using V = typename DVec<ND>::T;
@@ -730,6 +878,94 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
             }
             static_cast<V*>(c.a)[a.i] = av;
         }
+    }
+}
+
+// Settles the home atoms that k_force_stg listed as having a pair within the
+// LJ cut-off band: their force is the kernel's FP32 sum plus the exact-test
+// corrections, added in list order as if done inline (records are rebuilt
+// from global memory, identical to the staged ones).  One warp per listed
+// atom; its lanes test the atom's pairs in parallel.
+template <int ND, int KIND, int MODE, int PRM>
+__global__ void __launch_bounds__(32) k_band_stg(DevCtx c) {
+    __shared__ StgTable T;
+    const uint32_t lane = threadIdx.x;
+    const uint32_t nb = min(*c.bandn, c.n);
+    for (uint32_t it_k = blockIdx.x; it_k < nb; it_k += gridDim.x) {
+        const uint2 it = c.bandq[it_k];
+        const uint4 bd = c.blk[it.x];
+        const SysConst& S = c.sys[bd.x];
+        stg_setup<ND>(c, S, bd, T);
+        const HomeAtom a = stg_home<ND, false>(c, T, it.y);
+        const HomePre pre = home_pre(c, a);
+        const float4 Qi = pre.Qi;
+        const float4 ri = stg_get<ND>(c, S, T, nullptr, 0u, a.qi);
+        const uint32_t wi = stg_wi(ri);
+        Law<KIND> law0;
+        law0.set(12.0f * Qi.x * Qi.x, Qi.y, rcp_approx(Qi.y * Qi.y), Qi.z);
+        const float4 f0 = c.f32[a.i];
+        float f[3] = {f0.x, f0.y, f0.z};
+        for (uint32_t base = 0; base < pre.nn; base += 32u) {
+            const uint32_t k = base + lane;
+            float cv[3] = {0.f, 0.f, 0.f};
+            bool need = false;
+            if (k < pre.nn) {
+                const uint32_t w = __ldg(pre.row + (size_t)(k >> 1) * a.H);
+                const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
+                if (q != a.qi) {
+                    const float4 rj = stg_get<ND>(c, S, T, nullptr, 0u, q);
+                    float r[3];
+                    stg_disp<ND>(wi, ri, rj, r);
+                    float d2 = fmaf(r[1], r[1], r[0] * r[0]);
+                    if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
+                    Law<KIND> law = law0;
+                    if constexpr (PRM == 1) {
+                        const float sg = 0.5f * (Qi.y + c.prm32[stg_global(T, q)].y);
+                        law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
+                    } else if constexpr (PRM == 2) {
+                        const float4 Qj = c.prm32[stg_global(T, q)];
+                        const float sg = 0.5f * (Qi.y + Qj.y);
+                        law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
+                    }
+                    float dd;
+                    const float sc = law.lj_raw(d2, dd);
+                    if (fabsf(dd) <= law.band) {
+                        const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
+                        if (beyond != (dd > 0.0f)) {   // the FP32 test disagreed
+                            need = true;
+                            const float sg = beyond ? -sc : sc;
+#pragma unroll
+                            for (int d = 0; d < ND; d++) cv[d] = r[d] * sg;
+                        }
+                    }
+                }
+            }
+            // apply the corrections r * s in list order
+            uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1u;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const float v = __shfl_sync(0xFFFFFFFFu, cv[d], src);
+                    f[d] += v;
+                }
+            }
+        }
+        if (lane == 0) {
+            c.f32[a.i] = make_float4(f[0], f[1], f[2], 0.f);
+            if constexpr (MODE == FM_FORCES_A) {
+                const double m = c.m[a.i];
+                if (!(m <= 0.0 || isinf(m))) {
+                    const float im = c.invm32[a.i];
+                    double* ad = static_cast<double*>(c.a) + (size_t)a.i * (ND == 3 ? 4 : 2);
+                    ad[0] = (double)(f[0] * im);
+                    ad[1] = (double)(f[1] * im);
+                    if constexpr (ND == 3) ad[2] = (double)(f[2] * im);
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -838,14 +1074,24 @@ void launch_build_stg(const DevCtx& c, cudaStream_t s) {
     }
 }
 
+constexpr unsigned BAND_CTAS = 2048;
+
 template <int ND, int KIND, int MODE>
 static void force_stg_prm(const DevCtx& c, cudaStream_t s) {
     const size_t sm = stg_smem_force(c);
     const unsigned g = c.nblk + c.nsys;
+    if (KIND == KIND_LJCUT) cudaMemsetAsync(c.bandn, 0, sizeof(uint32_t), s);
     switch (c.stg_prm) {
         case 0: k_force_stg<ND, KIND, MODE, 0><<<g, STG_THREADS, sm, s>>>(c); break;
         case 1: k_force_stg<ND, KIND, MODE, 1><<<g, STG_THREADS, sm, s>>>(c); break;
         default: k_force_stg<ND, KIND, MODE, 2><<<g, STG_THREADS, sm, s>>>(c); break;
+    }
+    if (KIND == KIND_LJCUT) {
+        switch (c.stg_prm) {
+            case 0: k_band_stg<ND, KIND, MODE, 0><<<BAND_CTAS, 32, 0, s>>>(c); break;
+            case 1: k_band_stg<ND, KIND, MODE, 1><<<BAND_CTAS, 32, 0, s>>>(c); break;
+            default: k_band_stg<ND, KIND, MODE, 2><<<BAND_CTAS, 32, 0, s>>>(c); break;
+        }
     }
 }
 
