@@ -304,7 +304,7 @@ __global__ void k_gather(DevCtx c) {
     static_cast<V*>(c.x2)[k] = static_cast<const V*>(c.x)[o];
     static_cast<V*>(c.v2)[k] = static_cast<const V*>(c.v)[o];
     static_cast<V*>(c.a2)[k] = static_cast<const V*>(c.a)[o];
-    static_cast<V*>(c.f2)[k] = static_cast<const V*>(c.f)[o];
+    if (c.prec != PREC_MIXED) static_cast<V*>(c.f2)[k] = static_cast<const V*>(c.f)[o];   // FP64 forces: FP64 path only
     c.f32b[k] = c.f32[o];
     c.m2[k] = c.m[o];
     c.invm32b[k] = c.invm32[o];
@@ -328,7 +328,7 @@ __global__ void k_copyback(DevCtx c) {
     static_cast<V*>(c.lastloc)[k] = xk;
     static_cast<V*>(c.v)[k] = static_cast<const V*>(c.v2)[k];
     static_cast<V*>(c.a)[k] = static_cast<const V*>(c.a2)[k];
-    static_cast<V*>(c.f)[k] = static_cast<const V*>(c.f2)[k];
+    if (c.prec != PREC_MIXED) static_cast<V*>(c.f)[k] = static_cast<const V*>(c.f2)[k];
     c.f32[k] = c.f32b[k];
     c.m[k] = c.m2[k];
     c.invm32[k] = c.invm32b[k];
@@ -350,8 +350,9 @@ __global__ void k_copyback(DevCtx c) {
     B.w = 0.f;
     c.pos[2 * (size_t)(k)] = A;
     c.pos[2 * (size_t)(k) + 1] = B;
-    // position relative to the lower corner of its cell, for the list build
-    if (c.rank[k] != NOT_MEMBER) {
+    // position relative to the lower corner of its cell, for the warp list
+    // build (the cell-block build stages its own positions)
+    if (!c.staged && c.rank[k] != NOT_MEMBER) {
         const SysConst& S = c.sys[s];
         const uint32_t myb = c.bucket[k] - c.bucket_off[s];
         const uint32_t ci[3] = {myb % (uint32_t)S.nc[0], (myb / (uint32_t)S.nc[0]) % (uint32_t)S.nc[1],
