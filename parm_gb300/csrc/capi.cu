@@ -106,6 +106,9 @@ struct parm_system {
     bool stg_pending = false;    // grids changed under staged lists: switch back once every system rebuilt
     std::vector<uint32_t> stg_mark;   // which() of each system when the grids changed
     uint32_t stage_cap_override = 0;  // test hook (parm_debug_stage_cap)
+    // page-locked words read back on the stream: [0] status, [1] rebuild
+    // chains, [2, 2 + nsys) which() before a call, [2 + nsys, 2 + 2 nsys) after
+    uint32_t* hst = nullptr;
 
     ~parm_system() {
         clear_graphs();
@@ -118,6 +121,7 @@ struct parm_system {
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
+        if (hst) cudaFreeHost(hst);
         if (st) cudaStreamDestroy(st);
         if (st2) cudaStreamDestroy(st2);
     }
@@ -149,10 +153,12 @@ struct parm_system {
     }
     size_t vbytes() const { return nd == 3 ? 32 : 16; }
 
+    // one synchronisation: the status word travels to page-locked host memory
+    // on the stream, then the stream is drained
     int sync_status() {
+        CUDA_TRY(cudaMemcpyAsync(hst, c.status, 4, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        uint32_t stw = 0;
-        CUDA_TRY(cudaMemcpy(&stw, c.status, 4, cudaMemcpyDeviceToHost));
+        const uint32_t stw = hst[0];
         if (stw) {
             CUDA_TRY(cudaMemset(c.status, 0, 4));
             if (stw & ST_NBR_OVERFLOW)
@@ -160,11 +166,13 @@ struct parm_system {
                             "neighbour list capacity exceeded (" + std::to_string(c.maxnb) +
                                 " per atom); raise it with parm_set_nlist_capacity");
             if (stw & ST_IMAGE_RANGE)
-                return fail(PARM_ERR_RUNTIME, "an atom moved more than 127 box lengths from its neighbours' "
-                                              "frame (mixed precision)");
+                return fail(PARM_ERR_RUNTIME, "mixed precision: an atom left the coordinate frame of its "
+                                              "neighbourhood (positions changed by more than the frame allows "
+                                              "without a list rebuild)");
             if (stw & ST_TILE_OVERFLOW)
-                return fail(PARM_ERR_CAPACITY, "a tile of the mixed-precision kernel has more than " +
-                                                   std::to_string(TILE_ECAP) + " distinct neighbours");
+                return fail(PARM_ERR_CAPACITY, "mixed precision: a tile or cell block has more distinct "
+                                               "neighbours than its 16-bit index space (" +
+                                                   std::to_string(TILE_ECAP) + " per tile, 65535 per block)");
             if (stw & ST_SORT_CAP)
                 return fail(PARM_ERR_CAPACITY, "FP64 path: a neighbour list exceeded 256 entries");
             if (stw & ST_NONFINITE) return fail(PARM_ERR_RUNTIME, "non-finite atom position");
@@ -470,15 +478,70 @@ struct parm_system {
     }
 
     // resolve the rebuild test left pending by the last time step
+    // arm + IF(rebuild chain) as one cached graph (the rebuild test left
+    // pending by the last time step)
+    int build_flush_graph(GraphEntry& ge) {
+        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        cudaGraphConditionalHandle h;
+        CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        launch_arm(c, st, 0, 1, (unsigned long long)h);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        alignas(cudaGraphNodeParams) unsigned char cpbuf[sizeof(cudaGraphNodeParams)];
+        std::memset(cpbuf, 0, sizeof(cpbuf));
+        cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cpbuf);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+        CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CUDA_TRY(cudaStreamBeginCaptureToGraph(st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        launch_rebuild(c, st2);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamEndCapture(st2, &body));
+        CUDA_TRY(cudaStreamEndCapture(st, &ge.graph));
+        CUDA_TRY(cudaGraphInstantiate(&ge.exec, ge.graph, 0));
+        return PARM_OK;
+    }
+
     int flush() {
         TRY(upload_exclusions());
         if (!pending) return PARM_OK;
         pending = false;
-        launch_arm(c, st, 0, 0, 0);
-        launch_rebuild(c, st);
+        if (graph_k == 0) {
+            launch_arm(c, st, 0, 0, 0);
+            launch_rebuild(c, st);
+        } else {
+            const uint64_t key = ~0ull;   // no time-step graph uses this key
+            auto it = graphs.find(key);
+            if (it == graphs.end()) {
+                GraphEntry ge;
+                const int r = build_flush_graph(ge);
+                if (r != PARM_OK) {
+                    cudaStreamCaptureStatus cs;
+                    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                        cudaGraph_t junk;
+                        cudaStreamEndCapture(st, &junk);
+                        if (junk) cudaGraphDestroy(junk);
+                    }
+                    return r;
+                }
+                it = graphs.emplace(key, ge).first;
+            }
+            CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
+        }
         CUDA_TRY(cudaGetLastError());
-        TRY(sync_status());
-        return maybe_restage();
+        // no synchronisation here: the caller's own call ends with one, which
+        // reports any error of these kernels
+        return stg_pending ? maybe_restage() : PARM_OK;
     }
 
     int upload_params(const StepParams& p) {
@@ -545,8 +608,7 @@ struct parm_system {
 
     int run_steps(int mode, uint32_t nsteps) {
         TRY(upload_exclusions());
-        std::vector<uint32_t> which0(nsys), which1(nsys);
-        CUDA_TRY(cudaMemcpyAsync(which0.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(hst + 2, c.which, 4 * nsys, cudaMemcpyDeviceToHost, st));
         uint32_t done = 0;
         uint64_t launches = 0;
         if (graph_k == 0) {
@@ -617,14 +679,14 @@ struct parm_system {
             done += k;
         }
         pending = true;
+        CUDA_TRY(cudaMemcpyAsync(hst + 2 + nsys, c.which, 4 * nsys, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(hst + 1, c.chains, 4, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemsetAsync(c.chains, 0, 4, st));
         TRY(sync_status());
-        CUDA_TRY(cudaMemcpy(which1.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
         uint64_t rb = 0;
-        for (uint32_t s = 0; s < nsys; s++) rb += (uint64_t)(which1[s] - which0[s]);
+        for (uint32_t s = 0; s < nsys; s++) rb += (uint64_t)(hst[2 + nsys + s] - hst[2 + s]);
         n_rebuild += rb;
-        uint32_t chains = 0;
-        CUDA_TRY(cudaMemcpy(&chains, c.chains, 4, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemset(c.chains, 0, 4));
+        const uint32_t chains = hst[1];
         last_launches = graph_k == 0 ? launches : launches + (uint64_t)chains * chain_len();
         return maybe_restage();
     }
@@ -825,6 +887,9 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     if (cudaMallocHost(&S->h_params, sizeof(StepParams)) != cudaSuccess)
         return bail(fail(PARM_ERR_CUDA, "cudaMallocHost failed"));
     std::memset(S->h_params, 0, sizeof(StepParams));
+    if (cudaMallocHost(&S->hst, 4 * (2 + 2 * (size_t)nsys)) != cudaSuccess)
+        return bail(fail(PARM_ERR_CUDA, "cudaMallocHost failed"));
+    std::memset(S->hst, 0, 4 * (2 + 2 * (size_t)nsys));
     // identity order, masses 1, unit boxes
     std::vector<uint32_t> ident(n), sysid(n), nmr(n);
     for (uint32_t s = 0; s < nsys; s++)
