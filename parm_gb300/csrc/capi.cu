@@ -229,6 +229,7 @@ struct parm_system {
             }
             S.skin = skin;
             S.rlist_max = rl;
+            S.rec_lim2 = (2.0 * skin + 0.5) * (2.0 * skin + 0.5);
             S.cell_off = total;
             bucket_off[s] = total;
             total += S.ncell + 1;
@@ -242,12 +243,19 @@ struct parm_system {
         for (uint32_t s2 = 0; s2 < nsys; s2++)
             for (int d = 0; d < 3; d++) newnc.push_back(sys[s2].nc[d]);
         if (cell_mem && newnc == oldnc) {
-            // same grids: the cell arrays (and staged lists) stay valid
+            // same grids: the cell arrays (and staged lists) stay valid; the
+            // cell-block records move to the new box's frames
             CUDA_TRY(cudaMemcpyAsync(const_cast<SysConst*>(c.sys), sys.data(), sizeof(SysConst) * nsys,
                                      cudaMemcpyHostToDevice, st));
             CUDA_TRY(cudaStreamSynchronize(st));
             clear_graphs();
-            return plan_blocks();
+            TRY(plan_blocks());
+            if (c.staged) {
+                launch_reframe(c, st);
+                CUDA_TRY(cudaGetLastError());
+                TRY(sync_status());
+            }
+            return PARM_OK;
         }
         if (c.staged) {
             // the staged lists index the old grids: keep them as row-major lists
@@ -290,8 +298,10 @@ struct parm_system {
 
     // Cell blocks of the mixed path (staged.cu): blocks of Kx x Ky cells of
     // one z layer holding about 180 atoms; usable when every system has at
-    // least 3 cells per axis and the block frames fit the 9-bit coarse
-    // fields (+-32 length units around the block centre).  Sets stg_ok and, when the blocks are not usable, c.staged = 0.
+    // least 3 cells per axis and the packed coarse fields of the cell-block
+    // records fit: x (12 bits) spans the box, y and z (10 bits) a block's
+    // neighbourhood, each with 32 length units of head room for the list
+    // skin.  Sets stg_ok and, when the blocks are not usable, c.staged = 0.
     int plan_blocks() {
         stg_ok = false;
         if (prec != PREC_MIXED || kind < 0) {
@@ -314,10 +324,12 @@ struct parm_system {
             const int kx = std::max(1, std::min({(int)std::lround((double)cells / ky), STG_KX_MAX, S.nc[0] - 2}));
             const int nbx = (S.nc[0] + kx - 1) / kx, nby = (S.nc[1] + ky - 1) / ky;
             const double wx = std::ceil((double)S.nc[0] / nbx), wy = std::ceil((double)S.nc[1] / nby);
-            const double ex = (0.5 * wx + 1.0) * S.cellw[0] + margin;
-            const double ey = (0.5 * wy + 1.0) * S.cellw[1] + margin;
-            const double ez = nd == 3 ? 1.5 * S.cellw[2] + margin : 0.0;
-            if (ex >= 31.0 || ey >= 31.0 || ez >= 31.0) ok = false;   // 9-bit coarse fields (+-32)
+            // extents in the block frames (length units): staged fields stay
+            // in [0, 3840) / [0, 768) (units of 1/8, bias 256 for the margin)
+            const double ex = S.L[0] + 2.0 * S.cellw[0] + margin;
+            const double ey = (wy + 2.0) * S.cellw[1] + margin;
+            const double ez = nd == 3 ? 3.0 * S.cellw[2] + margin : 0.0;
+            if (margin >= 30.0 || ex >= 440.0 || ey >= 60.0 || ez >= 60.0) ok = false;
             worst = std::max(worst, a * (wx + 2) * (wy + 2) * (nd == 3 ? 3 : 1));
             const int nzl = nd == 3 ? S.nc[2] : 1;
             for (int z = 0; z < nzl; z++)
@@ -364,6 +376,7 @@ struct parm_system {
         for (uint32_t s = 0; s < nsys; s++)
             if (w[s] == stg_mark[s]) return PARM_OK;
         launch_compress_stg(c, st);
+        launch_reframe(c, st);
         CUDA_TRY(cudaGetLastError());
         c.staged = 1;
         stg_pending = false;
@@ -846,6 +859,8 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     if (precision == PARM_MIXED) {
         A(S->alloc(c.bandn, 1));
         A(S->alloc(c.bandq, n));
+        A(S->alloc(c.rec, n));
+        A(S->alloc(c.rframe, n));
     }
     {
         // reduction chunks: consecutive atoms of one system, at least one per system
@@ -1432,6 +1447,7 @@ static int set_staged(parm_system* S, bool on) {
         if (!S->stg_ok) return fail(PARM_ERR_ARG, "the cell-block kernel needs >= 3 cells per axis in every system");
         if (S->stg_pending) return PARM_OK;   // switches after the next rebuild of every system
         launch_compress_stg(S->c, S->st);
+        launch_reframe(S->c, S->st);
         S->c.staged = 1;
     } else {
         launch_expand_stg(S->c, S->st);

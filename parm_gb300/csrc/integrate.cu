@@ -68,6 +68,7 @@ __device__ __forceinline__ void store_posq(const DevCtx& c, uint32_t i, const do
     B.w = 0.f;
     c.pos[2 * (size_t)(i)] = A;
     c.pos[2 * (size_t)(i) + 1] = B;
+    if (c.staged) c.rec[i] = make_record(A, B, c.rframe[i]);
 }
 
 // Second half of the previous step (the reference's loop after set_forces):
@@ -206,6 +207,8 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
                 c.pos[2 * (size_t)i] = A;
             }
             c.pos[2 * (size_t)i + 1] = B;
+            if constexpr (MIXED)
+                if (c.staged) c.rec[i] = make_record(A, B, c.rframe[i]);
         }
         if (c.rank[i] != NOT_MEMBER) {
             const V l = static_cast<const V*>(c.lastloc)[i];
@@ -221,6 +224,11 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
                 dsq = disp_sq<ND>(xv, l);
             }
             valid = !(dsq != dsq);
+            // the cell-block records hold atoms within 2 skin + 1/2 of their
+            // position at the last build (far more than the rebuild test lets
+            // them move)
+            if constexpr (MIXED)
+                if (c.staged && dsq > c.sys[s].rec_lim2) atomicOr(c.status, ST_IMAGE_RANGE);
         }
     }
     check_accumulate(c, s, valid, dsq);

@@ -350,6 +350,20 @@ __global__ void k_copyback(DevCtx c) {
     B.w = 0.f;
     c.pos[2 * (size_t)(k)] = A;
     c.pos[2 * (size_t)(k) + 1] = B;
+    if (c.staged) {
+        // cell-block record in the frame of this build
+        float4 fr = make_float4(0.f, 0.f, 0.f, __uint_as_float(REC_BIAS | (REC_BIAS << 12) | (REC_BIAS << 22)));
+        if (c.rank[k] != NOT_MEMBER) {
+            const SysConst& S = c.sys[s];
+            uint32_t ci[3];
+            cell_coords(S, c.bucket[k] - c.bucket_off[s], ci);
+            bool ok;
+            fr = rec_frame<ND>(S, ci, A, B, ok);
+            if (!ok) atomicOr(c.status, ST_IMAGE_RANGE);
+        }
+        c.rframe[k] = fr;
+        c.rec[k] = make_record(A, B, fr);
+    }
     // position relative to the lower corner of its cell, for the warp list
     // build (the cell-block build stages its own positions)
     if (!c.staged && c.rank[k] != NOT_MEMBER) {
@@ -751,6 +765,29 @@ __global__ void k_posq(DevCtx c) {
     B.w = 0.f;
     c.pos[2 * (size_t)(k)] = A;
     c.pos[2 * (size_t)(k) + 1] = B;
+    if (c.staged) c.rec[k] = make_record(A, B, c.rframe[k]);
+}
+
+// the cell-block records of every atom in the frames of the current cells
+// (after a box change on the same cell grids, or when the mixed path moves to
+// the cell-block kernels between list builds)
+template <int ND>
+__global__ void k_reframe(DevCtx c) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    const uint32_t s = c.atom_sys[k];
+    float4 A, B;
+    ld_pos(c.pos, k, A, B);
+    float4 fr = make_float4(0.f, 0.f, 0.f, __uint_as_float(REC_BIAS | (REC_BIAS << 12) | (REC_BIAS << 22)));
+    if (c.rank[k] != NOT_MEMBER) {
+        const SysConst& S = c.sys[s];
+        uint32_t ci[3];
+        cell_coords(S, c.bucket[k] - c.bucket_off[s], ci);
+        bool ok;
+        fr = rec_frame<ND>(S, ci, A, B, ok);
+    }
+    c.rframe[k] = fr;
+    c.rec[k] = make_record(A, B, fr);
 }
 
 // ---------------------------------------------------------------------------
@@ -812,6 +849,12 @@ void launch_check(const DevCtx& c, cudaStream_t s) {
 
 void launch_numpairs(const DevCtx& c, cudaStream_t s) {
     k_count_half<<<grid_for(c.n), BLOCK, 0, s>>>(c);
+}
+
+void launch_reframe(const DevCtx& c, cudaStream_t s) {
+    if (!c.rec) return;
+    if (c.nd == 3) k_reframe<3><<<grid_for(c.n), BLOCK, 0, s>>>(c);
+    else k_reframe<2><<<grid_for(c.n), BLOCK, 0, s>>>(c);
 }
 
 void launch_posq(const DevCtx& c, cudaStream_t s) {

@@ -112,6 +112,9 @@ struct DevCtx {
     uint32_t stg_dia;     // list build: per-atom list diameters
     const uint4* blk;     // per block: (system, x0 | x1 << 16, y0 | y1 << 16, z)
     uint16_t* nbr16;      // staged lists (layout in staged.cu)
+    // per-atom cell-block records (mixed path): see make_record below
+    float4* rec;          // cell-block records (fine x, y, z, packed coarse fields), every step
+    float4* rframe;       // their frames (fine shift x, y, z, packed coarse offset), each build
     uint32_t* bandn;      // home atoms with a pair in the LJ cut-off band (this force launch)
     uint2* bandq;         // their (block, home index), up to n entries
 
@@ -152,6 +155,7 @@ void launch_check(const DevCtx& c, cudaStream_t s);
 void launch_tiles(const DevCtx& c, cudaStream_t s, int all);   // tiles of every system when all != 0
 void launch_numpairs(const DevCtx& c, cudaStream_t s);   // -> sysout[s] (as double)
 void launch_posq(const DevCtx& c, cudaStream_t s);
+void launch_reframe(const DevCtx& c, cudaStream_t s);
 // integrate.cu
 void launch_drift(const DevCtx& c, cudaStream_t s, int mode, bool with_kick);
 void launch_kick(const DevCtx& c, cudaStream_t s, int mode);
@@ -191,6 +195,63 @@ enum AtomWhat : int {
     AW_MOMENTUM = 1,   // nd + 1 comps (momentum, mass) over m > 0 finite atoms
     AW_MAXFORCE = 2,   // 1 comp: max |f|^2 over mobile atoms
 };
+
+// Cell-block record of an atom (mixed path), 16 bytes, the same for every
+// block.  The atom's frame is fixed at each list build: its periodic image m
+// (the one nearest to its cell) and, along y and z, the lower edge O of its
+// cell row on the 1/8 grid.  With L8 = L rounded to the 1/8 grid:
+//   packed coarse fields (units of 1/8, bias 256): x (bits 0-11)
+//   8 (X - m L8) + 256, y (bits 12-21) and z (bits 22-31) 8 (X - m L8 - O) + 256;
+//   fine part xf - m (L - L8) in FP32,
+// so that field / 8 - 32 + fine = x - m L - O.  Atoms stay within the list
+// skin of their cell between builds, so the fields stay far from their
+// limits; a block moves a record into its own frame with one packed integer
+// add per piece (and the fine part of a periodic shift).  The frame itself
+// is kept per atom as (fine shift x, y, z, packed coarse offset): packing is
+// linear, so the coarse fields are the packed 8 X plus the packed offset.
+constexpr int REC_BIAS = 256;
+
+// 8 O: the lower edge of cell row ci (any integer) along axis d on the 1/8 grid
+__device__ __forceinline__ int rec_origin8(const SysConst& S, int d, int ci) {
+    return (int)floorf(__fmul_rn(__fmul_rn((float)ci, S.cellw32[d]), 8.0f));
+}
+
+// the frame of a member atom with position view (A, B) in cell ci; `ok`
+// tells whether its fields are in range
+template <int ND>
+__device__ __forceinline__ float4 rec_frame(const SysConst& S, const uint32_t* ci, const float4& A, const float4& B,
+                                            bool& ok) {
+    const float X[3] = {A.x, A.y, A.z}, F[3] = {B.x, B.y, B.z};
+    int o[3] = {REC_BIAS, REC_BIAS, REC_BIAS};
+    float ff[3] = {0.f, 0.f, 0.f};
+    ok = true;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        const float cc = __fmul_rn((float)ci[d] + 0.5f, S.cellw32[d]);
+        const bool fin = fabsf(X[d]) < 1048576.0f;
+        const float m = fin ? rintf(__fmul_rn(__fadd_rn(X[d], F[d]) - cc, S.invLf[d])) : 0.f;
+        o[d] = REC_BIAS - (int)m * __float2int_rn(S.L8[d] * 8.0f) - (d == 0 ? 0 : rec_origin8(S, d, (int)ci[d]));
+        ff[d] = -m * S.Lr8[d];
+        const int g = __float2int_rz(X[d] * 8.0f) + o[d];
+        ok = ok && fin && g >= 0 && g < (d == 0 ? 4096 : 1024);
+    }
+    const uint32_t po = (uint32_t)o[0] + ((uint32_t)o[1] << 12) + ((uint32_t)o[2] << 22);
+    return make_float4(ff[0], ff[1], ff[2], __uint_as_float(po));
+}
+
+// record from the coarse/fine position view (A, B) and the frame
+__device__ __forceinline__ float4 make_record(const float4& A, const float4& B, const float4& fr) {
+    const uint32_t w = (uint32_t)__float2int_rz(A.x * 8.0f) + ((uint32_t)__float2int_rz(A.y * 8.0f) << 12) +
+                       ((uint32_t)__float2int_rz(A.z * 8.0f) << 22) + __float_as_uint(fr.w);
+    return make_float4(B.x + fr.x, B.y + fr.y, B.z + fr.z, __uint_as_float(w));
+}
+
+// cell coordinates of local bucket b
+__device__ __forceinline__ void cell_coords(const SysConst& S, uint32_t b, uint32_t* ci) {
+    ci[0] = b % (uint32_t)S.nc[0];
+    ci[1] = (b / (uint32_t)S.nc[0]) % (uint32_t)S.nc[1];
+    ci[2] = b / (uint32_t)(S.nc[0] * S.nc[1]);
+}
 
 constexpr int BLOCK = 256;
 constexpr uint32_t RED_CHUNK = 4096;   // atoms per reduction chunk

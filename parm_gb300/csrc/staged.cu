@@ -18,22 +18,26 @@
 // indices.  Kx <= nx - 2 and Ky <= ny - 2, so no atom appears twice in a
 // block's neighbourhood.
 //
-// Staged record (16 bytes) of atom j in the frame of block origin C (a point
-// of the 1/8 grid): the image n of j that lies next to its piece is
-// n = round((P - X_j) / L) (P: the piece's unwrapped centre); the coarse part
-// q = 8 * (X_j + n L8 - C) is an exact integer in [-256, 255] (L8: L rounded
-// to the 1/8 grid), stored as q + 256 in three 10-bit slots of one word; the
-// fine part xf_j + n (L - L8) is FP32.  A pair displacement is then
-// 0.125 * (q_i - q_j) + (f_i - f_j): the coarse difference is exact and only
-// the fine parts round, the accuracy of the coarse/fine split of the gather
-// kernel.  One 32-bit subtraction (W_i + 512 per slot) - W_j forms the three
-// biased differences at once (each in [1, 1023], so no borrow crosses a
-// slot), and OR-ing a slot into the mantissa of 1.5 * 2^20 (ulp 1/8) turns it
-// into 1.5 * 2^20 + (q_i - q_j + 512) / 8 exactly.
+// Staged record (16 bytes) of atom j: its cell-block record (kept per atom
+// by the list build and the time-step kernels; parm_ctx.cuh) moved into the
+// block's frame.  The block frame's origin is the lower edge of its first
+// neighbour cell along each axis (on the 1/8 grid); a piece adds one packed
+// constant K_p (its periodic shift and, along y and z, its row origin, in
+// units of 1/8) to the coarse fields and its periodic shift's fine part
+// s (L - L8) to the fine part.  Every staged field is then an exact integer
+// 8 * (local position) + 256 within [0, 3840) (x, 12 bits) or [0, 768)
+// (y, z, 10 bits), and a pair displacement is 0.125 * (q_i - q_j) +
+// (f_i - f_j): the coarse difference is exact and only the fine parts round.
+// One 32-bit subtraction (W_i + 256 per field) - W_j forms the three biased
+// differences at once (each in [0, 2^bits) for atoms less than 32 apart, so
+// no borrow crosses a field), and OR-ing a field into the mantissa of
+// 1.5 * 2^20 (ulp 1/8) turns it into 1.5 * 2^20 + (q_i - q_j + 256) / 8
+// exactly.
 //
 // The list build only screens candidates, so it stages plain FP32 positions
-// relative to C (0.125 q + f, one rounding); pairs within 2e-5 (relative, on
-// r^2) of the threshold are decided by the exact FP64 test.
+// relative to the centre of the block's neighbourhood (0.125 (q - c) + f, one
+// rounding); pairs within 2e-5 (relative, on r^2) of the threshold are
+// decided by the exact FP64 test.
 //
 // Lists.  Entries are 16-bit local indices.  The home atoms of a block are the
 // atoms of its own pieces in the z = 0 layer (one contiguous range of memory
@@ -54,10 +58,11 @@ struct StgTable {
     uint32_t g0[STG_PIECES_MAX];        // first atom of each piece
     uint32_t cnt[STG_PIECES_MAX];       // atoms in each piece
     uint32_t off[STG_PIECES_MAX + 1];   // local index of the first atom of each piece
-    float P[STG_PIECES_MAX][3];         // unwrapped centre of each piece
+    uint32_t K[STG_PIECES_MAX];         // packed coarse shift of each piece
+    float F[STG_PIECES_MAX][3];         // fine part of each piece's periodic shift
     uint32_t rowbase[STG_ROWS_MAX];     // bucket of cell x = 0 of each row
     uint32_t hoff[STG_KY_MAX + 1];      // home atoms before each home row
-    float C[3];                         // block frame origin (1/8 grid)
+    int pc[3];                          // 256 + 8 * (neighbourhood centre) (plain positions)
     uint32_t nrow, npiece, total, nhome, nyr;
     int x0, x1, y0, y1, z;
 };
@@ -75,36 +80,44 @@ __device__ void stg_setup(const DevCtx& c, const SysConst& S, const uint4& bd, S
     const int npiece = 3 * nrow;
     const uint32_t b0 = c.bucket_off[bd.x];
     const int nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
+    // block frame origin (units of 1/8): lower edge of the first neighbour cell
+    const int xb8 = rec_origin8(S, 0, x0 - 1), yb8 = rec_origin8(S, 1, y0 - 1);
+    const int zb8 = (ND == 3) ? rec_origin8(S, 2, z - 1) : 0;
     // one thread per piece (row r = t / 3, part t % 3: left cell, the block's
     // cells, right cell)
     for (int t = threadIdx.x; t < npiece; t += blockDim.x) {
         const int r = t / 3, part = t % 3;
         const int dz = (ND == 3) ? r / nyr - 1 : 0;
-        const int yy = y0 - 1 + r % nyr;
-        const int cy = wrap_idx(yy, ny), cz = (ND == 3) ? wrap_idx(z + dz, nz) : 0;
+        const int yy = y0 - 1 + r % nyr, zz = z + dz;
+        const int cy = wrap_idx(yy, ny), cz = (ND == 3) ? wrap_idx(zz, nz) : 0;
         const uint32_t rb = b0 + (uint32_t)((cz * ny + cy) * nx);
         if (part == 0) T.rowbase[r] = rb;
         uint32_t lo, hi;
-        float px;
+        int sx = 0;   // periodic shift of the piece along x (boxes)
         if (part == 0) {
             lo = rb + (uint32_t)wrap_idx(x0 - 1, nx);
             hi = lo + 1;
-            px = ((float)x0 - 0.5f) * S.cellw32[0];
+            sx = x0 == 0 ? -1 : 0;
         } else if (part == 1) {
             lo = rb + (uint32_t)x0;
             hi = rb + (uint32_t)x1;
-            px = 0.5f * (float)(x0 + x1) * S.cellw32[0];
         } else {
             lo = rb + (uint32_t)wrap_idx(x1, nx);
             hi = lo + 1;
-            px = ((float)x1 + 0.5f) * S.cellw32[0];
+            sx = x1 == nx ? 1 : 0;
         }
+        const int sy = yy < 0 ? -1 : (yy >= ny ? 1 : 0);
+        const int sz = (ND == 3) ? (zz < 0 ? -1 : (zz >= nz ? 1 : 0)) : 0;
         const uint32_t g = c.cell_start[lo];
         T.g0[t] = g;
         T.cnt[t] = c.cell_start[hi] - g;
-        T.P[t][0] = px;
-        T.P[t][1] = ((float)yy + 0.5f) * S.cellw32[1];
-        T.P[t][2] = (ND == 3) ? ((float)(z + dz) + 0.5f) * S.cellw32[2] : 0.f;
+        const int kx = sx * (int)(S.L8[0] * 8.0f) - xb8;
+        const int ky = rec_origin8(S, 1, cy) + sy * (int)(S.L8[1] * 8.0f) - yb8;
+        const int kz = (ND == 3) ? rec_origin8(S, 2, cz) + sz * (int)(S.L8[2] * 8.0f) - zb8 : 0;
+        T.K[t] = (uint32_t)kx + ((uint32_t)ky << 12) + ((uint32_t)kz << 22);
+        T.F[t][0] = (float)sx * S.Lr8[0];
+        T.F[t][1] = (float)sy * S.Lr8[1];
+        T.F[t][2] = (float)sz * S.Lr8[2];
     }
     __syncthreads();
     if (threadIdx.x < 32) {
@@ -138,48 +151,19 @@ __device__ void stg_setup(const DevCtx& c, const SysConst& S, const uint4& bd, S
             }
             T.hoff[y1 - y0] = h;
             T.nhome = h;
-            // frame origin: the block's centre rounded to the 1/8 grid
-            const double cx = 0.5 * (double)(x0 + x1) * S.cellw[0];
-            const double cy = 0.5 * (double)(y0 + y1) * S.cellw[1];
-            const double cz = (ND == 3) ? ((double)z + 0.5) * S.cellw[2] : 0.0;
-            T.C[0] = (float)(rint(cx * 8.0) * 0.125);
-            T.C[1] = (float)(rint(cy * 8.0) * 0.125);
-            T.C[2] = (float)(rint(cz * 8.0) * 0.125);
+            // centre of the neighbourhood in the block frame (plain positions)
+            T.pc[0] = REC_BIAS + (int)rint(4.0 * (double)(x1 - x0 + 2) * S.cellw[0]);
+            T.pc[1] = REC_BIAS + (int)rint(4.0 * (double)(y1 - y0 + 2) * S.cellw[1]);
+            T.pc[2] = REC_BIAS + ((ND == 3) ? (int)rint(12.0 * S.cellw[2]) : 0);
         }
     }
     __syncthreads();
 }
 
-// the staged record of an atom, from its position view (A: coarse, B: fine),
-// seen from piece centre P
-template <int ND>
-__device__ __forceinline__ float4 stg_convert(const DevCtx& c, const SysConst& S, const StgTable& T,
-                                              const float4& A, const float4& B, const float* P) {
-    const float kShift = 12582912.0f;
-    const float X[3] = {A.x, A.y, A.z}, F[3] = {B.x, B.y, B.z};
-    float fo[3] = {0.f, 0.f, 0.f};
-    uint32_t packed = 0;
-    bool bad = false;
-#pragma unroll
-    for (int d = 0; d < ND; d++) {
-        const float n = __fsub_rn(__fmaf_rn(P[d] - X[d], S.invLf[d], kShift), kShift);
-        const float u = __fmaf_rn(n, S.L8[d], __fsub_rn(X[d], T.C[d]));   // exact
-        fo[d] = __fmaf_rn(n, S.Lr8[d], F[d]);
-        int q = __float2int_rn(u * 8.0f);
-        bad |= !(fabsf(X[d]) < 1048576.0f) || q < -256 || q > 255;
-        q = q < -256 ? -256 : (q > 255 ? 255 : q);
-        packed |= (uint32_t)(q + 256) << (10 * d);
-    }
-    if (bad) atomicOr(c.status, ST_IMAGE_RANGE);
-    return make_float4(fo[0], fo[1], fo[2], __uint_as_float(packed));
-}
-
-template <int ND>
-__device__ __forceinline__ float4 stg_record(const DevCtx& c, const SysConst& S, const StgTable& T,
-                                             uint32_t j, const float* P) {
-    float4 A, B;
-    ld_pos(c.pos, j, A, B);
-    return stg_convert<ND>(c, S, T, A, B, P);
+// cell-block record R of an atom of piece p, moved into the block frame
+__device__ __forceinline__ float4 stg_shift(const StgTable& T, uint32_t p, const float4& R) {
+    return make_float4(R.x + T.F[p][0], R.y + T.F[p][1], R.z + T.F[p][2],
+                       __uint_as_float(__float_as_uint(R.w) + T.K[p]));
 }
 
 // piece of local index q (binary search over the offsets)
@@ -212,45 +196,44 @@ __device__ __forceinline__ float4 stg_get(const DevCtx& c, const SysConst& S, co
                                           const float4* srec, uint32_t cap, uint32_t q) {
     if (q < cap) return srec[q];
     const uint32_t p = stg_piece(T, q);
-    return stg_record<ND>(c, S, T, T.g0[p] + (q - T.off[p]), T.P[p]);
+    return stg_shift(T, p, c.rec[T.g0[p] + (q - T.off[p])]);
 }
 
-constexpr uint32_t STG_GUARD = 256u | (256u << 10) | (256u << 20);   // + 256 per slot
+constexpr uint32_t STG_GUARD = 256u | (256u << 12) | (256u << 22);   // + 256 per field
 constexpr uint32_t STG_MANT = 0x49C00000u;                           // 1.5 * 2^20, ulp 1/8
-constexpr float STG_K = 1572864.0f + 64.0f;                          // 1.5 * 2^20 + 512 / 8
+constexpr float STG_K = 1572864.0f + 32.0f;                          // 1.5 * 2^20 + 256 / 8
 
-// W_i + 512 per slot (the home atom's side of the packed subtraction)
-__device__ __forceinline__ uint32_t stg_wi(const float4& ri) { return __float_as_uint(ri.w) + 2u * STG_GUARD; }
+// W_i + 256 per field (the home atom's side of the packed subtraction)
+__device__ __forceinline__ uint32_t stg_wi(const float4& ri) { return __float_as_uint(ri.w) + STG_GUARD; }
 
 // displacement x_i - x_j from two packed records
 template <int ND>
 __device__ __forceinline__ void stg_disp(uint32_t wi, const float4& ri, const float4& rj, float* r) {
     const uint32_t D = wi - __float_as_uint(rj.w);
-    r[0] = (__uint_as_float((D & 0x3FFu) | STG_MANT) - STG_K) + (ri.x - rj.x);
-    r[1] = (__uint_as_float(((D >> 10) & 0x3FFu) | STG_MANT) - STG_K) + (ri.y - rj.y);
-    if constexpr (ND == 3) r[2] = (__uint_as_float((D >> 20) | STG_MANT) - STG_K) + (ri.z - rj.z);
+    r[0] = (__uint_as_float((D & 0xFFFu) | STG_MANT) - STG_K) + (ri.x - rj.x);
+    r[1] = (__uint_as_float(((D >> 12) & 0x3FFu) | STG_MANT) - STG_K) + (ri.y - rj.y);
+    if constexpr (ND == 3) r[2] = (__uint_as_float((D >> 22) | STG_MANT) - STG_K) + (ri.z - rj.z);
     else r[2] = 0.f;
 }
 
-// plain FP32 position relative to the block origin (list screening)
-__device__ __forceinline__ float4 stg_plain(const float4& rec, float w) {
+// plain FP32 position relative to the neighbourhood centre (list screening)
+__device__ __forceinline__ float4 stg_plain(const StgTable& T, const float4& rec, float w) {
     const uint32_t W = __float_as_uint(rec.w);
-    const float qx = (float)((int)(W & 0x3FFu) - 256), qy = (float)((int)((W >> 10) & 0x3FFu) - 256),
-                qz = (float)((int)(W >> 20) - 256);
+    const float qx = (float)((int)(W & 0xFFFu) - T.pc[0]), qy = (float)((int)((W >> 12) & 0x3FFu) - T.pc[1]),
+                qz = (float)((int)(W >> 22) - T.pc[2]);
     return make_float4(fmaf(qx, 0.125f, rec.x), fmaf(qy, 0.125f, rec.y), fmaf(qz, 0.125f, rec.z), w);
 }
 
-// warp-per-piece staging of the first `cap` local indices; EXTRA: 0 nothing,
-// 1 one float per atom (sigma), 2 the FP32 pair parameters; `plain`: FP32
-// positions with the list diameter in w instead of packed records
+// store the staged data of local index q (piece p, cell-block record R);
+// EXTRA: 0 nothing, 1 one float per atom (sigma), 2 the FP32 pair
+// parameters; `plain`: FP32 positions with the list diameter w instead of
+// packed records
 template <int ND, int EXTRA>
-__device__ __forceinline__ void stg_store(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec,
-                                          void* sext, uint32_t q, uint32_t p, const float4& A, const float4& B,
-                                          const float4& X, bool plain) {
-    const float P[3] = {T.P[p][0], T.P[p][1], T.P[p][2]};
-    const float4 rec = stg_convert<ND>(c, S, T, A, B, P);
+__device__ __forceinline__ void stg_store(const StgTable& T, float4* srec, void* sext, uint32_t q, uint32_t p,
+                                          const float4& R, const float4& X, float w, bool plain) {
+    const float4 rec = stg_shift(T, p, R);
     if (plain) {
-        srec[q] = stg_plain(rec, A.w);   // A.w: the list diameter
+        srec[q] = stg_plain(T, rec, w);
         return;
     }
     srec[q] = rec;
@@ -258,15 +241,21 @@ __device__ __forceinline__ void stg_store(const DevCtx& c, const SysConst& S, co
     else if constexpr (EXTRA == 2) static_cast<float4*>(sext)[q] = X;
 }
 
+// list diameter of atom j (the w of its coarse position view)
+__device__ __forceinline__ float stg_diam(const DevCtx& c, uint32_t j) {
+    return __ldg(reinterpret_cast<const float*>(c.pos + 2 * (size_t)j) + 3);
+}
+
 // Warp-per-piece staging of the first `cap` local indices.  Each warp takes
 // two pieces at a time and each lane issues the loads of up to four atoms
 // (two per piece) before converting any, so that their latencies overlap.
 template <int ND, int EXTRA>
 __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec, void* sext,
-                         uint32_t cap, int ext_sigma, bool plain = false) {
+                         uint32_t cap, int ext_sigma, bool plain = false, bool diam = false) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (uint32_t p0 = warp; p0 < T.npiece; p0 += 2 * nw) {
-        float4 A[4], B[4], X[4];
+        float4 R[4], X[4];
+        float w[4];
         uint32_t q[4], pc[4];
         bool ok[4];
 #pragma unroll
@@ -276,15 +265,17 @@ __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, 
             pc[k] = p;
             ok[k] = p < T.npiece && t < T.cnt[p] && T.off[p] + t < cap;
             q[k] = ok[k] ? T.off[p] + t : 0u;
+            w[k] = 0.f;
             if (ok[k]) {
                 const uint32_t j = T.g0[p] + t;
-                ld_pos(c.pos, j, A[k], B[k]);
+                R[k] = __ldg(&c.rec[j]);
+                if (diam) w[k] = stg_diam(c, j);
                 if constexpr (EXTRA != 0) X[k] = __ldg(&c.prm32[j]);
             }
         }
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (ok[k]) stg_store<ND, EXTRA>(c, S, T, srec, sext, q[k], pc[k], A[k], B[k], X[k], plain);
+            if (ok[k]) stg_store<ND, EXTRA>(T, srec, sext, q[k], pc[k], R[k], X[k], w[k], plain);
         // pieces longer than 64 atoms (large blocks of sparse systems)
 #pragma unroll 1
         for (int k = 0; k < 2; k++) {
@@ -292,10 +283,10 @@ __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, 
             if (p >= T.npiece) break;
             for (uint32_t t = lane + 64u; t < T.cnt[p] && T.off[p] + t < cap; t += 32u) {
                 const uint32_t j = T.g0[p] + t;
-                float4 a, b, x = make_float4(0.f, 0.f, 0.f, 0.f);
-                ld_pos(c.pos, j, a, b);
+                float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
                 if constexpr (EXTRA != 0) x = __ldg(&c.prm32[j]);
-                stg_store<ND, EXTRA>(c, S, T, srec, sext, T.off[p] + t, p, a, b, x, plain);
+                stg_store<ND, EXTRA>(T, srec, sext, T.off[p] + t, p, __ldg(&c.rec[j]), x,
+                                     diam ? stg_diam(c, j) : 0.f, plain);
             }
         }
     }
@@ -407,15 +398,14 @@ __device__ void stg_nonmembers(const DevCtx& c, uint32_t s, int zero_a) {
 // ---------------------------------------------------------------------------
 // list build: one CTA per block, one thread per home atom
 // ---------------------------------------------------------------------------
-template <int ND>
+// plain position of local index q; w: the list diameter (DIA) or 0
+template <int ND, int DIA>
 __device__ __forceinline__ float4 stg_get_plain(const DevCtx& c, const SysConst& S, const StgTable& T,
                                                 const float4* sp, uint32_t cap, uint32_t q) {
     if (q < cap) return sp[q];
     const uint32_t p = stg_piece(T, q);
     const uint32_t j = T.g0[p] + (q - T.off[p]);
-    float4 A, B;
-    ld_pos(c.pos, j, A, B);
-    return stg_plain(stg_convert<ND>(c, S, T, A, B, T.P[p]), A.w);
+    return stg_plain(T, stg_shift(T, p, c.rec[j]), DIA ? stg_diam(c, j) : 0.f);
 }
 
 template <int ND, int DIA, bool FULL>
@@ -424,8 +414,8 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
     const uint32_t maxnb = c.maxnb;
     uint16_t* out = c.nbr16;
     const float skin32 = (float)S.skin;
-    const float4 P = FULL ? sp[a.qi] : stg_get_plain<ND>(c, S, T, sp, cap, a.qi);
-    const float tu = P.w + skin32;
+    const float4 P = FULL ? sp[a.qi] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, a.qi);
+    const float tu = (DIA ? P.w : stg_diam(c, a.i)) + skin32;
     const float hiu = tu * tu * (1.0f + STG_BAND), lou = tu * tu * (1.0f - STG_BAND);
     const uint32_t oi = c.excl_off ? c.orig[a.i] : 0u;
     uint32_t k = 0;
@@ -446,7 +436,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
 #pragma unroll 8
                 for (uint32_t u = 0; u < m; u++) {
                     const uint32_t q = base + u;
-                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
+                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, q);
                     const float dx = P.x - Q.x, dyv = P.y - Q.y;
                     float rr = fmaf(dyv, dyv, dx * dx);
                     if constexpr (ND == 3) {
@@ -464,7 +454,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                     const uint32_t u = (uint32_t)__ffs(mask) - 1u;
                     mask &= mask - 1u;
                     const uint32_t q = base + u;
-                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND>(c, S, T, sp, cap, q);
+                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, q);
                     const float dx = P.x - Q.x, dyv = P.y - Q.y;
                     float rr = fmaf(dyv, dyv, dx * dx);
                     if constexpr (ND == 3) {
@@ -501,7 +491,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
 }
 
 template <int ND, int DIA>
-__global__ void __launch_bounds__(STG_THREADS) k_build_stg(DevCtx c) {
+__global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
     extern __shared__ float4 smem_b[];
     __shared__ StgTable T;
     if (blockIdx.x >= c.nblk) {
@@ -518,7 +508,7 @@ __global__ void __launch_bounds__(STG_THREADS) k_build_stg(DevCtx c) {
         return;
     }
     const uint32_t cap = c.stg_cap;
-    stg_load<ND, 0>(c, S, T, smem_b, nullptr, cap, 0, true);
+    stg_load<ND, 0>(c, S, T, smem_b, nullptr, cap, 0, true, DIA != 0);
     const bool full = T.total <= cap;
     for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
         const HomeAtom a = stg_home<ND>(c, T, h);
@@ -736,16 +726,16 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
             const uint32_t q0 = min(w & 0xFFFFu, qmax), q1 = min(w >> 16, qmax);
             const float4 ra = srec[q0], rb = srec[q1];
             const uint32_t D0 = wi - __float_as_uint(ra.w), D1 = wi - __float_as_uint(rb.w);
-            const f32x2 rx = add2(sub2(pk2(__uint_as_float((D0 & 0x3FFu) | STG_MANT),
-                                           __uint_as_float((D1 & 0x3FFu) | STG_MANT)), K2),
+            const f32x2 rx = add2(sub2(pk2(__uint_as_float((D0 & 0xFFFu) | STG_MANT),
+                                           __uint_as_float((D1 & 0xFFFu) | STG_MANT)), K2),
                                   pk2(ri.x - ra.x, ri.x - rb.x));
-            const f32x2 ry = add2(sub2(pk2(__uint_as_float(((D0 >> 10) & 0x3FFu) | STG_MANT),
-                                           __uint_as_float(((D1 >> 10) & 0x3FFu) | STG_MANT)), K2),
+            const f32x2 ry = add2(sub2(pk2(__uint_as_float(((D0 >> 12) & 0x3FFu) | STG_MANT),
+                                           __uint_as_float(((D1 >> 12) & 0x3FFu) | STG_MANT)), K2),
                                   pk2(ri.y - ra.y, ri.y - rb.y));
             f32x2 d2 = fma2(ry, ry, mul2(rx, rx));
             f32x2 rz = pk2(0.f, 0.f);
             if constexpr (ND == 3) {
-                rz = add2(sub2(pk2(__uint_as_float((D0 >> 20) | STG_MANT), __uint_as_float((D1 >> 20) | STG_MANT)),
+                rz = add2(sub2(pk2(__uint_as_float((D0 >> 22) | STG_MANT), __uint_as_float((D1 >> 22) | STG_MANT)),
                                K2),
                           pk2(ri.z - ra.z, ri.z - rb.z));
                 d2 = fma2(rz, rz, d2);
