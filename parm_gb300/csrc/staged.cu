@@ -433,10 +433,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
             for (uint32_t base = lo; base < hi; base += 32u) {
                 const uint32_t m = min(32u, hi - base);
                 uint32_t mask = 0u;
-#pragma unroll 8
-                for (uint32_t u = 0; u < m; u++) {
-                    const uint32_t q = base + u;
-                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, q);
+                auto screen = [&](const float4& Q) {
                     const float dx = P.x - Q.x, dyv = P.y - Q.y;
                     float rr = fmaf(dyv, dyv, dx * dx);
                     if constexpr (ND == 3) {
@@ -448,7 +445,26 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                         const float thr = 0.5f * (P.w + Q.w) + skin32;
                         hi2 = thr * thr * (1.0f + STG_BAND);
                     }
-                    mask |= (rr <= hi2 && q != a.qi) ? (1u << u) : 0u;
+                    return rr <= hi2;
+                };
+                if constexpr (FULL) {
+                    // all 32 slots (the stage has 32 records of padding past
+                    // its capacity), then the slots past the row and the
+                    // home atom itself are cleared
+                    const float4* sq = sp + base;
+#pragma unroll
+                    for (uint32_t u = 0; u < 16; u++) mask |= screen(sq[u]) ? (1u << u) : 0u;
+#pragma unroll
+                    for (uint32_t u = 0; u < 16; u++) mask |= screen(sq[16 + u]) ? (1u << (16 + u)) : 0u;
+                    if (m < 32u) mask &= (1u << m) - 1u;
+                    const uint32_t d = a.qi - base;
+                    if (d < 32u) mask &= ~(1u << d);
+                } else {
+#pragma unroll 8
+                    for (uint32_t u = 0; u < m; u++) {
+                        const uint32_t q = base + u;
+                        mask |= (screen(stg_get_plain<ND, DIA>(c, S, T, sp, cap, q)) && q != a.qi) ? (1u << u) : 0u;
+                    }
                 }
                 while (mask) {
                     const uint32_t u = (uint32_t)__ffs(mask) - 1u;
@@ -1010,7 +1026,8 @@ __global__ void __launch_bounds__(STG_THREADS) k_compress_stg(DevCtx c) {
 }
 
 // ---------------------------------------------------------------------------
-size_t stg_smem_build(const DevCtx& c) { return (size_t)c.stg_cap * sizeof(float4); }
+// the list build reads up to 31 records past a row's end: 32 records of padding
+size_t stg_smem_build(const DevCtx& c) { return ((size_t)c.stg_cap + 32) * sizeof(float4); }
 size_t stg_smem_force(const DevCtx& c) {
     const size_t ext = c.stg_prm == 1 ? sizeof(float) : (c.stg_prm == 2 ? sizeof(float4) : 0);
     return (size_t)c.stg_cap * (sizeof(float4) + ext);
