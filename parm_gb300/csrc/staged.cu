@@ -166,6 +166,26 @@ __device__ __forceinline__ float4 stg_shift(const StgTable& T, uint32_t p, const
                        __uint_as_float(__float_as_uint(R.w) + T.K[p]));
 }
 
+// one bulk request that brings [p, p + bytes) into L2 (16-byte aligned start
+// and size); it completes on its own and nothing waits for it
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// the records of the block's pieces (and, for the force kernel, the home
+// rows' lists) requested into L2 at once, ahead of the staging loads
+template <int ND>
+__device__ __forceinline__ void stg_prefetch(const DevCtx& c, const StgTable& T, bool lists) {
+    for (uint32_t t = threadIdx.x; t < T.npiece; t += blockDim.x)
+        if (T.cnt[t]) prefetch_l2(c.rec + T.g0[t], T.cnt[t] * 16u);
+    const uint32_t nhr = (uint32_t)(T.y1 - T.y0);
+    if (lists && threadIdx.x >= 128u && threadIdx.x - 128u < nhr) {
+        const uint32_t p = 3u * ((ND == 3 ? T.nyr : 0u) + (threadIdx.x - 128u) + 1u) + 1u;
+        // rows of maxnb 16-bit entries, maxnb a multiple of 8: 16-byte aligned
+        if (T.cnt[p]) prefetch_l2(c.nbr16 + (size_t)T.g0[p] * c.maxnb, T.cnt[p] * c.maxnb * 2u);
+    }
+}
+
 // piece of local index q (binary search over the offsets)
 __device__ __forceinline__ uint32_t stg_piece(const StgTable& T, uint32_t q) {
     uint32_t lo = 0, hi = T.npiece;   // off[lo] <= q < off[hi]
@@ -519,6 +539,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
     if (!c.flag[bd.x]) return;
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
+    stg_prefetch<ND>(c, T, false);
     if (T.total > 0xFFFFu) {   // more than 65535 atoms around one block
         if (threadIdx.x == 0) atomicOr(c.status, ST_TILE_OVERFLOW);
         return;
@@ -845,6 +866,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
     if (!c.active[bd.x]) return;   // frozen system: forces unchanged
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
+    stg_prefetch<ND>(c, T, true);
     const uint32_t cap = c.stg_cap;
     float4* srec = smem_f;
     void* sext = smem_f + cap;
