@@ -173,6 +173,9 @@ struct parm_system {
                 return fail(PARM_ERR_CAPACITY, "mixed precision: a tile or cell block has more distinct "
                                                "neighbours than its 16-bit index space (" +
                                                    std::to_string(TILE_ECAP) + " per tile, 65535 per block)");
+            if (stw & ST_STAGE_TIMEOUT)
+                return fail(PARM_ERR_RUNTIME, "mixed precision: a cell block's shared-memory copies did not "
+                                              "complete within the wait limit (forces of the call are invalid)");
             if (stw & ST_SORT_CAP)
                 return fail(PARM_ERR_CAPACITY, "FP64 path: a neighbour list exceeded 256 entries");
             if (stw & ST_NONFINITE) return fail(PARM_ERR_RUNTIME, "non-finite atom position");

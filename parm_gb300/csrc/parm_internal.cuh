@@ -33,6 +33,7 @@ enum StatusBits : uint32_t {
     ST_SORT_CAP = 1u << 3,       // FP64 path: a neighbour list longer than the in-thread sort buffer
     ST_TILE_OVERFLOW = 1u << 4,  // a tile had more distinct neighbours than its capacity
     ST_IMAGE_RANGE = 1u << 5,    // an atom is more than 7 box lengths from its tile frame
+    ST_STAGE_TIMEOUT = 1u << 6,  // a cell block's bulk copies did not complete within the wait limit
 };
 
 constexpr uint32_t NOT_MEMBER = 0xFFFFFFFFu;

@@ -313,6 +313,88 @@ __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, 
     __syncthreads();
 }
 
+// ---- bulk (TMA) staging: one asynchronous copy per piece into shared memory,
+// completion counted in bytes on one mbarrier ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// waits for phase 0 of the barrier, at most `limit` polls; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(0u)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Staging by bulk copies: every piece's records (and, EXTRA == 2, its FP32
+// pair parameters) are copied into shared memory as they lie in global
+// memory (one asynchronous copy per piece, 16-byte aligned, completion
+// counted on one mbarrier), then each warp moves its pieces' records into
+// the block frame in place.  Returns false (and flags ST_STAGE_TIMEOUT) when
+// the copies do not complete within the wait limit.
+template <int ND, int EXTRA>
+__device__ bool stg_load_bulk(const DevCtx& c, const StgTable& T, float4* srec, void* sext, uint32_t cap,
+                              uint64_t* bar) {
+    const uint32_t staged = min(T.total, cap);
+    const uint32_t per = (EXTRA == 2) ? 32u : 16u;
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_arrive_tx(bar, staged * per);
+    for (uint32_t p = threadIdx.x; p < T.npiece; p += blockDim.x) {
+        const uint32_t o = T.off[p];
+        if (o >= cap || T.cnt[p] == 0) continue;
+        const uint32_t n = min(T.cnt[p], cap - o);
+        bulk_g2s(srec + o, c.rec + T.g0[p], n * 16u, bar);
+        if constexpr (EXTRA == 2) bulk_g2s(static_cast<float4*>(sext) + o, c.prm32 + T.g0[p], n * 16u, bar);
+    }
+    bool ok = mbar_wait(bar, 1u << 22);
+    if (!ok) {
+        atomicOr(c.status, ST_STAGE_TIMEOUT);
+        mbar_wait(bar, 1u << 22);   // the copies in flight, once more with a limit
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t p = warp; p < T.npiece; p += nw) {
+        const uint32_t o = T.off[p];
+        if (o >= cap) continue;
+        const uint32_t n = min(T.cnt[p], cap - o);
+        const uint32_t K = T.K[p];
+        const float F0 = T.F[p][0], F1 = T.F[p][1], F2 = T.F[p][2];
+        for (uint32_t t = lane; t < n; t += 32u) {
+            float4 r = srec[o + t];
+            r.x += F0;
+            r.y += F1;
+            r.z += F2;
+            r.w = __uint_as_float(__float_as_uint(r.w) + K);
+            srec[o + t] = r;
+            if constexpr (EXTRA == 1) static_cast<float*>(sext)[o + t] = __ldg(&c.prm32[T.g0[p] + t].y);
+        }
+    }
+    __syncthreads();
+    return ok;
+}
+
 // home atom h -> (home row, global atom, local index, cell x)
 struct HomeAtom {
     uint32_t hr, i, qi, s0, H, hs;
@@ -879,7 +961,8 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
         a0 = stg_home<ND, false>(c, T, threadIdx.x);
         p0 = home_pre(c, a0);
     }
-    stg_load<ND, PRM>(c, S, T, srec, sext, cap, 1);
+    __shared__ uint64_t bar;
+    if (!stg_load_bulk<ND, PRM>(c, T, srec, sext, cap, &bar)) return;
     const bool full = T.total <= cap;
     for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
         const HomeAtom a = h == threadIdx.x ? a0 : stg_home<ND, false>(c, T, h);
