@@ -391,8 +391,7 @@ __device__ bool stg_load_bulk(const DevCtx& c, const StgTable& T, float4* srec, 
             if constexpr (EXTRA == 1) static_cast<float*>(sext)[o + t] = __ldg(&c.prm32[T.g0[p] + t].y);
         }
     }
-    __syncthreads();
-    return ok;
+    return __syncthreads_and(ok) != 0;   // the same answer in every thread
 }
 
 // home atom h -> (home row, global atom, local index, cell x)
