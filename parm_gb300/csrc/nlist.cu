@@ -250,35 +250,32 @@ __global__ void k_scatter(DevCtx c) {
     c.perm[c.cell_start[c.bucket[i]] + c.cslot[i]] = i;
 }
 
-// deterministic order inside a cell: ascending neighbour-list rank
-constexpr uint32_t CELLSORT_LOCAL = 48;
+// deterministic order inside a cell: ascending neighbour-list rank.  One warp
+// per cell: each lane holds one atom of the cell and counts the atoms ranked
+// before it (cells of up to 32 atoms; larger cells are sorted by lane 0).
 __global__ void k_cellsort(DevCtx c) {
-    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= c.nbucket) return;
-    uint32_t s = find_sys_of_bucket(c, b);
+    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (b >= c.nbucket) return;   // uniform in the warp
+    const uint32_t s = find_sys_of_bucket(c, b);
     if (!c.flag[s]) return;
-    uint32_t local = b - c.bucket_off[s];
+    const uint32_t local = b - c.bucket_off[s];
     if (local >= c.sys[s].ncell) return;  // non-member bucket is placed by nm_rank
     const uint32_t lo = c.cell_start[b], hi = c.cell_start[b + 1];
     const uint32_t cnt = hi - lo;
     if (cnt < 2) return;
-    if (cnt <= CELLSORT_LOCAL) {
-        uint32_t key[CELLSORT_LOCAL], val[CELLSORT_LOCAL];
-        for (uint32_t k = 0; k < cnt; k++) {
-            const uint32_t v = c.perm[lo + k];
-            const uint32_t rk = c.rank[v];
-            uint32_t p = k;
-            while (p > 0 && key[p - 1] > rk) {
-                key[p] = key[p - 1];
-                val[p] = val[p - 1];
-                p--;
-            }
-            key[p] = rk;
-            val[p] = v;
+    if (cnt <= 32u) {
+        const uint32_t v = lane < cnt ? c.perm[lo + lane] : 0u;
+        const uint32_t rk = lane < cnt ? c.rank[v] : 0xFFFFFFFFu;
+        uint32_t pos = 0;
+        for (uint32_t j = 0; j < cnt; j++) {
+            const uint32_t kj = __shfl_sync(0xFFFFFFFFu, rk, j);
+            pos += (kj < rk || (kj == rk && j < lane)) ? 1u : 0u;
         }
-        for (uint32_t k = 0; k < cnt; k++) c.perm[lo + k] = val[k];
+        __syncwarp();
+        if (lane < cnt) c.perm[lo + pos] = v;
         return;
     }
+    if (lane != 0) return;
     for (uint32_t k = lo + 1; k < hi; k++) {
         uint32_t v = c.perm[k];
         uint32_t key = c.rank[v];
@@ -807,7 +804,7 @@ void launch_rebuild(const DevCtx& c, cudaStream_t s) {
     k_scan_aux<<<1, SCAN_THREADS, 0, s>>>(c, nblk);
     k_scan_write<<<nblk, SCAN_THREADS, 0, s>>>(c);
     k_scatter<<<ga, BLOCK, 0, s>>>(c);
-    k_cellsort<<<grid_for(c.nbucket), BLOCK, 0, s>>>(c);
+    k_cellsort<<<(unsigned)(((size_t)c.nbucket * 32 + BLOCK - 1) / BLOCK), BLOCK, 0, s>>>(c);
     if (c.staged) {
         if (c.nd == 3) {
             k_gather<3><<<ga, BLOCK, 0, s>>>(c);
