@@ -519,6 +519,9 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
     const float tu = (DIA ? P.w : stg_diam(c, a.i)) + skin32;
     const float hiu = tu * tu * (1.0f + STG_BAND), lou = tu * tu * (1.0f - STG_BAND);
     const uint32_t oi = c.excl_off ? c.orig[a.i] : 0u;
+    // entry k of this atom: ob[(k / 2) * 2H + k % 2]
+    uint16_t* const ob = out + (size_t)a.s0 * maxnb + 2u * a.hs;
+    const uint32_t H2 = 2u * a.H;
     uint32_t k = 0;
 #pragma unroll 1
     for (int dz = 0; dz < (ND == 3 ? 3 : 1); dz++) {
@@ -533,20 +536,24 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
 #pragma unroll 1
             for (uint32_t base = lo; base < hi; base += 32u) {
                 const uint32_t m = min(32u, hi - base);
-                uint32_t mask = 0u;
-                auto screen = [&](const float4& Q) {
+                uint32_t mask = 0u, sure = 0u;
+                // bit of a candidate within the widened threshold (mask) and
+                // within the narrowed one (sure: kept without the exact test)
+                auto screen = [&](const float4& Q, uint32_t bit) {
                     const float dx = P.x - Q.x, dyv = P.y - Q.y;
                     float rr = fmaf(dyv, dyv, dx * dx);
                     if constexpr (ND == 3) {
                         const float dzv = P.z - Q.z;
                         rr = fmaf(dzv, dzv, rr);
                     }
-                    float hi2 = hiu;
+                    float hi2 = hiu, lo2 = lou;
                     if constexpr (DIA) {
                         const float thr = 0.5f * (P.w + Q.w) + skin32;
                         hi2 = thr * thr * (1.0f + STG_BAND);
+                        lo2 = thr * thr * (1.0f - STG_BAND);
                     }
-                    return rr <= hi2;
+                    mask |= rr <= hi2 ? bit : 0u;
+                    sure |= rr < lo2 ? bit : 0u;
                 };
                 if constexpr (FULL) {
                     // all 32 slots (the stage has 32 records of padding past
@@ -554,9 +561,9 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                     // home atom itself are cleared
                     const float4* sq = sp + base;
 #pragma unroll
-                    for (uint32_t u = 0; u < 16; u++) mask |= screen(sq[u]) ? (1u << u) : 0u;
+                    for (uint32_t u = 0; u < 16; u++) screen(sq[u], 1u << u);
 #pragma unroll
-                    for (uint32_t u = 0; u < 16; u++) mask |= screen(sq[16 + u]) ? (1u << (16 + u)) : 0u;
+                    for (uint32_t u = 0; u < 16; u++) screen(sq[16 + u], 1u << (16 + u));
                     if (m < 32u) mask &= (1u << m) - 1u;
                     const uint32_t d = a.qi - base;
                     if (d < 32u) mask &= ~(1u << d);
@@ -564,26 +571,14 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
 #pragma unroll 8
                     for (uint32_t u = 0; u < m; u++) {
                         const uint32_t q = base + u;
-                        mask |= (screen(stg_get_plain<ND, DIA>(c, S, T, sp, cap, q)) && q != a.qi) ? (1u << u) : 0u;
+                        if (q != a.qi) screen(stg_get_plain<ND, DIA>(c, S, T, sp, cap, q), 1u << u);
                     }
                 }
                 while (mask) {
                     const uint32_t u = (uint32_t)__ffs(mask) - 1u;
                     mask &= mask - 1u;
                     const uint32_t q = base + u;
-                    const float4 Q = FULL ? sp[q] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, q);
-                    const float dx = P.x - Q.x, dyv = P.y - Q.y;
-                    float rr = fmaf(dyv, dyv, dx * dx);
-                    if constexpr (ND == 3) {
-                        const float dzv = P.z - Q.z;
-                        rr = fmaf(dzv, dzv, rr);
-                    }
-                    float lo2 = lou;
-                    if constexpr (DIA) {
-                        const float thr = 0.5f * (P.w + Q.w) + skin32;
-                        lo2 = thr * thr * (1.0f - STG_BAND);
-                    }
-                    bool keep = rr < lo2;
+                    bool keep = (sure >> u) & 1u;
                     uint32_t j = 0xFFFFFFFFu;
                     if (!keep) {   // rare: the exact reference test
                         j = stg_global(T, q);
@@ -594,7 +589,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                         keep = !is_excluded_s(c, oi, c.orig[j]);
                     }
                     if (!keep) continue;
-                    if (k < maxnb) out[stg_entry16(a, maxnb, k)] = (uint16_t)q;
+                    if (k < maxnb) ob[(size_t)(k >> 1) * H2 + (k & 1u)] = (uint16_t)q;
                     k++;
                 }
             }
