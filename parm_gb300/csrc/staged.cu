@@ -519,10 +519,12 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
     const float tu = (DIA ? P.w : stg_diam(c, a.i)) + skin32;
     const float hiu = tu * tu * (1.0f + STG_BAND), lou = tu * tu * (1.0f - STG_BAND);
     const uint32_t oi = c.excl_off ? c.orig[a.i] : 0u;
-    // entry k of this atom: ob[(k / 2) * 2H + k % 2]
+    // entry k of this atom: ob[(k / 2) * 2H + k % 2], i.e. half k % 2 of the
+    // 32-bit word ow[(k / 2) * H] (maxnb is a multiple of 8)
     uint16_t* const ob = out + (size_t)a.s0 * maxnb + 2u * a.hs;
+    uint32_t* const ow = reinterpret_cast<uint32_t*>(ob);
     const uint32_t H2 = 2u * a.H;
-    uint32_t k = 0;
+    uint32_t k = 0, pend = 0u;
 #pragma unroll 1
     for (int dz = 0; dz < (ND == 3 ? 3 : 1); dz++) {
 #pragma unroll 1
@@ -574,6 +576,20 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                         if (q != a.qi) screen(stg_get_plain<ND, DIA>(c, S, T, sp, cap, q), 1u << u);
                     }
                 }
+                // entries are written as 32-bit words of two (the even one
+                // waits in `pend`)
+                if ((mask & ~sure) == 0u && !c.excl_off) {
+                    while (mask) {   // all kept
+                        const uint32_t q = base + (uint32_t)__ffs(mask) - 1u;
+                        mask &= mask - 1u;
+                        if (k < maxnb) {
+                            if (k & 1u) ow[(size_t)(k >> 1) * a.H] = pend | (q << 16);
+                            else pend = q;
+                        }
+                        k++;
+                    }
+                    continue;
+                }
                 while (mask) {
                     const uint32_t u = (uint32_t)__ffs(mask) - 1u;
                     mask &= mask - 1u;
@@ -589,11 +605,18 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                         keep = !is_excluded_s(c, oi, c.orig[j]);
                     }
                     if (!keep) continue;
-                    if (k < maxnb) ob[(size_t)(k >> 1) * H2 + (k & 1u)] = (uint16_t)q;
+                    if (k < maxnb) {
+                        if (k & 1u) ow[(size_t)(k >> 1) * a.H] = pend | (q << 16);
+                        else pend = q;
+                    }
                     k++;
                 }
             }
         }
+    }
+    {
+        const uint32_t kk = min(k, maxnb);
+        if (kk & 1u) ob[(size_t)(kk >> 1) * H2] = (uint16_t)pend;   // the last, unpaired entry
     }
     if (k > maxnb) {
         atomicOr(c.status, ST_NBR_OVERFLOW);
