@@ -100,6 +100,7 @@ struct parm_system {
     uint64_t last_launches = 0;
     // cell-block kernels of the mixed path (staged.cu)
     void* blk_mem = nullptr;
+    void* tab_mem = nullptr;
     void* nbr16_mem = nullptr;
     bool want_staged = true;     // prefer them when the grids allow
     bool stg_ok = false;         // the current grids allow them
@@ -117,6 +118,7 @@ struct parm_system {
         if (nbr_mem) cudaFree(nbr_mem);
         if (tlst_mem) cudaFree(tlst_mem);
         if (blk_mem) cudaFree(blk_mem);
+        if (tab_mem) cudaFree(tab_mem);
         if (nbr16_mem) cudaFree(nbr16_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
@@ -349,9 +351,13 @@ struct parm_system {
         }
         if (blk_mem) cudaFree(blk_mem);
         blk_mem = nullptr;
+        if (tab_mem) cudaFree(tab_mem);
+        tab_mem = nullptr;
         CUDA_TRY(cudaMalloc(&blk_mem, sizeof(uint4) * bl.size()));
         CUDA_TRY(cudaMemcpy(blk_mem, bl.data(), sizeof(uint4) * bl.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&tab_mem, (size_t)16 * STG_TAB_WORDS * bl.size()));
         c.blk = static_cast<const uint4*>(blk_mem);
+        c.stg_tab = static_cast<float4*>(tab_mem);
         c.nblk = (uint32_t)bl.size();
         c.stg_cap = (uint32_t)std::min(4096.0, std::ceil((1.5 * worst + 64.0) / 32.0) * 32.0);
         if (stage_cap_override) c.stg_cap = stage_cap_override;
@@ -367,6 +373,11 @@ struct parm_system {
             limits_set[dev] = true;
         }
         stg_ok = true;
+        if (c.staged) {
+            // fresh table memory: the tables of the current cells and box
+            launch_tables_stg(c, st);
+            CUDA_TRY(cudaGetLastError());
+        }
         return PARM_OK;
     }
 

@@ -111,6 +111,7 @@ struct DevCtx {
     uint32_t stg_prm;     // force kernel: 0 uniform parameters, 1 per-atom sigma, 2 all per atom
     uint32_t stg_dia;     // list build: per-atom list diameters
     const uint4* blk;     // per block: (system, x0 | x1 << 16, y0 | y1 << 16, z)
+    float4* stg_tab;      // per block: its table (STG_TAB_WORDS 16-byte words), set by the list build
     uint16_t* nbr16;      // staged lists (layout in staged.cu)
     // per-atom cell-block records (mixed path): see make_record below
     float4* rec;          // cell-block records (fine x, y, z, packed coarse fields), every step
@@ -156,6 +157,7 @@ void launch_tiles(const DevCtx& c, cudaStream_t s, int all);   // tiles of every
 void launch_numpairs(const DevCtx& c, cudaStream_t s);   // -> sysout[s] (as double)
 void launch_posq(const DevCtx& c, cudaStream_t s);
 void launch_reframe(const DevCtx& c, cudaStream_t s);
+void launch_tables_stg(const DevCtx& c, cudaStream_t s);
 // integrate.cu
 void launch_drift(const DevCtx& c, cudaStream_t s, int mode, bool with_kick);
 void launch_kick(const DevCtx& c, cudaStream_t s, int mode);
@@ -263,7 +265,8 @@ constexpr int STG_KY_MAX = 6;
 constexpr int STG_ROWS_MAX = 3 * (STG_KY_MAX + 2);
 constexpr int STG_PIECES_MAX = 3 * STG_ROWS_MAX;
 constexpr int STG_KX_MAX = 32;
-constexpr int STG_THREADS_HOST = 256;   // threads per block of the cell-block kernels
+constexpr int STG_THREADS_HOST = 256;
+constexpr uint32_t STG_TAB_WORDS = 160;   // 16-byte words per block table (>= its size)   // threads per block of the cell-block kernels
 
 inline unsigned grid_for(uint32_t n, int block = BLOCK) {
     unsigned g = (unsigned)((n + block - 1) / block);

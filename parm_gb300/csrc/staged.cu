@@ -54,7 +54,7 @@ constexpr int STG_THREADS = STG_THREADS_HOST;
 constexpr float STG_BAND = 2e-5f;   // relative band on r^2 decided by the exact FP64 test
 constexpr float CUT_BAND_S = 4e-6f; // LJ cut-off band (see pair32.cu)
 
-struct StgTable {
+struct __align__(16) StgTable {
     uint32_t g0[STG_PIECES_MAX];        // first atom of each piece
     uint32_t cnt[STG_PIECES_MAX];       // atoms in each piece
     uint32_t off[STG_PIECES_MAX + 1];   // local index of the first atom of each piece
@@ -67,7 +67,24 @@ struct StgTable {
     int x0, x1, y0, y1, z;
 };
 
+static_assert(sizeof(StgTable) <= 16 * STG_TAB_WORDS, "block table larger than its slot");
+constexpr uint32_t STG_TAB_USED = (uint32_t)((sizeof(StgTable) + 15) / 16);
+
 __device__ __forceinline__ int wrap_idx(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// The block tables depend on the cell arrays and the box only: the list
+// build (and the list conversion) store them, the per-step kernels load them.
+__device__ __forceinline__ void stg_store_table(const DevCtx& c, const StgTable& T, uint32_t b) {
+    const float4* src = reinterpret_cast<const float4*>(&T);
+    for (uint32_t t = threadIdx.x; t < STG_TAB_USED; t += blockDim.x)
+        c.stg_tab[(size_t)b * STG_TAB_WORDS + t] = src[t];
+}
+__device__ __forceinline__ void stg_load_table(const DevCtx& c, StgTable& T, uint32_t b) {
+    float4* dst = reinterpret_cast<float4*>(&T);
+    for (uint32_t t = threadIdx.x; t < STG_TAB_USED; t += blockDim.x)
+        dst[t] = __ldg(&c.stg_tab[(size_t)b * STG_TAB_WORDS + t]);
+    __syncthreads();
+}
 
 // fill the block table (all threads; ends with a barrier)
 template <int ND>
@@ -638,6 +655,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
     if (!c.flag[bd.x]) return;
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
+    stg_store_table(c, T, blockIdx.x);
     stg_prefetch<ND>(c, T, false);
     if (T.total > 0xFFFFu) {   // more than 65535 atoms around one block
         if (threadIdx.x == 0) atomicOr(c.status, ST_TILE_OVERFLOW);
@@ -964,7 +982,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
     const uint4 bd = c.blk[blockIdx.x];
     if (!c.active[bd.x]) return;   // frozen system: forces unchanged
     const SysConst& S = c.sys[bd.x];
-    stg_setup<ND>(c, S, bd, T);
+    stg_load_table(c, T, blockIdx.x);
     stg_prefetch<ND>(c, T, true);
     const uint32_t cap = c.stg_cap;
     float4* srec = smem_f;
@@ -1023,7 +1041,7 @@ __global__ void __launch_bounds__(32) k_band_stg(DevCtx c) {
         const uint2 it = c.bandq[it_k];
         const uint4 bd = c.blk[it.x];
         const SysConst& S = c.sys[bd.x];
-        stg_setup<ND>(c, S, bd, T);
+        stg_load_table(c, T, it.x);
         const HomeAtom a = stg_home<ND, false>(c, T, it.y);
         const HomePre pre = home_pre(c, a);
         const float4 Qi = pre.Qi;
@@ -1126,6 +1144,7 @@ __global__ void __launch_bounds__(STG_THREADS) k_compress_stg(DevCtx c) {
     const uint4 bd = c.blk[blockIdx.x];
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
+    stg_store_table(c, T, blockIdx.x);
     const uint32_t maxnb = c.maxnb;
     for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
         const HomeAtom a = stg_home<ND>(c, T, h);
@@ -1189,6 +1208,22 @@ int stg_set_smem_limits() {
     limits_nd<3>(most, most);
     limits_nd<2>(most, most);
     return (int)cudaGetLastError();
+}
+
+// the tables of every block (after a box change on the same cell grids)
+template <int ND>
+__global__ void __launch_bounds__(STG_THREADS) k_tables_stg(DevCtx c) {
+    __shared__ StgTable T;
+    if (blockIdx.x >= c.nblk) return;
+    const uint4 bd = c.blk[blockIdx.x];
+    stg_setup<ND>(c, c.sys[bd.x], bd, T);
+    stg_store_table(c, T, blockIdx.x);
+}
+
+void launch_tables_stg(const DevCtx& c, cudaStream_t s) {
+    if (!c.nblk) return;
+    if (c.nd == 3) k_tables_stg<3><<<c.nblk, STG_THREADS, 0, s>>>(c);
+    else k_tables_stg<2><<<c.nblk, STG_THREADS, 0, s>>>(c);
 }
 
 void launch_build_stg(const DevCtx& c, cudaStream_t s) {
