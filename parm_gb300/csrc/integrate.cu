@@ -15,6 +15,14 @@ namespace parm {
 
 __device__ __forceinline__ bool mobile(double m) { return !(m <= 0.0 || isinf(m)); }
 
+// the same test on the bit pattern (integer instructions, not the FP64 pipe):
+// NaN -> mobile; +-0, negative, +-inf -> not
+__device__ __forceinline__ bool mobile_bits(double m) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(m);
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    return mag > 0x7FF0000000000000ull || ((b >> 63) == 0ull && mag != 0ull && mag != 0x7FF0000000000000ull);
+}
+
 __device__ __forceinline__ void posq_split2(double x, float& X, float& xf) {
     double t = trunc(x * 8.0) * 0.125;
     X = (float)t;
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
         double* x = reinterpret_cast<double*>(&xv);
         double* v = reinterpret_cast<double*>(&vv);
         double* a = reinterpret_cast<double*>(&av);
-        const bool mob = mobile(m);
+        const bool mob = MIXED ? mobile_bits(m) : mobile(m);
         if constexpr (MIXED && MODE == DM_VERLET) {
             // leapfrog form of the same update: the previous step's closing
             // half kick and this step's opening one use the same force, so

@@ -792,7 +792,8 @@ void launch_tiles(const DevCtx& c, cudaStream_t s, int all);
 
 void launch_arm(const DevCtx& c, cudaStream_t s, int count_step, int use_cond,
                 unsigned long long handle) {
-    k_arm<<<1, 1024, 0, s>>>(c, count_step, use_cond, (cudaGraphConditionalHandle)handle);
+    const unsigned threads = c.nsys <= 32 ? 32u : (c.nsys <= 256 ? 256u : 1024u);
+    k_arm<<<1, threads, 0, s>>>(c, count_step, use_cond, (cudaGraphConditionalHandle)handle);
 }
 
 void launch_rebuild(const DevCtx& c, cudaStream_t s) {
