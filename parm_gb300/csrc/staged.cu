@@ -62,6 +62,7 @@ struct __align__(16) StgTable {
     float F[STG_PIECES_MAX][3];         // fine part of each piece's periodic shift
     uint32_t rowbase[STG_ROWS_MAX];     // bucket of cell x = 0 of each row
     uint32_t hoff[STG_KY_MAX + 1];      // home atoms before each home row
+    uint32_t hnmax[STG_KY_MAX];         // longest list of each home row (from the last build)
     int pc[3];                          // 256 + 8 * (neighbourhood centre) (plain positions)
     uint32_t nrow, npiece, total, nhome, nyr;
     int x0, x1, y0, y1, z;
@@ -79,6 +80,20 @@ __device__ __forceinline__ void stg_store_table(const DevCtx& c, const StgTable&
     for (uint32_t t = threadIdx.x; t < STG_TAB_USED; t += blockDim.x)
         c.stg_tab[(size_t)b * STG_TAB_WORDS + t] = src[t];
 }
+// longest list of each home row (all threads; ends with a barrier)
+template <int ND>
+__device__ void stg_row_nmax(const DevCtx& c, StgTable& T) {
+    for (uint32_t r = threadIdx.x; r < STG_KY_MAX; r += blockDim.x) T.hnmax[r] = 0u;
+    __syncthreads();
+    for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
+        uint32_t hr = 0;
+        while (h >= T.hoff[hr + 1]) hr++;
+        const uint32_t p = 3u * ((ND == 3 ? T.nyr : 0u) + hr + 1u) + 1u;
+        atomicMax(&T.hnmax[hr], c.nnb[T.g0[p] + (h - T.hoff[hr])]);
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ void stg_load_table(const DevCtx& c, StgTable& T, uint32_t b) {
     float4* dst = reinterpret_cast<float4*>(&T);
     for (uint32_t t = threadIdx.x; t < STG_TAB_USED; t += blockDim.x)
@@ -167,6 +182,7 @@ __device__ void stg_setup(const DevCtx& c, const SysConst& S, const uint4& bd, S
                 h += T.cnt[3 * (hbase + hr + 1) + 1];
             }
             T.hoff[y1 - y0] = h;
+            for (int r = 0; r < STG_KY_MAX; r++) T.hnmax[r] = 0u;
             T.nhome = h;
             // centre of the neighbourhood in the block frame (plain positions)
             T.pc[0] = REC_BIAS + (int)rint(4.0 * (double)(x1 - x0 + 2) * S.cellw[0]);
@@ -198,8 +214,12 @@ __device__ __forceinline__ void stg_prefetch(const DevCtx& c, const StgTable& T,
     const uint32_t nhr = (uint32_t)(T.y1 - T.y0);
     if (lists && threadIdx.x >= 128u && threadIdx.x - 128u < nhr) {
         const uint32_t p = 3u * ((ND == 3 ? T.nyr : 0u) + (threadIdx.x - 128u) + 1u) + 1u;
-        // rows of maxnb 16-bit entries, maxnb a multiple of 8: 16-byte aligned
-        if (T.cnt[p]) prefetch_l2(c.nbr16 + (size_t)T.g0[p] * c.maxnb, T.cnt[p] * c.maxnb * 2u);
+        // the row's lists are word-major (word w of atom h at w * H + h), so
+        // the words in use form a prefix; rows start 16-byte aligned (maxnb
+        // is a multiple of 8) and the prefix is rounded up inside the row
+        const uint32_t words = ((T.hnmax[threadIdx.x - 128u] + 1u) >> 1) * T.cnt[p];
+        const uint32_t bytes = min((words * 4u + 15u) & ~15u, T.cnt[p] * c.maxnb * 2u);
+        if (bytes) prefetch_l2(c.nbr16 + (size_t)T.g0[p] * c.maxnb, bytes);
     }
 }
 
@@ -640,6 +660,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
         k = maxnb;
     }
     c.nnb[a.i] = k;
+    atomicMax(const_cast<uint32_t*>(&T.hnmax[a.hr]), k);
 }
 
 template <int ND, int DIA>
@@ -655,7 +676,6 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
     if (!c.flag[bd.x]) return;
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
-    stg_store_table(c, T, blockIdx.x);
     stg_prefetch<ND>(c, T, false);
     if (T.total > 0xFFFFu) {   // more than 65535 atoms around one block
         if (threadIdx.x == 0) atomicOr(c.status, ST_TILE_OVERFLOW);
@@ -669,6 +689,8 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
         if (full) build_home<ND, DIA, true>(c, S, T, smem_b, cap, a);
         else build_home<ND, DIA, false>(c, S, T, smem_b, cap, a);
     }
+    __syncthreads();   // the home rows' longest lists are in the table now
+    stg_store_table(c, T, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1144,7 +1166,6 @@ __global__ void __launch_bounds__(STG_THREADS) k_compress_stg(DevCtx c) {
     const uint4 bd = c.blk[blockIdx.x];
     const SysConst& S = c.sys[bd.x];
     stg_setup<ND>(c, S, bd, T);
-    stg_store_table(c, T, blockIdx.x);
     const uint32_t maxnb = c.maxnb;
     for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
         const HomeAtom a = stg_home<ND>(c, T, h);
@@ -1164,6 +1185,9 @@ __global__ void __launch_bounds__(STG_THREADS) k_compress_stg(DevCtx c) {
             c.nbr16[stg_entry16(a, maxnb, k)] = (uint16_t)q;
         }
     }
+    __syncthreads();
+    stg_row_nmax<ND>(c, T);
+    stg_store_table(c, T, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1217,6 +1241,7 @@ __global__ void __launch_bounds__(STG_THREADS) k_tables_stg(DevCtx c) {
     if (blockIdx.x >= c.nblk) return;
     const uint4 bd = c.blk[blockIdx.x];
     stg_setup<ND>(c, c.sys[bd.x], bd, T);
+    stg_row_nmax<ND>(c, T);
     stg_store_table(c, T, blockIdx.x);
 }
 
