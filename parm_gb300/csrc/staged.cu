@@ -696,7 +696,10 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
 // ---------------------------------------------------------------------------
 // pair forces: one CTA per block, one thread per home atom.  PRM: 0 uniform
 // parameters, 1 per-atom sigma (epsilon and exponent / cut-off uniform),
-// 2 per-atom (sqrt(eps), sigma, third).
+// 2 per-atom (sqrt(eps), sigma, third).  A launch loads the block's table
+// (stored by the list build), requests the pieces' records and the used part
+// of the home rows' lists into L2, copies the records into shared memory with
+// one bulk asynchronous copy per piece and moves them into the block frame.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float rcp_approx(float x) {
     float y;
@@ -778,7 +781,7 @@ struct Law {
 };
 
 // per-home-atom data loaded from global memory before the pair loop (issued
-// ahead of the staging barrier for a thread's first home atom)
+// ahead of the staging wait for a thread's first home atom)
 struct HomePre {
     uint32_t nn, w0, w1;
     float4 Qi;   // (sqrt(eps), sigma, third, m6)
@@ -1010,7 +1013,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
     float4* srec = smem_f;
     void* sext = smem_f + cap;
     // the first home atom's global data is requested before the staging
-    // barrier, so its latency overlaps with the staging loads
+    // wait, so its latency overlaps with the bulk copies
     HomeAtom a0{};
     HomePre p0{};
     const bool has0 = threadIdx.x < T.nhome;
