@@ -1055,12 +1055,19 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
 // Settles the home atoms that k_force_stg listed as having a pair within the
 // LJ cut-off band: their force is the kernel's FP32 sum plus the exact-test
 // corrections, added in list order as if done inline (records are rebuilt
-// from global memory, identical to the staged ones).  One warp per listed
-// atom; its lanes test the atom's pairs in parallel.
+// from global memory, identical to the staged ones).  One CTA of BAND_WARPS
+// warps per listed atom: warp w tests the list's chunks w, w + BAND_WARPS,
+// ... of 32 entries in parallel (each lane one entry), the corrections are
+// collected per entry and one thread adds them in list order.
+constexpr uint32_t BAND_WARPS = 3;
+constexpr uint32_t BAND_MAXK = 512;   // longer lists: the corrections of one chunk at a time
+
 template <int ND, int KIND, int MODE, int PRM>
-__global__ void __launch_bounds__(32) k_band_stg(DevCtx c) {
+__global__ void __launch_bounds__(32 * BAND_WARPS) k_band_stg(DevCtx c) {
     __shared__ StgTable T;
-    const uint32_t lane = threadIdx.x;
+    __shared__ float4 corr[BAND_MAXK];
+    __shared__ uint32_t flags[BAND_MAXK / 32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t nb = min(*c.bandn, c.n);
     for (uint32_t it_k = blockIdx.x; it_k < nb; it_k += gridDim.x) {
         const uint2 it = c.bandq[it_k];
@@ -1074,56 +1081,78 @@ __global__ void __launch_bounds__(32) k_band_stg(DevCtx c) {
         const uint32_t wi = stg_wi(ri);
         Law<KIND> law0;
         law0.set(12.0f * Qi.x * Qi.x, Qi.y, rcp_approx(Qi.y * Qi.y), Qi.z);
+        // the correction of entry k (FP32 pair force kept or cut wrongly)
+        auto entry = [&](uint32_t k, float* cv) -> bool {
+            const uint32_t w = __ldg(pre.row + (size_t)(k >> 1) * a.H);
+            const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
+            if (q == a.qi) return false;
+            const float4 rj = stg_get<ND>(c, S, T, nullptr, 0u, q);
+            float r[3];
+            stg_disp<ND>(wi, ri, rj, r);
+            float d2 = fmaf(r[1], r[1], r[0] * r[0]);
+            if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
+            Law<KIND> law = law0;
+            if constexpr (PRM == 1) {
+                const float sg = 0.5f * (Qi.y + c.prm32[stg_global(T, q)].y);
+                law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
+            } else if constexpr (PRM == 2) {
+                const float4 Qj = c.prm32[stg_global(T, q)];
+                const float sg = 0.5f * (Qi.y + Qj.y);
+                law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
+            }
+            float dd;
+            const float sc = law.lj_raw(d2, dd);
+            if (fabsf(dd) > law.band) return false;
+            const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
+            if (beyond == (dd > 0.0f)) return false;   // the FP32 test agreed
+            const float sg = beyond ? -sc : sc;
+#pragma unroll
+            for (int d = 0; d < 3; d++) cv[d] = d < ND ? r[d] * sg : 0.f;
+            return true;
+        };
         const float4 f0 = c.f32[a.i];
         float f[3] = {f0.x, f0.y, f0.z};
-        for (uint32_t base = 0; base < pre.nn; base += 32u) {
-            const uint32_t k = base + lane;
-            float cv[3] = {0.f, 0.f, 0.f};
-            bool need = false;
-            if (k < pre.nn) {
-                const uint32_t w = __ldg(pre.row + (size_t)(k >> 1) * a.H);
-                const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
-                if (q != a.qi) {
-                    const float4 rj = stg_get<ND>(c, S, T, nullptr, 0u, q);
-                    float r[3];
-                    stg_disp<ND>(wi, ri, rj, r);
-                    float d2 = fmaf(r[1], r[1], r[0] * r[0]);
-                    if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
-                    Law<KIND> law = law0;
-                    if constexpr (PRM == 1) {
-                        const float sg = 0.5f * (Qi.y + c.prm32[stg_global(T, q)].y);
-                        law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
-                    } else if constexpr (PRM == 2) {
-                        const float4 Qj = c.prm32[stg_global(T, q)];
-                        const float sg = 0.5f * (Qi.y + Qj.y);
-                        law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
-                    }
-                    float dd;
-                    const float sc = law.lj_raw(d2, dd);
-                    if (fabsf(dd) <= law.band) {
-                        const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
-                        if (beyond != (dd > 0.0f)) {   // the FP32 test disagreed
-                            need = true;
-                            const float sg = beyond ? -sc : sc;
-#pragma unroll
-                            for (int d = 0; d < ND; d++) cv[d] = r[d] * sg;
-                        }
+        if (pre.nn <= BAND_MAXK) {
+            for (uint32_t t = threadIdx.x; t < BAND_MAXK / 32; t += blockDim.x) flags[t] = 0u;
+            __syncthreads();
+            for (uint32_t base = 32u * warp; base < pre.nn; base += 32u * BAND_WARPS) {
+                const uint32_t k = base + lane;
+                float cv[3];
+                if (k < pre.nn && entry(k, cv)) {
+                    corr[k] = make_float4(cv[0], cv[1], cv[2], 0.f);
+                    atomicOr(&flags[k >> 5], 1u << (k & 31u));
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (uint32_t wd = 0; wd < (pre.nn + 31u) / 32u; wd++) {
+                    uint32_t m = flags[wd];
+                    while (m) {
+                        const uint32_t k = 32u * wd + (uint32_t)__ffs(m) - 1u;
+                        m &= m - 1u;
+                        const float4 v = corr[k];
+                        f[0] += v.x;
+                        f[1] += v.y;
+                        f[2] += v.z;
                     }
                 }
             }
-            // apply the corrections r * s in list order
-            uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
-            while (mask) {
-                const int src = __ffs(mask) - 1;
-                mask &= mask - 1u;
+        } else if (warp == 0) {
+            // very long list: one warp, one chunk at a time, in list order
+            for (uint32_t base = 0; base < pre.nn; base += 32u) {
+                const uint32_t k = base + lane;
+                float cv[3] = {0.f, 0.f, 0.f};
+                const bool need = k < pre.nn && entry(k, cv);
+                uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
+                while (mask) {
+                    const int src = __ffs(mask) - 1;
+                    mask &= mask - 1u;
 #pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    const float v = __shfl_sync(0xFFFFFFFFu, cv[d], src);
-                    f[d] += v;
+                    for (int d = 0; d < 3; d++) f[d] += __shfl_sync(0xFFFFFFFFu, cv[d], src);
                 }
             }
         }
-        if (lane == 0) {
+        if (threadIdx.x == 0) {
             c.f32[a.i] = make_float4(f[0], f[1], f[2], 0.f);
             if constexpr (MODE == FM_FORCES_A) {
                 const double m = c.m[a.i];
@@ -1280,9 +1309,9 @@ static void force_stg_prm(const DevCtx& c, cudaStream_t s) {
     }
     if (KIND == KIND_LJCUT) {
         switch (c.stg_prm) {
-            case 0: k_band_stg<ND, KIND, MODE, 0><<<BAND_CTAS, 32, 0, s>>>(c); break;
-            case 1: k_band_stg<ND, KIND, MODE, 1><<<BAND_CTAS, 32, 0, s>>>(c); break;
-            default: k_band_stg<ND, KIND, MODE, 2><<<BAND_CTAS, 32, 0, s>>>(c); break;
+            case 0: k_band_stg<ND, KIND, MODE, 0><<<BAND_CTAS, 32 * BAND_WARPS, 0, s>>>(c); break;
+            case 1: k_band_stg<ND, KIND, MODE, 1><<<BAND_CTAS, 32 * BAND_WARPS, 0, s>>>(c); break;
+            default: k_band_stg<ND, KIND, MODE, 2><<<BAND_CTAS, 32 * BAND_WARPS, 0, s>>>(c); break;
         }
     }
 }
