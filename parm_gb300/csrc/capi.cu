@@ -669,7 +669,7 @@ struct parm_system {
             launch_kick(c, st, dmode);
             if (timing)
                 for (auto& q : e) cudaEventDestroy(q);
-            launches = (uint64_t)nsteps * (3 + chain_len()) + 1;
+            launches = (uint64_t)nsteps * (step_kernels() + chain_len()) + 1;
             done = nsteps;
         }
         while (done < nsteps) {
@@ -691,7 +691,7 @@ struct parm_system {
                 it = graphs.emplace(key, ge).first;
             }
             CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
-            launches += 3ull * k + 1;
+            launches += step_kernels() * k + 1;
             if (timing) {
                 CUDA_TRY(cudaStreamSynchronize(st));
                 for (uint32_t q = 0; q < k; q++) {
@@ -719,6 +719,11 @@ struct parm_system {
     }
 
     // kernels in one rebuild chain (launch_rebuild)
+    // kernels of one time step outside the rebuild chain: arm, kick-drift,
+    // forces (+ the cell-block kernel's band pass for the LJ cut-off)
+    uint64_t step_kernels() const {
+        return 3 + ((c.prec == PREC_MIXED && c.staged && kind == PARM_LJCUT) ? 1 : 0);
+    }
     uint64_t chain_len() const {
         if (c.prec == PREC_FP64) return 11;
         return (!c.staged && c.ntile && c.tiled) ? 11 : 10;
