@@ -281,37 +281,20 @@ __device__ __forceinline__ float4 stg_plain(const StgTable& T, const float4& rec
     return make_float4(fmaf(qx, 0.125f, rec.x), fmaf(qy, 0.125f, rec.y), fmaf(qz, 0.125f, rec.z), w);
 }
 
-// store the staged data of local index q (piece p, cell-block record R);
-// EXTRA: 0 nothing, 1 one float per atom (sigma), 2 the FP32 pair
-// parameters; `plain`: FP32 positions with the list diameter w instead of
-// packed records
-template <int ND, int EXTRA>
-__device__ __forceinline__ void stg_store(const StgTable& T, float4* srec, void* sext, uint32_t q, uint32_t p,
-                                          const float4& R, const float4& X, float w, bool plain) {
-    const float4 rec = stg_shift(T, p, R);
-    if (plain) {
-        srec[q] = stg_plain(T, rec, w);
-        return;
-    }
-    srec[q] = rec;
-    if constexpr (EXTRA == 1) static_cast<float*>(sext)[q] = X.y;   // sigma
-    else if constexpr (EXTRA == 2) static_cast<float4*>(sext)[q] = X;
-}
-
 // list diameter of atom j (the w of its coarse position view)
 __device__ __forceinline__ float stg_diam(const DevCtx& c, uint32_t j) {
     return __ldg(reinterpret_cast<const float*>(c.pos + 2 * (size_t)j) + 3);
 }
 
-// Warp-per-piece staging of the first `cap` local indices.  Each warp takes
-// two pieces at a time and each lane issues the loads of up to four atoms
-// (two per piece) before converting any, so that their latencies overlap.
-template <int ND, int EXTRA>
-__device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, float4* srec, void* sext,
-                         uint32_t cap, int ext_sigma, bool plain = false, bool diam = false) {
+// Staging for the list build: plain FP32 positions of the first `cap` local
+// indices (w: the list diameter when `diam`, else 0), warp per piece.  Each
+// warp takes two pieces at a time and each lane issues the loads of up to
+// four atoms (two per piece) before converting any, so that their latencies
+// overlap.
+__device__ void stg_load_plain(const DevCtx& c, const StgTable& T, float4* sp, uint32_t cap, bool diam) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (uint32_t p0 = warp; p0 < T.npiece; p0 += 2 * nw) {
-        float4 R[4], X[4];
+        float4 R[4];
         float w[4];
         uint32_t q[4], pc[4];
         bool ok[4];
@@ -327,12 +310,11 @@ __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, 
                 const uint32_t j = T.g0[p] + t;
                 R[k] = __ldg(&c.rec[j]);
                 if (diam) w[k] = stg_diam(c, j);
-                if constexpr (EXTRA != 0) X[k] = __ldg(&c.prm32[j]);
             }
         }
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (ok[k]) stg_store<ND, EXTRA>(T, srec, sext, q[k], pc[k], R[k], X[k], w[k], plain);
+            if (ok[k]) sp[q[k]] = stg_plain(T, stg_shift(T, pc[k], R[k]), w[k]);
         // pieces longer than 64 atoms (large blocks of sparse systems)
 #pragma unroll 1
         for (int k = 0; k < 2; k++) {
@@ -340,10 +322,7 @@ __device__ void stg_load(const DevCtx& c, const SysConst& S, const StgTable& T, 
             if (p >= T.npiece) break;
             for (uint32_t t = lane + 64u; t < T.cnt[p] && T.off[p] + t < cap; t += 32u) {
                 const uint32_t j = T.g0[p] + t;
-                float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-                if constexpr (EXTRA != 0) x = __ldg(&c.prm32[j]);
-                stg_store<ND, EXTRA>(T, srec, sext, T.off[p] + t, p, __ldg(&c.rec[j]), x,
-                                     diam ? stg_diam(c, j) : 0.f, plain);
+                sp[T.off[p] + t] = stg_plain(T, stg_shift(T, p, __ldg(&c.rec[j])), diam ? stg_diam(c, j) : 0.f);
             }
         }
     }
@@ -682,7 +661,7 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
         return;
     }
     const uint32_t cap = c.stg_cap;
-    stg_load<ND, 0>(c, S, T, smem_b, nullptr, cap, 0, true, DIA != 0);
+    stg_load_plain(c, T, smem_b, cap, DIA != 0);
     const bool full = T.total <= cap;
     for (uint32_t h = threadIdx.x; h < T.nhome; h += blockDim.x) {
         const HomeAtom a = stg_home<ND>(c, T, h);
@@ -796,57 +775,6 @@ __device__ __forceinline__ HomePre home_pre(const DevCtx& c, const HomeAtom& a) 
     p.w0 = __ldg(p.row);       // entries of the first two words (read even when
     p.w1 = __ldg(p.row + a.H); // the list is shorter: they lie inside its region)
     return p;
-}
-
-// rare: settle the pairs within the LJ cut-off band by the exact FP64 test
-// (add those the FP32 test cut, remove those it kept wrongly); kept out of
-// line so that the pair loop keeps its registers
-template <int ND, int KIND, int PRM>
-__device__ __forceinline__ float3 band_fix(const DevCtx& c, const SysConst& S, const StgTable& T, const float4* srec,
-                                        const void* sext, uint32_t cap, uint32_t ai, uint32_t aqi, uint32_t H,
-                                        float rx, float ry, float rz, uint32_t wi, float qx, float qy, float qz,
-                                        float e12, float isig2, float third, const uint32_t* row, uint32_t nn,
-                                        float fx, float fy, float fz) {
-    float f[3] = {fx, fy, fz};
-    const float4 ri = make_float4(rx, ry, rz, __uint_as_float(wi));
-    const float4 Qi = make_float4(qx, qy, qz, 0.f);
-    Law<KIND> law0;
-    law0.set(e12, Qi.y, isig2, third);
-    HomeAtom a;
-    a.i = ai;
-    a.qi = aqi;
-    a.H = H;
-    const float* ssig = static_cast<const float*>(sext);
-    const float4* sprm = static_cast<const float4*>(sext);
-    for (uint32_t k = 0; k < nn; k++) {
-        const uint32_t w = __ldg(row + (size_t)(k >> 1) * H);
-        const uint32_t q = stg_check(c, T, (k & 1u) ? (w >> 16) : (w & 0xFFFFu), a.qi);
-        if (q == a.qi) continue;
-        const float4 rj = stg_get<ND>(c, S, T, srec, cap, q);
-        float r[3];
-        stg_disp<ND>(wi, ri, rj, r);
-        float d2 = fmaf(r[1], r[1], r[0] * r[0]);
-        if constexpr (ND == 3) d2 = fmaf(r[2], r[2], d2);
-        Law<KIND> law = law0;
-        if constexpr (PRM == 1) {
-            const float sj = q < cap ? ssig[q] : c.prm32[stg_global(T, q)].y;
-            const float sg = 0.5f * (Qi.y + sj);
-            law.set(law0.e12, sg, rcp_approx(sg * sg), law0.third);
-        } else if constexpr (PRM == 2) {
-            const float4 Qj = q < cap ? sprm[q] : c.prm32[stg_global(T, q)];
-            const float sg = 0.5f * (Qi.y + Qj.y);
-            law.set(12.0f * Qi.x * Qj.x, sg, rcp_approx(sg * sg), fmaxf(Qi.z, Qj.z));
-        }
-        float dd;
-        const float sc = law.lj_raw(d2, dd);
-        if (fabsf(dd) > law.band) continue;
-        const bool beyond = lj_beyond_exact_s(c, S, a.i, stg_global(T, q), ND);
-        if (beyond == (dd > 0.0f)) continue;   // the FP32 test agreed
-        const float sg = beyond ? -sc : sc;
-#pragma unroll
-        for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sg, f[d]);
-    }
-    return make_float3(f[0], f[1], f[2]);
 }
 
 template <int ND, int KIND, int PRM, bool FULL>
