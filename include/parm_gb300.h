@@ -55,6 +55,13 @@ extern "C" {
 #define PARM_EVAL_CONTACTS 3 /* NListed::contacts          src/interaction.hpp:2124-2137 */
 #define PARM_EVAL_OVERLAPS 4 /* NListed::overlaps          src/interaction.hpp:2139-2150 */
 
+/* mean-square-displacement tracker outputs (parm_rsq_get) */
+#define PARM_RSQ_XYZ2 0   /* RsqTracker::xyz2   nwin x natoms x ndim  src/constraints.cpp:457-464, 510-518 */
+#define PARM_RSQ_XYZ4 1   /* RsqTracker::xyz4   nwin x natoms x ndim  src/constraints.cpp:466-473, 537-545 */
+#define PARM_RSQ_R2 2     /* RsqTracker::r2     nwin x natoms         src/constraints.cpp:520-535 */
+#define PARM_RSQ_R4 3     /* RsqTracker::r4     nwin x natoms         src/constraints.cpp:475-481, 547-555 */
+#define PARM_RSQ_COUNTS 4 /* RsqTracker::counts nwin                  src/constraints.cpp:556-564 */
+
 #define PARM_NOT_MEMBER 0xFFFFFFFFu
 
 typedef struct parm_system parm_system;
@@ -136,6 +143,23 @@ int parm_kinetic_energy(parm_system* s, const double* origin, double* out);
 int parm_momentum(parm_system* s, double* momentum, double* mass);
 /* max over mobile atoms of |f|^2, per system (minimisation convergence). */
 int parm_max_force_sq(parm_system* s, double* out);
+
+/* Mean-square-displacement tracker on the device, replacing RsqTracker
+ * (src/constraints.hpp:318-361, src/constraints.cpp:404-560): windows of
+ * skips[j] tracker updates; each window keeps, per atom (caller order), the
+ * position at its last update and running sums of squared displacements.
+ * Positions are measured from each system's centre of mass when usecom
+ * (AtomGroup::com), as is.  parm_rsq_start (re)starts the tracker at the
+ * current positions (RsqTracker constructor / reset); parm_rsq_update is one
+ * RsqTracker::update; while a tracker is running every time step of
+ * parm_verlet / parm_damped / parm_sol updates it at the end of the step
+ * (Collection::timestep calls update_trackers there), inside the step's
+ * CUDA graph.  parm_rsq_get writes the means (PARM_RSQ_*); a window that has
+ * not been updated yet divides by a zero count, as the reference does. */
+int parm_rsq_start(parm_system* s, const uint64_t* skips, uint32_t nwin, int usecom);
+int parm_rsq_update(parm_system* s);
+int parm_rsq_get(parm_system* s, int what, double* out);
+int parm_rsq_stop(parm_system* s);
 
 /* Freeze systems of a batch: time steps and force evaluations skip the
  * systems whose active[s] is 0 (their atoms, forces and neighbour lists stay

@@ -31,6 +31,8 @@ X, V, A, F, M = 1, 2, 4, 8, 16
 
 EVAL_ENERGY, EVAL_VIRIAL, EVAL_STRESS, EVAL_CONTACTS, EVAL_OVERLAPS = range(5)
 
+RSQ_XYZ2, RSQ_XYZ4, RSQ_R2, RSQ_R4, RSQ_COUNTS = range(5)
+
 NOT_MEMBER = 0xFFFFFFFF
 
 _u32p = C.POINTER(C.c_uint32)
@@ -63,6 +65,10 @@ SIGNATURES = {
     "parm_kinetic_energy": (C.c_int, [_h, _dp, _dp]),
     "parm_momentum": (C.c_int, [_h, _dp, _dp]),
     "parm_max_force_sq": (C.c_int, [_h, _dp]),
+    "parm_rsq_start": (C.c_int, [_h, _u64p, C.c_uint32, C.c_int]),
+    "parm_rsq_update": (C.c_int, [_h]),
+    "parm_rsq_get": (C.c_int, [_h, C.c_int, _dp]),
+    "parm_rsq_stop": (C.c_int, [_h]),
     "parm_get_step": (C.c_int, [_h, _u64p]),
     "parm_set_step": (C.c_int, [_h, C.c_uint64]),
     "parm_set_nlist_capacity": (C.c_int, [_h, C.c_uint32]),

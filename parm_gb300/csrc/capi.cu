@@ -102,6 +102,7 @@ struct parm_system {
     void* blk_mem = nullptr;
     void* tab_mem = nullptr;
     void* nbr16_mem = nullptr;
+    void* rsq_mem = nullptr;     // mean-square-displacement tracker arrays
     bool want_staged = true;     // prefer them when the grids allow
     bool stg_ok = false;         // the current grids allow them
     bool stg_pending = false;    // grids changed under staged lists: switch back once every system rebuilt
@@ -120,6 +121,7 @@ struct parm_system {
         if (blk_mem) cudaFree(blk_mem);
         if (tab_mem) cudaFree(tab_mem);
         if (nbr16_mem) cudaFree(nbr16_mem);
+        if (rsq_mem) cudaFree(rsq_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
@@ -624,6 +626,7 @@ struct parm_system {
             if (prec == PREC_FP64) launch_force64(c, st, fmode);
             else launch_force32(c, st, fmode);
             if (timing) CUDA_TRY(cudaEventRecordWithFlags(ge.ev[3 * step + 2], st, cudaEventRecordExternal));
+            launch_rsq(c, st, 0);   // trackers, at the end of the step (positions final)
             CUDA_TRY(cudaGetLastError());
         }
         launch_kick(c, st, dmode);   // second half of the chunk's last step
@@ -664,6 +667,7 @@ struct parm_system {
                     t_force += b;
                     n_force += 1;
                 }
+                launch_rsq(c, st, 0);
                 CUDA_TRY(cudaGetLastError());
             }
             launch_kick(c, st, dmode);
@@ -722,7 +726,8 @@ struct parm_system {
     // kernels of one time step outside the rebuild chain: arm, kick-drift,
     // forces (+ the cell-block kernel's band pass for the LJ cut-off)
     uint64_t step_kernels() const {
-        return 3 + ((c.prec == PREC_MIXED && c.staged && kind == PARM_LJCUT) ? 1 : 0);
+        return 3 + ((c.prec == PREC_MIXED && c.staged && kind == PARM_LJCUT) ? 1 : 0) +
+               (c.rsq_n ? (c.rsq_com ? 5 : 2) : 0);
     }
     uint64_t chain_len() const {
         if (c.prec == PREC_FP64) return 11;
@@ -1418,6 +1423,96 @@ int parm_momentum(parm_system* S, double* momentum, double* mass) {
             if (momentum) momentum[(size_t)s * S->nd + d] = v[(size_t)s * (S->nd + 1) + d];
         if (mass) mass[s] = v[(size_t)s * (S->nd + 1) + S->nd];
     }
+    return PARM_OK;
+}
+
+// ---- mean-square-displacement tracker (RsqTracker) ----
+int parm_rsq_start(parm_system* S, const uint64_t* skips, uint32_t nskip, int usecom) {
+    if (!S || !skips) return fail(PARM_ERR_ARG, "NULL argument");
+    if (nskip == 0 || nskip > 64) return fail(PARM_ERR_ARG, "1 to 64 time windows");
+    for (uint32_t j = 0; j < nskip; j++)
+        if (skips[j] == 0) return fail(PARM_ERR_ARG, "window lengths must be >= 1");
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    if (S->rsq_mem) cudaFree(S->rsq_mem);
+    S->rsq_mem = nullptr;
+    S->c.rsq_n = 0;
+    const size_t per = (size_t)nskip * S->n;
+    const size_t bytes = 8 * ((size_t)nskip + 1 + nskip + 3 * per * S->nd + per);
+    CUDA_TRY(cudaMalloc(&S->rsq_mem, bytes));
+    CUDA_TRY(cudaMemsetAsync(S->rsq_mem, 0, bytes, S->st));
+    unsigned long long* skip = static_cast<unsigned long long*>(S->rsq_mem);
+    CUDA_TRY(cudaMemcpyAsync(skip, skips, 8 * (size_t)nskip, cudaMemcpyHostToDevice, S->st));
+    S->c.rsq_skip = skip;
+    S->c.rsq_cnt = skip + nskip;
+    double* d = reinterpret_cast<double*>(S->c.rsq_cnt + nskip + 1);
+    S->c.rsq_past = d;
+    S->c.rsq_x2 = d + per * S->nd;
+    S->c.rsq_x4 = d + 2 * per * S->nd;
+    S->c.rsq_r4 = d + 3 * per * S->nd;
+    S->c.rsq_com = usecom ? 1u : 0u;
+    S->c.rsq_n = nskip;
+    S->clear_graphs();
+    launch_rsq(S->c, S->st, 1);   // the windows start at the current positions
+    CUDA_TRY(cudaGetLastError());
+    return S->sync_status();
+}
+
+int parm_rsq_update(parm_system* S) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (!S->c.rsq_n) return fail(PARM_ERR_ARG, "no tracker (parm_rsq_start)");
+    TRY(S->flush());
+    launch_rsq(S->c, S->st, 0);
+    CUDA_TRY(cudaGetLastError());
+    return S->sync_status();
+}
+
+int parm_rsq_get(parm_system* S, int what, double* out) {
+    if (!S || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    const uint32_t nw = S->c.rsq_n;
+    if (!nw) return fail(PARM_ERR_ARG, "no tracker (parm_rsq_start)");
+    if (what < PARM_RSQ_XYZ2 || what > PARM_RSQ_COUNTS) return fail(PARM_ERR_ARG, "unknown tracker output");
+    TRY(S->flush());
+    const size_t n = S->n, nd = (size_t)S->nd, per = (size_t)nw * n;
+    std::vector<unsigned long long> cnt(nw + 1);
+    CUDA_TRY(cudaMemcpyAsync(cnt.data(), S->c.rsq_cnt, 8 * (nw + 1), cudaMemcpyDeviceToHost, S->st));
+    std::vector<double> v;
+    if (what != PARM_RSQ_COUNTS) {
+        const double* src = what == PARM_RSQ_XYZ4 ? S->c.rsq_x4 : (what == PARM_RSQ_R4 ? S->c.rsq_r4 : S->c.rsq_x2);
+        v.resize(what == PARM_RSQ_R4 ? per : per * nd);
+        CUDA_TRY(cudaMemcpyAsync(v.data(), src, 8 * v.size(), cudaMemcpyDeviceToHost, S->st));
+    }
+    TRY(S->sync_status());
+    // means over each window's updates, as RsqTracker1::xyz2 / xyz4 / r4 and
+    // RsqTracker::r2 (the row sum of the xyz2 means)
+    for (uint32_t j = 0; j < nw; j++) {
+        const double count = (double)cnt[1 + j];
+        if (what == PARM_RSQ_COUNTS) {
+            out[j] = count;
+        } else if (what == PARM_RSQ_R2) {
+            for (size_t i = 0; i < n; i++) {
+                const double* row = &v[(j * n + i) * nd];
+                double sum = row[0] / count;
+                for (size_t d = 1; d < nd; d++) sum = sum + row[d] / count;
+                out[j * n + i] = sum;
+            }
+        } else if (what == PARM_RSQ_R4) {
+            for (size_t i = 0; i < n; i++) out[j * n + i] = v[j * n + i] / count;
+        } else {
+            for (size_t k = 0; k < n * nd; k++) out[j * n * nd + k] = v[j * n * nd + k] / count;
+        }
+    }
+    return PARM_OK;
+}
+
+int parm_rsq_stop(parm_system* S) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    if (S->rsq_mem) cudaFree(S->rsq_mem);
+    S->rsq_mem = nullptr;
+    S->c.rsq_n = 0;
+    S->clear_graphs();
     return PARM_OK;
 }
 

@@ -442,6 +442,14 @@ __global__ void k_atoms(DevCtx c, int what, const double* origin) {
 #pragma unroll
         for (int d = 0; d < ND; d++) c.red[(size_t)d * c.n + i] = ok ? v[d] * m : 0.0;
         c.red[(size_t)ND * c.n + i] = ok ? m : 0.0;
+    } else if (what == AW_COM) {
+        // AtomGroup::com / mass (box.cpp:228-247): skip m <= 0 or inf
+        bool ok = mobile(m);
+        V xv = static_cast<const V*>(c.x)[i];
+        const double* x = reinterpret_cast<const double*>(&xv);
+#pragma unroll
+        for (int d = 0; d < ND; d++) c.red[(size_t)d * c.n + i] = ok ? x[d] * m : 0.0;
+        c.red[(size_t)ND * c.n + i] = ok ? m : 0.0;
     } else {
         double q = 0.0;
         if (mobile(m)) {
@@ -530,6 +538,84 @@ __global__ void __launch_bounds__(RED_THREADS) k_sys_reduce(DevCtx c, int ncomp)
 void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp) {
     k_red_chunks<<<c.nchunk, RED_THREADS, 0, s>>>(c, ncomp);
     k_sys_reduce<<<c.nsys, RED_THREADS, 0, s>>>(c, ncomp);
+}
+
+// ---------------------------------------------------------------------------
+// Mean-square-displacement tracker: RsqTracker / RsqTracker1
+// (src/constraints.hpp:318-361, src/constraints.cpp:404-560).  Per atom (by
+// caller index) and window j: the position r = x - com at the window's last
+// update and the running sums of (r - r_past)^2 per axis, of its square, and
+// of the squared squared distance.  One update advances the tracker time t
+// and updates the windows whose length divides t, in the reference's
+// arithmetic (componentwise FP64, no contraction).
+// ---------------------------------------------------------------------------
+__global__ void k_rsq_tick(DevCtx c) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const unsigned long long t = c.rsq_cnt[0] + 1ull;
+    c.rsq_cnt[0] = t;
+    for (uint32_t j = 0; j < c.rsq_n; j++)
+        if (t % c.rsq_skip[j] == 0ull) c.rsq_cnt[1 + j] += 1ull;
+}
+
+template <int ND, bool INIT>
+__global__ void k_rsq(DevCtx c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    using V = typename DVec<ND>::T;
+    const uint32_t o = c.orig[i], s = c.atom_sys[i];
+    V xv = static_cast<const V*>(c.x)[i];
+    const double* x = reinterpret_cast<const double*>(&xv);
+    double r[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        // com: (sum of m x) / mass per axis, as AtomGroup::com; zero without
+        const double com = c.rsq_com ? c.sysout[(size_t)s * (ND + 1) + d] / c.sysout[(size_t)s * (ND + 1) + ND]
+                                     : 0.0;
+        r[d] = x[d] - com;
+    }
+    const unsigned long long t = c.rsq_cnt[0];
+    for (uint32_t j = 0; j < c.rsq_n; j++) {
+        const size_t base = ((size_t)j * c.n + o) * ND;
+        if (INIT) {
+#pragma unroll
+            for (int d = 0; d < ND; d++) c.rsq_past[base + d] = r[d];
+            continue;
+        }
+        if (t % c.rsq_skip[j] != 0ull) continue;
+        double ds[3], d4[3];
+        double dist4 = 0.0;
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            ds[d] = r[d] - c.rsq_past[base + d];
+            ds[d] = ds[d] * ds[d];
+            d4[d] = ds[d] * ds[d];
+            dist4 = dist4 + ds[d];
+        }
+        dist4 = dist4 * dist4;
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            c.rsq_x2[base + d] = c.rsq_x2[base + d] + ds[d];
+            c.rsq_x4[base + d] = c.rsq_x4[base + d] + d4[d];
+            c.rsq_past[base + d] = r[d];
+        }
+        c.rsq_r4[(size_t)j * c.n + o] = c.rsq_r4[(size_t)j * c.n + o] + dist4;
+    }
+}
+
+void launch_rsq(const DevCtx& c, cudaStream_t s, int init) {
+    if (!c.rsq_n) return;
+    if (c.rsq_com) {
+        launch_reduce_atoms(c, s, AW_COM, nullptr);
+        launch_sys_reduce(c, s, c.nd + 1);
+    }
+    if (!init) k_rsq_tick<<<1, 32, 0, s>>>(c);
+    if (c.nd == 3) {
+        if (init) k_rsq<3, true><<<grid_for(c.n), BLOCK, 0, s>>>(c);
+        else k_rsq<3, false><<<grid_for(c.n), BLOCK, 0, s>>>(c);
+    } else {
+        if (init) k_rsq<2, true><<<grid_for(c.n), BLOCK, 0, s>>>(c);
+        else k_rsq<2, false><<<grid_for(c.n), BLOCK, 0, s>>>(c);
+    }
 }
 
 }  // namespace parm

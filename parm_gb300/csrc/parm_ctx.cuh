@@ -136,6 +136,15 @@ struct DevCtx {
     StepParams* params;
 
     // reduction scratch
+    // mean-square-displacement tracker (RsqTracker); rsq_n == 0: none
+    uint32_t rsq_n;                      // time windows
+    uint32_t rsq_com;                    // measure from each system's centre of mass
+    const unsigned long long* rsq_skip;  // [rsq_n] window lengths (tracker updates)
+    unsigned long long* rsq_cnt;         // [0] tracker time; [1 + j] updates of window j
+    double* rsq_past;     // [rsq_n][n][nd] by caller index: position at the window's last update
+    double* rsq_x2;       // [rsq_n][n][nd] sums of squared displacements
+    double* rsq_x4;       // [rsq_n][n][nd] sums of their squares
+    double* rsq_r4;       // [rsq_n][n] sums of squared squared distances
     double* red;          // per-atom scratch (up to 12 doubles per atom)
     double* sysout;       // per-system outputs
     uint32_t nchunk;      // reduction chunks (up to RED_CHUNK atoms of one system)
@@ -166,6 +175,7 @@ void launch_scatter_in(const DevCtx& c, cudaStream_t s, const double* staging, u
 void launch_gather_out(const DevCtx& c, cudaStream_t s, double* staging, uint64_t stride,
                        uint32_t fields);
 void launch_reduce_atoms(const DevCtx& c, cudaStream_t s, int what, const double* origin);
+void launch_rsq(const DevCtx& c, cudaStream_t s, int init);   // tracker start (init) or update
 void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp);
 // pair64.cu / pair32.cu
 void launch_force64(const DevCtx& c, cudaStream_t s, int mode);
@@ -196,6 +206,7 @@ enum AtomWhat : int {
     AW_KINETIC = 0,    // 1 comp, AtomGroup::kinetic_energy(origin)
     AW_MOMENTUM = 1,   // nd + 1 comps (momentum, mass) over m > 0 finite atoms
     AW_MAXFORCE = 2,   // 1 comp: max |f|^2 over mobile atoms
+    AW_COM = 3,        // nd + 1 comps (sum of m x, mass) over m > 0 finite atoms
 };
 
 // Cell-block record of an atom (mixed path), 16 bytes, the same for every

@@ -11,6 +11,7 @@
 #ifndef PARM_GB300_COLLECTION_HPP
 #define PARM_GB300_COLLECTION_HPP
 
+#include <functional>
 #include <vector>
 
 #include "interaction.hpp"
@@ -32,6 +33,10 @@ class Collection {
     sptr<GpuLink> link;
     void attach();
     GpuLink& gpu();
+    //! trackers besides the neighbour list (updated after every step)
+    bool has_step_trackers() const;
+    //! push, step(k) for n steps (one at a time when such trackers exist), pull
+    void run_steps(uint n, const std::function<void(uint)>& step);
 
    public:
     Collection(sptr<Box> box, sptr<AtomVec> atoms,

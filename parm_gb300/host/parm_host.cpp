@@ -2,6 +2,7 @@
 // (wackywendell/parm src/box.*, src/trackers.*, src/interaction.hpp,
 // src/collection.*) on top of the C ABI of include/parm_gb300.h.
 #include <cstdlib>
+#include <functional>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -204,6 +205,79 @@ const std::vector<IDPair>& NeighborList::pairs() {
 }
 
 // ---------------------------------------------------------------------------
+// mean-square displacement (RsqTracker)
+RsqTracker::RsqTracker(sptr<AtomGroup> atoms, std::vector<unsigned long> ns, bool usecom)
+    : atoms(atoms), usecom(usecom) {
+    if (ns.empty()) throw std::invalid_argument("RsqTracker: no time windows");
+    for (unsigned long n : ns) skips.push_back((uint64_t)n);
+    uint32_t n = atoms->size();
+    parm_host_check(parm_create(&h, NDIM, 1, &n, PARM_FP64), "parm_create");
+    // positions are measured unwrapped: the box is not used
+    std::vector<double> L(NDIM, 1.0);
+    parm_host_check(parm_set_boxes(h, L.data()), "parm_set_boxes");
+    reset();
+}
+
+RsqTracker::~RsqTracker() {
+    if (h) parm_destroy(h);
+}
+
+void RsqTracker::push() {
+    const uint n = atoms->size();
+    const size_t stride = 4 * NDIM + 1;
+    buf.assign((size_t)n * stride, 0.0);
+    for (uint i = 0; i < n; i++) {
+        const Atom& a = (*atoms)[i];
+        for (int d = 0; d < NDIM; d++) buf[(size_t)i * stride + d] = a.x[d];
+        buf[(size_t)i * stride + 4 * NDIM] = a.m;
+    }
+    parm_host_check(parm_set_atoms(h, buf.data(), stride, PARM_X | PARM_M), "parm_set_atoms");
+}
+
+void RsqTracker::reset() {
+    push();
+    parm_host_check(parm_rsq_start(h, skips.data(), (uint32_t)skips.size(), usecom ? 1 : 0), "parm_rsq_start");
+}
+
+void RsqTracker::update(Box&) {
+    push();
+    parm_host_check(parm_rsq_update(h), "parm_rsq_update");
+}
+
+std::vector<double> RsqTracker::get(int what, size_t per_window) {
+    std::vector<double> v(skips.size() * per_window);
+    parm_host_check(parm_rsq_get(h, what, v.data()), "parm_rsq_get");
+    return v;
+}
+
+std::vector<VecRows> RsqTracker::rows(int what) {
+    const size_t n = atoms->size();
+    std::vector<double> v = get(what, n * NDIM);
+    std::vector<VecRows> out;
+    for (size_t j = 0; j < skips.size(); j++) {
+        VecRows m(n);
+        for (size_t i = 0; i < n; i++)
+            for (int d = 0; d < NDIM; d++) m(i, d) = v[(j * n + i) * NDIM + d];
+        out.push_back(m);
+    }
+    return out;
+}
+
+std::vector<std::vector<flt>> RsqTracker::lists(int what) {
+    const size_t n = atoms->size();
+    std::vector<double> v = get(what, n);
+    std::vector<std::vector<flt>> out;
+    for (size_t j = 0; j < skips.size(); j++) out.emplace_back(v.begin() + j * n, v.begin() + (j + 1) * n);
+    return out;
+}
+
+std::vector<VecRows> RsqTracker::xyz2() { return rows(PARM_RSQ_XYZ2); }
+std::vector<VecRows> RsqTracker::xyz4() { return rows(PARM_RSQ_XYZ4); }
+std::vector<std::vector<flt>> RsqTracker::r2() { return lists(PARM_RSQ_R2); }
+std::vector<std::vector<flt>> RsqTracker::r4() { return lists(PARM_RSQ_R4); }
+std::vector<flt> RsqTracker::counts() { return get(PARM_RSQ_COUNTS, 1); }
+
+// ---------------------------------------------------------------------------
 // interaction quantities
 flt gpu_evaluate(GpuLink& link, int what) {
     link.push();
@@ -256,8 +330,9 @@ void Collection::attach() {
         found = l;
     }
     for (auto& t : trackers) {
+        if (std::dynamic_pointer_cast<RsqTracker>(t)) continue;   // its own GPU handle
         auto nl = std::dynamic_pointer_cast<NeighborList>(t);
-        if (!nl) throw std::invalid_argument("parm_gb300: trackers must be NeighborList objects");
+        if (!nl) throw std::invalid_argument("parm_gb300: trackers must be NeighborList or RsqTracker objects");
         if (found && nl->gpu() != found)
             throw std::invalid_argument("parm_gb300: the tracker must be the interaction's NeighborList");
         found = nl->gpu();
@@ -372,13 +447,34 @@ void Collection::add_tracker(sptr<StateTracker> track) {
     update_trackers();
 }
 
-void CollectionVerlet::timesteps(uint n) {
+bool Collection::has_step_trackers() const {
+    for (auto& t : trackers)
+        if (!std::dynamic_pointer_cast<NeighborList>(t)) return true;
+    return false;
+}
+
+void Collection::run_steps(uint n, const std::function<void(uint)>& step) {
     if (!n) return;
     GpuLink& g = gpu();
     g.push();
     g.touch();
-    parm_host_check(parm_verlet(g.handle(), dt, n), "parm_verlet");
-    g.pull();
+    if (!has_step_trackers()) {
+        step(n);
+        g.pull();
+        return;
+    }
+    // trackers other than the neighbour list (which the GPU steps update
+    // themselves) see the positions at the end of every step
+    for (uint k = 0; k < n; k++) {
+        step(1);
+        g.pull();
+        for (auto& t : trackers)
+            if (!std::dynamic_pointer_cast<NeighborList>(t)) t->update(*box);
+    }
+}
+
+void CollectionVerlet::timesteps(uint n) {
+    run_steps(n, [this](uint k) { parm_host_check(parm_verlet(gpu().handle(), dt, k), "parm_verlet"); });
 }
 
 CollectionDamped::CollectionDamped(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
@@ -389,12 +485,9 @@ CollectionDamped::CollectionDamped(sptr<Box> box, sptr<AtomVec> atoms, const flt
 }
 
 void CollectionDamped::timesteps(uint n) {
-    if (!n) return;
-    GpuLink& g = gpu();
-    g.push();
-    g.touch();
-    parm_host_check(parm_damped(g.handle(), dt, damping, n), "parm_damped");
-    g.pull();
+    run_steps(n, [this](uint k) {
+        parm_host_check(parm_damped(gpu().handle(), dt, damping, k), "parm_damped");
+    });
 }
 
 CollectionSol::CollectionSol(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, const flt damping,
@@ -407,10 +500,7 @@ CollectionSol::CollectionSol(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, c
 }
 
 void CollectionSol::timesteps(uint n) {
-    if (!n) return;
-    GpuLink& g = gpu();
-    g.push();
-    g.touch();
-    parm_host_check(parm_sol(g.handle(), dt, damping, desT, key, n), "parm_sol");
-    g.pull();
+    run_steps(n, [this](uint k) {
+        parm_host_check(parm_sol(gpu().handle(), dt, damping, desT, key, k), "parm_sol");
+    });
 }

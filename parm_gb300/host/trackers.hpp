@@ -108,4 +108,36 @@ class NeighborList : public StateTracker {
     unsigned long long cache_epoch = ~0ull;
 };
 
+//! Mean-square displacement over windows of ns[j] updates
+//! (src/constraints.hpp:318-361, src/constraints.cpp:404-564), on the GPU
+//! (parm_rsq_*): the tracker holds its own GPU handle and sends it the
+//! atoms' positions and masses at each update.  A Collection updates it at
+//! the end of every time step, as the reference's update_trackers does.
+class RsqTracker : public StateTracker {
+   public:
+    RsqTracker(sptr<AtomGroup> atoms, std::vector<unsigned long> ns, bool usecom = true);
+    ~RsqTracker() override;
+    RsqTracker(const RsqTracker&) = delete;
+    RsqTracker& operator=(const RsqTracker&) = delete;
+    //! restart every window at the current positions
+    void reset();
+    void update(Box& box) override;
+    std::vector<VecRows> xyz2();
+    std::vector<std::vector<flt>> r2();
+    std::vector<VecRows> xyz4();
+    std::vector<std::vector<flt>> r4();
+    std::vector<flt> counts();
+
+   private:
+    sptr<AtomGroup> atoms;
+    std::vector<uint64_t> skips;
+    bool usecom;
+    parm_system* h = nullptr;
+    std::vector<double> buf;
+    void push();
+    std::vector<double> get(int what, size_t per_window);
+    std::vector<VecRows> rows(int what);
+    std::vector<std::vector<flt>> lists(int what);
+};
+
 #endif

@@ -184,6 +184,20 @@ struct Matrix {
     const flt& operator()(int a, int b) const { return c[a][b]; }
 };
 
+//! Rows of NDIM values (the reference's Eigen::Matrix<flt, Eigen::Dynamic,
+//! NDIM>: rows(), cols(), row(i), (i, d), size()).
+struct VecRows {
+    std::vector<Vec> r;
+    VecRows() {}
+    explicit VecRows(size_t n) : r(n, Vec::Zero()) {}
+    size_t rows() const { return r.size(); }
+    static constexpr size_t cols() { return NDIM; }
+    size_t size() const { return r.size() * NDIM; }
+    Vec row(size_t i) const { return r[i]; }
+    flt& operator()(size_t i, size_t d) { return r[i][d]; }
+    flt operator()(size_t i, size_t d) const { return r[i][d]; }
+};
+
 #ifdef VEC3D
 inline Vec vec() { return Vec(0, 0, 0); }
 #else

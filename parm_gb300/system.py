@@ -178,6 +178,28 @@ class System:
         check(self.lib.parm_max_force_sq(self.h, dptr(out)))
         return out
 
+    # -- mean-square-displacement tracker (RsqTracker) --
+    def rsq_start(self, skips, usecom: bool = True) -> None:
+        """(Re)start the device tracker at the current positions; windows of `skips` updates."""
+        sk = np.ascontiguousarray(np.asarray(skips, dtype=np.uint64).ravel())
+        self._rsq_n = len(sk)
+        check(self.lib.parm_rsq_start(self.h, sk.ctypes.data_as(C.POINTER(C.c_uint64)), len(sk), int(bool(usecom))))
+
+    def rsq_update(self) -> None:
+        check(self.lib.parm_rsq_update(self.h))
+
+    def rsq_get(self, what: int) -> np.ndarray:
+        """Means as RsqTracker returns them: xyz2/xyz4 (nwin, n, ndim), r2/r4 (nwin, n), counts (nwin,)."""
+        nw = self._rsq_n
+        shape = {capi.RSQ_XYZ2: (nw, self.n, self.ndim), capi.RSQ_XYZ4: (nw, self.n, self.ndim),
+                 capi.RSQ_R2: (nw, self.n), capi.RSQ_R4: (nw, self.n), capi.RSQ_COUNTS: (nw,)}[what]
+        out = np.zeros(shape)
+        check(self.lib.parm_rsq_get(self.h, int(what), dptr(out)))
+        return out
+
+    def rsq_stop(self) -> None:
+        check(self.lib.parm_rsq_stop(self.h))
+
     # -- integrators --
     def verlet(self, dt: float, nsteps: int = 1) -> None:
         check(self.lib.parm_verlet(self.h, float(dt), int(nsteps)))

@@ -27,3 +27,10 @@ def test_reference_ljatoms_compiles_against_host_api(tmp_path, built_lib):
         pytest.skip("reference sources not present")
     r = compile_program(REF_LJATOMS, tmp_path / "lj.o", link=False)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_rsq_tracker_program_builds(tmp_path, built_lib):
+    """A program using RsqTracker inside a Collection builds against the host API."""
+    src = Path(__file__).resolve().parent / "programs" / "rsq_tracker.cpp"
+    r = compile_program(src, tmp_path / "rsq")
+    assert r.returncode == 0, r.stderr[-3000:]
