@@ -277,6 +277,9 @@ def run_ours(args, rank, world, local_rank):
     tpa = g.autotune() if args.tpa == 0 else (g.set_threads_per_atom(args.tpa) or args.tpa)
     log(f"[rank {rank}] threads per atom: {tpa}")
     g.verlet(DT, args.warmup)
+    if args.rsq:
+        # the device mean-square-displacement tracker, updated inside every step
+        g.rsq_start([1, 10, 100], usecom=True)
     g.sync()
     e_start = g.energy()[0] + g.kinetic_energy()[0]
     stream = torch.cuda.ExternalStream(g.stream())
@@ -342,6 +345,8 @@ def run_ours(args, rank, world, local_rank):
                           else "fallback 6800 GB/s"}
     result["energy_drift_rel"] = {"per_1e5_steps": abs(e_end - e_start) / abs(e_start) * 1e5 / args.steps,
                                   "steps": args.steps}
+    if args.rsq:
+        result["config"]["msd_tracker"] = "device RsqTracker, windows of 1, 10, 100 steps, centre of mass"
 
     if args.only_timed:
         g.close()
@@ -645,6 +650,8 @@ def main():
                     help="time steps per CUDA graph launch (0: direct kernel launches, for profilers)")
     ap.add_argument("--tpa", type=int, default=0,
                     help="pair-kernel variant (0: autotune; 1/2/4 tiled, 100+t gather)")
+    ap.add_argument("--rsq", action="store_true",
+                    help="run the device mean-square-displacement tracker inside the timed steps")
     ap.add_argument("--only-timed", action="store_true",
                     help="run only the timed mixed-precision region (used for profiler captures)")
     ap.add_argument("--workload", default="lj1m", choices=["lj1m", "packings", "replicas", "disks"],

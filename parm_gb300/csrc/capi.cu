@@ -1438,7 +1438,7 @@ int parm_rsq_start(parm_system* S, const uint64_t* skips, uint32_t nskip, int us
     S->rsq_mem = nullptr;
     S->c.rsq_n = 0;
     const size_t per = (size_t)nskip * S->n;
-    const size_t bytes = 8 * ((size_t)nskip + 1 + nskip + 3 * per * S->nd + per);
+    const size_t bytes = 8 * ((size_t)nskip + 1 + nskip + 3 * per * S->nd + per + 3 * (size_t)S->nsys);
     CUDA_TRY(cudaMalloc(&S->rsq_mem, bytes));
     CUDA_TRY(cudaMemsetAsync(S->rsq_mem, 0, bytes, S->st));
     unsigned long long* skip = static_cast<unsigned long long*>(S->rsq_mem);
@@ -1450,6 +1450,7 @@ int parm_rsq_start(parm_system* S, const uint64_t* skips, uint32_t nskip, int us
     S->c.rsq_x2 = d + per * S->nd;
     S->c.rsq_x4 = d + 2 * per * S->nd;
     S->c.rsq_r4 = d + 3 * per * S->nd;
+    S->c.rsq_comv = S->c.rsq_r4 + per;
     S->c.rsq_com = usecom ? 1u : 0u;
     S->c.rsq_n = nskip;
     S->clear_graphs();

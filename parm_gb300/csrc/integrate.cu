@@ -549,30 +549,37 @@ void launch_sys_reduce(const DevCtx& c, cudaStream_t s, int ncomp) {
 // and updates the windows whose length divides t, in the reference's
 // arithmetic (componentwise FP64, no contraction).
 // ---------------------------------------------------------------------------
-__global__ void k_rsq_tick(DevCtx c) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const unsigned long long t = c.rsq_cnt[0] + 1ull;
-    c.rsq_cnt[0] = t;
-    for (uint32_t j = 0; j < c.rsq_n; j++)
-        if (t % c.rsq_skip[j] == 0ull) c.rsq_cnt[1 + j] += 1ull;
+// the update's preamble: the tracker time (thread 0; not at the start) and
+// each system's centre of mass, (sum of m x) / mass per axis as
+// AtomGroup::com (one thread per system)
+__global__ void k_rsq_prep(DevCtx c, int init) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0 && !init) {
+        const unsigned long long t = c.rsq_cnt[0] + 1ull;
+        c.rsq_cnt[0] = t;
+        for (uint32_t j = 0; j < c.rsq_n; j++)
+            if (t % c.rsq_skip[j] == 0ull) c.rsq_cnt[1 + j] += 1ull;
+    }
+    if (s >= c.nsys) return;
+    const int nd = c.nd;
+    for (int d = 0; d < nd; d++)
+        c.rsq_comv[(size_t)s * 3 + d] =
+            c.rsq_com ? c.sysout[(size_t)s * (nd + 1) + d] / c.sysout[(size_t)s * (nd + 1) + nd] : 0.0;
 }
 
+// one thread per atom in caller order (the tracker's arrays are read and
+// written in order; the position is gathered through the atom's slot)
 template <int ND, bool INIT>
 __global__ void k_rsq(DevCtx c) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= c.n) return;
     using V = typename DVec<ND>::T;
-    const uint32_t o = c.orig[i], s = c.atom_sys[i];
+    const uint32_t i = c.slot[o], s = c.atom_sys[i];
     V xv = static_cast<const V*>(c.x)[i];
     const double* x = reinterpret_cast<const double*>(&xv);
     double r[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int d = 0; d < ND; d++) {
-        // com: (sum of m x) / mass per axis, as AtomGroup::com; zero without
-        const double com = c.rsq_com ? c.sysout[(size_t)s * (ND + 1) + d] / c.sysout[(size_t)s * (ND + 1) + ND]
-                                     : 0.0;
-        r[d] = x[d] - com;
-    }
+    for (int d = 0; d < ND; d++) r[d] = x[d] - c.rsq_comv[(size_t)s * 3 + d];   // zero without com
     const unsigned long long t = c.rsq_cnt[0];
     for (uint32_t j = 0; j < c.rsq_n; j++) {
         const size_t base = ((size_t)j * c.n + o) * ND;
@@ -608,7 +615,7 @@ void launch_rsq(const DevCtx& c, cudaStream_t s, int init) {
         launch_reduce_atoms(c, s, AW_COM, nullptr);
         launch_sys_reduce(c, s, c.nd + 1);
     }
-    if (!init) k_rsq_tick<<<1, 32, 0, s>>>(c);
+    k_rsq_prep<<<(c.nsys + 255) / 256, 256, 0, s>>>(c, init);
     if (c.nd == 3) {
         if (init) k_rsq<3, true><<<grid_for(c.n), BLOCK, 0, s>>>(c);
         else k_rsq<3, false><<<grid_for(c.n), BLOCK, 0, s>>>(c);

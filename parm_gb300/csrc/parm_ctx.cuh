@@ -145,6 +145,7 @@ struct DevCtx {
     double* rsq_x2;       // [rsq_n][n][nd] sums of squared displacements
     double* rsq_x4;       // [rsq_n][n][nd] sums of their squares
     double* rsq_r4;       // [rsq_n][n] sums of squared squared distances
+    double* rsq_comv;     // [nsys][3] centre of mass of each system at the current update (or 0)
     double* red;          // per-atom scratch (up to 12 doubles per atom)
     double* sysout;       // per-system outputs
     uint32_t nchunk;      // reduction chunks (up to RED_CHUNK atoms of one system)
