@@ -1,20 +1,23 @@
 // parm_gb300 host API: time-step loops with the interface of the reference's
 // src/collection.hpp (wackywendell/parm), run on the GPU.
 //
-// A Collection here drives one GPU handle: its interactions and trackers are
-// the NListed interaction and NeighborList of one AtomVec (constraints and
-// other interactions are outside this library and rejected).  timestep()
-// uploads the Atom records, runs one step of the reference's algorithm on the
-// GPU and downloads the records, so code that reads or edits atoms[i]
-// between steps behaves as with the reference; timesteps(n) runs n steps with
-// one upload and one download.
+// A Collection here drives one GPU handle: its interaction is the NListed
+// interaction of one AtomVec and its neighbour list, whose update the GPU
+// steps make themselves (constraints and other interactions are outside this
+// library and rejected).  timestep() uploads the Atom records, runs one step
+// of the reference's algorithm on the GPU and downloads the records, so code
+// that reads or edits atoms[i] between steps behaves as with the reference;
+// timesteps(n) runs n steps with one upload and one download, or, when the
+// Collection holds other trackers (RsqTracker, EnergyTracker or the
+// caller's own), one step at a time with the trackers updated after each,
+// as the reference's timestep does.
 #ifndef PARM_GB300_COLLECTION_HPP
 #define PARM_GB300_COLLECTION_HPP
 
 #include <functional>
 #include <vector>
 
-#include "interaction.hpp"
+#include "constraints.hpp"
 
 //! Constraints are not part of this library; the type exists so that
 //! constructor signatures match the reference's.

@@ -278,6 +278,37 @@ std::vector<std::vector<flt>> RsqTracker::r4() { return lists(PARM_RSQ_R4); }
 std::vector<flt> RsqTracker::counts() { return get(PARM_RSQ_COUNTS, 1); }
 
 // ---------------------------------------------------------------------------
+// EnergyTracker (src/constraints.cpp:366-402)
+void EnergyTracker::update(Box& box) {
+    if (n_skipped + 1 < n_skip) {
+        n_skipped += 1;
+        return;
+    }
+    n_skipped = 0;
+    const uint Natoms = atoms->size();
+    flt curU = 0, curK = 0;
+    for (uint i = 0; i < Natoms; ++i) {
+        Atom& curatom = atoms->get(i);
+        curK += curatom.v.squaredNorm() * curatom.m / 2;
+    }
+    for (auto& it : interactions) curU += it->energy(box);
+    curU -= U0;
+    Ks += curK;
+    Us += curU;
+    Es += curK + curU;
+    Ksq += curK * curK;
+    Usq += curU * curU;
+    Esq += (curK + curU) * (curK + curU);
+    N++;
+}
+
+void EnergyTracker::set_U0(Box& box) {
+    flt curU = 0;
+    for (auto& it : interactions) curU += it->energy(box);
+    set_U0(curU);
+}
+
+// ---------------------------------------------------------------------------
 // interaction quantities
 flt gpu_evaluate(GpuLink& link, int what) {
     link.push();
@@ -330,9 +361,9 @@ void Collection::attach() {
         found = l;
     }
     for (auto& t : trackers) {
-        if (std::dynamic_pointer_cast<RsqTracker>(t)) continue;   // its own GPU handle
+        // other trackers are updated on the host after every step
         auto nl = std::dynamic_pointer_cast<NeighborList>(t);
-        if (!nl) throw std::invalid_argument("parm_gb300: trackers must be NeighborList or RsqTracker objects");
+        if (!nl) continue;
         if (found && nl->gpu() != found)
             throw std::invalid_argument("parm_gb300: the tracker must be the interaction's NeighborList");
         found = nl->gpu();

@@ -1,4 +1,5 @@
-"""Device mean-square-displacement tracker (parm_rsq_*) against the reference.
+"""State trackers: the device mean-square-displacement tracker (parm_rsq_*) against the
+reference, and the host API's trackers inside Collections.
 
 * the reference's own known answers (RSQTest, pyparm/tests.py:504-569), with
   the tracker updated explicitly after each move;
@@ -168,3 +169,18 @@ def test_host_api_rsq_tracker(tmp_path):
     for s in range(1, 13):
         col.update(pos[s])
     _check_program(out, "COL", col, exact=False)
+
+
+def test_host_api_energy_tracker(tmp_path):
+    """EnergyTracker and a caller-defined tracker inside a CollectionVerlet (updated after every step)."""
+    import subprocess
+    from pathlib import Path
+    from host_api import compile_program
+    src = Path(__file__).resolve().parent / "programs" / "energy_tracker.cpp"
+    exe = tmp_path / "energy_tracker"
+    r = compile_program(src, exe)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "UPDATES 12 SAMPLES 4 4" in run.stdout
+    assert "ENERGY OK" in run.stdout

@@ -34,3 +34,10 @@ def test_rsq_tracker_program_builds(tmp_path, built_lib):
     src = Path(__file__).resolve().parent / "programs" / "rsq_tracker.cpp"
     r = compile_program(src, tmp_path / "rsq")
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_energy_tracker_program_builds(tmp_path, built_lib):
+    """EnergyTracker and a caller-defined tracker in a Collection build against the host API."""
+    src = Path(__file__).resolve().parent / "programs" / "energy_tracker.cpp"
+    r = compile_program(src, tmp_path / "et")
+    assert r.returncode == 0, r.stderr[-3000:]
