@@ -43,6 +43,7 @@ class System:
         check(self.lib.parm_create(C.byref(h), ndim, self.nsys, u32ptr(self.sizes), prec))
         self.h = h
         self.stride = 4 * ndim + 1
+        self._rsq_n = 0
 
     # -- lifetime --
     def close(self) -> None:
@@ -190,7 +191,7 @@ class System:
 
     def rsq_get(self, what: int) -> np.ndarray:
         """Means as RsqTracker returns them: xyz2/xyz4 (nwin, n, ndim), r2/r4 (nwin, n), counts (nwin,)."""
-        nw = self._rsq_n
+        nw = max(self._rsq_n, 1)   # without a tracker the call reports the error
         shape = {capi.RSQ_XYZ2: (nw, self.n, self.ndim), capi.RSQ_XYZ4: (nw, self.n, self.ndim),
                  capi.RSQ_R2: (nw, self.n), capi.RSQ_R4: (nw, self.n), capi.RSQ_COUNTS: (nw,)}[what]
         out = np.zeros(shape)
@@ -199,6 +200,7 @@ class System:
 
     def rsq_stop(self) -> None:
         check(self.lib.parm_rsq_stop(self.h))
+        self._rsq_n = 0
 
     # -- integrators --
     def verlet(self, dt: float, nsteps: int = 1) -> None:
