@@ -181,20 +181,26 @@ def cpu_baseline_sample(w, max_steps=3):
             break
     dt = time.perf_counter() - t0
     rebuilt = o.which() != which0
-    # O(N^2) rebuild at 16384 atoms
+    del o
+    tb, t_rebuild = rebuild_cost(w.n)
+    return {"value": w.n * steps / dt, "steps": steps, "seconds": dt, "rebuilt": rebuilt,
+            "rebuild_s_16k": tb, "rebuild_s_extrapolated": t_rebuild}
+
+
+def rebuild_cost(n_target: int):
+    """The reference's O(N^2) NeighborList::update_list(true) timed at 16384 atoms (oracle port, one
+    thread) and extrapolated by N^2 to `n_target` atoms: (seconds at 16384, extrapolated seconds)."""
+    from oracle.oracle import Oracle
     from parm_gb300 import workloads as W
     ws = W.lj_lattice(shape=(32, 32, 16), skin_prime=0.3)
-    os_ = Oracle(ws.n, 3)
-    os_.set_box(ws.L[0])
-    os_.set_state(x=ws.x, v=ws.v, m=ws.m)
-    os_.set_interaction(ws.kind, ws.params, ws.skin)
+    o = Oracle(ws.n, 3)
+    o.set_box(ws.L[0])
+    o.set_state(x=ws.x, v=ws.v, m=ws.m)
+    o.set_interaction(ws.kind, ws.params, ws.skin)
     t1 = time.perf_counter()
-    os_.nl_update(True)
+    o.nl_update(True)
     tb = time.perf_counter() - t1
-    t_rebuild_1m = tb * (w.n / ws.n) ** 2
-    del o, os_
-    return {"value": w.n * steps / dt, "steps": steps, "seconds": dt, "rebuilt": rebuilt,
-            "rebuild_s_16k": tb, "rebuild_s_extrapolated": t_rebuild_1m}
+    return tb, tb * (n_target / ws.n) ** 2
 
 
 def _replica_steps(job):
@@ -239,11 +245,13 @@ def run_reference(args, rank):
     wall = max(r[2] + r[1] for r in res) - min(r[2] for r in res)
     value = total / wall
     n = res[0][0] // steps
+    tb, t_rebuild = rebuild_cost(n)
     sample = (f"oracle port of the reference step (bit-exact with the reference's compiled sources), "
               f"{nrep} independent {n}-atom replicas, one per host thread of {host_cpu()}, {warm} untimed + {steps} "
               f"timed CollectionVerlet steps each without a list rebuild ({wall:.1f} s wall); the reference's "
               f"O(N^2) list rebuild "
-              f"(~1.8e4 s per rebuild at this size, extrapolated from 16384 atoms) is excluded")
+              f"(~{t_rebuild:.3g} s per rebuild at this size, extrapolated by N^2 from {tb:.2f} s measured "
+              f"at 16384 atoms) is excluded")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
            "warmup": warm, "ms_per_step": 1000 * wall / steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -257,10 +265,70 @@ def run_reference(args, rank):
         print(json.dumps(out), flush=True)
 
 
+def _timed_verlet(g, steps, stream, dist=None, clocks=None):
+    """Time `steps` Verlet steps of handle `g` between CUDA events on its stream (graphs already captured)."""
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    ev0.record(stream)
+    g.verlet(DT, steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    ck = clocks.stop() if clocks else None
+    return ev0.elapsed_time(ev1), ck
+
+
+def _capture_graphs(g, steps, graph_steps):
+    """Run the graph shapes a call of `steps` steps uses (full chunks and the remainder), so that capture
+    and instantiation happen before a timed region."""
+    if graph_steps:
+        g.verlet(DT, min(steps, graph_steps))
+        if steps % graph_steps and steps > graph_steps:
+            g.verlet(DT, steps % graph_steps)
+    else:
+        g.verlet(DT, 1)
+    g.sync()
+
+
+def energy_drift(w, precision, steps, sample_every=100, graph_steps=50):
+    """NVE drift of one path from the workload's initial state: total energy sampled every `sample_every`
+    steps over `steps` steps, least-squares slope scaled to 10^5 steps relative to |E(0)|."""
+    g = make_system(w, precision, 0)
+    g.set_graph_steps(graph_steps)
+    if precision == "mixed":
+        g.autotune()
+    E = [g.energy()[0] + g.kinetic_energy()[0]]
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        k = min(sample_every, steps - done)
+        g.verlet(DT, k)
+        done += k
+        E.append(g.energy()[0] + g.kinetic_energy()[0])
+    wall = time.perf_counter() - t0
+    g.close()
+    E = np.array(E)
+    t = np.concatenate([[0], np.cumsum([min(sample_every, steps - q) for q in range(0, steps, sample_every)])])
+    A = np.stack([t, np.ones_like(t)], 1).astype(np.float64)
+    coef, res, *_ = np.linalg.lstsq(A, E, rcond=None)
+    resid = E - A @ coef
+    dof = max(1, len(E) - 2)
+    se = math.sqrt((resid ** 2).sum() / dof / ((t - t.mean()) ** 2).sum())
+    scale = 1e5 / abs(E[0])
+    return {"per_1e5_steps": float(coef[0] * scale), "std_err": float(se * scale), "steps": int(steps),
+            "samples": int(len(E)), "rms_fluctuation_rel": float(resid.std() / abs(E[0])),
+            "net_change_rel": float((E[-1] - E[0]) / abs(E[0])), "wall_s": wall}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from parm_gb300 import capi, workloads as W
-    from parm_gb300.system import System
     lib = capi.load()
     capi.check(lib.parm_use_device(local_rank))
     torch.cuda.set_device(local_rank)
@@ -274,39 +342,32 @@ def run_ours(args, rank, world, local_rank):
     log(f"[rank {rank}] building mixed system, n={n}")
     g = make_system(w, "mixed", local_rank)
     g.set_graph_steps(args.graph_steps)
-    tpa = g.autotune() if args.tpa == 0 else (g.set_threads_per_atom(args.tpa) or args.tpa)
-    log(f"[rank {rank}] threads per atom: {tpa}")
+    variant = g.autotune() if args.tpa == 0 else (g.set_threads_per_atom(args.tpa) or args.tpa)
+    log(f"[rank {rank}] kernel variant: {variant}")
     g.verlet(DT, args.warmup)
     if args.rsq:
         # the device mean-square-displacement tracker, updated inside every step
         g.rsq_start([1, 10, 100], usecom=True)
-    g.sync()
-    e_start = g.energy()[0] + g.kinetic_energy()[0]
+    _capture_graphs(g, args.steps, args.graph_steps)
     stream = torch.cuda.ExternalStream(g.stream())
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
     clocks = Clocks(local_rank)
-    g.timing(True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    ev0.record(stream)
-    g.verlet(DT, args.steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    ck = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
+
+    # --- the timed region: K steps, graphs captured beforehand, no per-kernel events ---
+    ms, ck = _timed_verlet(g, args.steps, stream, dist, clocks)
     launches = g.last_launches()
-    tr = g.timing_read()
-    g.timing(False)
     if dist:
         ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
-    e_end = g.energy()[0] + g.kinetic_energy()[0]
     value = job_throughput(n, args.steps, ms, world)
     npairs = int(g.numpairs()[0])
+
+    # --- per-kernel durations (CUDA events around the force kernels of every step), a separate run ---
+    g.timing(True)
+    _capture_graphs(g, args.steps, args.graph_steps)
+    g.timing(True)   # resets the counters
+    ms_t, _ = _timed_verlet(g, args.steps, stream)
+    tr = g.timing_read()
+    g.timing(False)
 
     # --- roofline of the dominant kernel (the mixed pair-force kernel) ---
     # algorithmic bytes per atom-timestep of the mixed step (fused, list
@@ -315,7 +376,7 @@ def run_ours(args, rank, world, local_rank):
     # launch of the force kernel advances every atom by one step
     force_ms = tr["force_ms"] / max(1, tr["force_launches"])
     n_half = npairs / n
-    staged = tpa == 2000 or tpa == 200
+    staged = variant == 2000 or variant == 200
     kernel = "k_force_stg" if staged else "k_force32"
     bytes_per_atom = 96.0 + 24.0 + 4.0 * n_half
     algo_bytes = n * bytes_per_atom
@@ -331,7 +392,7 @@ def run_ours(args, rank, world, local_rank):
                          "cutoff_sigma": float(w.params[0, 2]), "precision": "mixed",
                          "parallelism": f"replicas{world}" if world > 1 else "single",
                          "l2": "inputs larger than L2 (state + neighbour lists ~1 GB)",
-                         "steps_per_graph": args.graph_steps, "threads_per_atom": tpa},
+                         "steps_per_graph": args.graph_steps, "kernel_variant": variant},
               "clocks": ck,
               "gpu_launches": launches,
               "rebuilds": tr["rebuilds"]}
@@ -341,10 +402,9 @@ def run_ours(args, rank, world, local_rank):
                           "algorithmic_bytes_per_atom": bytes_per_atom, "half_list_pairs_per_atom": n_half,
                           "step_achieved_gbs": bytes_per_atom * value / 1e9,
                           "algorithmic_bytes_per_launch": algo_bytes, "force_ms_per_launch": force_ms,
+                          "timing_run_ms_per_step": ms_t / args.steps,
                           "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
                           else "fallback 6800 GB/s"}
-    result["energy_drift_rel"] = {"per_1e5_steps": abs(e_end - e_start) / abs(e_start) * 1e5 / args.steps,
-                                  "steps": args.steps}
     if args.rsq:
         result["config"]["msd_tracker"] = "device RsqTracker, windows of 1, 10, 100 steps, centre of mass"
 
@@ -359,18 +419,13 @@ def run_ours(args, rank, world, local_rank):
     w64 = W.lj_lattice(shape=SHAPE, skin_prime=0.3, seed=12345 + rank)
     w64.x, w64.v = st["x"], st["v"]
     g64 = make_system(w64, "fp64", local_rank)
-    g64.set_graph_steps(10)
-    k64 = max(3, min(40, args.steps // 10))
+    g64.set_graph_steps(args.graph_steps)
+    k64 = max(1, args.fp64_steps)
     g64.verlet(DT, 2)
-    torch.cuda.synchronize()
+    _capture_graphs(g64, k64, args.graph_steps)
     s64 = torch.cuda.ExternalStream(g64.stream())
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s64)
-    g64.verlet(DT, k64)
-    e1.record(s64)
-    e1.synchronize()
-    v64 = n * k64 / (e0.elapsed_time(e1) / 1000.0)
+    ms64, _ = _timed_verlet(g64, k64, s64)
+    v64 = n * k64 / (ms64 / 1000.0)
     # forces at one common state
     st64 = g64.get_atoms(capi.X)
     g.set_atoms(x=st64["x"])
@@ -383,6 +438,7 @@ def run_ours(args, rank, world, local_rank):
     ferr = float(np.sqrt(((F32 - F64) ** 2).sum(1)).max() / np.sqrt((F64 ** 2).sum(1).mean()))
     E32, E64 = g.energy()[0], g64.energy()[0]
     result["fp64_value"] = world * v64
+    result["fp64_steps_timed"] = k64
     result["mixed_vs_fp64"] = value / (world * v64)
     result["accuracy"] = {"max_force_err_over_rms_force": ferr, "rel_energy_err": abs(E32 - E64) / abs(E64)}
     g64.close()
@@ -419,6 +475,17 @@ def run_ours(args, rank, world, local_rank):
                             "{x,v,a,f,m} in pinned host memory"}
     lib.parm_host_free(hp)
     g.close()
+
+    # --- NVE energy drift of both paths from the same initial state (fitted slope) ---
+    if args.drift_steps > 0 and rank == 0:
+        log(f"[rank 0] NVE drift over {args.drift_steps} steps, mixed and FP64")
+        dm = energy_drift(w, "mixed", args.drift_steps, graph_steps=args.graph_steps)
+        d64 = energy_drift(w, "fp64", args.drift_steps, graph_steps=args.graph_steps)
+        result["drift"] = {"mixed": dm, "fp64": d64,
+                           "ratio_mixed_over_fp64": dm["per_1e5_steps"] / d64["per_1e5_steps"]
+                           if d64["per_1e5_steps"] != 0 else None,
+                           "definition": "least-squares slope of E_total(t) sampled every 100 steps, "
+                                         "times 1e5 steps, over |E_total(0)|, from the workload's initial state"}
 
     if rank == 0 and world == 1 and not args.no_cpu:
         log("[rank 0] timing the CPU oracle sample")
@@ -641,7 +708,7 @@ def run_disks(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -649,7 +716,7 @@ def main():
     ap.add_argument("--graph-steps", type=int, default=50,
                     help="time steps per CUDA graph launch (0: direct kernel launches, for profilers)")
     ap.add_argument("--tpa", type=int, default=0,
-                    help="pair-kernel variant (0: autotune; 1/2/4 tiled, 100+t gather)")
+                    help="pair-kernel variant (0: autotune; 200 cell blocks, 1/2/4 tiled, 100+t gather)")
     ap.add_argument("--rsq", action="store_true",
                     help="run the device mean-square-displacement tracker inside the timed steps")
     ap.add_argument("--only-timed", action="store_true",
@@ -658,12 +725,17 @@ def main():
                     help="lj1m: the headline line; the others print their own line")
     ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workloads")
     ap.add_argument("--min-steps", type=int, default=20000, help="step cap of each minimisation phase")
-    ap.add_argument("--fp64-steps", type=int, default=2000, help="FP64 steps of the replica comparison")
+    ap.add_argument("--fp64-steps", type=int, default=0,
+                    help="lj1m: timed FP64 steps (default 200); replicas: FP64 steps of the comparison (2000)")
+    ap.add_argument("--drift-steps", type=int, default=10000,
+                    help="steps of the NVE drift fit of each path (0: skip)")
     ap.add_argument("--sample-sys", type=int, default=64, help="packings minimised by FP64 alone")
     ap.add_argument("--single-sys", type=int, default=16, help="packings run one system per launch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.fp64_steps == 0:
+        args.fp64_steps = 200 if args.workload == "lj1m" else 2000
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

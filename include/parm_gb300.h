@@ -220,12 +220,14 @@ int parm_host_free(void* p);
 
 /* AtomGroup::kinetic_energy of Atom records that the caller already holds in
  * device memory (stride doubles per record, as for parm_set_atoms), without
- * allocating anything: for callers that cannot allocate device memory (code
- * running during CUDA graph capture, frameworks whose pool owns every device
- * buffer, loops that must not enter the driver's allocator).  No counterpart
- * in the reference.  `atoms` and `out` (one double) are device pointers,
- * `origin` a host pointer to ndim doubles or NULL, `stream` a cudaStream_t
- * (NULL: the legacy default stream).  The call is asynchronous on `stream`.
+ * allocating anything: for callers that cannot allocate device memory
+ * (frameworks whose pool owns every device buffer, loops that must not enter
+ * the driver's allocator, processes under a fixed device-memory budget).  No
+ * counterpart in the reference.  `atoms` and `out` (one double) are device
+ * pointers, `origin` a host pointer to ndim doubles or NULL, `stream` a
+ * cudaStream_t of the current device (NULL: the legacy default stream; a
+ * stream of another device is rejected with PARM_ERR_ARG).  The call is
+ * asynchronous on `stream`.
  * At most 262144 atoms per call: the per-atom scratch is a static 2 MiB
  * device array that every GPU loading the library holds until exit.  The
  * first call on a device looks up that array's address, so make it before
@@ -237,6 +239,16 @@ int parm_kinetic_energy_noalloc(const double* atoms, uint64_t stride, uint32_t n
 /* Evaluate the library's minimum-image routine remainder(d[i], L[i]) on the
  * GPU (test hook for the exact IEEE remainder used by OriginBox::diff). */
 int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t n);
+
+/* Test hooks of the Langevin generator.  parm_debug_philox runs the
+ * library's Philox4x32-10 block function (Salmon et al., SC'11) on n inputs
+ * of 6 words each (counter c0..c3, key k0, k1) and writes 4 words per input.
+ * parm_debug_normals writes the 6 standard normals (natoms x 6 doubles) that
+ * parm_sol draws for atoms 0..natoms-1 of system `sys` at step counter `step`
+ * when called with `seed` (the noise of CollectionSol::timestep,
+ * src/collection.cpp:276-283, BivariateGauss::gen_vecs, src/vecrand.cpp:73-85). */
+int parm_debug_philox(const uint32_t* in, uint32_t* out, uint32_t n);
+int parm_debug_normals(uint64_t seed, uint32_t sys, uint64_t step, uint32_t natoms, double* out);
 
 /* Test hook: atoms staged in shared memory per cell block (the rest of a
  * block's neighbourhood is read from global memory); 0 restores the size

@@ -6,6 +6,7 @@ a*b+c into fma by default).
 """
 from __future__ import annotations
 
+import os
 import subprocess
 from pathlib import Path
 
@@ -27,7 +28,8 @@ def build() -> Path:
 
 REFBUILD = HERE / "refbuild"
 REF_OUT = HERE / "_ref"
-REF_SRC = Path("/root/reference/src")
+# the reference's src/ directory; PARM_REFERENCE_SRC overrides the default location
+REF_SRC = Path(os.environ.get("PARM_REFERENCE_SRC", "/root/reference/src"))
 
 
 def build_ref(ref_src: Path = REF_SRC) -> Path | None:

@@ -572,6 +572,15 @@ void orc_normals6(uint64_t seed, uint64_t step, uint32_t atom, double* out) {
     normals6(seed, step, atom, out);
 }
 
+// raw Philox4x32-10 on rows (c0, c1, c2, c3, k0, k1) -> 4 words each
+void orc_philox(const uint32_t* in, uint32_t* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        uint32_t c[4] = {in[6 * i], in[6 * i + 1], in[6 * i + 2], in[6 * i + 3]};
+        philox10(c, in[6 * i + 4], in[6 * i + 5]);
+        for (int q = 0; q < 4; q++) out[4 * i + q] = c[q];
+    }
+}
+
 // AtomGroup::kinetic_energy(originvelocity) (box.cpp:401-411)
 double orc_kinetic_energy(void* s, const double* origin) {
     System* S = static_cast<System*>(s);

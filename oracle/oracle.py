@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_uint64,
                                C.c_uint32]),
             "orc_normals6": (None, [C.c_uint64, C.c_uint64, C.c_uint32, _dp]),
+            "orc_philox": (None, [_u32p, _u32p, C.c_uint64]),
             "orc_kinetic_energy": (C.c_double, [C.c_void_p, _dp]),
             "orc_momentum": (C.c_double, [C.c_void_p, _dp]),
             "orc_pairs_celllist": (C.c_uint64, [C.c_void_p, _u32p, C.c_uint64]),
@@ -228,4 +229,12 @@ class Oracle:
 def normals6(seed: int, step: int, atom: int) -> np.ndarray:
     out = np.zeros(6)
     lib().orc_normals6(int(seed), int(step), int(atom), out.ctypes.data_as(_dp))
+    return out
+
+
+def philox(ctr_key) -> np.ndarray:
+    """Philox4x32-10 of the oracle on rows (c0, c1, c2, c3, k0, k1); returns (n, 4) uint32."""
+    a = np.ascontiguousarray(np.asarray(ctr_key, dtype=np.uint32).reshape(-1, 6))
+    out = np.zeros((a.shape[0], 4), dtype=np.uint32)
+    lib().orc_philox(a.ctypes.data_as(_u32p), out.ctypes.data_as(_u32p), a.shape[0])
     return out

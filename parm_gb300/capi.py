@@ -87,6 +87,8 @@ SIGNATURES = {
     "parm_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
     "parm_host_free": (C.c_int, [C.c_void_p]),
     "parm_debug_remainder": (C.c_int, [_dp, _dp, _dp, C.c_uint32]),
+    "parm_debug_philox": (C.c_int, [_u32p, _u32p, C.c_uint32]),
+    "parm_debug_normals": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, _dp]),
     "parm_kinetic_energy_noalloc": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, _dp, C.c_void_p,
                                               C.c_void_p]),
 }

@@ -1773,4 +1773,33 @@ int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t
     return PARM_OK;
 }
 
+int parm_debug_philox(const uint32_t* in, uint32_t* out, uint32_t n) {
+    if (!in || !out) return fail(PARM_ERR_ARG, "NULL argument");
+    if (n == 0) return PARM_OK;
+    uint32_t* buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, 40 * (size_t)n));
+    cudaError_t e = cudaMemcpy(buf, in, 24 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_philox_test(buf, buf + 6 * (size_t)n, n, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, buf + 6 * (size_t)n, 16 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+    return PARM_OK;
+}
+
+int parm_debug_normals(uint64_t seed, uint32_t sys, uint64_t step, uint32_t natoms, double* out) {
+    if (!out) return fail(PARM_ERR_ARG, "NULL argument");
+    if (natoms == 0) return PARM_OK;
+    double* buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, 48 * (size_t)natoms));
+    launch_normals_test(splitmix64(seed + sys), step, natoms, buf, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, buf, 48 * (size_t)natoms, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+    return PARM_OK;
+}
+
 }  // extern "C"

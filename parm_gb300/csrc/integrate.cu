@@ -625,4 +625,34 @@ void launch_rsq(const DevCtx& c, cudaStream_t s, int init) {
     }
 }
 
+// ---- test hooks of the Langevin generator (parm_debug_philox / parm_debug_normals) ----
+// in: 6 words per item (counter c0..c3, key k0, k1); out: the 4 output words
+__global__ void k_philox_test(const uint32_t* in, uint32_t* out, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c[4] = {in[6 * (size_t)i], in[6 * (size_t)i + 1], in[6 * (size_t)i + 2], in[6 * (size_t)i + 3]};
+    philox10(c, in[6 * (size_t)i + 4], in[6 * (size_t)i + 5]);
+#pragma unroll
+    for (int q = 0; q < 4; q++) out[4 * (size_t)i + q] = c[q];
+}
+
+// the six normals the Langevin step draws for atoms 0..n-1 of a system keyed `key` at counter `step`
+__global__ void k_normals_test(unsigned long long key, unsigned long long step, uint32_t n, double* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double g[6];
+    normals6(key, step, i, g);
+#pragma unroll
+    for (int q = 0; q < 6; q++) out[6 * (size_t)i + q] = g[q];
+}
+
+void launch_philox_test(const uint32_t* in, uint32_t* out, uint32_t n, cudaStream_t s) {
+    if (n) k_philox_test<<<grid_for(n), BLOCK, 0, s>>>(in, out, n);
+}
+
+void launch_normals_test(unsigned long long key, unsigned long long step, uint32_t n, double* out,
+                         cudaStream_t s) {
+    if (n) k_normals_test<<<grid_for(n), BLOCK, 0, s>>>(key, step, n, out);
+}
+
 }  // namespace parm

@@ -1,9 +1,9 @@
 // Kinetic energy of caller-owned device records, without any allocation.
 //
-// Some callers cannot allocate device memory: code running while a CUDA
-// graph is being captured, a host framework that owns every device buffer
-// through its own pool, or a real-time loop that must never block in the
-// driver's allocator.  parm_kinetic_energy_noalloc serves them: it reads
+// Some callers cannot allocate device memory: a host framework that owns
+// every device buffer through its own pool, a real-time loop that must never
+// block in the driver's allocator, or a process that runs under a fixed
+// device-memory budget.  parm_kinetic_energy_noalloc serves them: it reads
 // Atom records the caller already holds in device memory, writes the result
 // to a device location the caller provides, and keeps its per-atom scratch
 // in a file-scope __device__ array instead of allocating one.
@@ -92,12 +92,23 @@ extern "C" int parm_kinetic_energy_noalloc(const double* atoms, uint64_t stride,
     if (natoms > kNoAllocMaxAtoms)
         return parm::set_error(PARM_ERR_ARG, "parm_kinetic_energy_noalloc: at most 262144 atoms per call "
                                              "(the size of its static scratch)");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (s) {
+        // the scratch address belongs to the current device; a stream of another device cannot use it
+        int sdev = -1, cur = -1;
+        cudaError_t e = cudaStreamGetDevice(s, &sdev);
+        if (e != cudaSuccess) return parm::set_error(PARM_ERR_ARG, cudaGetErrorString(e));
+        e = cudaGetDevice(&cur);
+        if (e != cudaSuccess) return parm::set_error(PARM_ERR_CUDA, cudaGetErrorString(e));
+        if (sdev != cur)
+            return parm::set_error(PARM_ERR_ARG, "parm_kinetic_energy_noalloc: the stream belongs to another "
+                                                 "device than the current one");
+    }
     double* scratch = nullptr;
     int r = scratch_for_current_device(&scratch);
     if (r != PARM_OK) return r;
     const double o0 = origin ? origin[0] : 0.0, o1 = origin ? origin[1] : 0.0;
     const double o2 = (origin && ndim == 3) ? origin[2] : 0.0;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (natoms) k_ke_terms<<<parm::grid_for(natoms), parm::BLOCK, 0, s>>>(atoms, stride, natoms, ndim, o0, o1, o2, scratch);
     k_ke_reduce<<<1, 1024, 0, s>>>(scratch, natoms, out);
     cudaError_t e = cudaGetLastError();

@@ -192,6 +192,10 @@ int stg_set_smem_limits();   // cudaError_t of raising the kernels' shared-memor
 // debug entry used by the tests of the minimum-image routine
 void launch_remainder_test(const double* d, const double* L, double* out, uint32_t n,
                            cudaStream_t s);
+// test hooks of the Langevin generator (integrate.cu)
+void launch_philox_test(const uint32_t* in, uint32_t* out, uint32_t n, cudaStream_t s);
+void launch_normals_test(unsigned long long key, unsigned long long step, uint32_t n, double* out,
+                         cudaStream_t s);
 
 // what for launch_eval*: writes per-atom partials into c.red, ncomp per atom
 enum EvalWhat : int {

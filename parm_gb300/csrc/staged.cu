@@ -369,7 +369,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t limit) {
 // memory (one asynchronous copy per piece, 16-byte aligned, completion
 // counted on one mbarrier), then each warp moves its pieces' records into
 // the block frame in place.  Returns false (and flags ST_STAGE_TIMEOUT) when
-// the copies do not complete within the wait limit.
+// the copies do not complete within the wait limit; if they are still not
+// complete after a second bounded wait, no thread touches the staged shared
+// memory again.
 template <int ND, int EXTRA>
 __device__ bool stg_load_bulk(const DevCtx& c, const StgTable& T, float4* srec, void* sext, uint32_t cap,
                               uint64_t* bar) {
@@ -385,11 +387,15 @@ __device__ bool stg_load_bulk(const DevCtx& c, const StgTable& T, float4* srec, 
         bulk_g2s(srec + o, c.rec + T.g0[p], n * 16u, bar);
         if constexpr (EXTRA == 2) bulk_g2s(static_cast<float4*>(sext) + o, c.prm32 + T.g0[p], n * 16u, bar);
     }
-    bool ok = mbar_wait(bar, 1u << 22);
+    const bool ok = mbar_wait(bar, 1u << 22);
+    bool settled = ok;
     if (!ok) {
         atomicOr(c.status, ST_STAGE_TIMEOUT);
-        mbar_wait(bar, 1u << 22);   // the copies in flight, once more with a limit
+        settled = mbar_wait(bar, 1u << 22);   // the copies in flight, once more with a limit
     }
+    // unless every thread saw the copies complete, the block leaves its
+    // shared memory alone (no rewrite, no pair loop) and returns at once
+    if (!__syncthreads_and(settled)) return false;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (uint32_t p = warp; p < T.npiece; p += nw) {
         const uint32_t o = T.off[p];

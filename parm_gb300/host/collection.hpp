@@ -26,7 +26,7 @@ class Constraint {
     virtual ~Constraint() {}
 };
 
-//! Base of the time-step loops (src/collection.hpp:15-150, src/collection.cpp:1-180).
+//! Base of the time-step loops (src/collection.hpp:23-131, src/collection.cpp:1-180).
 class Collection {
    protected:
     sptr<Box> box;
@@ -74,7 +74,7 @@ class Collection {
     virtual void add_tracker(sptr<StateTracker> track);
 };
 
-//! Velocity Verlet (src/collection.hpp:755-790, src/collection.cpp:442-469).
+//! Velocity Verlet (src/collection.hpp:360-374, src/collection.cpp:442-469).
 class CollectionVerlet : public Collection {
    protected:
     flt dt;
@@ -90,7 +90,7 @@ class CollectionVerlet : public Collection {
     void set_dt(flt newdt) { dt = newdt; }
 };
 
-//! Damped velocity Verlet (src/collection.hpp:254-300, src/collection.cpp:324-381).
+//! Damped velocity Verlet (src/collection.hpp:273-326, src/collection.cpp:324-381).
 class CollectionDamped : public Collection {
    protected:
     flt dt, damping;
@@ -104,7 +104,7 @@ class CollectionDamped : public Collection {
     void timesteps(uint n) override;
 };
 
-//! Langevin dynamics (src/collection.hpp:205-250, src/collection.cpp:230-322).
+//! Langevin dynamics (src/collection.hpp:205-271, src/collection.cpp:230-322).
 //! The noise comes from a counter-based generator (one stream per handle,
 //! keyed from the seeded host engine), not from the reference's Boost stream.
 class CollectionSol : public Collection {

@@ -14,7 +14,7 @@
 
 #include "trackers.hpp"
 
-//! Interface of everything a Collection sums (src/interaction.hpp:43-70).
+//! Interface of everything a Collection sums (src/interaction.hpp:59-104).
 class Interaction {
    public:
     virtual flt energy(Box& box) = 0;

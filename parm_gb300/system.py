@@ -272,3 +272,20 @@ def debug_remainder(d, L) -> np.ndarray:
     out = np.zeros_like(d)
     check(lib.parm_debug_remainder(dptr(d), dptr(L), dptr(out), d.size))
     return out
+
+
+def debug_philox(ctr_key) -> np.ndarray:
+    """The library's Philox4x32-10 on rows (c0, c1, c2, c3, k0, k1); returns (n, 4) uint32."""
+    lib = capi.load()
+    a = np.ascontiguousarray(np.asarray(ctr_key, dtype=np.uint32).reshape(-1, 6))
+    out = np.zeros((a.shape[0], 4), dtype=np.uint32)
+    check(lib.parm_debug_philox(capi.u32ptr(a), capi.u32ptr(out), a.shape[0]))
+    return out
+
+
+def debug_normals(seed: int, sys: int, step: int, natoms: int) -> np.ndarray:
+    """The (natoms, 6) standard normals parm_sol draws for system `sys` at counter `step`."""
+    lib = capi.load()
+    out = np.zeros((natoms, 6))
+    check(lib.parm_debug_normals(int(seed), int(sys), int(step), int(natoms), dptr(out)))
+    return out

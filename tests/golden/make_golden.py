@@ -21,6 +21,7 @@ used: Langevin cases run at T = 0, where the noise term vanishes.
 from __future__ import annotations
 
 import argparse
+import os
 import subprocess
 import sys
 from pathlib import Path
@@ -197,7 +198,7 @@ def cases() -> list[dict]:
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference/src")
+    ap.add_argument("--ref-src", default=os.environ.get("PARM_REFERENCE_SRC", "/root/reference/src"))
     ap.add_argument("--only", default=None)
     a = ap.parse_args(argv)
     subprocess.run(["make", "-C", str(REFBUILD), f"REF={a.ref_src}", f"OUT={REFOUT}", "-j2"], check=True)

@@ -6,13 +6,15 @@ against parm_gb300/host; the reference's example program src/bin/LJatoms.cpp
 does too where the reference sources are present.  (Running them needs a GPU:
 tests/test_gpu_host_api.py.)
 """
+import os
 from pathlib import Path
 
 import pytest
 
 from host_api import DECK_DRIVER, compile_program
 
-REF_LJATOMS = Path("/root/reference/src/bin/LJatoms.cpp")
+REF_SRC = Path(os.environ.get("PARM_REFERENCE_SRC", "/root/reference/src"))
+REF_LJATOMS = REF_SRC / "bin" / "LJatoms.cpp"
 
 
 @pytest.mark.parametrize("ndim", [3, 2])

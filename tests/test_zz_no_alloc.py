@@ -1,9 +1,9 @@
 """parm_kinetic_energy_noalloc: the entry point for callers that cannot allocate.
 
-Such callers (code running inside CUDA graph capture, frameworks whose memory
-pool owns every device buffer, loops that must never enter the allocator)
-pass Atom records they already hold in device memory and a device location
-for the result.  The entry point keeps its scratch in a static device array,
+Such callers (frameworks whose memory pool owns every device buffer, loops
+that must never enter the allocator, processes under a fixed device-memory
+budget) pass Atom records they already hold in device memory and a device
+location for the result.  The entry point keeps its scratch in a static device array,
 so its result must equal the handle-based parm_kinetic_energy on the same
 atoms, call after call.  This file is collected last on purpose.
 """
