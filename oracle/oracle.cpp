@@ -443,6 +443,242 @@ void System::sol(double dt, double damping, double T, double c0, double c1, doub
     update_trackers();
 }
 
+
+// ---------------------------------------------------------------------------
+// Conjugate-gradient minimisers: CollectionNLCG (positions and the box's
+// log-volume, collection.hpp:400-475, collection.cpp:494-829) and
+// CollectionNLCGV (positions only, collection.hpp:490-566,
+// collection.cpp:894-1168), restated on one System with the reference's
+// sequential sums.
+// ---------------------------------------------------------------------------
+struct Nlcg {
+    bool boxed = true;   // CollectionNLCG (true) or CollectionNLCGV (false)
+    // parameters (collection.hpp:407-425)
+    double dt = 0, seceps = 1e-20, kappa = 10, alphamax = 2, afrac = 0, dxmax = 100, stepmax = 1e-3,
+           kmax = 1000, P0 = 0, maxdV = 0;
+    uint32_t secmax = 40;
+    // state kept between time steps
+    double Knew = 0, k = 0, vl = 0, fl = 0, al = 0;
+    double alpha = 0, beta = 0, betaused = 0, dxsum = 0, alphavmax = 0;
+    uint32_t sec = 0;
+
+    // OriginBox::V (box.hpp:112): the product of the side lengths
+    static double volume(const System& S) {
+        double V = S.L[0] * S.L[1];
+        if (S.nd == 3) V = V * S.L[2];
+        return V;
+    }
+    // CollectionNLCG::get_length_squared (collection.cpp:641-649)
+    static double lensq(const System& S) { return S.nd == 3 ? std::pow(volume(S), 2.0 / 3.0) : volume(S); }
+
+    // fdota / fdotf / fdotv / vdotv (collection.cpp:651-705, 910-975)
+    double dot_sum(const System& S, const std::vector<double>& p, const std::vector<double>& q) const {
+        double r = 0;
+        for (uint32_t i = 0; i < S.n; i++) {
+            if (!System::mobile(S.m[i])) continue;
+            r += dotv(&p[i * S.nd], &q[i * S.nd], S.nd);
+        }
+        return r;
+    }
+    double fdota(const System& S) const {
+        double r = dot_sum(S, S.f, S.a);
+        return boxed ? r / lensq(S) + fl * al : r;
+    }
+    double fdotv(const System& S) const {
+        double r = dot_sum(S, S.f, S.v);
+        return boxed ? r / lensq(S) + fl * vl : r;
+    }
+    double vdotv(const System& S) const {
+        double r = dot_sum(S, S.v, S.v);
+        return boxed ? r / lensq(S) + vl * vl : r;
+    }
+
+    // CollectionNLCG::stepx (collection.cpp:621-639) / CollectionNLCGV::stepx (900-908)
+    void stepx(System& S, double dx) const {
+        if (boxed) {
+            const double Lfac = std::exp(dx * vl / (kappa * S.nd));
+            for (uint32_t i = 0; i < S.n; i++)
+                for (int d = 0; d < S.nd; d++) {
+                    double& x = S.x[i * S.nd + d];
+                    x *= Lfac;
+                    x += S.v[i * S.nd + d] * dx;
+                }
+            for (int d = 0; d < S.nd; d++) S.L[d] *= Lfac;   // OriginBox::resize (box.hpp:125-128)
+        } else {
+            for (uint32_t i = 0; i < S.n; i++) {
+                if (!System::mobile(S.m[i])) continue;
+                for (int d = 0; d < S.nd; d++) S.x[i * S.nd + d] += S.v[i * S.nd + d] * dx;
+            }
+        }
+    }
+
+    // Collection::set_forces_get_pressure(false) (collection.cpp:181-208)
+    static double forces_pressure(System& S) {
+        std::fill(S.f.begin(), S.f.end(), 0.0);
+        double p = 0;
+        if (S.kind >= 0) S.nlisted_set_forces(true, &p, nullptr);
+        for (uint32_t i = 0; i < S.n; i++)
+            if (!System::mobile(S.m[i]))
+                for (int d = 0; d < S.nd; d++) S.a[i * S.nd + d] = 0;
+        return p;
+    }
+
+    // CollectionNLCG::set_forces(constraints_and_a, setV) (collection.cpp:534-566);
+    // CollectionNLCGV has Collection::set_forces (collection.cpp:159-179)
+    void set_forces(System& S, bool constraints_and_a, bool setV = true) {
+        if (!boxed) {
+            S.collection_set_forces(constraints_and_a);
+            return;
+        }
+        const double V = volume(S);
+        if (setV) {
+            const double interacP = forces_pressure(S);
+            fl = ((interacP / S.nd) - (P0 * V)) / kappa;
+            if (constraints_and_a) {
+                al = fl;
+                vl = fl;
+            }
+        } else {
+            S.collection_set_forces(false);
+        }
+        if (constraints_and_a) {
+            for (uint32_t i = 0; i < S.n; i++) {
+                if (!System::mobile(S.m[i])) {
+                    for (int d = 0; d < S.nd; d++) S.v[i * S.nd + d] = S.a[i * S.nd + d] = 0;
+                    continue;
+                }
+                for (int d = 0; d < S.nd; d++) S.a[i * S.nd + d] = S.v[i * S.nd + d] = S.f[i * S.nd + d];
+            }
+            Knew = fdota(S);
+        }
+    }
+
+    // CollectionNLCG::reset (collection.cpp:525-532) / CollectionNLCGV::reset (977-988)
+    void reset(System& S) {
+        k = 0;
+        if (boxed) {
+            set_forces(S, true, true);
+            for (size_t q = 0; q < S.v.size(); q++) S.v[q] = S.a[q];
+            vl = al;
+        } else {
+            S.collection_set_forces(false);
+            for (uint32_t i = 0; i < S.n; i++) {
+                if (!System::mobile(S.m[i])) continue;
+                for (int d = 0; d < S.nd; d++) S.v[i * S.nd + d] = S.a[i * S.nd + d] = S.f[i * S.nd + d];
+            }
+        }
+    }
+
+    // CollectionNLCG::descend (collection.cpp:811-829) / CollectionNLCGV::descend (990-1005)
+    void descend(System& S) {
+        set_forces(S, false, true);
+        for (uint32_t i = 0; i < S.n; i++) {
+            if (!System::mobile(S.m[i])) continue;
+            for (int d = 0; d < S.nd; d++) S.v[i * S.nd + d] = S.a[i * S.nd + d] = S.f[i * S.nd + d];
+        }
+        if (boxed) {
+            al = fl;
+            vl = fl;
+        }
+        stepx(S, dt);
+        S.update_trackers();
+    }
+
+    // CollectionNLCG::timestep (collection.cpp:682-809) / CollectionNLCGV::timestep (1019-1168)
+    void timestep(System& S) {
+        stepx(S, dt);
+        set_forces(S, false, true);
+        double eta0 = -fdotv(S);
+        double eta;
+        stepx(S, -dt);
+        S.update_trackers();
+        alpha = -dt;
+        set_forces(S, false, true);
+        dxsum = 0;
+        const double vdv = vdotv(S);
+        for (sec = 0; sec < secmax; sec++) {
+            eta = -fdotv(S);
+            double alphafac = -eta / std::abs(eta0 - eta);
+            if (std::abs(eta0 - eta) <= 1e-12 * std::abs(eta)) {
+                alphafac = alphamax > 0 ? alphamax : 1.1;
+                sec = sec > 0 ? sec * 2 - 1 : 1;
+            }
+            if (alphamax > 0 && alphafac > alphamax) alphafac = alphamax;
+            if (alphamax > 0 && alphafac < -alphamax) alphafac = -alphamax;
+            alpha = std::abs(alpha) * alphafac;
+            const double newdxsum = std::abs(dxsum + alpha);
+            if (dxmax > 0 && newdxsum > dxmax) {
+                k = 0;
+                break;
+            }
+            if (boxed) {
+                const double dVoverV = std::expm1(std::abs(dxsum + alpha) * vl / (kappa * S.nd));
+                if (maxdV > 0 && dVoverV > maxdV) {
+                    k = 0;
+                    break;
+                }
+            }
+            dxsum += alpha;
+            stepx(S, alpha);
+            if (!boxed) S.update_trackers();
+            set_forces(S, false, true);
+            eta0 = eta;
+            if (alpha * alpha * vdv < seceps * seceps) break;
+            if ((sec > 1) && (afrac > 0) && (std::abs(alpha) < std::abs(dxsum)) &&
+                (std::abs(alpha) / std::abs(dxsum) < afrac))
+                break;
+            if (stepmax > 0 && dxsum * dxsum * vdv > stepmax * stepmax) {
+                k = 0;
+                break;
+            }
+        }
+        alphavmax = std::sqrt(alpha * alpha * vdv);
+        const double Kold = Knew;
+        const double Kmid = fdota(S);
+        for (uint32_t i = 0; i < S.n; i++) {
+            if (boxed && !System::mobile(S.m[i])) {
+                for (int d = 0; d < S.nd; d++) S.a[i * S.nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < S.nd; d++) S.a[i * S.nd + d] = S.f[i * S.nd + d];
+        }
+        al = fl;
+        Knew = fdota(S);
+        beta = (Knew - Kmid) / Kold;
+        betaused = beta;
+        k++;
+        if (k >= kmax || std::isinf(betaused) || std::isnan(betaused) || betaused <= 0) {
+            k = 0;
+            betaused = 0;
+        } else if (betaused > 1) {
+            betaused = 1;
+        }
+        for (uint32_t i = 0; i < S.n; i++) {
+            if (boxed && !System::mobile(S.m[i])) {
+                for (int d = 0; d < S.nd; d++) S.v[i * S.nd + d] = 0;
+                continue;
+            }
+            for (int d = 0; d < S.nd; d++) S.v[i * S.nd + d] = S.a[i * S.nd + d] + S.v[i * S.nd + d] * betaused;
+        }
+        if (boxed) vl = al + betaused * vl;
+    }
+};
+
+// the parameter / state vectors of the C ABI (PARM_NLCG_P_*, PARM_NLCG_S_*)
+void nlcg_set(Nlcg& G, const double* p) {
+    G.dt = p[0]; G.P0 = p[1]; G.kappa = p[2]; G.kmax = p[3]; G.secmax = (uint32_t)p[4]; G.seceps = p[5];
+    G.alphamax = p[6]; G.afrac = p[7]; G.dxmax = p[8]; G.stepmax = p[9]; G.maxdV = p[10];
+}
+void nlcg_get_state(const Nlcg& G, double* o) {
+    const double v[11] = {G.Knew, G.k, G.vl, G.fl, G.al, G.alpha, G.beta, G.betaused, G.dxsum, G.alphavmax,
+                          (double)G.sec};
+    for (int q = 0; q < 11; q++) o[q] = v[q];
+}
+void nlcg_set_state(Nlcg& G, const double* o) {
+    G.Knew = o[0]; G.k = o[1]; G.vl = o[2]; G.fl = o[3]; G.al = o[4]; G.alpha = o[5]; G.beta = o[6];
+    G.betaused = o[7]; G.dxsum = o[8]; G.alphavmax = o[9]; G.sec = (uint32_t)o[10];
+}
+
 }  // namespace
 
 extern "C" {
@@ -566,6 +802,33 @@ void orc_sol(void* s, double dt, double damping, double T, double c0, double c1,
     System* S = static_cast<System*>(s);
     for (uint32_t k = 0; k < nsteps; k++)
         S->sol(dt, damping, T, c0, c1, c2, x11, x21, x22, seed, step0 + k);
+}
+
+// CollectionNLCG / CollectionNLCGV on the oracle system: create with the
+// parameter vector (dt, P0, kappa, kmax, secmax, seceps, alphamax, afrac,
+// dxmax, stepmax, maxdV); the state vector is (Knew, k, vl, fl, al, alpha,
+// beta, betaused, dxsum, alphavmax, sec)
+void* orc_nlcg_create(int boxed, const double* params) {
+    Nlcg* G = new Nlcg();
+    G->boxed = boxed != 0;
+    nlcg_set(*G, params);
+    return G;
+}
+void orc_nlcg_destroy(void* g) { delete static_cast<Nlcg*>(g); }
+void orc_nlcg_set_params(void* g, const double* params) { nlcg_set(*static_cast<Nlcg*>(g), params); }
+void orc_nlcg_get_state(void* g, double* out) { nlcg_get_state(*static_cast<Nlcg*>(g), out); }
+void orc_nlcg_set_state(void* g, const double* in) { nlcg_set_state(*static_cast<Nlcg*>(g), in); }
+void orc_nlcg_set_forces(void* g, void* s, int constraints_and_a) {
+    static_cast<Nlcg*>(g)->set_forces(*static_cast<System*>(s), constraints_and_a != 0, true);
+}
+void orc_nlcg_reset(void* g, void* s) { static_cast<Nlcg*>(g)->reset(*static_cast<System*>(s)); }
+void orc_nlcg_descend(void* g, void* s) { static_cast<Nlcg*>(g)->descend(*static_cast<System*>(s)); }
+void orc_nlcg_timestep(void* g, void* s, uint32_t nsteps) {
+    for (uint32_t q = 0; q < nsteps; q++) static_cast<Nlcg*>(g)->timestep(*static_cast<System*>(s));
+}
+void orc_get_box(void* s, double* L) {
+    System* S = static_cast<System*>(s);
+    for (int d = 0; d < S->nd; d++) L[d] = S->L[d];
 }
 
 void orc_normals6(uint64_t seed, uint64_t step, uint32_t atom, double* out) {

@@ -51,6 +51,16 @@ def lib() -> C.CDLL:
                                C.c_uint32]),
             "orc_normals6": (None, [C.c_uint64, C.c_uint64, C.c_uint32, _dp]),
             "orc_philox": (None, [_u32p, _u32p, C.c_uint64]),
+            "orc_nlcg_create": (C.c_void_p, [C.c_int, _dp]),
+            "orc_nlcg_destroy": (None, [C.c_void_p]),
+            "orc_nlcg_set_params": (None, [C.c_void_p, _dp]),
+            "orc_nlcg_get_state": (None, [C.c_void_p, _dp]),
+            "orc_nlcg_set_state": (None, [C.c_void_p, _dp]),
+            "orc_nlcg_set_forces": (None, [C.c_void_p, C.c_void_p, C.c_int]),
+            "orc_nlcg_reset": (None, [C.c_void_p, C.c_void_p]),
+            "orc_nlcg_descend": (None, [C.c_void_p, C.c_void_p]),
+            "orc_nlcg_timestep": (None, [C.c_void_p, C.c_void_p, C.c_uint32]),
+            "orc_get_box": (None, [C.c_void_p, _dp]),
             "orc_kinetic_energy": (C.c_double, [C.c_void_p, _dp]),
             "orc_momentum": (C.c_double, [C.c_void_p, _dp]),
             "orc_pairs_celllist": (C.c_uint64, [C.c_void_p, _u32p, C.c_uint64]),
@@ -238,3 +248,63 @@ def philox(ctr_key) -> np.ndarray:
     out = np.zeros((a.shape[0], 4), dtype=np.uint32)
     lib().orc_philox(a.ctypes.data_as(_u32p), out.ctypes.data_as(_u32p), a.shape[0])
     return out
+
+
+NLCG_PARAMS = ("dt", "P0", "kappa", "kmax", "secmax", "seceps", "alphamax", "afrac", "dxmax", "stepmax", "maxdV")
+NLCG_STATE = ("Knew", "k", "vl", "fl", "al", "alpha", "beta", "betaused", "dxsum", "alphavmax", "sec")
+
+
+def nlcg_params(dt, P0=0.0, kappa=10.0, kmax=1000, secmax=40, seceps=1e-20, alphamax=2.0, afrac=0.0,
+                dxmax=100.0, stepmax=1e-3, maxdV=0.0) -> np.ndarray:
+    """CollectionNLCG's parameter vector, defaults of its constructor (collection.cpp:494-523)."""
+    return np.array([dt, P0, kappa, kmax, secmax, seceps, alphamax, afrac, dxmax, stepmax, maxdV],
+                    dtype=np.float64)
+
+
+def nlcgv_params(dt, kmax=1000, secmax=10, seceps=1e-4, alphamax=0.0, afrac=0.0, dxmax=0.0,
+                 stepmax=0.0) -> np.ndarray:
+    """CollectionNLCGV's parameter vector, defaults of its constructor (collection.cpp:877-898);
+    P0, kappa and maxdV do not apply."""
+    return np.array([dt, 0.0, 1.0, kmax, secmax, seceps, alphamax, afrac, dxmax, stepmax, 0.0],
+                    dtype=np.float64)
+
+
+class OracleNLCG:
+    """CollectionNLCG (boxed) / CollectionNLCGV on an Oracle system."""
+
+    def __init__(self, orc: "Oracle", params, boxed=True):
+        self.o = orc
+        self.L_ = lib()
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self.g = self.L_.orc_nlcg_create(1 if boxed else 0, _d(p))
+
+    def __del__(self):
+        if getattr(self, "g", None):
+            self.L_.orc_nlcg_destroy(self.g)
+            self.g = None
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self.L_.orc_nlcg_set_params(self.g, _d(p))
+
+    def state(self) -> dict:
+        out = np.zeros(len(NLCG_STATE))
+        self.L_.orc_nlcg_get_state(self.g, _d(out))
+        return dict(zip(NLCG_STATE, out))
+
+    def set_forces(self, constraints_and_a=True):
+        self.L_.orc_nlcg_set_forces(self.g, self.o.h, 1 if constraints_and_a else 0)
+
+    def reset(self):
+        self.L_.orc_nlcg_reset(self.g, self.o.h)
+
+    def descend(self):
+        self.L_.orc_nlcg_descend(self.g, self.o.h)
+
+    def timestep(self, n=1):
+        self.L_.orc_nlcg_timestep(self.g, self.o.h, int(n))
+
+    def box(self) -> np.ndarray:
+        out = np.zeros(self.o.ndim)
+        self.L_.orc_get_box(self.o.h, _d(out))
+        return out

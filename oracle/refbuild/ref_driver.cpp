@@ -5,8 +5,13 @@
 // Input (whitespace separated): kind integrator nsteps dt damping T skin
 //   L[NDIM]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2
 //   norder order[norder]   nign (a b)[nign]   nout out_steps[nout]
+//   integrators 3 and 4 add one line: dt P0 kappa kmax secmax seceps alphamax afrac
+//   dxmax stepmax maxdV
 // kind: 0 NListed<EpsSigCutAtom,LennardJonesCutPair>, 1 <EpsSigExpAtom,RepulsionPair>,
-//       2 <EpsSigAtom,LJRepulsePair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0)
+//       2 <EpsSigAtom,LJRepulsePair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
+//       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
+//       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
+//       4 CollectionNLCGV (constructor, then reset())
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -63,6 +68,9 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
     for (auto& q : ign) q = rdu();
     std::vector<int> outs(rdu());
     for (auto& q : outs) q = (int)rd();
+    double cg[11] = {0};
+    if (integ >= 3)
+        for (double& q : cg) q = rd();
 
     boost::shared_ptr<OriginBox> obox(new OriginBox(L));
     boost::shared_ptr<AtomVec> atoms(new AtomVec(ms));
@@ -86,9 +94,30 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
     std::vector<boost::shared_ptr<Interaction> > is(1, inter);
     std::vector<boost::shared_ptr<StateTracker> > ts(1, nl);
     boost::shared_ptr<Collection> col;
+    boost::shared_ptr<CollectionNLCG> cg3;
+    boost::shared_ptr<CollectionNLCGV> cg4;
+    std::vector<boost::shared_ptr<Constraint> > cs;
     if (integ == 0) col.reset(new CollectionVerlet(obox, atoms, dt, is, ts));
     else if (integ == 1) col.reset(new CollectionDamped(obox, atoms, dt, damping, is, ts));
-    else col.reset(new CollectionSol(obox, atoms, dt, damping, T, is, ts));
+    else if (integ == 2) col.reset(new CollectionSol(obox, atoms, dt, damping, T, is, ts));
+    else if (integ == 3) {
+        cg3.reset(new CollectionNLCG(obox, atoms, cg[0], cg[1], is, ts, cs, cg[2], cg[3], (uint)cg[4], cg[5]));
+        cg3->set_max_alpha(cg[6]);
+        cg3->set_max_alpha_fraction(cg[7]);
+        cg3->set_max_dx(cg[8]);
+        cg3->set_max_step(cg[9]);
+        cg3->maxdV = cg[10];
+        cg3->set_forces(true, true);
+        col = cg3;
+    } else {
+        cg4.reset(new CollectionNLCGV(obox, atoms, cg[0], is, ts, cs, cg[3], (uint)cg[4], cg[5]));
+        cg4->set_max_alpha(cg[6]);
+        cg4->set_max_alpha_fraction(cg[7]);
+        cg4->set_max_dx(cg[8]);
+        cg4->set_max_step(cg[9]);
+        cg4->reset();
+        col = cg4;
+    }
 
     Matrix st = inter->stress(*obox);
     std::printf("INIT %.17g %.17g %llu %llu %u\n", inter->energy(*obox), inter->pressure(*obox),
@@ -108,6 +137,19 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
             step++;
         }
         std::printf("STEP %d %u %.17g %.17g\n", step, nl->which(), inter->energy(*obox), atoms->kinetic_energy());
+        if (integ >= 3) {
+            const Vec Lb = obox->box_shape();
+            std::printf("NLCG");
+            pvec(Lb);
+            if (cg3)
+                std::printf(" %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %u\n", cg3->Knew, cg3->k,
+                            cg3->vl, cg3->fl, cg3->al, cg3->alpha, cg3->beta, cg3->betaused, cg3->dxsum,
+                            cg3->alphavmax, cg3->sec);
+            else
+                std::printf(" %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %u\n", cg4->Knew, cg4->k,
+                            cg4->vl, cg4->fl, cg4->al, cg4->alpha, cg4->beta, cg4->betaused, cg4->dxsum,
+                            cg4->alphavmax, cg4->sec);
+        }
         for (unsigned i = 0; i < N; i++) {
             pvec((*atoms)[i].x);
             pvec((*atoms)[i].v);

@@ -33,7 +33,7 @@ ROOT = HERE.parents[1]
 REFBUILD = ROOT / "oracle" / "refbuild"
 REFOUT = ROOT / "oracle" / "_ref"
 
-VERLET, DAMPED, SOL = 0, 1, 2
+VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE = 0, 1, 2
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
@@ -49,6 +49,8 @@ def _deck(c: dict) -> str:
     ig = c["ignores"].reshape(-1)
     out.append(f"{len(ig) // 2} " + " ".join(str(int(q)) for q in ig))
     out.append(f"{len(c['out_steps'])} " + " ".join(str(int(q)) for q in c["out_steps"]))
+    if c["integ"] >= NLCG:
+        out.append(" ".join(repr(float(q)) for q in c["cg"]))
     assert nd in (2, 3)
     return "\n".join(out) + "\n"
 
@@ -72,7 +74,7 @@ def _parse(text: str, n: int, nd: int) -> dict:
     counts = np.array([int(h[3]), int(h[4]), int(h[5])], dtype=np.int64)
     stress = np.array([float(t) for t in nxt()]).reshape(nd, nd)
     fa = np.array([[float(t) for t in nxt()] for _ in range(n)]).reshape(n, 2 * nd)
-    steps, which, energy, ke, st = [], [], [], [], []
+    steps, which, energy, ke, st, cgl = [], [], [], [], [], []
     while pos < len(lines):
         h = nxt()
         assert h[0] == "STEP"
@@ -80,9 +82,15 @@ def _parse(text: str, n: int, nd: int) -> dict:
         which.append(int(h[2]))
         energy.append(float(h[3]))
         ke.append(float(h[4]))
+        if pos < len(lines) and lines[pos].startswith("NLCG"):
+            cgl.append([float(t) for t in nxt()[1:]])
         st.append(np.array([[float(t) for t in nxt()] for _ in range(n)]).reshape(n, 4 * nd))
     st = np.array(st).reshape(len(steps), n, 4 * nd)
-    return {"pairs": pairs, "init": init, "init_counts": counts, "stress": stress,
+    extra = {}
+    if cgl:
+        cg = np.array(cgl)
+        extra = {"box_steps": cg[:, :nd], "cg_state_steps": cg[:, nd:]}
+    return {**extra, "pairs": pairs, "init": init, "init_counts": counts, "stress": stress,
             "f0": fa[:, :nd], "a0": fa[:, nd:], "steps": np.array(steps, dtype=np.int64),
             "which_steps": np.array(which, dtype=np.int64), "energy_steps": np.array(energy),
             "ke_steps": np.array(ke), "x_steps": st[:, :, 0:nd], "v_steps": st[:, :, nd:2 * nd],
@@ -90,9 +98,10 @@ def _parse(text: str, n: int, nd: int) -> dict:
 
 
 def _case(name, kind, integ, nsteps, dt, L, x, v, m, params, skin, out_steps, damping=0.0, T=0.0,
-          order=None, ignores=None):
+          order=None, ignores=None, cg=None):
     n = len(m)
-    return {"name": name, "kind": kind, "integ": integ, "nsteps": nsteps, "dt": float(dt),
+    extra = {} if cg is None else {"cg": np.asarray(cg, dtype=np.float64)}
+    return {**extra, "name": name, "kind": kind, "integ": integ, "nsteps": nsteps, "dt": float(dt),
             "damping": float(damping), "T": float(T), "skin": float(skin),
             "L": np.asarray(L, dtype=np.float64), "x": np.asarray(x, dtype=np.float64),
             "v": np.asarray(v, dtype=np.float64), "m": np.asarray(m, dtype=np.float64),
@@ -193,6 +202,38 @@ def cases() -> list[dict]:
     params = np.tile([1.0, 2.0, 2.0], (n, 1))     # cut = sigma = 2.0, list radius 2.5
     out.append(_case("edges64_pairs", REPULSION, VERLET, 50, 0.005, Lb, x, rng.normal(0, 0.3, (n, 3)),
                      np.ones(n), params, 0.5, [1, 20, 50]))
+    # 9. CollectionNLCG (box and positions), 3D harmonic spheres from phi = 0.4 at the goal
+    #    pressure 1e-3, set up as pyparm's packmin.Minimizer (dt 0.1, kappa 10, kmax 1000,
+    #    secmax 40, seceps 1e-20, alphamax 2, dxmax 100, stepmax 1e-3); one immobile atom
+    rng = np.random.default_rng(41)
+    n = 64
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lp = (np.sum(np.pi * sig ** 3 / 6) / 0.4) ** (1 / 3)
+    m = np.ones(n)
+    m[5] = np.inf
+    cg = [0.1, 1e-3, 10.0, 1000, 40, 1e-20, 2.0, 0.0, 100.0, 1e-3, 0.0]
+    out.append(_case("nlcg64_pack", REPULSION, NLCG, 200, 0.1, [Lp] * 3, rng.uniform(0, Lp, (n, 3)),
+                     np.zeros((n, 3)), m, np.stack([np.ones(n), sig, np.full(n, 2.0)], 1), 0.4,
+                     [0, 1, 2, 3, 5, 10, 30, 100, 200], cg=cg))
+    # 10. CollectionNLCG in 2D, Hertzian (exponent 2.5) disks from phi = 0.6, goal pressure 1e-2
+    rng = np.random.default_rng(42)
+    n = 80
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lq = np.sqrt(np.sum(np.pi * sig ** 2 / 4) / 0.6)
+    cg = [0.1, 1e-2, 10.0, 1000, 40, 1e-20, 2.0, 0.0, 100.0, 1e-3, 0.0]
+    out.append(_case("nlcg80_2d_pack", REPULSION, NLCG, 150, 0.1, [Lq, Lq], rng.uniform(0, Lq, (n, 2)),
+                     np.zeros((n, 2)), np.ones(n), np.stack([np.ones(n), sig, np.full(n, 2.5)], 1), 0.4,
+                     [0, 1, 2, 5, 10, 50, 150], cg=cg))
+    # 11. CollectionNLCGV (positions only, fixed box), 3D harmonic spheres at phi = 0.7,
+    #     the constructor's defaults (kmax 1000, secmax 10, seceps 1e-4)
+    rng = np.random.default_rng(43)
+    n = 100
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lv = (np.sum(np.pi * sig ** 3 / 6) / 0.7) ** (1 / 3)
+    cg = [0.01, 0.0, 1.0, 1000, 10, 1e-4, 0.0, 0.0, 0.0, 0.0, 0.0]
+    out.append(_case("nlcgv100_fixed", REPULSION, NLCGV, 200, 0.01, [Lv] * 3, rng.uniform(0, Lv, (n, 3)),
+                     np.zeros((n, 3)), np.ones(n), np.stack([np.ones(n), sig, np.full(n, 2.0)], 1), 0.3,
+                     [0, 1, 2, 5, 10, 50, 200], cg=cg))
     return out
 
 

@@ -6,7 +6,11 @@ reference's outputs for it: the neighbour pair list after ``update_list(true)``,
 forces, accelerations, energy, pressure, stress, contacts and overlaps after
 ``Collection::initialize`` (src/collection.cpp:13-19), and positions,
 velocities, accelerations, forces, energy, kinetic energy and the list's
-``which()`` counter at the recorded steps.
+``which()`` counter at the recorded steps.  The conjugate-gradient cases
+(CollectionNLCG / CollectionNLCGV) add their parameter vector ``cg`` and, per
+recorded step, the box (``box_steps``) and the minimiser's state
+(``cg_state_steps``: Knew, k, vl, fl, al, alpha, beta, betaused, dxsum,
+alphavmax, sec).
 """
 from __future__ import annotations
 
@@ -15,7 +19,7 @@ from pathlib import Path
 import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-VERLET, DAMPED, SOL = 0, 1, 2
+VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 
 
 def names() -> list[str]:

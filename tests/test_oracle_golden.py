@@ -4,13 +4,15 @@ The fixtures were produced by the reference's sources compiled as they are
 (``tests/golden/make_golden.py``); the oracle must reproduce every recorded
 number bit for bit: the neighbour list (its order too), forces and
 accelerations, energy, pressure, stress, contact and overlap counts, and the
-trajectories of CollectionVerlet, CollectionDamped and CollectionSol (T = 0).
+trajectories of CollectionVerlet, CollectionDamped and CollectionSol (T = 0),
+and the conjugate-gradient minimisers CollectionNLCG (box included) and
+CollectionNLCGV with their scalar state.
 """
 import numpy as np
 import pytest
 
-from golden_cases import DAMPED, SOL, VERLET, load, names
-from oracle.oracle import Oracle
+from golden_cases import DAMPED, NLCG, NLCGV, SOL, VERLET, load, names
+from oracle.oracle import NLCG_STATE, Oracle, OracleNLCG
 
 CASES = names()
 
@@ -26,11 +28,24 @@ def replay(d):
     return o
 
 
-def step_to(o, d, done, target):
+def minimiser(o, d):
+    """Collection set-up of the conjugate-gradient cases, as the fixture driver does it."""
+    if d["integ"] == NLCG:
+        g = OracleNLCG(o, d["cg"], boxed=True)
+        g.set_forces(True)
+    else:
+        g = OracleNLCG(o, d["cg"], boxed=False)
+        g.reset()
+    return g
+
+
+def step_to(o, d, done, target, g=None):
     k = target - done
     if k <= 0:
         return
-    if d["integ"] == VERLET:
+    if g is not None:
+        g.timestep(k)
+    elif d["integ"] == VERLET:
         o.verlet(d["dt"], k)
     elif d["integ"] == DAMPED:
         o.damped(d["dt"], d["damping"], k)
@@ -49,6 +64,7 @@ def test_oracle_matches_reference(name):
     o = replay(d)
     np.testing.assert_array_equal(o.pairs(), d["pairs"])
     o.initialize()
+    g = minimiser(o, d) if d["integ"] >= NLCG else None
     st = o.get_state()
     np.testing.assert_array_equal(st["f"], d["f0"])
     np.testing.assert_array_equal(st["a"], d["a0"])
@@ -61,8 +77,13 @@ def test_oracle_matches_reference(name):
     assert o.which() == d["init_counts"][2]
     done = 0
     for i, s in enumerate(d["steps"]):
-        step_to(o, d, done, int(s))
+        step_to(o, d, done, int(s), g)
         done = int(s)
+        if g is not None:
+            np.testing.assert_array_equal(g.box(), d["box_steps"][i], err_msg=f"box at step {s}")
+            state = g.state()
+            np.testing.assert_array_equal([state[k] for k in NLCG_STATE], d["cg_state_steps"][i],
+                                          err_msg=f"minimiser state at step {s}")
         st = o.get_state()
         for key in ("x", "v", "a", "f"):
             np.testing.assert_array_equal(st[key], d[f"{key}_steps"][i], err_msg=f"{key} at step {s}")
