@@ -136,6 +136,61 @@ int parm_verlet(parm_system* s, double dt, uint32_t nsteps);
 int parm_damped(parm_system* s, double dt, double damping, uint32_t nsteps);
 int parm_sol(parm_system* s, double dt, double damping, double T, uint64_t seed, uint32_t nsteps);
 
+/* Conjugate-gradient minimisers, every system with its own line search:
+ *   boxed != 0: CollectionNLCG (src/collection.hpp:400-475, src/collection.cpp:494-829),
+ *     positions and the box's log-volume, H = U + P0 V; the boxes change
+ *     (parm_get_boxes reads them);
+ *   boxed == 0: CollectionNLCGV (src/collection.hpp:490-566, src/collection.cpp:877-1168),
+ *     positions only.
+ * params: nsys x PARM_NLCG_NPARAM doubles in the order of PARM_NLCG_P_*;
+ * state (parm_nlcg_get_state / parm_nlcg_set_state): nsys x PARM_NLCG_NSTATE
+ * doubles in the order of PARM_NLCG_S_* (the reference's public members).
+ * parm_nlcg_init starts every system with all state variables 0 (the
+ * constructors); parm_nlcg_set_params changes parameters only (set_max_alpha,
+ * set_max_dx, ... and P0, dt, kappa without the reset the reference's setters
+ * add: call parm_nlcg_reset for that).  The directions live in the atoms' v
+ * and a fields, as in the reference.  Mixed-precision handles switch to the
+ * per-atom gather kernel (parm_set_threads_per_atom(101)).  Sums over atoms
+ * and pairs are parallel: the scalars agree with the reference to rounding. */
+#define PARM_NLCG_NPARAM 11
+#define PARM_NLCG_P_DT 0
+#define PARM_NLCG_P_P0 1
+#define PARM_NLCG_P_KAPPA 2
+#define PARM_NLCG_P_KMAX 3
+#define PARM_NLCG_P_SECMAX 4
+#define PARM_NLCG_P_SECEPS 5
+#define PARM_NLCG_P_ALPHAMAX 6
+#define PARM_NLCG_P_AFRAC 7
+#define PARM_NLCG_P_DXMAX 8
+#define PARM_NLCG_P_STEPMAX 9
+#define PARM_NLCG_P_MAXDV 10
+#define PARM_NLCG_NSTATE 11
+#define PARM_NLCG_S_KNEW 0
+#define PARM_NLCG_S_K 1
+#define PARM_NLCG_S_VL 2
+#define PARM_NLCG_S_FL 3
+#define PARM_NLCG_S_AL 4
+#define PARM_NLCG_S_ALPHA 5
+#define PARM_NLCG_S_BETA 6
+#define PARM_NLCG_S_BETAUSED 7
+#define PARM_NLCG_S_DXSUM 8
+#define PARM_NLCG_S_ALPHAVMAX 9
+#define PARM_NLCG_S_SEC 10
+int parm_nlcg_init(parm_system* s, int boxed, const double* params);
+int parm_nlcg_set_params(parm_system* s, const double* params);
+int parm_nlcg_get_state(parm_system* s, double* state);
+int parm_nlcg_set_state(parm_system* s, const double* state);
+/* CollectionNLCG::set_forces(constraints_and_a, true) (collection.cpp:534-566);
+ * for CollectionNLCGV, Collection::set_forces (collection.cpp:159-179). */
+int parm_nlcg_set_forces(parm_system* s, int constraints_and_a);
+/* reset() (collection.cpp:525-532, 977-988), descend() (811-829, 990-1005),
+ * `nsteps` calls of timestep() (682-809, 1019-1168). */
+int parm_nlcg_reset(parm_system* s);
+int parm_nlcg_descend(parm_system* s);
+int parm_nlcg_timestep(parm_system* s, uint32_t nsteps);
+/* Current box side lengths, nsys*ndim doubles (OriginBox::box_shape, src/box.hpp:114). */
+int parm_get_boxes(parm_system* s, double* L);
+
 /* AtomGroup::kinetic_energy(origin) per system (src/box.cpp:401-411);
  * origin: nsys*ndim doubles or NULL. */
 int parm_kinetic_energy(parm_system* s, const double* origin, double* out);

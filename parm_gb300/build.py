@@ -41,6 +41,7 @@ CUDA_UNITS = {
     "staged.cu": [],
     "capi.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "nlcg.cu": ["-fmad=false"],
 }
 HOST_UNITS = ["parm_host.cpp"]
 # the host API is built once per dimension, like the reference (-DVEC3D / -DVEC2D)

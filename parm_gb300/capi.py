@@ -35,6 +35,10 @@ RSQ_XYZ2, RSQ_XYZ4, RSQ_R2, RSQ_R4, RSQ_COUNTS = range(5)
 
 NOT_MEMBER = 0xFFFFFFFF
 
+# conjugate-gradient minimisers: parameter and state vectors (PARM_NLCG_P_* / PARM_NLCG_S_*)
+NLCG_PARAMS = ("dt", "P0", "kappa", "kmax", "secmax", "seceps", "alphamax", "afrac", "dxmax", "stepmax", "maxdV")
+NLCG_STATE = ("Knew", "k", "vl", "fl", "al", "alpha", "beta", "betaused", "dxsum", "alphavmax", "sec")
+
 _u32p = C.POINTER(C.c_uint32)
 _u64p = C.POINTER(C.c_uint64)
 _dp = C.POINTER(C.c_double)
@@ -88,6 +92,15 @@ SIGNATURES = {
     "parm_host_free": (C.c_int, [C.c_void_p]),
     "parm_debug_remainder": (C.c_int, [_dp, _dp, _dp, C.c_uint32]),
     "parm_debug_philox": (C.c_int, [_u32p, _u32p, C.c_uint32]),
+    "parm_nlcg_init": (C.c_int, [_h, C.c_int, _dp]),
+    "parm_nlcg_set_params": (C.c_int, [_h, _dp]),
+    "parm_nlcg_get_state": (C.c_int, [_h, _dp]),
+    "parm_nlcg_set_state": (C.c_int, [_h, _dp]),
+    "parm_nlcg_set_forces": (C.c_int, [_h, C.c_int]),
+    "parm_nlcg_reset": (C.c_int, [_h]),
+    "parm_nlcg_descend": (C.c_int, [_h]),
+    "parm_nlcg_timestep": (C.c_int, [_h, C.c_uint32]),
+    "parm_get_boxes": (C.c_int, [_h, _dp]),
     "parm_debug_normals": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, _dp]),
     "parm_kinetic_energy_noalloc": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, _dp, C.c_void_p,
                                               C.c_void_p]),

@@ -59,7 +59,7 @@ struct GraphEntry {
     uint32_t k = 0;
 };
 
-enum StepMode { SM_VERLET = 0, SM_DAMPED = 1, SM_SOL = 2 };
+enum StepMode { SM_VERLET = 0, SM_DAMPED = 1, SM_SOL = 2, SM_NLCG = 3, SM_NLCGV = 4 };
 }  // namespace
 
 namespace parm {
@@ -111,6 +111,9 @@ struct parm_system {
     // page-locked words read back on the stream: [0] status, [1] rebuild
     // chains, [2, 2 + nsys) which() before a call, [2 + nsys, 2 + 2 nsys) after
     uint32_t* hst = nullptr;
+    // conjugate-gradient minimisers (nlcg.cu): per-system state and flags
+    void* nlcg_mem = nullptr;
+    bool nlcg_boxed = true;
 
     ~parm_system() {
         clear_graphs();
@@ -122,6 +125,7 @@ struct parm_system {
         if (tab_mem) cudaFree(tab_mem);
         if (nbr16_mem) cudaFree(nbr16_mem);
         if (rsq_mem) cudaFree(rsq_mem);
+        if (nlcg_mem) cudaFree(nlcg_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
@@ -466,12 +470,12 @@ struct parm_system {
         return PARM_OK;
     }
 
-    uint32_t estimate_capacity() const {
+    uint32_t estimate_capacity(double density_factor = 1.0) const {
         double worst = 8.0;
         for (uint32_t s = 0; s < nsys; s++) {
             const SysConst& S = sys[s];
             double V = S.L[0] * S.L[1] * (nd == 3 ? S.L[2] : 1.0);
-            double rho = natoms[s] / V;
+            double rho = density_factor * natoms[s] / V;
             double rl = S.rlist_max;
             double vol = (nd == 3) ? 4.18879020478639 * rl * rl * rl : 3.14159265358979 * rl * rl;
             worst = std::max(worst, rho * vol);
@@ -720,6 +724,217 @@ struct parm_system {
         const uint32_t chains = hst[1];
         last_launches = graph_k == 0 ? launches : launches + (uint64_t)chains * chain_len();
         return maybe_restage();
+    }
+
+    // ---- conjugate-gradient minimisers (CollectionNLCG / CollectionNLCGV) ----
+    // contexts of the minimiser's kernels: the rebuild works on any grid
+    // (per-pair minimum image along single-cell axes, as boxes may shrink
+    // below three cells), the pair kernels use the per-atom lists; `cs`
+    // evaluates only the systems flagged in nlcg_step
+    void nlcg_ctx(DevCtx& cb, DevCtx& cs) const {
+        cb = c;
+        cb.any_wrap = 1;
+        cb.staged = 0;
+        cs = cb;
+        cs.active = c.nlcg_step;
+    }
+
+    // Collection::set_forces_get_pressure(false) of the flagged systems
+    // (boxed: + the virial and fl); Collection::set_forces(false) for NLCGV
+    void nlcg_forces(const DevCtx& cb, const DevCtx& cs, cudaStream_t q) {
+        if (prec == PREC_FP64) launch_force64(cs, q, FM_FORCES);
+        else launch_force32(cs, q, FM_FORCES);
+        if (!nlcg_boxed) return;
+        if (prec == PREC_FP64) launch_eval64(cs, q, EV_VIRIAL);
+        else launch_eval32(cs, q, EV_VIRIAL);
+        launch_sys_reduce(cb, q, 1);
+        launch_nlcg_ctl(cb, q, NP_FL, 0, 0);
+    }
+
+    // a conditional node (IF or WHILE on handle h) after the captured work
+    // of `q`; `emit` fills its body, captured on st2
+    template <class F>
+    int nlcg_cond_node(cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, F&& emit) {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        alignas(cudaGraphNodeParams) unsigned char cpbuf[sizeof(cudaGraphNodeParams)];
+        std::memset(cpbuf, 0, sizeof(cpbuf));
+        cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cpbuf);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = type;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+        CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CUDA_TRY(cudaStreamBeginCaptureToGraph(st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        emit(st2);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamEndCapture(st2, &body));
+        return PARM_OK;
+    }
+
+    int nlcg_new_handle(cudaGraphConditionalHandle& h) {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        return PARM_OK;
+    }
+
+    // the displacement test and, where it fires, the rebuild (update_trackers)
+    int nlcg_update_trackers(const DevCtx& cb, bool graph) {
+        launch_check(cb, st);
+        if (!graph) {
+            launch_arm(cb, st, 0, 0, 0);
+            launch_rebuild(cb, st);
+            CUDA_TRY(cudaGetLastError());
+            return PARM_OK;
+        }
+        cudaGraphConditionalHandle h;
+        TRY(nlcg_new_handle(h));
+        launch_arm(cb, st, 0, 1, (unsigned long long)h);
+        CUDA_TRY(cudaGetLastError());
+        return nlcg_cond_node(h, cudaGraphCondTypeIf, [&](cudaStream_t q) { launch_rebuild(cb, q); });
+    }
+
+    // one secant iteration (collection.cpp:716-790, 1075-1131) on stream q
+    void nlcg_secant(const DevCtx& cb, const DevCtx& cs, cudaStream_t q, int use_cond, unsigned long long h) {
+        launch_nlcg_terms(cb, q, NT_FV, c.nlcg_loop);
+        launch_sys_reduce(cb, q, 1);
+        launch_nlcg_ctl(cb, q, NP_PRE, 0, 0);
+        launch_nlcg_stepx(cb, q);
+        launch_nlcg_box(cb, q);
+        if (!nlcg_boxed) {
+            // CollectionNLCGV updates its trackers after every secant step
+            launch_check(cb, q);
+            launch_arm(cb, q, 0, 0, 0);
+            launch_rebuild(cb, q);
+        }
+        nlcg_forces(cb, cs, q);
+        launch_nlcg_ctl(cb, q, NP_POST, use_cond, h);
+    }
+
+    // CollectionNLCG::timestep / CollectionNLCGV::timestep for every active system
+    int nlcg_emit_step(bool graph, uint32_t max_sec) {
+        DevCtx cb, cs;
+        nlcg_ctx(cb, cs);
+        launch_nlcg_ctl(cb, st, NP_BEGIN, 0, 0);
+        launch_nlcg_stepx(cb, st);
+        launch_nlcg_box(cb, st);
+        nlcg_forces(cb, cs, st);
+        launch_nlcg_terms(cb, st, NT_FV, c.nlcg_step);
+        launch_sys_reduce(cb, st, 1);
+        launch_nlcg_ctl(cb, st, NP_ETA0, 0, 0);
+        launch_nlcg_stepx(cb, st);
+        launch_nlcg_box(cb, st);
+        TRY(nlcg_update_trackers(cb, graph));
+        nlcg_forces(cb, cs, st);
+        launch_nlcg_terms(cb, st, NT_VV, c.nlcg_step);
+        launch_sys_reduce(cb, st, 1);
+        CUDA_TRY(cudaGetLastError());
+        if (graph) {
+            cudaGraphConditionalHandle h;
+            TRY(nlcg_new_handle(h));
+            launch_nlcg_ctl(cb, st, NP_LOOPINIT, 1, (unsigned long long)h);
+            CUDA_TRY(cudaGetLastError());
+            TRY(nlcg_cond_node(h, cudaGraphCondTypeWhile,
+                               [&](cudaStream_t q) { nlcg_secant(cb, cs, q, 1, (unsigned long long)h); }));
+        } else {
+            launch_nlcg_ctl(cb, st, NP_LOOPINIT, 0, 0);
+            for (uint32_t it = 0; it <= 2 * max_sec + 2; it++) {
+                CUDA_TRY(cudaMemcpyAsync(hst, c.nlcg_any, 4, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                if (!hst[0]) break;
+                nlcg_secant(cb, cs, st, 0, 0);
+                CUDA_TRY(cudaGetLastError());
+            }
+        }
+        launch_nlcg_terms(cb, st, NT_FA_FF, c.active);
+        launch_sys_reduce(cb, st, 2);
+        launch_nlcg_ctl(cb, st, NP_FINISH, 0, 0);
+        launch_nlcg_atoms(cb, st, NA_FINISH);
+        CUDA_TRY(cudaGetLastError());
+        return PARM_OK;
+    }
+
+    // the boxes after minimiser calls (the device rescales them)
+    int nlcg_sync_boxes() {
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaMemcpy(sys.data(), c.sys, sizeof(SysConst) * nsys, cudaMemcpyDeviceToHost));
+        c.any_wrap = 0;
+        for (uint32_t s = 0; s < nsys; s++)
+            for (int d = 0; d < nd; d++) {
+                L[(size_t)s * nd + d] = sys[s].L[d];
+                if (sys[s].nc[d] < 3) c.any_wrap = 1;
+            }
+        return PARM_OK;
+    }
+
+    // before a minimiser call: pending tests resolved, list capacity for a
+    // denser box than the current one (minimisation compresses)
+    int nlcg_prepare() {
+        if (!c.nlcg) return fail(PARM_ERR_RUNTIME, "parm_nlcg_init has not been called on this handle");
+        if (kind < 0) return fail(PARM_ERR_RUNTIME, "no interaction installed");
+        TRY(flush());
+        uint32_t need = estimate_capacity(1.5);
+        if (need > c.maxnb) TRY(set_capacity(need));
+        return PARM_OK;
+    }
+
+    int nlcg_run(uint32_t nsteps) {
+        TRY(nlcg_prepare());
+        std::vector<double> hp((size_t)nsys * (sizeof(NlcgSys) / 8));
+        uint32_t max_sec = 0;
+        CUDA_TRY(cudaMemcpy(hp.data(), c.nlcg, sizeof(NlcgSys) * nsys, cudaMemcpyDeviceToHost));
+        for (uint32_t s = 0; s < nsys; s++)
+            max_sec = std::max(max_sec, (uint32_t)std::min(1e6, hp[(size_t)s * (sizeof(NlcgSys) / 8) + 4]));
+        uint64_t launches = 0;
+        const int mode = nlcg_boxed ? SM_NLCG : SM_NLCGV;
+        if (graph_k == 0) {
+            for (uint32_t k = 0; k < nsteps; k++) TRY(nlcg_emit_step(false, max_sec));
+        } else {
+            uint32_t done = 0;
+            while (done < nsteps) {
+                const uint32_t k = std::min(graph_k, nsteps - done);
+                const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)k << 1);
+                auto it = graphs.find(key);
+                if (it == graphs.end()) {
+                    GraphEntry ge;
+                    ge.k = k;
+                    int r = PARM_OK;
+                    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+                    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+                    for (uint32_t q = 0; q < k && r == PARM_OK; q++) r = nlcg_emit_step(true, max_sec);
+                    cudaGraph_t g = nullptr;
+                    e = cudaStreamEndCapture(st, &g);
+                    if (r != PARM_OK) {
+                        if (g) cudaGraphDestroy(g);
+                        return r;
+                    }
+                    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+                    ge.graph = g;
+                    e = cudaGraphInstantiate(&ge.exec, ge.graph, 0);
+                    if (e != cudaSuccess) {
+                        cudaGraphDestroy(g);
+                        return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+                    }
+                    it = graphs.emplace(key, ge).first;
+                }
+                CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
+                launches += 1;
+                done += k;
+            }
+        }
+        last_launches = launches;
+        TRY(sync_status());
+        return nlcg_sync_boxes();
     }
 
     // kernels in one rebuild chain (launch_rebuild)
@@ -1770,6 +1985,175 @@ int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t
     cudaError_t e = cudaMemcpy(out, buf + 2 * (size_t)n, 8 * (size_t)n, cudaMemcpyDeviceToHost);
     cudaFree(buf);
     if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+    return PARM_OK;
+}
+
+// ---- conjugate-gradient minimisers ----
+static constexpr int kNlcgWords = (int)(sizeof(NlcgSys) / 8);
+
+static int nlcg_read(parm_system* S, std::vector<double>& hp) {
+    hp.assign((size_t)S->nsys * kNlcgWords, 0.0);
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    CUDA_TRY(cudaMemcpy(hp.data(), S->c.nlcg, sizeof(NlcgSys) * S->nsys, cudaMemcpyDeviceToHost));
+    return PARM_OK;
+}
+
+static int nlcg_write(parm_system* S, const std::vector<double>& hp) {
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    CUDA_TRY(cudaMemcpy(S->c.nlcg, hp.data(), sizeof(NlcgSys) * S->nsys, cudaMemcpyHostToDevice));
+    return PARM_OK;
+}
+
+static int nlcg_check_params(const double* p, bool boxed) {
+    if (!(p[0] == p[0]) || !(p[3] == p[3]) || !(p[4] >= 0.0 && p[4] <= 1e6) || p[4] != std::floor(p[4]))
+        return fail(PARM_ERR_ARG, "minimiser parameters: dt and kmax must be numbers, secmax an integer "
+                                  "in [0, 1e6]");
+    if (boxed && !(p[2] > 0.0)) return fail(PARM_ERR_ARG, "CollectionNLCG: kappa must be > 0");
+    return PARM_OK;
+}
+
+int parm_nlcg_init(parm_system* S, int boxed, const double* params) {
+    if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
+    for (uint32_t s = 0; s < S->nsys; s++) TRY(nlcg_check_params(params + (size_t)s * PARM_NLCG_NPARAM, boxed != 0));
+    if (S->prec == PREC_MIXED && (S->c.staged || S->c.tiled || S->want_staged))
+        TRY(parm_set_threads_per_atom(S, 101));   // the minimiser uses the per-atom lists
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    if (!S->nlcg_mem) {
+        const size_t bytes = sizeof(NlcgSys) * (size_t)S->nsys + 8 * (size_t)S->nsys + 16;
+        CUDA_TRY(cudaMalloc(&S->nlcg_mem, bytes));
+        CUDA_TRY(cudaMemset(S->nlcg_mem, 0, bytes));
+        char* b = static_cast<char*>(S->nlcg_mem);
+        S->c.nlcg = reinterpret_cast<NlcgSys*>(b);
+        S->c.nlcg_step = reinterpret_cast<uint32_t*>(b + sizeof(NlcgSys) * (size_t)S->nsys);
+        S->c.nlcg_loop = S->c.nlcg_step + S->nsys;
+        S->c.nlcg_any = S->c.nlcg_loop + S->nsys;
+    }
+    // a fresh minimiser: the parameters given, every state variable 0
+    // (the reference constructors' initialiser lists)
+    std::vector<double> hp((size_t)S->nsys * kNlcgWords, 0.0);
+    for (uint32_t s = 0; s < S->nsys; s++)
+        for (int q = 0; q < PARM_NLCG_NPARAM; q++)
+            hp[(size_t)s * kNlcgWords + q] = params[(size_t)s * PARM_NLCG_NPARAM + q];
+    TRY(nlcg_write(S, hp));
+    S->nlcg_boxed = boxed != 0;
+    S->c.nlcg_boxed = boxed ? 1u : 0u;
+    S->clear_graphs();
+    return PARM_OK;
+}
+
+int parm_nlcg_set_params(parm_system* S, const double* params) {
+    if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
+    if (!S->c.nlcg) return fail(PARM_ERR_RUNTIME, "parm_nlcg_init has not been called on this handle");
+    for (uint32_t s = 0; s < S->nsys; s++)
+        TRY(nlcg_check_params(params + (size_t)s * PARM_NLCG_NPARAM, S->nlcg_boxed));
+    std::vector<double> hp;
+    TRY(nlcg_read(S, hp));
+    for (uint32_t s = 0; s < S->nsys; s++)
+        for (int q = 0; q < PARM_NLCG_NPARAM; q++)
+            hp[(size_t)s * kNlcgWords + q] = params[(size_t)s * PARM_NLCG_NPARAM + q];
+    return nlcg_write(S, hp);
+}
+
+int parm_nlcg_get_state(parm_system* S, double* state) {
+    if (!S || !state) return fail(PARM_ERR_ARG, "NULL argument");
+    if (!S->c.nlcg) return fail(PARM_ERR_RUNTIME, "parm_nlcg_init has not been called on this handle");
+    std::vector<double> hp;
+    TRY(nlcg_read(S, hp));
+    for (uint32_t s = 0; s < S->nsys; s++)
+        for (int q = 0; q < PARM_NLCG_NSTATE; q++)
+            state[(size_t)s * PARM_NLCG_NSTATE + q] = hp[(size_t)s * kNlcgWords + PARM_NLCG_NPARAM + q];
+    return PARM_OK;
+}
+
+int parm_nlcg_set_state(parm_system* S, const double* state) {
+    if (!S || !state) return fail(PARM_ERR_ARG, "NULL argument");
+    if (!S->c.nlcg) return fail(PARM_ERR_RUNTIME, "parm_nlcg_init has not been called on this handle");
+    std::vector<double> hp;
+    TRY(nlcg_read(S, hp));
+    for (uint32_t s = 0; s < S->nsys; s++)
+        for (int q = 0; q < PARM_NLCG_NSTATE; q++)
+            hp[(size_t)s * kNlcgWords + PARM_NLCG_NPARAM + q] = state[(size_t)s * PARM_NLCG_NSTATE + q];
+    return nlcg_write(S, hp);
+}
+
+// CollectionNLCG::set_forces(constraints_and_a, true) (src/collection.cpp:534-566);
+// CollectionNLCGV: Collection::set_forces (src/collection.cpp:159-179)
+static int nlcg_set_forces_impl(parm_system* S, bool c_and_a) {
+    DevCtx cb, cs;
+    S->nlcg_ctx(cb, cs);
+    if (!S->nlcg_boxed) {
+        const int mode = c_and_a ? FM_FORCES_A : FM_FORCES;
+        if (S->prec == PREC_FP64) launch_force64(cb, S->st, mode);
+        else launch_force32(cb, S->st, mode);
+        CUDA_TRY(cudaGetLastError());
+        return PARM_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(S->c.nlcg_step, S->c.active, 4 * (size_t)S->nsys, cudaMemcpyDeviceToDevice, S->st));
+    S->nlcg_forces(cb, cs, S->st);
+    launch_nlcg_atoms(cb, S->st, NA_IMMOBILE_A);
+    if (c_and_a) {
+        launch_nlcg_atoms(cb, S->st, NA_SETF);
+        launch_nlcg_terms(cb, S->st, NT_FA_FF, S->c.active);
+        launch_sys_reduce(cb, S->st, 2);
+        launch_nlcg_ctl(cb, S->st, NP_SETF, 0, 0);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return PARM_OK;
+}
+
+int parm_nlcg_set_forces(parm_system* S, int constraints_and_a) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->nlcg_prepare());
+    TRY(nlcg_set_forces_impl(S, constraints_and_a != 0));
+    return S->sync_status();
+}
+
+int parm_nlcg_reset(parm_system* S) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->nlcg_prepare());
+    DevCtx cb, cs;
+    S->nlcg_ctx(cb, cs);
+    if (S->nlcg_boxed) {
+        // CollectionNLCG::reset (collection.cpp:525-532)
+        TRY(nlcg_set_forces_impl(S, true));
+        launch_nlcg_atoms(cb, S->st, NA_RESET);
+        launch_nlcg_ctl(cb, S->st, NP_RESET, 0, 0);
+    } else {
+        // CollectionNLCGV::reset (collection.cpp:977-988)
+        launch_nlcg_ctl(cb, S->st, NP_RESET, 0, 0);
+        TRY(nlcg_set_forces_impl(S, false));
+        launch_nlcg_atoms(cb, S->st, NA_DESCEND);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return S->sync_status();
+}
+
+int parm_nlcg_descend(parm_system* S) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    TRY(S->nlcg_prepare());
+    DevCtx cb, cs;
+    S->nlcg_ctx(cb, cs);
+    // descend (collection.cpp:811-829, 990-1005): forces, v = a = f, stepx(dt), trackers
+    TRY(nlcg_set_forces_impl(S, false));
+    launch_nlcg_atoms(cb, S->st, NA_DESCEND);
+    launch_nlcg_ctl(cb, S->st, NP_DESCEND, 0, 0);
+    launch_nlcg_stepx(cb, S->st);
+    launch_nlcg_box(cb, S->st);
+    TRY(S->nlcg_update_trackers(cb, false));
+    TRY(S->sync_status());
+    return S->nlcg_sync_boxes();
+}
+
+int parm_nlcg_timestep(parm_system* S, uint32_t nsteps) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (nsteps == 0) return PARM_OK;
+    return S->nlcg_run(nsteps);
+}
+
+int parm_get_boxes(parm_system* S, double* L) {
+    if (!S || !L) return fail(PARM_ERR_ARG, "NULL argument");
+    std::copy(S->L.begin(), S->L.end(), L);
     return PARM_OK;
 }
 

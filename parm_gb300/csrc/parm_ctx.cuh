@@ -33,6 +33,17 @@ struct StepParams {
     unsigned long long step;   // Langevin counter, advanced once per step
 };
 
+// Per-system state of the conjugate-gradient minimisers CollectionNLCG /
+// CollectionNLCGV (nlcg.cu).  The first 11 doubles are the C ABI's parameter
+// vector, the next 11 its state vector (include/parm_gb300.h).
+struct NlcgSys {
+    double dt, P0, kappa, kmax, secmax, seceps, alphamax, afrac, dxmax, stepmax, maxdV;
+    double Knew, k, vl, fl, al, alpha, beta, betaused, dxsum, alphavmax, sec;
+    // within a time step
+    double eta, eta0, vdv, dx, lfac;
+    double iters;   // secant iterations of this time step (a bound on the loop besides sec)
+};
+
 struct DevCtx {
     int nd;
     int prec;
@@ -135,6 +146,13 @@ struct DevCtx {
     uint32_t* chains;     // rebuild-chain executions (for launch accounting)
     StepParams* params;
 
+    // conjugate-gradient minimisers (nlcg.cu)
+    NlcgSys* nlcg;        // per system, or null before parm_nlcg_init
+    uint32_t* nlcg_step;  // per system: moves in the current stepx (and is evaluated after it)
+    uint32_t* nlcg_loop;  // per system: still in its secant loop
+    uint32_t* nlcg_any;   // [0]: some system is still in its secant loop
+    uint32_t nlcg_boxed;  // CollectionNLCG (box scaled with kappa) rather than CollectionNLCGV
+
     // reduction scratch
     // mean-square-displacement tracker (RsqTracker); rsq_n == 0: none
     uint32_t rsq_n;                      // time windows
@@ -183,6 +201,32 @@ void launch_force64(const DevCtx& c, cudaStream_t s, int mode);
 void launch_force32(const DevCtx& c, cudaStream_t s, int mode);
 void launch_eval64(const DevCtx& c, cudaStream_t s, int what);
 void launch_eval32(const DevCtx& c, cudaStream_t s, int what);
+// nlcg.cu (conjugate-gradient minimisers)
+enum NlcgPhase : int {
+    NP_BEGIN = 0,     // stepx(dt) of a time step
+    NP_FL = 1,        // fl from the virial in sysout (boxed)
+    NP_ETA0 = 2,      // eta0 = -fdotv; stepx(-dt) next
+    NP_LOOPINIT = 3,  // vdv = vdotv; secant loop starts
+    NP_PRE = 4,       // secant iteration before its step
+    NP_POST = 5,      // secant iteration after its step
+    NP_FINISH = 6,    // Polak-Ribiere update of the direction's scalars
+    NP_SETF = 7,      // end of set_forces(true, true): al = vl = fl, Knew
+    NP_RESET = 8,     // end of reset(): vl = al, k = 0
+    NP_DESCEND = 9,   // descend(): al = vl = fl (boxed), stepx(dt) next
+};
+enum NlcgTerms : int { NT_FV = 0, NT_VV = 1, NT_FA_FF = 2 };
+enum NlcgAtoms : int {
+    NA_FINISH = 0,    // a = f, v = a + v betaused
+    NA_SETF = 1,      // set_forces(true): a = v = f (mobile), 0 otherwise
+    NA_RESET = 2,     // reset(): v = a (every atom)
+    NA_DESCEND = 3,   // descend(): v = a = f (mobile)
+    NA_IMMOBILE_A = 4 // immobile atoms: a = 0 (Collection::set_forces_get_pressure)
+};
+void launch_nlcg_stepx(const DevCtx& c, cudaStream_t s);
+void launch_nlcg_box(const DevCtx& c, cudaStream_t s);
+void launch_nlcg_ctl(const DevCtx& c, cudaStream_t s, int phase, int use_cond, unsigned long long handle);
+void launch_nlcg_terms(const DevCtx& c, cudaStream_t s, int what, const uint32_t* mask);
+void launch_nlcg_atoms(const DevCtx& c, cudaStream_t s, int what);
 // staged.cu (mixed path, cell blocks)
 void launch_build_stg(const DevCtx& c, cudaStream_t s);
 void launch_force_stg(const DevCtx& c, cudaStream_t s, int mode);

@@ -124,4 +124,95 @@ class CollectionSol : public Collection {
     void set_temperature(flt T) { desT = T; }
 };
 
+//! Conjugate-gradient energy minimisation of positions and the box's
+//! log-volume, H = U + P0 V (src/collection.hpp:400-475,
+//! src/collection.cpp:494-829), run on the GPU (parm_nlcg_*): each time step
+//! (the secant line search included) is one GPU call.  The public members
+//! are the reference's; they are sent to the GPU before and read back after
+//! every call, so code that reads or sets them behaves as with the
+//! reference.  The box (an OriginBox) is rescaled on the GPU and copied back.
+//! Trackers other than the neighbour list are updated after each time step.
+class CollectionNLCG : public Collection {
+   public:
+    flt dt;
+    flt seceps;
+    uint secmax;
+    flt kappa;
+    flt alphamax, afrac, dxmax, stepmax, kmax;
+    flt P0;
+    flt Knew;
+    flt k;
+    flt vl, fl, al;
+    flt alpha, beta, betaused, dxsum, alphavmax, maxdV;
+    uint sec;
+
+    CollectionNLCG(sptr<OriginBox> box, sptr<AtomVec> atoms, const flt dt, const flt P0,
+                   std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+                   std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+                   std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>(), const flt kappa = 10.0,
+                   const flt kmax = 1000, const uint secmax = 40, const flt seceps = 1e-20);
+
+    //! host sums over the Atom records, as the reference defines them
+    flt get_length_squared();
+    flt fdota();
+    flt fdotf();
+    flt fdotv();
+    flt vdotv();
+    flt kinetic_energy() override;   // masses ignored
+    flt pressure() override;
+    flt hamiltonian();
+    void set_forces(bool constraints_and_a = true) override { set_forces(constraints_and_a, true); }
+    void set_forces(bool constraints_and_a, bool setV);
+
+    void timestep() override { timesteps(1); }
+    void timesteps(uint n) override;
+    void descend();
+    void reset();
+
+    void set_dt(flt newdt) {
+        dt = newdt;
+        reset();
+    }
+    void set_pressure_goal(flt P) {
+        P0 = P;
+        reset();
+    }
+    flt get_pressure_goal() { return P0; }
+    void set_kappa(flt kk) {
+        kappa = kk;
+        reset();
+    }
+    void set_max_alpha(flt a) { alphamax = a; }
+    void set_max_alpha_fraction(flt a) { afrac = a; }
+    void set_max_dx(flt d) { dxmax = d; }
+    void set_max_step(flt m) { stepmax = m; }
+
+   protected:
+    bool boxed = true;
+    parm_system* inited = nullptr;   // the handle the GPU minimiser was set up on
+    //! push the Atom records, the box and this object's members to the GPU
+    GpuLink& gpu_push();
+    //! read members, Atom records and the box back
+    void gpu_pull(GpuLink& g);
+    void gpu_params(double* p) const;
+};
+
+//! Conjugate-gradient energy minimisation of positions in a fixed box
+//! (src/collection.hpp:490-566, src/collection.cpp:877-1168), on the GPU.
+class CollectionNLCGV : public CollectionNLCG {
+   public:
+    CollectionNLCGV(sptr<Box> box, sptr<AtomVec> atoms, const flt dt,
+                    std::vector<sptr<Interaction>> is = std::vector<sptr<Interaction>>(),
+                    std::vector<sptr<StateTracker>> ts = std::vector<sptr<StateTracker>>(),
+                    std::vector<sptr<Constraint>> cs = std::vector<sptr<Constraint>>(), const flt kmax = 1000,
+                    const uint secmax = 10, const flt seceps = 1e-4);
+    flt kinetic_energy() override { return atoms->kinetic_energy(); }
+    flt pressure() override;
+    void set_forces(bool constraints_and_a = true) override { Collection::set_forces(constraints_and_a); }
+    void set_dt(flt newdt) {
+        dt = newdt;
+        reset();
+    }
+};
+
 #endif

@@ -162,6 +162,16 @@ void GpuLink::pull() {
                     "parm_get_atoms");
 }
 
+void GpuLink::sync_box() {
+    std::vector<double> Lg(NDIM);
+    parm_host_check(parm_get_boxes(h, Lg.data()), "parm_get_boxes");
+    OriginBox& ob = *std::dynamic_pointer_cast<OriginBox>(bx);
+    Vec v;
+    for (int d = 0; d < NDIM; d++) v[d] = Lg[d];
+    ob.resize_to(v);
+    lastbox = Lg;
+}
+
 // ---------------------------------------------------------------------------
 // NeighborList
 NeighborList::NeighborList(sptr<Box> box, sptr<AtomVec> atoms, const flt skin)
@@ -534,4 +544,206 @@ void CollectionSol::timesteps(uint n) {
     run_steps(n, [this](uint k) {
         parm_host_check(parm_sol(gpu().handle(), dt, damping, desT, key, k), "parm_sol");
     });
+}
+
+// ---------------------------------------------------------------------------
+// CollectionNLCG / CollectionNLCGV (src/collection.cpp:494-1168)
+CollectionNLCG::CollectionNLCG(sptr<OriginBox> box, sptr<AtomVec> atoms, const flt dt, const flt P0,
+                               std::vector<sptr<Interaction>> is, std::vector<sptr<StateTracker>> ts,
+                               std::vector<sptr<Constraint>> cs, const flt kappa, const flt kmax, const uint secmax,
+                               const flt seceps)
+    : Collection(box, atoms, is, ts, cs),
+      dt(dt),
+      seceps(seceps),
+      secmax(secmax),
+      kappa(kappa),
+      alphamax(2.0),
+      afrac(0),
+      dxmax(100),
+      stepmax(1e-3),
+      kmax(kmax),
+      P0(P0),
+      Knew(0),
+      k(0),
+      vl(0),
+      fl(0),
+      al(0),
+      alpha(0),
+      beta(0),
+      betaused(0),
+      dxsum(0),
+      alphavmax(0),
+      maxdV(0),
+      sec(0) {}
+
+static sptr<OriginBox> origin_box(sptr<Box> b) {
+    sptr<OriginBox> ob = std::dynamic_pointer_cast<OriginBox>(b);
+    if (!ob) throw std::invalid_argument("parm_gb300: the GPU minimisers need a periodic OriginBox");
+    return ob;
+}
+
+CollectionNLCGV::CollectionNLCGV(sptr<Box> box, sptr<AtomVec> atoms, const flt dt, std::vector<sptr<Interaction>> is,
+                                 std::vector<sptr<StateTracker>> ts, std::vector<sptr<Constraint>> cs, const flt kmax,
+                                 const uint secmax, const flt seceps)
+    : CollectionNLCG(origin_box(box), atoms, dt, 0.0, is, ts, cs, 10.0, kmax, secmax, seceps) {
+    boxed = false;
+    alphamax = 0;
+    afrac = 0;
+    dxmax = 0;
+    stepmax = 0;
+}
+
+void CollectionNLCG::gpu_params(double* p) const {
+    const double v[PARM_NLCG_NPARAM] = {dt, P0, kappa, kmax, (double)secmax, seceps, alphamax, afrac,
+                                        dxmax, stepmax, maxdV};
+    for (int q = 0; q < PARM_NLCG_NPARAM; q++) p[q] = v[q];
+}
+
+GpuLink& CollectionNLCG::gpu_push() {
+    GpuLink& g = gpu();
+    g.push();
+    g.touch();
+    double p[PARM_NLCG_NPARAM];
+    gpu_params(p);
+    if (inited != g.handle()) {
+        parm_host_check(parm_nlcg_init(g.handle(), boxed ? 1 : 0, p), "parm_nlcg_init");
+        inited = g.handle();
+    } else {
+        parm_host_check(parm_nlcg_set_params(g.handle(), p), "parm_nlcg_set_params");
+    }
+    const double st[PARM_NLCG_NSTATE] = {Knew, k, vl, fl, al, alpha, beta, betaused, dxsum, alphavmax, (double)sec};
+    parm_host_check(parm_nlcg_set_state(g.handle(), st), "parm_nlcg_set_state");
+    return g;
+}
+
+void CollectionNLCG::gpu_pull(GpuLink& g) {
+    double st[PARM_NLCG_NSTATE];
+    parm_host_check(parm_nlcg_get_state(g.handle(), st), "parm_nlcg_get_state");
+    Knew = st[PARM_NLCG_S_KNEW];
+    k = st[PARM_NLCG_S_K];
+    vl = st[PARM_NLCG_S_VL];
+    fl = st[PARM_NLCG_S_FL];
+    al = st[PARM_NLCG_S_AL];
+    alpha = st[PARM_NLCG_S_ALPHA];
+    beta = st[PARM_NLCG_S_BETA];
+    betaused = st[PARM_NLCG_S_BETAUSED];
+    dxsum = st[PARM_NLCG_S_DXSUM];
+    alphavmax = st[PARM_NLCG_S_ALPHAVMAX];
+    sec = (uint)st[PARM_NLCG_S_SEC];
+    g.pull();
+    if (boxed) g.sync_box();
+}
+
+flt CollectionNLCG::get_length_squared() {
+    if (!boxed) return 1.0;
+#ifdef VEC2D
+    return box->V();
+#else
+    return std::pow(box->V(), 2.0 / 3.0);
+#endif
+}
+
+// the four sums of src/collection.cpp:651-705 (boxed) and 910-975 (fixed box)
+static flt mobile_sum(AtomVec& av, Vec Atom::*p, Vec Atom::*q) {
+    flt r = 0;
+    for (uint i = 0; i < av.size(); i++) {
+        Atom& a = av[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        r += (a.*p).dot(a.*q);
+    }
+    return r;
+}
+flt CollectionNLCG::fdota() {
+    const flt r = mobile_sum(*atoms, &Atom::f, &Atom::a);
+    return boxed ? r / get_length_squared() + fl * al : r;
+}
+flt CollectionNLCG::fdotf() {
+    const flt r = mobile_sum(*atoms, &Atom::f, &Atom::f);
+    return boxed ? r / get_length_squared() + fl * fl : r;
+}
+flt CollectionNLCG::fdotv() {
+    const flt r = mobile_sum(*atoms, &Atom::f, &Atom::v);
+    return boxed ? r / get_length_squared() + fl * vl : r;
+}
+flt CollectionNLCG::vdotv() {
+    const flt r = mobile_sum(*atoms, &Atom::v, &Atom::v);
+    return boxed ? r / get_length_squared() + vl * vl : r;
+}
+
+// CollectionNLCG::kinetic_energy (collection.cpp:572-587): masses ignored
+flt CollectionNLCG::kinetic_energy() {
+    flt E = 0;
+    const flt Lfac = std::exp(vl / (kappa * NDIM));
+    for (uint i = 0; i < atoms->size(); i++) {
+        Atom& a = (*atoms)[i];
+        if (a.m <= 0 || std::isinf(a.m)) continue;
+        const Vec v = a.v + (a.x * Lfac);
+        E += v.squaredNorm();
+    }
+    return E / 2.0;
+}
+
+// CollectionNLCG::pressure (collection.cpp:589-599), CollectionNLCGV::pressure (1007-1017)
+flt CollectionNLCG::pressure() {
+    const flt V = box->V();
+    flt E = 0;
+    for (auto& it : interactions) E += it->pressure(*box);
+    return E / V / flt(NDIM);
+}
+flt CollectionNLCGV::pressure() { return CollectionNLCG::pressure(); }
+
+flt CollectionNLCG::hamiltonian() { return potential_energy() + P0 * (box->V()); }
+
+void CollectionNLCG::set_forces(bool constraints_and_a, bool setV) {
+    if (!setV || !link || interactions.empty()) {
+        // Collection::set_forces(false) and, when asked, the direction reset
+        // of collection.cpp:553-564 on the Atom records
+        Collection::set_forces(false);
+        if (!constraints_and_a) return;
+        for (uint i = 0; i < atoms->size(); i++) {
+            Atom& a = (*atoms)[i];
+            if (a.m <= 0 || std::isinf(a.m)) {
+                a.v = Vec::Zero();
+                a.a = Vec::Zero();
+                continue;
+            }
+            a.a = a.f;
+            a.v = a.f;
+        }
+        Knew = fdota();
+        return;
+    }
+    GpuLink& g = gpu_push();
+    parm_host_check(parm_nlcg_set_forces(g.handle(), constraints_and_a ? 1 : 0), "parm_nlcg_set_forces");
+    gpu_pull(g);
+}
+
+void CollectionNLCG::reset() {
+    GpuLink& g = gpu_push();
+    parm_host_check(parm_nlcg_reset(g.handle()), "parm_nlcg_reset");
+    gpu_pull(g);
+}
+
+void CollectionNLCG::descend() {
+    GpuLink& g = gpu_push();
+    parm_host_check(parm_nlcg_descend(g.handle()), "parm_nlcg_descend");
+    gpu_pull(g);
+    for (auto& t : trackers)
+        if (!std::dynamic_pointer_cast<NeighborList>(t)) t->update(*box);
+}
+
+void CollectionNLCG::timesteps(uint n) {
+    if (!n) return;
+    GpuLink& g = gpu_push();
+    if (!has_step_trackers()) {
+        parm_host_check(parm_nlcg_timestep(g.handle(), n), "parm_nlcg_timestep");
+        gpu_pull(g);
+        return;
+    }
+    for (uint q = 0; q < n; q++) {
+        parm_host_check(parm_nlcg_timestep(g.handle(), 1), "parm_nlcg_timestep");
+        gpu_pull(g);
+        for (auto& t : trackers)
+            if (!std::dynamic_pointer_cast<NeighborList>(t)) t->update(*box);
+    }
 }

@@ -39,6 +39,8 @@ class GpuLink {
     void push();
     //! download the Atom records
     void pull();
+    //! copy the GPU's box (rescaled by a minimiser) into the host OriginBox
+    void sync_box();
     parm_system* handle() { return h; }
     sptr<Box> box() { return bx; }
     sptr<AtomVec> atoms() { return atomv; }

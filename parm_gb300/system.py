@@ -212,6 +212,43 @@ class System:
     def sol(self, dt: float, damping: float, T: float, seed: int, nsteps: int = 1) -> None:
         check(self.lib.parm_sol(self.h, float(dt), float(damping), float(T), int(seed), int(nsteps)))
 
+    # -- conjugate-gradient minimisers (CollectionNLCG / CollectionNLCGV) --
+    def nlcg_init(self, params, boxed: bool = True) -> None:
+        """Start a minimiser per system; params: (11,) or (nsys, 11) in the order of capi.NLCG_PARAMS."""
+        p = _as_f64(params, (self.nsys, len(capi.NLCG_PARAMS)))
+        check(self.lib.parm_nlcg_init(self.h, 1 if boxed else 0, dptr(p)))
+
+    def nlcg_set_params(self, params) -> None:
+        p = _as_f64(params, (self.nsys, len(capi.NLCG_PARAMS)))
+        check(self.lib.parm_nlcg_set_params(self.h, dptr(p)))
+
+    def nlcg_state(self) -> np.ndarray:
+        """(nsys, 11) state in the order of capi.NLCG_STATE."""
+        out = np.zeros((self.nsys, len(capi.NLCG_STATE)))
+        check(self.lib.parm_nlcg_get_state(self.h, dptr(out)))
+        return out
+
+    def nlcg_set_state(self, state) -> None:
+        st = _as_f64(state, (self.nsys, len(capi.NLCG_STATE)))
+        check(self.lib.parm_nlcg_set_state(self.h, dptr(st)))
+
+    def nlcg_set_forces(self, constraints_and_a: bool = True) -> None:
+        check(self.lib.parm_nlcg_set_forces(self.h, 1 if constraints_and_a else 0))
+
+    def nlcg_reset(self) -> None:
+        check(self.lib.parm_nlcg_reset(self.h))
+
+    def nlcg_descend(self) -> None:
+        check(self.lib.parm_nlcg_descend(self.h))
+
+    def nlcg_timestep(self, nsteps: int = 1) -> None:
+        check(self.lib.parm_nlcg_timestep(self.h, int(nsteps)))
+
+    def boxes(self) -> np.ndarray:
+        out = np.zeros((self.nsys, self.ndim))
+        check(self.lib.parm_get_boxes(self.h, dptr(out)))
+        return out
+
     def step_counter(self) -> int:
         v = C.c_uint64()
         check(self.lib.parm_get_step(self.h, C.byref(v)))

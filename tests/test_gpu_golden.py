@@ -11,11 +11,11 @@ pressures and stresses are parallel sums, held to 1e-12 relative.
 import numpy as np
 import pytest
 
-from golden_cases import DAMPED, VERLET, load, names
+from golden_cases import DAMPED, NLCG, VERLET, load, names
 
 pytestmark = pytest.mark.gpu
 
-CASES = names()
+CASES = [n for n in names() if load(n)["integ"] < NLCG]   # the minimiser cases: test_gpu_nlcg.py
 RTOL = 1e-12
 
 

@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from golden_cases import load, names
+from golden_cases import NLCG, load, names
 from host_api import DECK_DRIVER, compile_program
 
 sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
@@ -34,6 +34,23 @@ def drivers(tmp_path_factory, built_lib):
     return out
 
 
+def _check_minimiser(got, d):
+    """CollectionNLCG / CollectionNLCGV through the host API: the same bars as the C ABI test
+    (tests/test_gpu_nlcg.py), the sums being parallel."""
+    from test_gpu_nlcg import RTOL_EARLY, RTOL_LATE, EARLY, rel_err
+    np.testing.assert_array_equal(got["pairs"], d["pairs"])
+    np.testing.assert_allclose(got["init"], d["init"], rtol=1e-12, atol=1e-13)
+    assert rel_err(got["f0"], d["f0"]) <= 1e-12
+    np.testing.assert_array_equal(got["steps"], d["steps"])
+    for i, s in enumerate(d["steps"]):
+        tol = RTOL_EARLY if s <= EARLY else RTOL_LATE
+        for key in ("x", "v", "f"):
+            err = rel_err(got[f"{key}_steps"][i], d[f"{key}_steps"][i])
+            assert err <= tol, f"{key} at step {s}: {err:.3e}"
+        assert rel_err(got["box_steps"][i], d["box_steps"][i]) <= tol
+        assert abs(got["energy_steps"][i] - d["energy_steps"][i]) <= tol * max(abs(d["energy_steps"][0]), 1e-300)
+
+
 def _close(got, want, exact, what):
     if exact:
         np.testing.assert_array_equal(got, want, err_msg=what)
@@ -46,12 +63,15 @@ def _close(got, want, exact, what):
 def test_host_api_matches_reference(drivers, name):
     d = load(name)
     case = {k: d[k] for k in ("kind", "integ", "nsteps", "dt", "damping", "T", "skin", "L", "x", "v", "m",
-                              "params", "order", "ignores", "out_steps")}
+                              "params", "order", "ignores", "out_steps", "cg") if k in d}
     deck = MG._deck(case)
     r = subprocess.run([str(drivers[d["ndim"]])], input=deck, capture_output=True, text=True, timeout=600,
                        env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
     assert r.returncode == 0, r.stderr[-2000:]
     got = MG._parse(r.stdout, d["n"], d["ndim"])
+    if d["integ"] >= NLCG:
+        _check_minimiser(got, d)
+        return
     exact = not (d["kind"] == 1 and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
     np.testing.assert_array_equal(got["pairs"], d["pairs"])
     np.testing.assert_array_equal(got["init_counts"], d["init_counts"])

@@ -14,7 +14,6 @@ import pytest
 from host_api import DECK_DRIVER, compile_program
 
 REF_SRC = Path(os.environ.get("PARM_REFERENCE_SRC", "/root/reference/src"))
-REF_LJATOMS = REF_SRC / "bin" / "LJatoms.cpp"
 
 
 @pytest.mark.parametrize("ndim", [3, 2])
@@ -24,10 +23,21 @@ def test_deck_driver_builds_against_host_api(tmp_path, built_lib, ndim):
     assert (tmp_path / f"drv{ndim}").exists()
 
 
-def test_reference_ljatoms_compiles_against_host_api(tmp_path, built_lib):
-    if not REF_LJATOMS.exists():
+@pytest.mark.parametrize("prog", ["LJatoms.cpp", "packer.cpp"])
+def test_reference_programs_build_against_host_api(tmp_path, built_lib, prog):
+    """The reference's example programs (src/bin/LJatoms.cpp: CollectionVerlet; src/bin/packer.cpp:
+    CollectionNLCG) compile and link unchanged against the host API."""
+    src = REF_SRC / "bin" / prog
+    if not src.exists():
         pytest.skip("reference sources not present")
-    r = compile_program(REF_LJATOMS, tmp_path / "lj.o", link=False)
+    r = compile_program(src, tmp_path / prog.replace(".cpp", ""))
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_packing_program_builds(tmp_path, built_lib):
+    """The CollectionNLCG packing program of the GPU tests builds against the host API."""
+    src = Path(__file__).resolve().parent / "programs" / "nlcg_packing.cpp"
+    r = compile_program(src, tmp_path / "packing")
     assert r.returncode == 0, r.stderr[-3000:]
 
 
