@@ -1,7 +1,7 @@
 // A packing program on the C++ host API's CollectionNLCG: 80 harmonic spheres
 // (40 of diameter 1.0, 40 of 1.4) placed at random in a dilute periodic box
 // are compressed by conjugate-gradient minimisation of U + P V through goal
-// pressures 1e-4 .. 1e-7; each stage runs 1000 time steps at a time until
+// pressures 1e-4, 1e-5, ..., 1e-8; each stage runs 1000 time steps at a time until
 // |P/P0 - 1| < 1e-4 and the largest force is below 1e-14.  It uses the calls
 // a packing driver of the reference makes (set_pressure_goal, timestep,
 // pressure, hamiltonian, kinetic_energy, the NeighborList as a tracker) and

@@ -22,8 +22,8 @@ pytestmark = pytest.mark.gpu
 
 CASES = [n for n in names() if load(n)["integ"] >= NLCG]
 EARLY = 10
-RTOL_EARLY = 1e-9
-RTOL_LATE = 1e-5
+RTOL_EARLY = 1e-12
+RTOL_LATE = 1e-6
 
 
 def rel_err(got, want) -> float:
@@ -166,7 +166,8 @@ def test_long_run_against_oracle():
 
 
 def test_mixed_precision_reaches_the_same_packing():
-    """The mixed path minimises a packing to the FP64 path's box and energy (relative 1e-4)."""
+    """The mixed path minimises a packing to the FP64 path's box (relative 1e-4) and energy (1e-3:
+    the two runs follow slightly different paths into the same basin)."""
     from parm_gb300 import workloads as W
     from helpers import make_gpu
     w = W.small_random(n=400, ndim=3, kind=1, seed=92, phi=0.6, skin=0.3)
@@ -184,13 +185,14 @@ def test_mixed_precision_reaches_the_same_packing():
         g.close()
     (L64, E64, F64), (L32, E32, F32) = res["fp64"], res["mixed"]
     assert abs(L32 - L64) <= 1e-4 * L64, res
-    assert abs(E32 - E64) <= 1e-4 * abs(E64) + 1e-9, res
+    assert abs(E32 - E64) <= 1e-3 * abs(E64) + 1e-9, res
 
 
 def test_packing_program_runs(tmp_path, built_lib):
     """A packing program on the host API's CollectionNLCG (tests/programs/nlcg_packing.cpp, the calls
-    the reference's src/bin/packer.cpp makes): 80 harmonic spheres compressed through four goal
-    pressures, each stage ending on |P/P0 - 1| < 1e-4 and max |F| < 1e-14 at a jammed density."""
+    the reference's src/bin/packer.cpp makes): 80 harmonic spheres compressed through five goal
+    pressures (1e-4 .. 1e-8), each stage ending on |P/P0 - 1| < 1e-4 and max |F| < 1e-14, at a
+    jammed density."""
     from pathlib import Path
     from host_api import compile_program
     src = Path(__file__).resolve().parent / "programs" / "nlcg_packing.cpp"
@@ -201,7 +203,7 @@ def test_packing_program_runs(tmp_path, built_lib):
                        env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
     assert r.returncode == 0, r.stderr[-2000:]
     stages = [line.split() for line in r.stdout.splitlines() if line.startswith("stage")]
-    assert len(stages) == 4, r.stdout[-3000:]
+    assert len(stages) == 5, r.stdout[-3000:]
     for st in stages:
         assert abs(float(st[4])) < 1e-4 and float(st[5]) < 1e-14, st
     phi = float(stages[-1][6])
