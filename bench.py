@@ -511,15 +511,30 @@ def _sync_time(g):
     return time.perf_counter()
 
 
-def _minimise(g, dt, damping, tol, max_steps, chunk, active=None):
-    """Damped steps until every system's max |F| < tol; converged systems are frozen."""
+# CollectionNLCGV (fixed box) parameters of the packing minimisations: the
+# constructor's defaults (src/collection.cpp:877-898) with dt = 0.1
+CG_PARAMS = np.array([0.1, 0.0, 1.0, 1000, 10, 1e-4, 0.0, 0.0, 0.0, 0.0, 0.0])
+
+
+def _cg_handle(ws, precision, tune=False):
+    """A handle with CollectionNLCGV set up on every system (Collection initialise, then reset())."""
+    g = make_system(ws, precision, 0)
+    g.set_graph_steps(25)
+    variant = g.autotune() if (tune and precision == "mixed") else None
+    g.nlcg_init(CG_PARAMS, boxed=False)
+    g.nlcg_reset()
+    return g, variant
+
+
+def _minimise_cg(g, tol, max_steps, chunk):
+    """Conjugate-gradient time steps until every system's max |F| < tol (converged systems frozen)."""
     nsys = g.nsys
-    act = np.ones(nsys, bool) if active is None else active.copy()
+    act = np.ones(nsys, bool)
     steps = np.zeros(nsys, dtype=np.int64)
     done = 0
     while done < max_steps and act.any():
         g.set_active(act)
-        g.damped(dt, damping, chunk)
+        g.nlcg_timestep(chunk)
         steps[act] += chunk
         done += chunk
         fmax = np.sqrt(g.max_force_sq())
@@ -528,87 +543,82 @@ def _minimise(g, dt, damping, tol, max_steps, chunk, active=None):
     return steps, np.sqrt(g.max_force_sq())
 
 
-def _phase_state(g):
-    st = g.get_atoms()
-    return st["x"], st["v"]
+def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False):
+    """Mixed-precision conjugate-gradient bulk phase, then an FP64 phase from its positions to max|F| < tol64."""
+    g, variant = _cg_handle(ws, "mixed", tune)
+    ta = _sync_time(g)
+    s32, f32 = _minimise_cg(g, tol32, cap32, chunk)
+    x = g.get_atoms(1)["x"]
+    tb = _sync_time(g)
+    g.close()
+    from parm_gb300 import workloads as W
+    w64 = W.Workload(ws.name, ws.ndim, ws.sizes, ws.L, x, np.zeros_like(x), ws.m, ws.kind, ws.params, ws.skin)
+    g64, _ = _cg_handle(w64, "fp64")
+    tc = _sync_time(g64)
+    s64, f64 = _minimise_cg(g64, tol64, cap64, chunk)
+    td = _sync_time(g64)
+    E = g64.energy()
+    g64.close()
+    return {"variant": variant, "t32": tb - ta, "t64": td - tc, "f32": f32, "f64": f64, "E": E, "s32": s32,
+            "s64": s64}
 
 
 def run_packings(args):
-    """Batched 3D packings: damped minimisation, mixed-precision bulk then FP64 finish.
+    """Batched 3D packings minimised by the conjugate-gradient minimiser (CollectionNLCGV, fixed box).
 
-    A packing is one minimisation with a fixed step budget (the systems near
-    jamming converge too slowly for a max|F| criterion to bound the run):
-    S damped steps in mixed precision, then S/10 in FP64; systems whose
-    max |F| falls below the tolerance of a phase stop early (frozen).
-    Reported: packings/s of the batch, the same protocol run one system per
-    handle and launch (speed-up), and the final-energy error against a pure
-    FP64 minimisation with the same total budget on a sample of systems.
+    Every system: a mixed-precision phase until max |F| < 1e-7 (FP32 forces),
+    then an FP64 phase until max |F| < 1e-12; converged systems are frozen
+    while the others continue.  A packing counts only when its system reached
+    max |F| < 1e-12 within the step caps.  Reported: converged packings/s of
+    the batch, the converged fraction, the same protocol run one system per
+    handle and launch (speed-up), and the final-energy error of converged
+    systems against an FP64-only minimisation of a sample of systems.
     """
-    from parm_gb300 import workloads as W
+    from parm_gb300 import shard, workloads as W
     nsys = args.nsys or 4096
-    w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=0.1)
-    dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
-    cap32, cap64, chunk = args.min_steps, max(args.min_steps // 10, 200), 200
+    w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=args.skin)
+    tol32, tol64, chunk = 1e-7, 1e-12, 250
+    cap32, cap64 = args.min_steps, args.min_steps
     log(f"packings: {nsys} systems, {w.n} atoms")
-
-    def protocol(ws):
-        g = make_system(ws, "mixed", 0)
-        g.set_graph_steps(50)
-        kern = g.autotune()
-        ta = _sync_time(g)
-        s32, f32 = _minimise(g, dt, damping, tol32, cap32, chunk)
-        x, v = _phase_state(g)
-        g.close()
-        w64 = W.Workload(ws.name, 3, ws.sizes, ws.L, x, np.zeros_like(v), ws.m, ws.kind, ws.params, ws.skin)
-        g64 = make_system(w64, "fp64", 0)
-        g64.set_graph_steps(50)
-        tb = _sync_time(g64)
-        s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
-        tc = _sync_time(g64)
-        E = g64.energy()
-        g64.close()
-        return {"kernel": kern, "t32": tb - ta, "t64": tc - tb, "f32": f32, "f64": f64, "E": E,
-                "s32": s32, "s64": s64}
-
-    def sub(lo, hi):
-        o0, o1 = int(sum(w.sizes[:lo])), int(sum(w.sizes[:hi]))
-        return W.Workload(w.name, 3, w.sizes[lo:hi], w.L[lo:hi], w.x[o0:o1], w.v[o0:o1], w.m[o0:o1], w.kind,
-                          w.params[o0:o1], w.skin)
-
-    r = protocol(w)
+    r = _cg_protocol(w, tol32, tol64, cap32, cap64, chunk, tune=True)
     wall = r["t32"] + r["t64"]
-    value = nsys / wall
-    # pure FP64 minimisation of a sample, same total budget
+    conv = r["f64"] < tol64
+    value = float(conv.sum()) / wall
+    # FP64-only minimisation of a sample (same tolerance and total cap)
     ns = min(nsys, args.sample_sys)
-    gr = make_system(sub(0, ns), "fp64", 0)
-    gr.set_graph_steps(50)
-    _minimise(gr, dt, damping, tol64, cap32 + cap64, chunk)
+    gr, _ = _cg_handle(shard.select(w, list(range(ns))), "fp64")
+    _, fr = _minimise_cg(gr, tol64, cap32 + cap64, chunk)
     Er = gr.energy()
     gr.close()
+    both = conv[:ns] & (fr < tol64)
     rel = np.abs(r["E"][:ns] - Er) / np.maximum(np.abs(Er), 1e-300)
     # one system per handle and launch sequence, same protocol
     nsingle = min(nsys, args.single_sys)
-    t_single = 0.0
+    t_single, c_single = 0.0, 0
     for q in range(nsingle):
-        rs = protocol(sub(q, q + 1))
+        rs = _cg_protocol(shard.select(w, [q]), tol32, tol64, cap32, cap64, chunk)
         t_single += rs["t32"] + rs["t64"]
-    single_rate = nsingle / t_single
-    out = {"metric": "packings/s (batched 3D soft-sphere damped minimisation, mixed bulk + FP64 finish)",
+        c_single += int((rs["f64"] < tol64).sum())
+    single_rate = c_single / t_single
+    sizes = np.asarray(w.sizes)
+    out = {"metric": "converged packings/s (batched 3D soft-sphere conjugate-gradient minimisation to max|F| < 1e-12)",
            "value": value, "unit": "packings/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
            "config": {"workload": f"packings_{nsys}_systems", "systems": nsys, "atoms": w.n,
-                      "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5,
-                      "integrator": "CollectionDamped", "dt": dt, "damping": damping,
-                      "steps_mixed": cap32, "steps_fp64": cap64, "tol_mixed": tol32, "tol_fp64": tol64,
-                      "kernel": r["kernel"]},
+                      "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "skin": w.skin,
+                      "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
+                      "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_mixed": cap32, "step_cap_fp64": cap64,
+                      "steps_per_check": chunk, "kernel_variant": r["variant"]},
            "wall_s": wall, "mixed_s": r["t32"], "fp64_s": r["t64"],
-           "mixed_atom_steps_per_s": float((r["s32"] * np.array(w.sizes)).sum() / r["t32"]),
-           "fp64_atom_steps_per_s": float((r["s64"] * np.array(w.sizes)).sum() / r["t64"]),
-           "converged_fp64_tol": int((r["f64"] < tol64).sum()),
-           "max_force_median": {"after_mixed": float(np.median(r["f32"])), "after_fp64": float(np.median(r["f64"]))},
-           "energy_rel_err_vs_fp64": {"systems": ns, "median": float(np.median(rel)), "max": float(rel.max())},
-           "one_system_per_launch": {"systems": nsingle, "packings_per_s": single_rate,
-                                     "batched_speedup": value / single_rate}}
+           "converged": int(conv.sum()), "converged_fraction": float(conv.mean()),
+           "steps_median": {"mixed": float(np.median(r["s32"])), "fp64": float(np.median(r["s64"]))},
+           "mixed_atom_steps_per_s": float((r["s32"] * sizes).sum() / r["t32"]),
+           "fp64_atom_steps_per_s": float((r["s64"] * sizes).sum() / max(r["t64"], 1e-9)),
+           "max_force": {"after_mixed_median": float(np.median(r["f32"])), "after_fp64_max": float(r["f64"].max())},
+           "energy_rel_err_vs_fp64": {"systems": int(both.sum()), "median": float(np.median(rel[both])) if both.any() else None,
+                                      "max": float(rel[both].max()) if both.any() else None},
+           "one_system_per_launch": {"systems": nsingle, "converged": c_single, "packings_per_s": single_rate,
+                                     "batched_speedup": value / single_rate if single_rate > 0 else None}}
     print(json.dumps(out), flush=True)
 
 
@@ -668,39 +678,30 @@ def run_replicas(args):
 
 
 def run_disks(args):
-    """2D bidisperse harmonic disks: mixed bulk minimisation, FP64 finish, vs FP64 alone."""
+    """2D bidisperse harmonic disks at phi = 0.84: conjugate-gradient minimisation (CollectionNLCGV),
+    a mixed-precision phase then FP64 until max|F| < 1e-12, against an FP64-only minimisation."""
     from parm_gb300 import workloads as W
-    w = W.soft_disks(n=65536, phi=0.84, exponent=2.0, seed=2, skin=0.1)
-    dt, damping, tol32, tol64 = 0.01, 1.0, 1e-6, 1e-12
-    cap, chunk = args.min_steps, 500
-    cap64 = max(cap // 10, chunk)
-    g = make_system(w, "mixed", 0)
-    g.set_graph_steps(50)
-    tpa = g.autotune()
-    t0 = _sync_time(g)
-    s32, f32 = _minimise(g, dt, damping, tol32, cap, chunk)
-    x, v = _phase_state(g)
-    w64 = W.Workload(w.name, 2, w.sizes, w.L, x, np.zeros_like(v), w.m, w.kind, w.params, w.skin)
-    g64 = make_system(w64, "fp64", 0)
-    g64.set_graph_steps(50)
-    t1 = _sync_time(g64)
-    s64, f64 = _minimise(g64, dt, damping, tol64, cap64, chunk)
-    t2 = _sync_time(g64)
-    E = float(g64.energy()[0])
-    gr = make_system(w, "fp64", 0)
-    gr.set_graph_steps(50)
+    w = W.soft_disks(n=65536, phi=0.84, exponent=2.0, seed=2, skin=args.skin)
+    tol32, tol64, chunk = 1e-7, 1e-12, 1000
+    cap = args.min_steps
+    r = _cg_protocol(w, tol32, tol64, cap, cap, chunk, tune=True)
+    gr, _ = _cg_handle(w, "fp64")
     t3 = _sync_time(gr)
-    sr, fr = _minimise(gr, dt, damping, tol64, cap + cap64, chunk)
+    sr, fr = _minimise_cg(gr, tol64, 2 * cap, chunk)
     t4 = _sync_time(gr)
     Er = float(gr.energy()[0])
-    out = {"metric": "seconds for the 65536-disk 2D damped minimisation (mixed bulk + FP64 finish, fixed budget)",
-           "value": t2 - t0, "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "strong",
+    gr.close()
+    E = float(r["E"][0])
+    out = {"metric": "seconds to minimise 65536 2D disks at phi 0.84 to max|F| < 1e-12 (mixed bulk + FP64 finish)",
+           "value": r["t32"] + r["t64"], "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "strong",
            "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
-           "config": {"workload": "disks2d_65536", "phi": 0.84, "exponent": 2.0, "dt": dt, "damping": damping,
-                      "tol_mixed": tol32, "tol_fp64": tol64, "steps_mixed": cap, "steps_fp64": cap64, "kernel": tpa},
-           "steps_mixed": int(s32[0]), "steps_fp64": int(s64[0]), "max_force": float(f64[0]),
-           "energy": E, "fp64_alone": {"seconds": t4 - t3, "steps": int(sr[0]), "max_force": float(fr[0]),
-                                       "energy": Er},
+           "config": {"workload": "disks2d_65536", "phi": 0.84, "exponent": 2.0, "skin": w.skin,
+                      "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
+                      "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_each_phase": cap, "kernel_variant": r["variant"]},
+           "steps_mixed": int(r["s32"][0]), "steps_fp64": int(r["s64"][0]), "max_force": float(r["f64"][0]),
+           "converged": bool(r["f64"][0] < tol64), "energy": E,
+           "fp64_alone": {"seconds": t4 - t3, "steps": int(sr[0]), "max_force": float(fr[0]), "energy": Er,
+                          "converged": bool(fr[0] < tol64)},
            "energy_rel_diff": abs(E - Er) / max(abs(Er), 1e-300)}
     print(json.dumps(out), flush=True)
 
@@ -725,6 +726,7 @@ def main():
                     help="lj1m: the headline line; the others print their own line")
     ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workloads")
     ap.add_argument("--min-steps", type=int, default=20000, help="step cap of each minimisation phase")
+    ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin of the packing workloads")
     ap.add_argument("--fp64-steps", type=int, default=0,
                     help="lj1m: timed FP64 steps (default 200); replicas: FP64 steps of the comparison (2000)")
     ap.add_argument("--drift-steps", type=int, default=10000,

@@ -102,6 +102,14 @@ int parm_get_atoms(parm_system* s, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* s, int kind, const double* params, const uint32_t* rank,
                          double skin);
 
+/* List diameters given to NeighborList::add(atom, diameter)
+ * (src/trackers.hpp:194-201) instead of the pair parameters' max_size():
+ * natoms doubles in caller order, NaN where the parameters decide; NULL
+ * clears them.  A member with an explicit diameter may have all parameters
+ * 0 (added to the list only, as the reference allows: its pairs carry no
+ * force).  Takes effect with the next rebuild (ignorechanged = true). */
+int parm_set_list_diameters(parm_system* s, const double* diam);
+
 /* NeighborList::ignore(a, b) (src/trackers.hpp:190-193). */
 int parm_nlist_ignore(parm_system* s, uint32_t a, uint32_t b);
 

@@ -741,6 +741,19 @@ int orc_add_atom(void* s, uint32_t i, const double* p) {
     return 0;
 }
 
+// NeighborList::add(atom, diameter) (trackers.hpp:194-201): a member without
+// pair parameters (an NListed on the list sees its default-constructed atom)
+int orc_add_member(void* s, uint32_t i, double diameter) {
+    System* S = static_cast<System*>(s);
+    if (i >= S->n || S->has_params[i]) return -1;
+    S->has_params[i] = 1;
+    S->members.push_back(i);
+    S->diameters.push_back(diameter);
+    for (int d = 0; d < S->nd; d++) S->lastlocs.push_back(S->x[i * S->nd + d]);
+    S->ignorechanged = true;
+    return 0;
+}
+
 // NeighborList::ignore (trackers.hpp:190-193)
 void orc_ignore(void* s, uint32_t i, uint32_t j) {
     System* S = static_cast<System*>(s);

@@ -33,6 +33,7 @@ def lib() -> C.CDLL:
             "orc_set_interaction": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
             "orc_add_atom": (C.c_int, [C.c_void_p, C.c_uint32, _dp]),
             "orc_ignore": (None, [C.c_void_p, C.c_uint32, C.c_uint32]),
+            "orc_add_member": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double]),
             "orc_nl_update": (C.c_int, [C.c_void_p, C.c_int]),
             "orc_nl_which": (C.c_uint32, [C.c_void_p]),
             "orc_nl_numpairs": (C.c_uint64, [C.c_void_p]),
@@ -152,6 +153,10 @@ class Oracle:
         for i in order:
             p = np.ascontiguousarray(params[i])
             assert self.L_.orc_add_atom(self.h, int(i), _d(p)) == 0
+
+    def add_member(self, i, diameter):
+        """NeighborList::add(atom, diameter): a list member without pair parameters."""
+        assert self.L_.orc_add_member(self.h, int(i), float(diameter)) == 0
 
     def ignore(self, a, b):
         self.L_.orc_ignore(self.h, int(a), int(b))

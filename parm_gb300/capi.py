@@ -57,6 +57,7 @@ SIGNATURES = {
     "parm_get_atoms": (C.c_int, [_h, _dp, C.c_uint64, C.c_uint32]),
     "parm_set_interaction": (C.c_int, [_h, C.c_int, _dp, _u32p, C.c_double]),
     "parm_nlist_ignore": (C.c_int, [_h, C.c_uint32, C.c_uint32]),
+    "parm_set_list_diameters": (C.c_int, [_h, _dp]),
     "parm_nlist_update": (C.c_int, [_h, C.c_int, _u8p]),
     "parm_nlist_which": (C.c_int, [_h, _u32p]),
     "parm_nlist_numpairs": (C.c_int, [_h, _u64p]),

@@ -78,6 +78,7 @@ struct parm_system {
     int kind = -1;
     double skin = 0.0;
     std::vector<double> prm_in;      // n*3 (global order)
+    std::vector<double> ldiam;       // explicit list diameters (global order; NaN: from the parameters), or empty
     std::vector<uint32_t> rank_in;   // global order
     std::vector<std::set<uint32_t>> excl;
     bool have_excl = false, excl_dirty = false;
@@ -201,6 +202,7 @@ struct parm_system {
             any_member = true;
             const double* p = &prm_in[3 * (size_t)i];
             double d = (kind == PARM_LJCUT) ? p[1] * p[2] : p[1];
+            if (!ldiam.empty() && std::isfinite(ldiam[i])) d = ldiam[i];
             dmax = std::max(dmax, d);
         }
         const double rl = dmax + skin;
@@ -329,8 +331,9 @@ struct parm_system {
                 if (S.nc[d] < 3) ok = false;
             if (!ok) break;
             const double a = std::max(1e-3, (double)natoms[s] / S.ncell);
-            // about 0.7 home atoms per thread: the fullest blocks still fit one pass
-            const int cells = std::max(1, (int)std::lround(0.7 * STG_THREADS_HOST / a));
+            // about 0.85 home atoms per thread: nearly every block still fits one
+            // pass of its threads, and few threads idle in the pair loop
+            const int cells = std::max(1, (int)std::lround(0.85 * STG_THREADS_HOST / a));
             const int ky = std::max(1, std::min({(int)std::lround(std::sqrt(cells / 2.0)), STG_KY_MAX, S.nc[1] - 2}));
             const int kx = std::max(1, std::min({(int)std::lround((double)cells / ky), STG_KX_MAX, S.nc[0] - 2}));
             const int nbx = (S.nc[0] + kx - 1) / kx, nby = (S.nc[1] + ky - 1) / ky;
@@ -1345,11 +1348,14 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             prm[g] = a;
             prm32[g] = make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
             diam[g] = (kind == PARM_LJCUT) ? a.p1 * a.p2 : a.p1;   // A::max_size()
+            const bool explicit_d = !S->ldiam.empty() && std::isfinite(S->ldiam[g]);
+            if (explicit_d) diam[g] = S->ldiam[g];   // NeighborList::add(atom, diameter)
             if (S->rank_in[g] == PARM_NOT_MEMBER) {
                 nmr[g] = nm++;
                 continue;
             }
-            if (!(a.p1 > 0.0) || !(a.p0 >= 0.0)) return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
+            if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0)))
+                return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
             if (first) {
                 e0 = a.p0;
                 s0 = a.p1;
@@ -1362,6 +1368,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             if (a.p1 != 1.0) uni &= ~UNI_SIG_ONE;
         }
     }
+    // explicit list diameters: no uniform-threshold shortcut in the list builds
+    if (!S->ldiam.empty()) uni &= ~UNI_SIG;
     if (!(uni & UNI_SIG)) uni &= ~UNI_SIG_ONE;
     // internal order of the device arrays
     std::vector<uint32_t> orig(n);
@@ -1395,6 +1403,21 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     S->stg_pending = false;
     if (S->c.staged != was) S->clear_graphs();
     return S->request_rebuild_all();  // ignorechanged = true
+}
+
+int parm_set_list_diameters(parm_system* S, const double* diam) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (!diam) {
+        S->ldiam.clear();
+    } else {
+        for (uint32_t i = 0; i < S->n; i++)
+            if (diam[i] < 0.0 || std::isinf(diam[i])) return fail(PARM_ERR_ARG, "list diameters must be >= 0 or NaN");
+        S->ldiam.assign(diam, diam + S->n);
+    }
+    if (S->kind < 0) return PARM_OK;   // applied by the next parm_set_interaction
+    const std::vector<double> prm = S->prm_in;
+    const std::vector<uint32_t> rk = S->rank_in;
+    return parm_set_interaction(S, S->kind, prm.data(), rk.data(), S->skin);
 }
 
 int parm_nlist_ignore(parm_system* S, uint32_t a, uint32_t b) {

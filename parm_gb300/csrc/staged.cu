@@ -834,6 +834,7 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
         // the two entries of each list word together, in packed FP32 pairs:
         // even entries accumulate in the low half, odd ones in the high half
         const f32x2 K2 = pk2(STG_K, STG_K), is2 = pk2(law0.isig2, law0.isig2), C2 = pk2(law0.C, law0.C);
+        const f32x2 P1_2 = pk2(1.0f, 1.0f);
         f32x2 fx = pk2(0.f, 0.f), fy = fx, fz = fx;
         auto pair2 = [&](uint32_t w) {
             const uint32_t q0 = min(w & 0xFFFFu, qmax), q1 = min(w >> 16, qmax);
@@ -861,7 +862,10 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
             const f32x2 ir3 = mul2(ir2, ir);
             const f32x2 t = mul2(C2, ir4);
             float s0, s1;
-            upk2(sub2(mul2(t, ir3), t), s0, s1);   // 12 eps / sigma^2 * ir^4 (ir^3 - 1)
+            // 12 eps / sigma^2 * ir^4 (ir^3 - 1); ir^3 - 1 is exact for ir^3 in
+            // [1/2, 2] (the strongly repulsive and the attractive well's pairs),
+            // so the product is the only rounding there
+            upk2(mul2(t, sub2(ir3, P1_2)), s0, s1);
             const float dd0 = r0 - law0.cut2, dd1 = r1 - law0.cut2;
             if constexpr (KIND == KIND_LJCUT) dmin = fminf(dmin, fminf(fabsf(dd0), fabsf(dd1)) - law0.band);
             const f32x2 sc = pk2(dd0 > 0.0f ? 0.0f : s0, dd1 > 0.0f ? 0.0f : s1);
@@ -931,7 +935,7 @@ __device__ __forceinline__ void force_home(const DevCtx& c, const SysConst& S, c
 }
 
 template <int ND, int KIND, int MODE, int PRM>
-__global__ void __launch_bounds__(STG_THREADS, 4) k_force_stg(DevCtx c) {
+__global__ void __launch_bounds__(STG_THREADS, 5) k_force_stg(DevCtx c) {
     extern __shared__ float4 smem_f[];
     __shared__ StgTable T;
     if (blockIdx.x >= c.nblk) {

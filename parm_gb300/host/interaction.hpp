@@ -2,14 +2,22 @@
 // reference's src/interaction.hpp (wackywendell/parm), evaluated on the GPU.
 //
 // NListed<A, P> is the reference's neighbour-listed pair interaction
-// (src/interaction.hpp:1896-1945); the atom types carry the per-atom
+// (src/interaction.hpp:1876-1945); the atom types carry the per-atom
 // parameters and the pair types select the pair law:
 //   NListed<EpsSigCutAtom, LennardJonesCutPair>  LJ cut at sigcut * sigma
 //   NListed<EpsSigExpAtom, RepulsionPair>         soft repulsion, exponent n
 //   NListed<EpsSigAtom,    LJRepulsePair>         WCA (repulsive LJ)
+// Sums over the pair list (forces, energies, virials, stresses) run on the
+// GPU.  A pair object (get_pair, pair_iter) also evaluates its own energy and
+// force on the host, with the reference's formulas, for code that inspects
+// single pairs.
 #ifndef PARM_GB300_INTERACTION_HPP
 #define PARM_GB300_INTERACTION_HPP
 
+#include <algorithm>
+#include <stdexcept>
+#include <string>
+#include <typeinfo>
 #include <vector>
 
 #include "trackers.hpp"
@@ -19,11 +27,23 @@ class Interaction {
    public:
     virtual flt energy(Box& box) = 0;
     virtual void set_forces(Box& box) = 0;
-    virtual flt set_forces_get_pressure(Box& box) = 0;
+    virtual flt set_forces_get_pressure(Box& box) {
+        throw std::runtime_error(std::string("set_forces_get_pressure not defined for class ") +
+                                 typeid(*this).name());
+    }
     virtual flt pressure(Box& box) = 0;
+    virtual Matrix stress(Box& box) {
+        throw std::runtime_error(std::string("stress not defined for class ") + typeid(*this).name());
+    }
     virtual ~Interaction() {}
-    //! the GPU handle behind the interaction (every interaction here has one)
+};
+
+//! An interaction evaluated on the GPU: the handle behind it.  Collections
+//! step the atoms of the GPU interaction they hold.
+class GpuInteraction {
+   public:
     virtual sptr<GpuLink> gpu() = 0;
+    virtual ~GpuInteraction() {}
 };
 
 //! (epsilon, sigma) per atom (src/interaction.hpp:857-865).
@@ -55,7 +75,12 @@ struct EpsSigExpAtom : public AtomID {
     flt max_size() { return sigma; }
 };
 
-// pair laws (the GPU evaluates them; these types select the law)
+// Pair laws.  Each pair type holds its pair's constants (combined from the
+// two atoms as the reference combines them) and its two atoms; `kind` and
+// `params` tell the GPU which law and which per-atom numbers to use.
+
+//! Truncated LJ, V = eps((1 - sigma^6/r^6)^2 - 1) - V(cut)
+//! (src/interaction.hpp:238-281, 967-987).
 struct LennardJonesCutPair {
     static const int kind = PARM_LJCUT;
     static void params(const EpsSigCutAtom& a, double p[3]) {
@@ -63,7 +88,38 @@ struct LennardJonesCutPair {
         p[1] = a.sigma;
         p[2] = a.sigcut;
     }
+    flt epsilon, sigma, cut_distance, cut_energy;
+    AtomID atom1, atom2;
+    LennardJonesCutPair(EpsSigCutAtom a1, EpsSigCutAtom a2)
+        : epsilon(std::sqrt(a1.epsilon * a2.epsilon)),
+          sigma((a1.sigma + a2.sigma) / 2),
+          cut_distance(std::max(a1.sigcut, a2.sigcut)),
+          atom1(a1),
+          atom2(a2) {
+        const flt rsix = std::pow(cut_distance, 6);
+        const flt mid = (1 - 1 / rsix);
+        cut_energy = epsilon * (mid * mid - 1);
+    }
+    flt energy(Box& box) {
+        const flt rsq = box.diff(atom1->x, atom2->x).squaredNorm() / (sigma * sigma);
+        if (rsq > (cut_distance * cut_distance)) return 0;
+        const flt rsix = rsq * rsq * rsq;
+        const flt mid = (1 - 1 / rsix);
+        return epsilon * (mid * mid - 1) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        const Vec diff = box.diff(atom1->x, atom2->x);
+        const flt dsq = diff.squaredNorm();
+        const flt rsq = dsq / (sigma * sigma);
+        if (rsq > (cut_distance * cut_distance)) return Vec::Zero();
+        const flt rsix = rsq * rsq * rsq;
+        const flt fmagTimesR = 12 * epsilon / rsix * (1 / rsix - 1);
+        return diff * (fmagTimesR / dsq);
+    }
 };
+
+//! Soft repulsion, V = eps/n (1 - r/sigma)^n for r < sigma
+//! (src/interaction.hpp:1528-1590).
 struct RepulsionPair {
     static const int kind = PARM_REPULSION;
     static void params(const EpsSigExpAtom& a, double p[3]) {
@@ -71,13 +127,56 @@ struct RepulsionPair {
         p[1] = a.sigma;
         p[2] = a.exponent;
     }
+    flt eps, sig, exponent;
+    AtomID atom1, atom2;
+    RepulsionPair(EpsSigExpAtom a1, EpsSigExpAtom a2)
+        : eps(std::sqrt(a1.eps * a2.eps)),
+          sig((a1.sigma + a2.sigma) / 2.0),
+          exponent((a1.exponent + a2.exponent) / 2.0),
+          atom1(a1),
+          atom2(a2) {}
+    flt energy(Box& box) {
+        const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
+        if (dsq > sig * sig) return 0.0;
+        const flt R = std::sqrt(dsq);
+        return eps * std::pow(1.0 - (R / sig), exponent) / exponent;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq > sig * sig) return Vec::Zero();
+        const flt R = std::sqrt(dsq);
+        return rij * (eps * std::pow(1.0 - (R / sig), exponent - 1) / sig / R);
+    }
 };
+
+//! WCA, V = eps (1 - sigma^6/r^6)^2 for r < sigma (src/interaction.hpp:119-152, 875-891).
 struct LJRepulsePair {
     static const int kind = PARM_LJREPULSE;
     static void params(const EpsSigAtom& a, double p[3]) {
         p[0] = a.epsilon;
         p[1] = a.sigma;
         p[2] = 0.0;
+    }
+    flt epsilon, sigma;
+    AtomID atom1, atom2;
+    LJRepulsePair(EpsSigAtom a1, EpsSigAtom a2)
+        : epsilon(std::sqrt(a1.epsilon * a2.epsilon)), sigma((a1.sigma + a2.sigma) / 2), atom1(a1), atom2(a2) {}
+    flt energy(Box& box) {
+        const flt rsq = box.diff(atom1->x, atom2->x).squaredNorm() / (sigma * sigma);
+        if (rsq > 1) return 0;
+        const flt rsix = rsq * rsq * rsq;
+        const flt mid = (1 - 1 / rsix);
+        return epsilon * (mid * mid);
+    }
+    Vec forces(Box& box) {
+        const Vec diff = box.diff(atom1->x, atom2->x);
+        const flt dsq = diff.squaredNorm();
+        const flt rsq = dsq / (sigma * sigma);
+        if (rsq > 1) return Vec::Zero();
+        const flt rsix = rsq * rsq * rsq;
+        const flt fmagTimesR = 12 * epsilon / rsix * (1 / rsix - 1);
+        return diff * (fmagTimesR / dsq);
     }
 };
 
@@ -87,26 +186,50 @@ Matrix gpu_stress(GpuLink& link);
 //! NListed::set_forces: pair forces added to the atoms' current forces
 void gpu_add_forces(GpuLink& link);
 
-//! Neighbour-listed pair interaction (src/interaction.hpp:1896-1945).
+//! Neighbour-listed pair interaction (src/interaction.hpp:1876-1945).  The
+//! NeighborList may be its own (constructor with a skin) or one the caller
+//! made (NListed(atoms, neighbours), as pyparm's Repulsion(atoms, nl) does);
+//! one NListed evaluates the pairs of a NeighborList.
 template <class A, class P>
-class NListed : public Interaction {
+class NListed : public Interaction, public GpuInteraction {
    public:
+    NListed(sptr<AtomVec> vec, sptr<NeighborList> neighbors)
+        : link(neighbors->gpu()), neighbors(neighbors), atoms(vec->size()) {
+        if (link->atoms() != vec) throw std::invalid_argument("NListed: the NeighborList tracks another AtomVec");
+    }
     NListed(sptr<Box> box, sptr<AtomVec> atomv, const flt skin)
-        : link(new GpuLink(box, atomv, skin)), neighbors(new NeighborList(link)) {}
+        : link(new GpuLink(box, atomv, skin)), neighbors(new NeighborList(link)), atoms(atomv->size()) {}
     void add(A atm) {
         double p[3];
         P::params(atm, p);
-        link->add(atm.n(), P::kind, p);
-        atoms.push_back(atm);
+        link->add(atm.n(), P::kind, p, this);
+        atoms.at(atm.n()) = atm;
     }
+    //! the pair of an IDPair of the neighbour list, with its constants
+    P get_pair(IDPair& pair) { return P(atoms[pair.first().n()], atoms[pair.last().n()]); }
+    A& getatom(uint n) { return atoms[n]; }
+    //! the pairs of the current neighbour list, in its order (NListed::update_pairs)
+    std::vector<P>& pair_iter() {
+        const std::vector<IDPair>& ps = neighbors->pairs();
+        pairs.clear();
+        pairs.reserve(ps.size());
+        for (const IDPair& q : ps) pairs.push_back(P(atoms[q.first().n()], atoms[q.last().n()]));
+        return pairs;
+    }
+    //! energy of one pair (NListed::energy(box, pair))
+    flt energy(Box& box, IDPair& pair) { return get_pair(pair).energy(box); }
     flt energy(Box& box) override { return gpu_evaluate(*link, PARM_EVAL_ENERGY); }
     //! sum of r . f over the listed pairs (src/interaction.hpp:2124-2163)
     flt pressure(Box& box) override { return gpu_evaluate(*link, PARM_EVAL_VIRIAL); }
-    Matrix stress(Box& box) { return gpu_stress(*link); }
+    Matrix stress(Box& box) override { return gpu_stress(*link); }
     void set_forces(Box& box) override { gpu_add_forces(*link); }
     flt set_forces_get_pressure(Box& box) override {
         gpu_add_forces(*link);
         return pressure(box);
+    }
+    Matrix set_forces_get_stress(Box& box) {
+        gpu_add_forces(*link);
+        return stress(box);
     }
     unsigned long long contacts(Box& box) {
         return (unsigned long long)gpu_evaluate(*link, PARM_EVAL_CONTACTS);
@@ -122,7 +245,8 @@ class NListed : public Interaction {
    private:
     sptr<GpuLink> link;
     sptr<NeighborList> neighbors;
-    std::vector<A> atoms;
+    std::vector<A> atoms;   // indexed by AtomVec index; unset entries are A()
+    std::vector<P> pairs;
 };
 
 #endif

@@ -117,23 +117,40 @@ GpuLink::GpuLink(sptr<Box> box, sptr<AtomVec> atoms, flt skin) : bx(box), atomv(
         throw std::invalid_argument("parm_gb300: the GPU path supports periodic OriginBox boxes");
     params.assign(3 * (size_t)atomv->size(), 0.0);
     rank.assign(atomv->size(), PARM_NOT_MEMBER);
+    ldiam.assign(atomv->size(), std::nan(""));
 }
 
 GpuLink::~GpuLink() {
     if (h) parm_destroy(h);
 }
 
-void GpuLink::add(uint atom, int k, const double p[3]) {
+void GpuLink::add(uint atom, int k, const double p[3], const void* owner) {
     if (atom >= atomv->size()) throw std::out_of_range("NListed::add: atom not in this AtomVec");
+    if (owner_ && owner != owner_)
+        throw std::invalid_argument("parm_gb300: one NListed interaction per NeighborList");
     if (kind >= 0 && k != kind) throw std::invalid_argument("NListed::add: one pair law per interaction");
     if (rank[atom] != PARM_NOT_MEMBER) throw std::invalid_argument("NListed::add: atom added twice");
+    owner_ = owner;
     kind = k;
     for (int q = 0; q < 3; q++) params[3 * (size_t)atom + q] = p[q];
     rank[atom] = nmembers++;
     interaction_dirty = true;
 }
 
-void GpuLink::ignore(uint a, uint b) { pending_ignores.emplace_back(a, b); }
+void GpuLink::add_member(uint atom, double diameter) {
+    if (atom >= atomv->size()) throw std::out_of_range("NeighborList::add: atom not in this AtomVec");
+    if (rank[atom] != PARM_NOT_MEMBER) throw std::invalid_argument("NeighborList::add: atom added twice");
+    if (!(diameter >= 0.0)) throw std::invalid_argument("NeighborList::add: diameter must be >= 0");
+    rank[atom] = nmembers++;
+    ldiam[atom] = diameter;
+    any_ldiam = true;
+    interaction_dirty = true;
+}
+
+void GpuLink::ignore(uint a, uint b) {
+    pending_ignores.emplace_back(a, b);
+    nignored++;
+}
 
 void GpuLink::push() {
     if (!h) {
@@ -147,8 +164,12 @@ void GpuLink::push() {
         parm_host_check(parm_set_boxes(h, lv.data()), "parm_set_boxes");
         lastbox = lv;
     }
-    if (interaction_dirty && kind >= 0) {
-        parm_host_check(parm_set_interaction(h, kind, params.data(), rank.data(), skin_), "parm_set_interaction");
+    if (interaction_dirty && nmembers > 0) {
+        if (any_ldiam) parm_host_check(parm_set_list_diameters(h, ldiam.data()), "parm_set_list_diameters");
+        // members without an NListed carry no parameters: any law with zero
+        // epsilon gives them no force
+        parm_host_check(parm_set_interaction(h, kind >= 0 ? kind : PARM_REPULSION, params.data(), rank.data(), skin_),
+                        "parm_set_interaction");
         interaction_dirty = false;
     }
     for (auto& pr : pending_ignores) parm_host_check(parm_nlist_ignore(h, pr.first, pr.second), "parm_nlist_ignore");
@@ -366,8 +387,13 @@ Collection::Collection(sptr<Box> box, sptr<AtomVec> atoms, std::vector<sptr<Inte
 void Collection::attach() {
     sptr<GpuLink> found;
     for (auto& it : interactions) {
-        sptr<GpuLink> l = it->gpu();
-        if (found && l != found) throw std::invalid_argument("parm_gb300: one NListed interaction per Collection");
+        GpuInteraction* gi = dynamic_cast<GpuInteraction*>(it.get());
+        if (!gi)
+            throw std::invalid_argument("parm_gb300: a Collection steps its atoms on the GPU; its interaction must be "
+                                        "an NListed interaction");
+        sptr<GpuLink> l = gi->gpu();
+        if (found && l != found)
+            throw std::invalid_argument("parm_gb300: one NListed interaction (one neighbour list) per Collection");
         found = l;
     }
     for (auto& t : trackers) {

@@ -32,9 +32,14 @@ class GpuLink {
     GpuLink& operator=(const GpuLink&) = delete;
 
     //! NListed::add: per-atom parameters (kind: PARM_LJCUT, ...) and the
-    //! atom's position in the neighbour list (insertion order)
-    void add(uint atom, int kind, const double p[3]);
+    //! atom's position in the neighbour list (insertion order); `owner` is
+    //! the NListed adding it (one NListed per neighbour list)
+    void add(uint atom, int kind, const double p[3], const void* owner);
+    //! NeighborList::add(atom, diameter): a list member with its own list
+    //! diameter and no pair parameters (its pairs carry no force)
+    void add_member(uint atom, double diameter);
     void ignore(uint a, uint b);
+    uint ignored() const { return nignored; }
     //! upload box, interaction and Atom records (create the handle if needed)
     void push();
     //! download the Atom records
@@ -58,7 +63,11 @@ class GpuLink {
     int kind = -1;
     std::vector<double> params;
     std::vector<uint32_t> rank;
+    std::vector<double> ldiam;   // explicit list diameters (NaN: the parameters' max_size())
+    bool any_ldiam = false;
+    const void* owner_ = nullptr;
     uint nmembers = 0;
+    uint nignored = 0;
     bool interaction_dirty = false;
     std::vector<std::pair<uint, uint>> pending_ignores;
     std::vector<double> lastbox;
@@ -97,11 +106,24 @@ class NeighborList : public StateTracker {
     uint which();
     uint numpairs();
     void ignore(AtomID a, AtomID b) { link->ignore(a.n(), b.n()); }
+    //! NeighborList::add(a, diameter) (src/trackers.hpp:194-201): a member
+    //! with the given list diameter (NListed::add calls it with max_size())
+    void add(AtomID a, flt diameter) { link->add_member(a.n(), diameter); }
+    uint ignore_size() const { return link->ignored(); }
     uint size() const { return link->members(); }
     flt skin() const { return link->skin(); }
+    AtomVec& vec() { return *link->atoms(); }
     //! the current pairs in the reference's order
     const std::vector<IDPair>& pairs();
     IDPair get(uint i) { return pairs().at(i); }
+    std::vector<IDPair>::iterator begin() {
+        pairs();
+        return cache.begin();
+    }
+    std::vector<IDPair>::iterator end() {
+        pairs();
+        return cache.end();
+    }
     sptr<GpuLink> gpu() { return link; }
 
    private:

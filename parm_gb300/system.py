@@ -102,6 +102,14 @@ class System:
         check(self.lib.parm_set_interaction(self.h, kind, dptr(p), u32ptr(rk) if rk is not None else None,
                                             float(skin)))
 
+    def set_list_diameters(self, diam) -> None:
+        """NeighborList::add(atom, diameter): explicit list diameters (NaN: from the parameters); None clears."""
+        if diam is None:
+            check(self.lib.parm_set_list_diameters(self.h, None))
+            return
+        d = _as_f64(diam, (self.n,))
+        check(self.lib.parm_set_list_diameters(self.h, dptr(d)))
+
     def ignore(self, a: int, b: int) -> None:
         check(self.lib.parm_nlist_ignore(self.h, int(a), int(b)))
 

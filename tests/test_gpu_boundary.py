@@ -1,0 +1,90 @@
+"""The reference's interaction / neighbour-list interface beyond the time steps, on the GPU.
+
+* NeighborList::add(atom, diameter) through parm_set_list_diameters: members
+  with their own list diameter and no pair parameters; pair list (order
+  included), forces and energy bit-exact against the oracle's restatement;
+* the host API's NListed(atoms, neighbours), list iteration, per-pair
+  evaluation, set_forces_get_stress, the virtual stress and the rejection of
+  interactions a Collection cannot step (tests/programs/host_api_extras.cpp);
+* an LJ program written like the reference's src/bin/LJatoms.cpp
+  (tests/programs/lj_verlet.cpp): 20000 CollectionVerlet time steps, one
+  timestep() call at a time, with the total energy conserved.
+"""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from host_api import compile_program
+from parm_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+PROGRAMS = Path(__file__).resolve().parent / "programs"
+
+
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_list_diameters_match_oracle(ndim):
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    w = W.small_random(n=400, ndim=ndim, kind=1, seed=60 + ndim, phi=0.5, skin=0.3)
+    n, nm = w.n, 40
+    params = w.params.copy()
+    params[n - nm:] = 0.0                       # list members without pair parameters
+    rng = np.random.default_rng(5)
+    dia = np.full(n, np.nan)
+    dia[n - nm:] = rng.uniform(0.8, 1.6, nm)
+    order = np.concatenate([rng.permutation(n - nm), np.arange(n - nm, n)])
+    rank = np.empty(n, dtype=np.uint32)
+    rank[order] = np.arange(n, dtype=np.uint32)
+    g = System(n, ndim=ndim, precision="fp64")
+    g.set_boxes(w.L)
+    g.set_atoms(x=w.x, v=w.v, a=np.zeros_like(w.x), f=np.zeros_like(w.x), m=w.m)
+    g.set_list_diameters(dia)
+    g.set_interaction(w.kind, params, w.skin, rank=rank)
+    o = Oracle(n, ndim)
+    o.set_box(w.L[0])
+    o.set_state(x=w.x, v=w.v, m=w.m)
+    o.set_interaction(w.kind, params, w.skin, order=[int(i) for i in order[: n - nm]])
+    for i in order[n - nm:]:
+        o.add_member(int(i), dia[i])
+    g.nlist_update(True)
+    o.nl_update(True)
+    assert np.array_equal(g.pairs(), o.pairs())
+    g.set_forces(True)
+    o.set_forces(True)
+    st, ref = g.get_atoms(), o.get_state()
+    assert np.array_equal(st["f"], ref["f"])
+    assert np.all(st["f"][n - nm:] == 0.0)
+    assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-14)
+    g.close()
+
+
+def _run(src, tmp_path, ndim=3, timeout=900):
+    exe = tmp_path / src.stem
+    r = compile_program(src, exe, ndim=ndim)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=timeout, cwd=tmp_path,
+                       env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
+    return r.stdout
+
+
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_host_api_extras_program(tmp_path, built_lib, ndim):
+    out = _run(PROGRAMS / "host_api_extras.cpp", tmp_path, ndim)
+    checks = [line.split() for line in out.splitlines() if line.startswith("check")]
+    assert len(checks) >= 12, out
+    failed = [c[1] for c in checks if c[2] != "1"]
+    assert not failed, out
+
+
+def test_lj_program_conserves_energy(tmp_path, built_lib):
+    out = _run(PROGRAMS / "lj_verlet.cpp", tmp_path)
+    E0 = float(next(line.split()[1] for line in out.splitlines() if line.startswith("E0")))
+    E = np.array([float(line.split()[3]) for line in out.splitlines() if line.startswith("block")])
+    assert len(E) == 20
+    # total energy per atom stays within 1e-3 of its start over 20000 steps (the cut-off
+    # potential's force jumps give a small random walk; no drift)
+    assert np.abs(E - E0).max() <= 1e-3 * 200, (E0, E)
