@@ -516,14 +516,31 @@ def _sync_time(g):
 CG_PARAMS = np.array([0.1, 0.0, 1.0, 1000, 10, 1e-4, 0.0, 0.0, 0.0, 0.0, 0.0])
 
 
-def _cg_handle(ws, precision, tune=False):
+def _cg_handle(ws, precision, tune=False, cell_scale=1.0):
     """A handle with CollectionNLCGV set up on every system (Collection initialise, then reset())."""
     g = make_system(ws, precision, 0)
     g.set_graph_steps(25)
+    if cell_scale != 1.0:
+        g.set_cell_scale(cell_scale)
+        g.nlist_update(False)
     variant = g.autotune() if (tune and precision == "mixed") else None
     g.nlcg_init(CG_PARAMS, boxed=False)
     g.nlcg_reset()
     return g, variant
+
+
+def _cg_prepare(g):
+    g.nlcg_init(CG_PARAMS, boxed=False)
+    g.nlcg_reset()
+
+
+def _tuned(w, make, step, skins, prepare=None):
+    """The workload with the autotuned skin, the cell scale, and the tuner's summary."""
+    from dataclasses import replace
+    from parm_gb300 import autotune
+    res = autotune.tune(w, make, step, skins, cell_scales=(1.0, 1.5), prepare=prepare)
+    log(f"autotune: skin {res['skin']}, cell scale {res['cell_scale']}, variant {res['variant']}")
+    return replace(w, skin=res["skin"]), res["cell_scale"], autotune.summarise(res)
 
 
 def _minimise_cg(g, tol, max_steps, chunk):
@@ -543,9 +560,9 @@ def _minimise_cg(g, tol, max_steps, chunk):
     return steps, np.sqrt(g.max_force_sq())
 
 
-def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False):
+def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False, cell_scale=1.0):
     """Mixed-precision conjugate-gradient bulk phase, then an FP64 phase from its positions to max|F| < tol64."""
-    g, variant = _cg_handle(ws, "mixed", tune)
+    g, variant = _cg_handle(ws, "mixed", tune, cell_scale)
     ta = _sync_time(g)
     s32, f32 = _minimise_cg(g, tol32, cap32, chunk)
     x = g.get_atoms(1)["x"]
@@ -553,7 +570,7 @@ def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False):
     g.close()
     from parm_gb300 import workloads as W
     w64 = W.Workload(ws.name, ws.ndim, ws.sizes, ws.L, x, np.zeros_like(x), ws.m, ws.kind, ws.params, ws.skin)
-    g64, _ = _cg_handle(w64, "fp64")
+    g64, _ = _cg_handle(w64, "fp64", cell_scale=cell_scale)
     tc = _sync_time(g64)
     s64, f64 = _minimise_cg(g64, tol64, cap64, chunk)
     td = _sync_time(g64)
@@ -580,7 +597,10 @@ def run_packings(args):
     tol32, tol64, chunk = 1e-7, 1e-12, 250
     cap32, cap64 = args.min_steps, args.min_steps
     log(f"packings: {nsys} systems, {w.n} atoms")
-    r = _cg_protocol(w, tol32, tol64, cap32, cap64, chunk, tune=True)
+    # skin, cell width and kernel variant tuned on the batch's first systems
+    w, cscale, tuned = _tuned(w, lambda ws: make_system(ws, "mixed", 0), lambda g, k: g.nlcg_timestep(k),
+                              (0.05, 0.1, 0.2, 0.3), prepare=_cg_prepare)
+    r = _cg_protocol(w, tol32, tol64, cap32, cap64, chunk, tune=True, cell_scale=cscale)
     wall = r["t32"] + r["t64"]
     conv = r["f64"] < tol64
     value = float(conv.sum()) / wall
@@ -596,7 +616,7 @@ def run_packings(args):
     nsingle = min(nsys, args.single_sys)
     t_single, c_single = 0.0, 0
     for q in range(nsingle):
-        rs = _cg_protocol(shard.select(w, [q]), tol32, tol64, cap32, cap64, chunk)
+        rs = _cg_protocol(shard.select(w, [q]), tol32, tol64, cap32, cap64, chunk, cell_scale=cscale)
         t_single += rs["t32"] + rs["t64"]
         c_single += int((rs["f64"] < tol64).sum())
     single_rate = c_single / t_single
@@ -608,7 +628,7 @@ def run_packings(args):
                       "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "skin": w.skin,
                       "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
                       "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_mixed": cap32, "step_cap_fp64": cap64,
-                      "steps_per_check": chunk, "kernel_variant": r["variant"]},
+                      "steps_per_check": chunk, "kernel_variant": r["variant"], "autotune": tuned},
            "wall_s": wall, "mixed_s": r["t32"], "fp64_s": r["t64"],
            "converged": int(conv.sum()), "converged_fraction": float(conv.mean()),
            "steps_median": {"mixed": float(np.median(r["s32"])), "fp64": float(np.median(r["s64"]))},
@@ -637,9 +657,19 @@ def run_replicas(args):
     steps, chunk = args.steps, 1000
     steps64 = min(steps, args.fp64_steps)
     res = {}
+
+    def make(ws):
+        g = make_system(ws, "mixed", 0)
+        g.set_graph_steps(50)
+        return g
+    w, cscale, tuned = _tuned(w, make, lambda g, k: g.sol(dt, damping, T, seed, k), (0.1, 0.2, 0.3, 0.45))
+    res["autotune"] = tuned
     for prec, nst in (("mixed", steps), ("fp64", steps64)):
         g = make_system(w, prec, 0)
         g.set_graph_steps(50)
+        if cscale != 1.0:
+            g.set_cell_scale(cscale)
+            g.nlist_update(False)
         if prec == "mixed":
             res["kernel"] = g.autotune()
         x0 = g.get_atoms(1)["x"]
@@ -667,7 +697,7 @@ def run_replicas(args):
            "data": "synthetic",
            "config": {"workload": f"wca_replicas_{nrep}", "replicas": nrep, "atoms": w.n, "n_range": [256, 32768],
                       "rho_range": [0.5, 0.9], "T": T, "damping": damping, "dt": dt, "steps": steps,
-                      "fp64_steps": steps64, "kernel": res["kernel"]},
+                      "fp64_steps": steps64, "kernel": res["kernel"], "skin": w.skin, "autotune": res["autotune"]},
            "fp64_value": res["fp64"]["atom_steps_per_s"],
            "mixed_vs_fp64": res["mixed"]["atom_steps_per_s"] / res["fp64"]["atom_steps_per_s"],
            "msd_batch_mean_rel_diff": [float(q) for q in msd_rel],

@@ -260,6 +260,12 @@ int parm_get_threads_per_atom(parm_system* s, uint32_t* tpa);
  * neighbours_per_iteration.  The state is left unchanged. */
 int parm_autotune(parm_system* s, uint32_t* tpa);
 
+/* Cells of the list builds no narrower than `scale` (1 .. 16, default 1)
+ * times the largest list radius: wider cells scan more candidates per atom
+ * in a rebuild and, for the cell-block kernels, change the blocks.  Results
+ * do not depend on it; the lists are rebuilt at the next update. */
+int parm_set_cell_scale(parm_system* s, double scale);
+
 /* Steps captured per CUDA graph launch (default 16; 0 launches kernels directly). */
 int parm_set_graph_steps(parm_system* s, uint32_t k);
 

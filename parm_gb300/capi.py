@@ -79,6 +79,7 @@ SIGNATURES = {
     "parm_set_nlist_capacity": (C.c_int, [_h, C.c_uint32]),
     "parm_get_nlist_capacity": (C.c_int, [_h, _u32p]),
     "parm_set_graph_steps": (C.c_int, [_h, C.c_uint32]),
+    "parm_set_cell_scale": (C.c_int, [_h, C.c_double]),
     "parm_set_threads_per_atom": (C.c_int, [_h, C.c_uint32]),
     "parm_autotune": (C.c_int, [_h, _u32p]),
     "parm_get_threads_per_atom": (C.c_int, [_h, _u32p]),

@@ -109,6 +109,7 @@ struct parm_system {
     bool stg_pending = false;    // grids changed under staged lists: switch back once every system rebuilt
     std::vector<uint32_t> stg_mark;   // which() of each system when the grids changed
     uint32_t stage_cap_override = 0;  // test hook (parm_debug_stage_cap)
+    double cell_scale = 1.0;          // cells no narrower than cell_scale x the list radius
     // page-locked words read back on the stream: [0] status, [1] rebuild
     // chains, [2, 2 + nsys) which() before a call, [2 + nsys, 2 + 2 nsys) after
     uint32_t* hst = nullptr;
@@ -216,7 +217,7 @@ struct parm_system {
             for (int d = 0; d < 3; d++) S.nc[d] = 1;
             if (any_member && rl > 0.0) {
                 for (int d = 0; d < nd; d++) {
-                    double w = rl * (1.0 + 1e-9);
+                    double w = rl * cell_scale * (1.0 + 1e-9);
                     double q = std::floor(S.L[d] / w);
                     int ncd = q >= 3.0 ? (int)std::min(q, 1024.0) : 1;
                     S.nc[d] = ncd;
@@ -242,6 +243,7 @@ struct parm_system {
             }
             S.skin = skin;
             S.rlist_max = rl;
+            S.cellmin = rl * cell_scale * (1.0 + 1e-9);
             S.rec_lim2 = (2.0 * skin + 0.5) * (2.0 * skin + 0.5);
             S.cell_off = total;
             bucket_off[s] = total;
@@ -1861,6 +1863,17 @@ int parm_get_threads_per_atom(parm_system* S, uint32_t* tpa) {
     else if (S->c.staged) *tpa = 200;
     else *tpa = S->c.tiled ? S->c.tpa : 100 + S->c.tpa;
     return PARM_OK;
+}
+
+int parm_set_cell_scale(parm_system* S, double scale) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (!(scale >= 1.0 && scale <= 16.0)) return fail(PARM_ERR_ARG, "cell scale must be in [1, 16]");
+    TRY(S->flush());
+    if (scale == S->cell_scale) return PARM_OK;
+    S->cell_scale = scale;
+    TRY(S->setup_cells());
+    // the next update rebuilds every list on the new grid
+    return S->kind >= 0 ? S->request_rebuild_all() : PARM_OK;
 }
 
 int parm_debug_stage_cap(parm_system* S, uint32_t cap) {

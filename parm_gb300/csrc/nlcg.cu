@@ -151,7 +151,7 @@ __global__ void k_nlcg_box(DevCtx c) {
     if (s >= c.nsys || !c.nlcg_step[s]) return;
     SysConst& S = const_cast<SysConst&>(c.sys[s]);
     const double f = c.nlcg[s].lfac;
-    const double w = S.rlist_max * (1.0 + 1e-9);
+    const double w = S.cellmin;
     const uint32_t ncell_old = S.ncell;
     bool regrid = false;
 #pragma unroll

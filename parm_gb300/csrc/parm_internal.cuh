@@ -46,6 +46,7 @@ struct SysConst {
     float L8[3], Lr8[3];   // L rounded to the 1/8 grid (exact in FP32) and L - L8
     double skin;
     double rlist_max;   // largest (d_i + d_j)/2 + skin
+    double cellmin;     // narrowest allowed cell (the list radius times the cell scale, with a margin)
     double rec_lim2;    // (2 skin + 1/2)^2: displacement limit of the cell-block records
     int nc[3];          // cells per axis (1 or >= 3)
     float cellw_inv[3]; // nc / L

@@ -265,6 +265,10 @@ class System:
     def set_step_counter(self, step: int) -> None:
         check(self.lib.parm_set_step(self.h, int(step)))
 
+    def set_cell_scale(self, scale: float) -> None:
+        """Cells no narrower than `scale` times the list radius (results do not depend on it)."""
+        check(self.lib.parm_set_cell_scale(self.h, float(scale)))
+
     def set_graph_steps(self, k: int) -> None:
         check(self.lib.parm_set_graph_steps(self.h, int(k)))
 

@@ -88,3 +88,22 @@ def test_lj_program_conserves_energy(tmp_path, built_lib):
     # total energy per atom stays within 1e-3 of its start over 20000 steps (the cut-off
     # potential's force jumps give a small random walk; no drift)
     assert np.abs(E - E0).max() <= 1e-3 * 200, (E0, E)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cell_scale_leaves_results_unchanged(precision):
+    """Wider cells (parm_set_cell_scale) change how lists are built, not what they hold."""
+    from helpers import make_gpu
+    w = W.small_random(n=3000, ndim=3, kind=0, seed=71, phi=0.4, skin=0.3)
+    out = []
+    for scale in (1.0, 1.7):
+        g = make_gpu(w, precision)
+        g.set_cell_scale(scale)
+        g.nlist_update(True)
+        g.set_forces(True)
+        g.verlet(0.001, 30)
+        out.append((g.pairs(), g.get_atoms()))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for k in ("x", "v", "f"):
+        np.testing.assert_array_equal(out[0][1][k], out[1][1][k])
