@@ -92,8 +92,10 @@ def test_lj_program_conserves_energy(tmp_path, built_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_cell_scale_leaves_results_unchanged(precision):
-    """Wider cells (parm_set_cell_scale) change how lists are built, not what they hold."""
-    from helpers import make_gpu
+    """Wider cells (parm_set_cell_scale) change how lists are built, not what they hold: the same
+    pairs in the same order; FP64 forces and trajectories bit for bit, mixed forces within the mixed
+    path's tolerance (a different cell grid can select another kernel variant)."""
+    from helpers import force_error, make_gpu
     w = W.small_random(n=3000, ndim=3, kind=0, seed=71, phi=0.4, skin=0.3)
     out = []
     for scale in (1.0, 1.7):
@@ -101,9 +103,14 @@ def test_cell_scale_leaves_results_unchanged(precision):
         g.set_cell_scale(scale)
         g.nlist_update(True)
         g.set_forces(True)
+        f0 = g.get_atoms(8)["f"]
         g.verlet(0.001, 30)
-        out.append((g.pairs(), g.get_atoms()))
+        out.append((g.pairs(), f0, g.get_atoms()))
         g.close()
     assert np.array_equal(out[0][0], out[1][0])
-    for k in ("x", "v", "f"):
-        np.testing.assert_array_equal(out[0][1][k], out[1][1][k])
+    if precision == "fp64":
+        np.testing.assert_array_equal(out[0][1], out[1][1])
+        for k in ("x", "v", "f"):
+            np.testing.assert_array_equal(out[0][2][k], out[1][2][k])
+    else:
+        assert force_error(out[1][1], out[0][1]) <= 1e-5
