@@ -40,6 +40,10 @@ extern "C" {
 #define PARM_LJCUT 0     /* NListed<EpsSigCutAtom, LennardJonesCutPair>; params (epsilon, sigma, sigcut) */
 #define PARM_REPULSION 1 /* NListed<EpsSigExpAtom, RepulsionPair>;      params (eps, sigma, exponent) */
 #define PARM_LJREPULSE 2 /* NListed<EpsSigAtom, LJRepulsePair>;         params (epsilon, sigma, unused) */
+#define PARM_LJATTRACTCUT 3 /* NListed<EpsSigCutAtom, LJAttractCutPair> (pyparm's LJAttractCut):
+                               LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
+                               1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
+                               on the per-atom kernels */
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u

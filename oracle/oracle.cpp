@@ -37,7 +37,7 @@
 
 namespace {
 
-enum PairKind { LJCUT = 0, REPULSION = 1, LJREPULSE = 2 };
+enum PairKind { LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3 };
 
 struct V3 {
     double c[3] = {0, 0, 0};
@@ -101,6 +101,22 @@ struct System {
             double rsix = std::pow(pc.third, 6);
             double mid = (1 - 1 / rsix);
             pc.cut_energy = pc.eps * (mid * mid - 1);
+        } else if (kind == LJATTRACT) {
+            // LJAttractCutPair(EpsSigCutAtom, EpsSigCutAtom) (interaction.hpp:1020-1027)
+            // and LJAttractCut ctor (interaction.hpp:203-208): cut_energy = LJAttract::energy(cut) * eps
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2;
+            pc.third = std::max(A.p2, B.p2);
+            double e;   // LJAttract::energy(rsig) (interaction.hpp:170-177)
+            if (pc.third < 1) {
+                e = -1;
+            } else {
+                double rsq = pc.third * pc.third;
+                double rsix = rsq * rsq * rsq;
+                double mid = (1 - 1 / rsix);
+                e = mid * mid - 1;
+            }
+            pc.cut_energy = e * pc.eps;
         } else if (kind == REPULSION) {
             // RepulsionPair(EpsSigExpAtom, EpsSigExpAtom) (interaction.hpp:1532-1537)
             pc.eps = std::sqrt(A.p0 * B.p0);
@@ -127,6 +143,20 @@ struct System {
             double rsix = rsq * rsq * rsq;
             double mid = (1 - 1 / rsix);
             return pc.eps * (mid * mid - 1) - pc.cut_energy;
+        } else if (kind == LJATTRACT) {
+            // LJAttractCut::energy (interaction.hpp:211-216), LJAttract::energy (162-169)
+            if (pc.eps == 0) return 0;
+            if (dsq > (pc.third * pc.third * pc.sig * pc.sig)) return 0;
+            double rsq = dsq / (pc.sig * pc.sig);
+            double e;
+            if (rsq < 1) {
+                e = -pc.eps;
+            } else {
+                double rsix = rsq * rsq * rsq;
+                double mid = (1 - 1 / rsix);
+                e = pc.eps * (mid * mid - 1);
+            }
+            return e - pc.cut_energy;
         } else if (kind == REPULSION) {
             // RepulsionPair::energy (interaction.hpp:1544-1550)
             if (dsq > pc.sig * pc.sig) return 0.0;
@@ -153,6 +183,16 @@ struct System {
             double rsix = rsq * rsq * rsq;
             double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
             s = fmagTimesR / dsq;
+        } else if (kind == LJATTRACT) {
+            // LJAttractCut::forces (interaction.hpp:219-229)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (pc.eps == 0 || rsq < 1 || rsq > (pc.third * pc.third)) {
+                for (int d = 0; d < nd; d++) fo[d] = 0;
+                return false;
+            }
+            double rsix = rsq * rsq * rsq;
+            double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
+            s = fmagTimesR / dsq;
         } else if (kind == REPULSION) {
             // RepulsionPair::forces (interaction.hpp:1551-1556)
             if (dsq > pc.sig * pc.sig) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
@@ -172,7 +212,7 @@ struct System {
 
     double max_size(uint32_t i) const {
         // EpsSigCutAtom::max_size (interaction.hpp:904), EpsSigExpAtom (1464), EpsSigAtom (864)
-        if (kind == LJCUT) return params[i].p1 * params[i].p2;
+        if (kind == LJCUT || kind == LJATTRACT) return params[i].p1 * params[i].p2;
         return params[i].p1;
     }
 
@@ -719,7 +759,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 2) return -1;
+    if (kind < 0 || kind > 3) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;

@@ -8,7 +8,7 @@
 //   integrators 3 and 4 add one line: dt P0 kappa kmax secmax seceps alphamax afrac
 //   dxmax stepmax maxdV
 // kind: 0 NListed<EpsSigCutAtom,LennardJonesCutPair>, 1 <EpsSigExpAtom,RepulsionPair>,
-//       2 <EpsSigAtom,LJRepulsePair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
+//       2 <EpsSigAtom,LJRepulsePair>, 3 <EpsSigCutAtom,LJAttractCutPair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
 //       4 CollectionNLCGV (constructor, then reset())
@@ -166,5 +166,6 @@ int main() {
     double dt = rd(), damping = rd(), T = rd(), skin = rd();
     if (kind == 0) return run<EpsSigCutAtom, LennardJonesCutPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 1) return run<EpsSigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 3) return run<EpsSigCutAtom, LJAttractCutPair>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

@@ -26,6 +26,7 @@ MIXED = 1
 LJCUT = 0
 REPULSION = 1
 LJREPULSE = 2
+LJATTRACTCUT = 3
 
 X, V, A, F, M = 1, 2, 4, 8, 16
 

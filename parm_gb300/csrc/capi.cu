@@ -202,7 +202,7 @@ struct parm_system {
             if (kind < 0 || rank_in[i] == PARM_NOT_MEMBER) continue;
             any_member = true;
             const double* p = &prm_in[3 * (size_t)i];
-            double d = (kind == PARM_LJCUT) ? p[1] * p[2] : p[1];
+            double d = (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) ? p[1] * p[2] : p[1];
             if (!ldiam.empty() && std::isfinite(ldiam[i])) d = ldiam[i];
             dmax = std::max(dmax, d);
         }
@@ -319,7 +319,9 @@ struct parm_system {
     // skin.  Sets stg_ok and, when the blocks are not usable, c.staged = 0.
     int plan_blocks() {
         stg_ok = false;
-        if (prec != PREC_MIXED || kind < 0) {
+        // the cell-block kernels serve the LJ, repulsion and WCA laws; the
+        // attractive LJ runs on the per-atom kernels
+        if (prec != PREC_MIXED || kind < 0 || kind == PARM_LJATTRACTCUT) {
             c.staged = 0;
             return PARM_OK;
         }
@@ -1313,7 +1315,7 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > 2) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > 3) return fail(PARM_ERR_ARG, "unknown pair kind");
     if (!(skin >= 0.0) || !std::isfinite(skin)) return fail(PARM_ERR_ARG, "skin must be >= 0");
     TRY(S->flush());
     CUDA_TRY(cudaStreamSynchronize(S->st));
@@ -1347,9 +1349,21 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             const double* p = &params[3 * (size_t)g];
             AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], 0.0};
             if (kind == PARM_LJCUT) a.p3 = 1 - 1 / std::pow(a.p2, 6);  // LennardJonesCut ctor
+            if (kind == PARM_LJATTRACTCUT) {
+                // LJAttract::energy(cut) (interaction.hpp:170-177), times epsilon in the pair
+                const double rsig = a.p2;
+                if (rsig < 1) {
+                    a.p3 = -1;
+                } else {
+                    const double rsq = rsig * rsig;
+                    const double rsix = rsq * rsq * rsq;
+                    const double mid = (1 - 1 / rsix);
+                    a.p3 = mid * mid - 1;
+                }
+            }
             prm[g] = a;
             prm32[g] = make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
-            diam[g] = (kind == PARM_LJCUT) ? a.p1 * a.p2 : a.p1;   // A::max_size()
+            diam[g] = (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) ? a.p1 * a.p2 : a.p1;   // A::max_size()
             const bool explicit_d = !S->ldiam.empty() && std::isfinite(S->ldiam[g]);
             if (explicit_d) diam[g] = S->ldiam[g];   // NeighborList::add(atom, diameter)
             if (S->rank_in[g] == PARM_NOT_MEMBER) {

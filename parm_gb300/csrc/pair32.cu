@@ -113,11 +113,11 @@ __global__ void __launch_bounds__(BLOCK) k_force32(DevCtx c) {
                     e12 = (KIND == KIND_REPULSION) ? eps : 12.0f * eps;
                     sig = 0.5f * (Qi.y + Qj.y);
                     isig2 = __fdividef(1.0f, sig * sig);
-                    third = (KIND == KIND_LJCUT) ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
+                    third = cut_kind<KIND>() ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
                 }
                 bool near_cut;
                 float sc = scale32<KIND>(d2, e12, sig, isig2, third, near_cut);
-                if constexpr (KIND == KIND_LJCUT) {
+                if constexpr (cut_kind<KIND>()) {
                     // pairs within the band are added here as if inside the
                     // cut-off and settled by the exact test after the loop
                     if (near_cut) {
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(BLOCK) k_force32(DevCtx c) {
                 for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sc, f[d]);
             }
         }
-        if constexpr (KIND == KIND_LJCUT) {
+        if constexpr (cut_kind<KIND>()) {
             if (any_band) {
                 // rare: remove the band pairs that the exact FP64 test puts
                 // beyond the cut-off (same FP32 contribution as added above)
@@ -265,11 +265,11 @@ __global__ void __launch_bounds__(TILE_ATOMS * TPA) k_force32t(DevCtx c) {
                 e12 = (KIND == KIND_REPULSION) ? eps : 12.0f * eps;
                 sig = 0.5f * (Qi.y + Qj.y);
                 isig2 = __fdividef(1.0f, sig * sig);
-                third = (KIND == KIND_LJCUT) ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
+                third = cut_kind<KIND>() ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
             }
             bool near_cut;
             float sc = scale32<KIND>(d2, e12, sig, isig2, third, near_cut);
-            if constexpr (KIND == KIND_LJCUT) {
+            if constexpr (cut_kind<KIND>()) {
                 if (near_cut) {   // settled by the exact test after the loop
                     const float rsq = d2 * isig2;
                     const float ir = __fdividef(1.0f, rsq);
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(TILE_ATOMS * TPA) k_force32t(DevCtx c) {
 #pragma unroll
             for (int d = 0; d < ND; d++) f[d] = fmaf(r[d], sc, f[d]);
         }
-        if constexpr (KIND == KIND_LJCUT) {
+        if constexpr (cut_kind<KIND>()) {
             if (any_band) {
                 for (uint32_t k = sub; k < nn; k += TPA) {
                     const uint32_t e = lst[(size_t)k * TILE_ATOMS];
@@ -360,8 +360,8 @@ __global__ void __launch_bounds__(BLOCK) k_eval32(DevCtx c, int what) {
             if constexpr (ND == 3) d2 += r[2] * r[2];
             const float4 Qj = c.prm32[j];
             float eps = Qi.x * Qj.x, sig = 0.5f * (Qi.y + Qj.y);
-            float third = (KIND == KIND_LJCUT) ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
-            float m6 = (KIND == KIND_LJCUT) ? (Qj.z > Qi.z ? Qj.w : Qi.w) : 0.f;
+            float third = cut_kind<KIND>() ? fmaxf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
+            float m6 = cut_kind<KIND>() ? (Qj.z > Qi.z ? Qj.w : Qi.w) : 0.f;
             if (what == EV_ENERGY || what == EV_CONTACTS || what == EV_OVERLAPS) {
                 float e = energy32<KIND>(d2, eps, sig, third, m6);
                 if (what == EV_ENERGY) acc[0] += (double)e;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(BLOCK) k_eval32(DevCtx c, int what) {
                 bool near_cut;
                 const float e12 = (KIND == KIND_REPULSION) ? eps : 12.0f * eps;
                 float sc = scale32<KIND>(d2, e12, sig, 1.0f / (sig * sig), third, near_cut);
-                if constexpr (KIND == KIND_LJCUT) {
+                if constexpr (cut_kind<KIND>()) {
                     if (near_cut && lj_beyond_exact(c, S, i, j, ND)) sc = 0.0f;
                     else if (near_cut) {
                         const float rsq = d2 / (sig * sig);
@@ -439,6 +439,7 @@ static void force32_nd_kind(const DevCtx& c, cudaStream_t s, int mode) {
 template <int ND>
 static void force32_nd(const DevCtx& c, cudaStream_t s, int mode) {
     if (c.kind == KIND_LJCUT) force32_nd_kind<ND, KIND_LJCUT>(c, s, mode);
+    else if (c.kind == KIND_LJATTRACT) force32_nd_kind<ND, KIND_LJATTRACT>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force32_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force32_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -453,6 +454,7 @@ template <int ND>
 static void eval32_nd(const DevCtx& c, cudaStream_t s, int what) {
     unsigned g = grid_for(c.n);
     if (c.kind == KIND_LJCUT) k_eval32<ND, KIND_LJCUT><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJATTRACT) k_eval32<ND, KIND_LJATTRACT><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval32<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval32<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

@@ -7,6 +7,7 @@
 //   LennardJonesCut + LennardJonesCutPair   238-281, 967-987
 //   RepulsionPair                           1528-1590
 //   LJRepulsive + LJRepulsePair             119-152, 875-891
+//   LJAttractCut + LJAttractCutPair         154-236, 1020-1050
 //
 // Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
 // scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
@@ -34,8 +35,8 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
     // eps = sqrt(e1*e2) (sqrt(e*e) == e exactly, so uniform epsilon skips it)
     p.eps = (uni & UNI_EPS) ? A.p0 : sqrt(A.p0 * B.p0);
     p.sig = (uni & UNI_SIG) ? A.p1 : (A.p1 + B.p1) / 2;
-    if constexpr (KIND == KIND_LJCUT) {
-        // cut = max(a1.sigcut, a2.sigcut); its pow(cut, 6) term travels with it
+    if constexpr (cut_kind<KIND>()) {
+        // cut = max(a1.sigcut, a2.sigcut); its cut-energy term travels with it
         bool b_larger = B.p2 > A.p2;
         p.third = b_larger ? B.p2 : A.p2;
         p.m6 = b_larger ? B.p3 : A.p3;
@@ -66,6 +67,15 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
         double pw = (p.third == 2.0) ? b : pow(b, p.third - 1);   // pow(b, 1) == b exactly
         s = p.eps * pw / p.sig / R;
         return true;
+    } else if constexpr (KIND == KIND_LJATTRACT) {
+        // LJAttractCut::forces (interaction.hpp:219-229)
+        if (p.eps == 0) return false;
+        double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
+        if (rsq < 1 || rsq > (p.third * p.third)) return false;
+        double rsix = rsq * rsq * rsq;
+        double fmagTimesR = 12 * p.eps / rsix * (1 / rsix - 1);
+        s = fmagTimesR / dsq;
+        return true;
     } else {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
         if (rsq > 1) return false;
@@ -91,6 +101,20 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         double b = 1.0 - (R / p.sig);
         double pw = (p.third == 2.0) ? b * b : pow(b, p.third);   // pow(b, 2) == b*b exactly
         return p.eps * pw / p.third;
+    } else if constexpr (KIND == KIND_LJATTRACT) {
+        // LJAttractCut::energy (interaction.hpp:211-216) with LJAttract::energy (162-169)
+        if (p.eps == 0) return 0.0;
+        if (dsq > (p.third * p.third * p.sig * p.sig)) return 0.0;
+        double rsq = dsq / (p.sig * p.sig);
+        double e;
+        if (rsq < 1) {
+            e = -p.eps;
+        } else {
+            double rsix = rsq * rsq * rsq;
+            double mid = (1 - 1 / rsix);
+            e = p.eps * (mid * mid - 1);
+        }
+        return e - p.m6 * p.eps;
     } else {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
         if (rsq > 1) return 0.0;
@@ -106,7 +130,7 @@ __device__ __forceinline__ bool beyond32(float d2, float sig32i, float sig32j, f
                                          float th32j, uint32_t uni) {
     float sg = (uni & UNI_SIG) ? sig32i : 0.5f * (sig32i + sig32j);
     float rc;
-    if constexpr (KIND == KIND_LJCUT) rc = sg * fmaxf(th32i, th32j);
+    if constexpr (cut_kind<KIND>()) rc = sg * fmaxf(th32i, th32j);
     else rc = sg;
     return d2 > rc * rc * 1.0002f;
 }
@@ -268,6 +292,7 @@ static void force64_nd_kind(const DevCtx& c, cudaStream_t s, int mode) {
 template <int ND>
 static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     if (c.kind == KIND_LJCUT) force64_nd_kind<ND, KIND_LJCUT>(c, s, mode);
+    else if (c.kind == KIND_LJATTRACT) force64_nd_kind<ND, KIND_LJATTRACT>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -280,6 +305,7 @@ template <int ND>
 static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     unsigned g = grid_for(c.n);
     if (c.kind == KIND_LJCUT) k_eval64<ND, KIND_LJCUT><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJATTRACT) k_eval64<ND, KIND_LJATTRACT><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

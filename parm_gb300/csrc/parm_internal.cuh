@@ -22,7 +22,11 @@
 
 namespace parm {
 
-enum PairKind : int { KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2 };
+enum PairKind : int { KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2, KIND_LJATTRACT = 3 };
+// kinds whose pair cut-off is max(sigcut_i, sigcut_j) sigma_ij, with a force
+// that jumps there (LJ truncated without shift)
+template <int KIND>
+__host__ __device__ constexpr bool cut_kind() { return KIND == KIND_LJCUT || KIND == KIND_LJATTRACT; }
 enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 // status bits (device word, read back by the host after synchronising calls)
@@ -60,6 +64,7 @@ struct SysConst {
 
 // per-atom FP64 parameters of the pair interaction (kind dependent)
 //   LJCUT:     p0 = epsilon, p1 = sigma, p2 = sigcut, p3 = 1 - 1/pow(sigcut, 6)
+//   LJATTRACT: p0 = epsilon, p1 = sigma, p2 = sigcut, p3 = LJAttract::energy(sigcut)
 //   REPULSION: p0 = eps,     p1 = sigma, p2 = exponent
 //   LJREPULSE: p0 = epsilon, p1 = sigma
 struct AtomPrm {

@@ -1,6 +1,7 @@
 // FP32 pair laws shared by the mixed-precision pair kernels (pair32.cu,
 // staged.cu).  Same laws as the FP64 path (reference src/interaction.hpp:
-// LennardJonesCut 238-281, RepulsionPair 1528-1590, LJRepulsive 119-152).
+// LennardJonesCut 238-281, RepulsionPair 1528-1590, LJRepulsive 119-152,
+// LJAttractCut 154-236).
 #pragma once
 #include "parm_ctx.cuh"
 
@@ -20,13 +21,16 @@ template <int KIND>
 __device__ __forceinline__ float scale32(float d2, float e12, float sig, float isig2, float third,
                                          bool& near_cut) {
     near_cut = false;
-    if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
+    if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE || KIND == KIND_LJATTRACT) {
         const float rsq = d2 * isig2;
-        const float cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
-        if constexpr (KIND == KIND_LJCUT) near_cut = fabsf(rsq - cut2) <= CUT_BAND * cut2;
+        const float cut2 = cut_kind<KIND>() ? third * third : 1.0f;
+        if constexpr (cut_kind<KIND>()) near_cut = fabsf(rsq - cut2) <= CUT_BAND * cut2;
         const float ir = __fdividef(1.0f, rsq);
         const float ir3 = ir * ir * ir;   // 1 / rsix
         const float sc = e12 * ir3 * (ir3 - 1.0f) * ir * isig2;   // fmagTimesR / dsq
+        // LJAttractCut: no force inside sigma (the force is continuous there)
+        if constexpr (KIND == KIND_LJATTRACT)
+            if (rsq < 1.0f) return 0.0f;
         return rsq > cut2 ? 0.0f : sc;
     } else {
         if (d2 > sig * sig) return 0.0f;
@@ -45,7 +49,17 @@ __device__ __forceinline__ float scale32(float d2, float e12, float sig, float i
 
 template <int KIND>
 __device__ __forceinline__ float energy32(float d2, float eps, float sig, float third, float m6) {
-    if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
+    if constexpr (KIND == KIND_LJATTRACT) {
+        float rsq = d2 / (sig * sig);
+        if (eps == 0.0f || rsq > third * third) return 0.0f;
+        float e = -eps;
+        if (rsq >= 1.0f) {
+            float ir3 = 1.0f / (rsq * rsq * rsq);
+            float mid = 1.0f - ir3;
+            e = eps * (mid * mid - 1.0f);
+        }
+        return e - m6 * eps;
+    } else if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJREPULSE) {
         float rsq = d2 / (sig * sig);
         float cut2 = (KIND == KIND_LJCUT) ? third * third : 1.0f;
         if (rsq > cut2) return 0.0f;

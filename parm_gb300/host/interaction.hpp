@@ -7,6 +7,7 @@
 //   NListed<EpsSigCutAtom, LennardJonesCutPair>  LJ cut at sigcut * sigma
 //   NListed<EpsSigExpAtom, RepulsionPair>         soft repulsion, exponent n
 //   NListed<EpsSigAtom,    LJRepulsePair>         WCA (repulsive LJ)
+//   NListed<EpsSigCutAtom, LJAttractCutPair>     attractive LJ cut at sigcut * sigma
 // Sums over the pair list (forces, energies, virials, stresses) run on the
 // GPU.  A pair object (get_pair, pair_iter) also evaluates its own energy and
 // force on the host, with the reference's formulas, for code that inspects
@@ -174,6 +175,55 @@ struct LJRepulsePair {
         const flt dsq = diff.squaredNorm();
         const flt rsq = dsq / (sigma * sigma);
         if (rsq > 1) return Vec::Zero();
+        const flt rsix = rsq * rsq * rsq;
+        const flt fmagTimesR = 12 * epsilon / rsix * (1 / rsix - 1);
+        return diff * (fmagTimesR / dsq);
+    }
+};
+
+//! Attractive LJ (pyparm's LJAttractCut): V = eps((1 - sigma^6/r^6)^2 - 1) for
+//! sigma <= r <= cut, -eps inside sigma, shifted by V(cut)
+//! (src/interaction.hpp:154-236, 1020-1050).
+struct LJAttractCutPair {
+    static const int kind = PARM_LJATTRACTCUT;
+    static void params(const EpsSigCutAtom& a, double p[3]) {
+        p[0] = a.epsilon;
+        p[1] = a.sigma;
+        p[2] = a.sigcut;
+    }
+    flt epsilon, sigma, cut_distance, cut_energy;
+    AtomID atom1, atom2;
+    LJAttractCutPair(EpsSigCutAtom a1, EpsSigCutAtom a2)
+        : epsilon(std::sqrt(a1.epsilon * a2.epsilon)),
+          sigma((a1.sigma + a2.sigma) / 2),
+          cut_distance(std::max(a1.sigcut, a2.sigcut)),
+          atom1(a1),
+          atom2(a2) {
+        flt e = -1;   // the unit-epsilon attraction at the cut
+        if (cut_distance >= 1) {
+            const flt rsq = cut_distance * cut_distance;
+            const flt rsix = rsq * rsq * rsq;
+            const flt mid = (1 - 1 / rsix);
+            e = mid * mid - 1;
+        }
+        cut_energy = e * epsilon;
+    }
+    flt energy(Box& box) {
+        if (epsilon == 0) return 0;
+        const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
+        if (dsq > (cut_distance * cut_distance * sigma * sigma)) return 0;
+        const flt rsq = dsq / (sigma * sigma);
+        if (rsq < 1) return -epsilon - cut_energy;
+        const flt rsix = rsq * rsq * rsq;
+        const flt mid = (1 - 1 / rsix);
+        return epsilon * (mid * mid - 1) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        if (epsilon == 0) return Vec::Zero();
+        const Vec diff = box.diff(atom1->x, atom2->x);
+        const flt dsq = diff.squaredNorm();
+        const flt rsq = dsq / (sigma * sigma);
+        if (rsq < 1 || rsq > (cut_distance * cut_distance)) return Vec::Zero();
         const flt rsix = rsq * rsq * rsq;
         const flt fmagTimesR = 12 * epsilon / rsix * (1 / rsix - 1);
         return diff * (fmagTimesR / dsq);

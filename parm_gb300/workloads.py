@@ -123,6 +123,6 @@ def small_random(n=64, ndim=3, kind=0, phi=0.3, bidisperse=True, seed=0, skin=0.
         Lside = np.sqrt(np.sum(np.pi * sig ** 2 / 4) / phi)
     x = rng.uniform(0, Lside, size=(n, ndim))
     v = rng.normal(size=(n, ndim))
-    third = {0: LJ_SIGCUT, 1: exponent, 2: 0.0}[kind]
+    third = {0: LJ_SIGCUT, 1: exponent, 2: 0.0, 3: LJ_SIGCUT}[kind]
     params = np.stack([np.full(n, 1.2), sig, np.full(n, third)], 1)
     return Workload(f"small{n}", ndim, [n], np.full((1, ndim), Lside), x, v, sig ** ndim, kind, params, skin, {})

@@ -34,7 +34,7 @@ REFBUILD = ROOT / "oracle" / "refbuild"
 REFOUT = ROOT / "oracle" / "_ref"
 
 VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
-LJCUT, REPULSION, LJREPULSE = 0, 1, 2
+LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -202,6 +202,15 @@ def cases() -> list[dict]:
     params = np.tile([1.0, 2.0, 2.0], (n, 1))     # cut = sigma = 2.0, list radius 2.5
     out.append(_case("edges64_pairs", REPULSION, VERLET, 50, 0.005, Lb, x, rng.normal(0, 0.3, (n, 3)),
                      np.ones(n), params, 0.5, [1, 20, 50]))
+    # 12. LJAttractCutPair (pyparm's LJAttractCut): attraction only, per-atom epsilon and sigma,
+    #     Verlet from a jittered lattice
+    rng = np.random.default_rng(51)
+    L, x, v = lj_lattice_deck((8, 8, 8), 51)
+    n = len(x)
+    eps = rng.choice([0.8, 1.2], n)
+    sg = rng.choice([1.0, 1.2], n)
+    out.append(_case("ljattract512_verlet", LJATTRACT, VERLET, 300, 0.002, L, x, v, np.ones(n),
+                     np.stack([eps, sg, np.full(n, cut)], 1), 0.3, [1, 10, 100, 300]))
     # 9. CollectionNLCG (box and positions), 3D harmonic spheres from phi = 0.4 at the goal
     #    pressure 1e-3, set up as pyparm's packmin.Minimizer (dt 0.1, kappa 10, kmax 1000,
     #    secmax 40, seceps 1e-20, alphamax 2, dxmax 100, stepmax 1e-3); one immobile atom

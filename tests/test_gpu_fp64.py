@@ -31,7 +31,7 @@ def test_remainder_matches_ieee():
     assert np.array_equal(np.signbit(got), np.signbit(want))
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
 @pytest.mark.parametrize("ndim", [2, 3])
 def test_pairs_and_forces_bit_exact(kind, ndim):
     w = W.small_random(n=500, ndim=ndim, kind=kind, seed=3 * kind + ndim, phi=0.45)

@@ -78,6 +78,22 @@ def test_mixed_wca_fluid():
     assert err <= FORCE_TOL, err
 
 
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_mixed_attractive_lj(ndim):
+    """LJAttractCutPair (per-atom epsilon and sigma) on the mixed path's per-atom kernels."""
+    w = W.small_random(n=3000, ndim=ndim, kind=3, seed=33 + ndim, phi=0.35, skin=0.3)
+    m = make_gpu(w, "mixed")
+    o = make_oracle(w)
+    m.nlist_update(True)
+    o.nl_update(True)
+    assert np.array_equal(m.pairs(), o.pairs())
+    m.set_forces(True)
+    o.set_forces(True)
+    err = force_error(m.get_atoms()["f"], o.get_state()["f"])
+    assert err <= FORCE_TOL, err
+    assert abs(m.energy()[0] - o.energy()) <= ENERGY_TOL * abs(o.energy())
+
+
 def test_mixed_2d_disks():
     w = W.soft_disks(n=4096, phi=0.84)
     m = make_gpu(w, "mixed")
@@ -90,22 +106,36 @@ def test_mixed_2d_disks():
     assert err <= FORCE_TOL, err
 
 
+def _drift(g, steps, every):
+    """Least-squares slope of the total energy (per 10^5 steps, relative to |E(0)|) and its standard error."""
+    E = [g.energy()[0] + g.kinetic_energy()[0]]
+    for _ in range(steps // every):
+        g.verlet(0.002, every)
+        E.append(g.energy()[0] + g.kinetic_energy()[0])
+    E = np.array(E)
+    t = np.arange(len(E), dtype=np.float64) * every
+    A = np.stack([t, np.ones_like(t)], 1)
+    coef = np.linalg.lstsq(A, E, rcond=None)[0]
+    resid = E - A @ coef
+    se = np.sqrt((resid ** 2).sum() / (len(E) - 2) / ((t - t.mean()) ** 2).sum())
+    scale = 1e5 / abs(E[0])
+    return coef[0] * scale, se * scale
+
+
 def test_mixed_nve_drift_comparable(lj32k):
-    """NVE energy drift of the mixed path stays within a few times the FP64 path's."""
+    """NVE energy drift of the mixed path is the FP64 path's: over 20000 steps from the same state the
+    fitted slopes (per 10^5 steps, relative) differ by less than three combined standard errors plus
+    1e-5, and the mixed slope is below 1e-4."""
     w = lj32k
     out = {}
     for prec in ("fp64", "mixed"):
         g = make_gpu(w, prec)
         g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
-        E = []
-        for _ in range(20):
-            g.verlet(0.002, 50)
-            E.append(g.energy()[0] + g.kinetic_energy()[0])
-        t = np.arange(len(E))
-        slope = np.polyfit(t, E, 1)[0] / 50   # per step
-        out[prec] = abs(slope) * 1e5 / abs(np.mean(E))
-    # drift per 1e5 steps, relative to |E|
-    assert out["mixed"] <= max(5 * out["fp64"], 1e-4), out
+        out[prec] = _drift(g, 20000, 100)
+        g.close()
+    (d64, se64), (d32, se32) = out["fp64"], out["mixed"]
+    assert abs(d32 - d64) <= 3 * np.hypot(se32, se64) + 1e-5, out
+    assert abs(d32) <= 1e-4, out
 
 
 @pytest.mark.parametrize("tpa", [200, 1, 2, 4, 101, 104, 108, 116, 132])
