@@ -399,6 +399,8 @@ struct parm_system {
     int maybe_restage() {
         if (!stg_pending || !want_staged || !stg_ok || c.staged) return PARM_OK;
         std::vector<uint32_t> w(nsys);
+        // the handle's stream does not order with the legacy stream of cudaMemcpy
+        CUDA_TRY(cudaStreamSynchronize(st));
         CUDA_TRY(cudaMemcpy(w.data(), c.which, 4 * nsys, cudaMemcpyDeviceToHost));
         for (uint32_t s = 0; s < nsys; s++)
             if (w[s] == stg_mark[s]) return PARM_OK;
@@ -473,6 +475,7 @@ struct parm_system {
 
     int request_rebuild_all() {
         std::vector<uint32_t> ones(nsys, 1u);
+        CUDA_TRY(cudaStreamSynchronize(st));   // a pending test on the stream may still read the flags
         CUDA_TRY(cudaMemcpy(c.force_rb, ones.data(), 4 * nsys, cudaMemcpyHostToDevice));
         return PARM_OK;
     }
@@ -899,6 +902,7 @@ struct parm_system {
         TRY(nlcg_prepare());
         std::vector<double> hp((size_t)nsys * (sizeof(NlcgSys) / 8));
         uint32_t max_sec = 0;
+        CUDA_TRY(cudaStreamSynchronize(st));
         CUDA_TRY(cudaMemcpy(hp.data(), c.nlcg, sizeof(NlcgSys) * nsys, cudaMemcpyDeviceToHost));
         for (uint32_t s = 0; s < nsys; s++)
             max_sec = std::max(max_sec, (uint32_t)std::min(1e6, hp[(size_t)s * (sizeof(NlcgSys) / 8) + 4]));
@@ -1448,6 +1452,7 @@ int parm_nlist_ignore(parm_system* S, uint32_t a, uint32_t b) {
     uint32_t sa = (uint32_t)(std::upper_bound(S->off.begin(), S->off.end(), a) - S->off.begin() - 1);
     uint32_t sb = (uint32_t)(std::upper_bound(S->off.begin(), S->off.end(), b) - S->off.begin() - 1);
     uint32_t one = 1;
+    CUDA_TRY(cudaStreamSynchronize(S->st));
     CUDA_TRY(cudaMemcpy(S->c.force_rb + sa, &one, 4, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.force_rb + sb, &one, 4, cudaMemcpyHostToDevice));
     return PARM_OK;
@@ -1482,6 +1487,7 @@ int parm_nlist_update(parm_system* S, int force, uint8_t* rebuilt) {
 int parm_nlist_which(parm_system* S, uint32_t* which) {
     if (!S || !which) return fail(PARM_ERR_ARG, "NULL argument");
     TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));   // the pending test may still run on the handle's stream
     CUDA_TRY(cudaMemcpy(which, S->c.which, 4 * S->nsys, cudaMemcpyDeviceToHost));
     return PARM_OK;
 }
@@ -1502,6 +1508,7 @@ int parm_nlist_pairs(parm_system* S, uint32_t sys, uint32_t* pairs, uint64_t cap
     if (sys >= S->nsys) return fail(PARM_ERR_ARG, "system index out of range");
     TRY(S->flush());
     TRY(S->rowmajor());
+    CUDA_TRY(cudaStreamSynchronize(S->st));   // lists of a pending rebuild, complete
     const uint32_t o = S->off[sys], na = S->natoms[sys], mx = S->c.maxnb;
     std::vector<uint32_t> nnb(na), rank(S->n), orig(na), nbr((size_t)na * mx);
     CUDA_TRY(cudaMemcpy(nnb.data(), S->c.nnb + o, 4 * (size_t)na, cudaMemcpyDeviceToHost));

@@ -243,12 +243,14 @@ void gpu_add_forces(GpuLink& link);
 template <class A, class P>
 class NListed : public Interaction, public GpuInteraction {
    public:
-    NListed(sptr<AtomVec> vec, sptr<NeighborList> neighbors)
-        : link(neighbors->gpu()), neighbors(neighbors), atoms(vec->size()) {
+    NListed(sptr<AtomVec> vec, sptr<NeighborList> neighbors) : link(neighbors->gpu()), neighbors(neighbors) {
         if (link->atoms() != vec) throw std::invalid_argument("NListed: the NeighborList tracks another AtomVec");
+        init_atoms(*vec);
     }
     NListed(sptr<Box> box, sptr<AtomVec> atomv, const flt skin)
-        : link(new GpuLink(box, atomv, skin)), neighbors(new NeighborList(link)), atoms(atomv->size()) {}
+        : link(new GpuLink(box, atomv, skin)), neighbors(new NeighborList(link)) {
+        init_atoms(*atomv);
+    }
     void add(A atm) {
         double p[3];
         P::params(atm, p);
@@ -293,9 +295,16 @@ class NListed : public Interaction, public GpuInteraction {
     sptr<GpuLink> gpu() override { return link; }
 
    private:
+    // every entry names its atom, with default parameters until add() sets
+    // them: a list member that no add() gave parameters (NeighborList::add)
+    // then forms pairs of zero force, as on the GPU
+    void init_atoms(AtomVec& v) {
+        atoms.reserve(v.size());
+        for (uint i = 0; i < v.size(); i++) atoms.push_back(A(v.get_id(i), A()));
+    }
     sptr<GpuLink> link;
     sptr<NeighborList> neighbors;
-    std::vector<A> atoms;   // indexed by AtomVec index; unset entries are A()
+    std::vector<A> atoms;   // indexed by AtomVec index
     std::vector<P> pairs;
 };
 

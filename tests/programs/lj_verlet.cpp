@@ -3,7 +3,9 @@
 // own NeighborList, atoms placed one at a time with update_list(true) and
 // energy() after each, a CollectionVerlet with the list as a tracker,
 // reset_com_velocity and scale_velocities_to_energy, then blocks of 1000
-// timestep() calls with the energies printed after each block.
+// timestep() calls with the energies printed after each block.  As in the
+// reference's program, the interaction is added after the Collection's
+// initialisation, so the first step starts from zero accelerations.
 // Prints "E0 <energy>" and "block <k> E <energy> K <kinetic> U <potential>".
 #include <cmath>
 #include <cstdio>
