@@ -321,7 +321,14 @@ def energy_drift(w, precision, steps, sample_every=100, graph_steps=50):
     dof = max(1, len(E) - 2)
     se = math.sqrt((resid ** 2).sum() / dof / ((t - t.mean()) ** 2).sum())
     scale = 1e5 / abs(E[0])
-    return {"per_1e5_steps": float(coef[0] * scale), "std_err": float(se * scale), "steps": int(steps),
+    # the energy error is correlated over many steps, so the least-squares error understates the slope's
+    # spread; the spread of the slopes of five consecutive blocks gives a second estimate
+    nb = 5
+    blk = [q for q in np.array_split(np.arange(len(E)), nb) if len(q) >= 3]
+    bslopes = [np.polyfit(t[q], E[q], 1)[0] for q in blk]
+    se_blk = float(np.std(bslopes, ddof=1) / math.sqrt(len(bslopes)) * scale) if len(bslopes) > 1 else None
+    return {"per_1e5_steps": float(coef[0] * scale), "std_err": float(se * scale), "std_err_blocks": se_blk,
+            "block_slopes_per_1e5_steps": [float(b * scale) for b in bslopes], "steps": int(steps),
             "samples": int(len(E)), "rms_fluctuation_rel": float(resid.std() / abs(E[0])),
             "net_change_rel": float((E[-1] - E[0]) / abs(E[0])), "wall_s": wall}
 

@@ -106,36 +106,57 @@ def test_mixed_2d_disks():
     assert err <= FORCE_TOL, err
 
 
-def _drift(g, steps, every):
-    """Least-squares slope of the total energy (per 10^5 steps, relative to |E(0)|) and its standard error."""
-    E = [g.energy()[0] + g.kinetic_energy()[0]]
+def _lj_replicas(nrep, shape, steps=300):
+    """nrep independent LJ lattices (own jitter and velocities) in one handle, melted with the FP64 path."""
+    reps = [W.lj_lattice(shape=shape, skin_prime=0.3, seed=1000 + q) for q in range(nrep)]
+    r0 = reps[0]
+    w = W.Workload("lj_replicas", 3, [r.n for r in reps], np.concatenate([r.L for r in reps]),
+                   np.concatenate([r.x for r in reps]), np.concatenate([r.v for r in reps]),
+                   np.concatenate([r.m for r in reps]), r0.kind, np.concatenate([r.params for r in reps]), r0.skin)
+    g = make_gpu(w, "fp64")
+    g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
+    g.verlet(0.002, steps)
+    st = g.get_atoms()
+    g.close()
+    w.x, w.v = st["x"], st["v"]
+    return w
+
+
+def _drift_slopes(g, steps, every):
+    """Per-system least-squares slope of the total energy over `steps` steps (sampled every `every`),
+    per 10^5 steps and relative to that system's |E(0)|."""
+    E = [g.energy() + g.kinetic_energy()]
     for _ in range(steps // every):
         g.verlet(0.002, every)
-        E.append(g.energy()[0] + g.kinetic_energy()[0])
-    E = np.array(E)
+        E.append(g.energy() + g.kinetic_energy())
+    E = np.array(E)                      # (samples, nsys)
     t = np.arange(len(E), dtype=np.float64) * every
-    A = np.stack([t, np.ones_like(t)], 1)
-    coef = np.linalg.lstsq(A, E, rcond=None)[0]
-    resid = E - A @ coef
-    se = np.sqrt((resid ** 2).sum() / (len(E) - 2) / ((t - t.mean()) ** 2).sum())
-    scale = 1e5 / abs(E[0])
-    return coef[0] * scale, se * scale
+    tc = t - t.mean()
+    slope = (tc[:, None] * (E - E.mean(0))).sum(0) / (tc ** 2).sum()
+    return slope * 1e5 / np.abs(E[0])
 
 
-def test_mixed_nve_drift_comparable(lj32k):
-    """NVE energy drift of the mixed path is the FP64 path's: over 20000 steps from the same state the
-    fitted slopes (per 10^5 steps, relative) differ by less than three combined standard errors plus
-    1e-5, and the mixed slope is below 1e-4."""
-    w = lj32k
+def test_mixed_nve_drift_comparable():
+    """NVE energy drift of the mixed path is the FP64 path's.  16 independent 4096-atom LJ replicas run
+    20000 steps on each path from the same states; the mean fitted slope (per 10^5 steps, relative) of
+    the two paths differs by less than four standard errors of the replica spread plus 1e-5, and the
+    mixed path's mean slope is below 1e-4.  (A single trajectory's least-squares error understates the
+    slope's spread: the energy error is correlated over many steps.)"""
+    nrep = 16
+    w = _lj_replicas(nrep, (16, 16, 16))
     out = {}
     for prec in ("fp64", "mixed"):
         g = make_gpu(w, prec)
+        g.set_graph_steps(50)
         g.nlist_update(False); g.set_forces(True); g.nlist_update(False)
-        out[prec] = _drift(g, 20000, 100)
+        out[prec] = _drift_slopes(g, 20000, 100)
         g.close()
-    (d64, se64), (d32, se32) = out["fp64"], out["mixed"]
-    assert abs(d32 - d64) <= 3 * np.hypot(se32, se64) + 1e-5, out
-    assert abs(d32) <= 1e-4, out
+    m64, m32 = out["fp64"].mean(), out["mixed"].mean()
+    se64, se32 = out["fp64"].std(ddof=1) / np.sqrt(nrep), out["mixed"].std(ddof=1) / np.sqrt(nrep)
+    info = {"fp64": (m64, se64), "mixed": (m32, se32)}
+    print("drift per 1e5 steps (mean, standard error):", info)
+    assert abs(m32 - m64) <= 4 * np.hypot(se32, se64) + 1e-5, info
+    assert abs(m32) <= 1e-4, info
 
 
 @pytest.mark.parametrize("tpa", [200, 1, 2, 4, 101, 104, 108, 116, 132])
