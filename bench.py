@@ -423,6 +423,9 @@ def run_ours(args, rank, world, local_rank):
 
     # --- FP64 path on the same system, and mixed-vs-FP64 error at one state ---
     st = g.get_atoms(capi.X | capi.V | capi.A)
+    # the equilibrated state after the timed runs: start of the drift fits
+    from dataclasses import replace
+    w_eq = replace(w, x=st["x"].copy(), v=st["v"].copy())
     w64 = W.lj_lattice(shape=SHAPE, skin_prime=0.3, seed=12345 + rank)
     w64.x, w64.v = st["x"], st["v"]
     g64 = make_system(w64, "fp64", local_rank)
@@ -486,13 +489,14 @@ def run_ours(args, rank, world, local_rank):
     # --- NVE energy drift of both paths from the same initial state (fitted slope) ---
     if args.drift_steps > 0 and rank == 0:
         log(f"[rank 0] NVE drift over {args.drift_steps} steps, mixed and FP64")
-        dm = energy_drift(w, "mixed", args.drift_steps, graph_steps=args.graph_steps)
-        d64 = energy_drift(w, "fp64", args.drift_steps, graph_steps=args.graph_steps)
+        dm = energy_drift(w_eq, "mixed", args.drift_steps, graph_steps=args.graph_steps)
+        d64 = energy_drift(w_eq, "fp64", args.drift_steps, graph_steps=args.graph_steps)
         result["drift"] = {"mixed": dm, "fp64": d64,
                            "ratio_mixed_over_fp64": dm["per_1e5_steps"] / d64["per_1e5_steps"]
                            if d64["per_1e5_steps"] != 0 else None,
                            "definition": "least-squares slope of E_total(t) sampled every 100 steps, "
-                                         "times 1e5 steps, over |E_total(0)|, from the workload's initial state"}
+                                         "times 1e5 steps, over |E_total(0)|, both paths from the same state: "
+                                         "the mixed run's state after its warm-up and timed steps"}
 
     if rank == 0 and world == 1 and not args.no_cpu:
         log("[rank 0] timing the CPU oracle sample")
@@ -550,11 +554,16 @@ def _tuned(w, make, step, skins, prepare=None):
     return replace(w, skin=res["skin"]), res["cell_scale"], autotune.summarise(res)
 
 
-def _minimise_cg(g, tol, max_steps, chunk):
-    """Conjugate-gradient time steps until every system's max |F| < tol (converged systems frozen)."""
+def _minimise_cg(g, tol, max_steps, chunk, stall=0):
+    """Conjugate-gradient time steps until every system's max |F| < tol (finished systems frozen).
+
+    stall > 0: a system also finishes when its max |F| fell by less than a
+    factor 2 over its last `stall` checks (the floor of FP32 forces, for the
+    mixed-precision phase)."""
     nsys = g.nsys
     act = np.ones(nsys, bool)
     steps = np.zeros(nsys, dtype=np.int64)
+    hist = []
     done = 0
     while done < max_steps and act.any():
         g.set_active(act)
@@ -562,16 +571,21 @@ def _minimise_cg(g, tol, max_steps, chunk):
         steps[act] += chunk
         done += chunk
         fmax = np.sqrt(g.max_force_sq())
-        act &= ~(fmax < tol)
+        hist.append(fmax)
+        fin = fmax < tol
+        if stall and len(hist) > stall:
+            fin |= fmax > 0.5 * hist[-1 - stall]
+        act &= ~fin
     g.set_active(np.ones(nsys, bool))
     return steps, np.sqrt(g.max_force_sq())
 
 
-def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False, cell_scale=1.0):
-    """Mixed-precision conjugate-gradient bulk phase, then an FP64 phase from its positions to max|F| < tol64."""
+def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False, cell_scale=1.0, stall=4):
+    """Mixed-precision conjugate-gradient bulk phase (until max|F| < tol32 or its FP32 floor), then an FP64
+    phase from its positions to max|F| < tol64."""
     g, variant = _cg_handle(ws, "mixed", tune, cell_scale)
     ta = _sync_time(g)
-    s32, f32 = _minimise_cg(g, tol32, cap32, chunk)
+    s32, f32 = _minimise_cg(g, tol32, cap32, chunk, stall)
     x = g.get_atoms(1)["x"]
     tb = _sync_time(g)
     g.close()
@@ -590,9 +604,10 @@ def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False, cell_scale=1
 def run_packings(args):
     """Batched 3D packings minimised by the conjugate-gradient minimiser (CollectionNLCGV, fixed box).
 
-    Every system: a mixed-precision phase until max |F| < 1e-7 (FP32 forces),
-    then an FP64 phase until max |F| < 1e-12; converged systems are frozen
-    while the others continue.  A packing counts only when its system reached
+    Every system: a mixed-precision phase until max |F| < 1e-10 or until it
+    stops improving (FP32 forces: less than a factor 2 in 1000 steps), then an
+    FP64 phase until max |F| < 1e-12; finished systems are frozen while the
+    others continue.  A packing counts only when its system reached
     max |F| < 1e-12 within the step caps.  Reported: converged packings/s of
     the batch, the converged fraction, the same protocol run one system per
     handle and launch (speed-up), and the final-energy error of converged
@@ -601,8 +616,8 @@ def run_packings(args):
     from parm_gb300 import shard, workloads as W
     nsys = args.nsys or 4096
     w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=args.skin)
-    tol32, tol64, chunk = 1e-7, 1e-12, 250
-    cap32, cap64 = args.min_steps, args.min_steps
+    tol32, tol64, chunk = 1e-10, 1e-12, 250
+    cap32, cap64 = args.min_steps, args.fp64_cap
     log(f"packings: {nsys} systems, {w.n} atoms")
     # skin, cell width and kernel variant tuned on the batch's first systems
     w, cscale, tuned = _tuned(w, lambda ws: make_system(ws, "mixed", 0), lambda g, k: g.nlcg_timestep(k),
@@ -643,10 +658,14 @@ def run_packings(args):
                       "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "skin": w.skin,
                       "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
                       "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_mixed": cap32, "step_cap_fp64": cap64,
+                      "mixed_phase_end": "max|F| < tol_mixed, or less than a factor 2 over 4 checks",
                       "steps_per_check": chunk, "kernel_variant": r["variant"], "autotune": tuned},
            "wall_s": wall, "mixed_s": r["t32"], "fp64_s": r["t64"],
            "converged": int(conv.sum()), "converged_fraction": float(conv.mean()),
            "steps_median": {"mixed": float(np.median(r["s32"])), "fp64": float(np.median(r["s64"]))},
+           "steps_p90": {"mixed": float(np.percentile(r["s32"], 90)), "fp64": float(np.percentile(r["s64"], 90))},
+           "converged_within_fp64_steps": {str(k): int((conv & (r["s64"] <= k)).sum())
+                                           for k in (500, 1000, 2000, 5000, 10000, 20000) if k <= cap64},
            "mixed_atom_steps_per_s": float((r["s32"] * sizes).sum() / r["t32"]),
            "fp64_atom_steps_per_s": float((r["s64"] * sizes).sum() / max(r["t64"], 1e-9)),
            "max_force": {"after_mixed_median": float(np.median(r["f32"])), "after_fp64_max": float(r["f64"].max())},
@@ -731,7 +750,7 @@ def run_disks(args):
     a mixed-precision phase then FP64 until max|F| < 1e-12, against an FP64-only minimisation."""
     from parm_gb300 import workloads as W
     w = W.soft_disks(n=65536, phi=0.84, exponent=2.0, seed=2, skin=args.skin)
-    tol32, tol64, chunk = 1e-7, 1e-12, 1000
+    tol32, tol64, chunk = 1e-10, 1e-12, 1000
     cap = args.min_steps
     r = _cg_protocol(w, tol32, tol64, cap, cap, chunk, tune=True)
     gr, _ = _cg_handle(w, "fp64")
@@ -746,12 +765,15 @@ def run_disks(args):
            "vs_baseline": None, "dtype": "f32/f64 (mixed) then f64", "data": "synthetic",
            "config": {"workload": "disks2d_65536", "phi": 0.84, "exponent": 2.0, "skin": w.skin,
                       "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
-                      "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_each_phase": cap, "kernel_variant": r["variant"]},
+                      "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_each_phase": cap, "kernel_variant": r["variant"],
+                      "mixed_phase_end": "max|F| < tol_mixed, or less than a factor 2 over 4 checks"},
            "steps_mixed": int(r["s32"][0]), "steps_fp64": int(r["s64"][0]), "max_force": float(r["f64"][0]),
            "converged": bool(r["f64"][0] < tol64), "energy": E,
            "fp64_alone": {"seconds": t4 - t3, "steps": int(sr[0]), "max_force": float(fr[0]), "energy": Er,
                           "converged": bool(fr[0] < tol64)},
-           "energy_rel_diff": abs(E - Er) / max(abs(Er), 1e-300)}
+           "energy_rel_diff": abs(E - Er) / max(abs(Er), 1e-300),
+           "energy_per_atom": {"mixed_then_fp64": E / w.n, "fp64_alone": Er / w.n},
+           "note": "energies per atom below 1e-16 mean an unjammed minimum (no overlaps left): both zero"}
     print(json.dumps(out), flush=True)
 
 
@@ -775,6 +797,7 @@ def main():
                     help="lj1m: the headline line; the others print their own line")
     ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workloads")
     ap.add_argument("--min-steps", type=int, default=20000, help="step cap of each minimisation phase")
+    ap.add_argument("--fp64-cap", type=int, default=10000, help="packings: step cap of the FP64 phase")
     ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin of the packing workloads")
     ap.add_argument("--fp64-steps", type=int, default=0,
                     help="lj1m: timed FP64 steps (default 200); replicas: FP64 steps of the comparison (2000)")
