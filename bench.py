@@ -604,10 +604,9 @@ def _cg_protocol(ws, tol32, tol64, cap32, cap64, chunk, tune=False, cell_scale=1
 def run_packings(args):
     """Batched 3D packings minimised by the conjugate-gradient minimiser (CollectionNLCGV, fixed box).
 
-    Every system: a mixed-precision phase until max |F| < 1e-10 or until it
-    stops improving (FP32 forces: less than a factor 2 in 1000 steps), then an
-    FP64 phase until max |F| < 1e-12; finished systems are frozen while the
-    others continue.  A packing counts only when its system reached
+    Every system: a mixed-precision phase until max |F| < 1e-7 (about the
+    error of FP32 forces on these contacts), then an FP64 phase until
+    max |F| < 1e-12; finished systems are frozen while the others continue.  A packing counts only when its system reached
     max |F| < 1e-12 within the step caps.  Reported: converged packings/s of
     the batch, the converged fraction, the same protocol run one system per
     handle and launch (speed-up), and the final-energy error of converged
@@ -616,13 +615,14 @@ def run_packings(args):
     from parm_gb300 import shard, workloads as W
     nsys = args.nsys or 4096
     w = W.packings(nsys=nsys, nmin=64, nmax=4096, phi_lo=0.62, phi_hi=0.66, exponent=2.5, seed=3, skin=args.skin)
-    tol32, tol64, chunk = 1e-10, 1e-12, 250
+    # FP32 forces on these contacts carry ~1e-7 of error, so the mixed phase ends at 1e-7
+    tol32, tol64, chunk = 1e-7, 1e-12, 250
     cap32, cap64 = args.min_steps, args.fp64_cap
     log(f"packings: {nsys} systems, {w.n} atoms")
     # skin, cell width and kernel variant tuned on the batch's first systems
     w, cscale, tuned = _tuned(w, lambda ws: make_system(ws, "mixed", 0), lambda g, k: g.nlcg_timestep(k),
                               (0.05, 0.1, 0.2, 0.3), prepare=_cg_prepare)
-    r = _cg_protocol(w, tol32, tol64, cap32, cap64, chunk, tune=True, cell_scale=cscale)
+    r = _cg_protocol(w, tol32, tol64, cap32, cap64, chunk, tune=True, cell_scale=cscale, stall=0)
     wall = r["t32"] + r["t64"]
     conv = r["f64"] < tol64
     value = float(conv.sum()) / wall
@@ -646,7 +646,7 @@ def run_packings(args):
     nsingle = min(nsys, args.single_sys)
     t_single, c_single = 0.0, 0
     for q in range(nsingle):
-        rs = _cg_protocol(shard.select(w, [q]), tol32, tol64, cap32, cap64, chunk, cell_scale=cscale)
+        rs = _cg_protocol(shard.select(w, [q]), tol32, tol64, cap32, cap64, chunk, cell_scale=cscale, stall=0)
         t_single += rs["t32"] + rs["t64"]
         c_single += int((rs["f64"] < tol64).sum())
     single_rate = c_single / t_single
@@ -658,7 +658,7 @@ def run_packings(args):
                       "n_range": [64, 4096], "phi_range": [0.62, 0.66], "exponent": 2.5, "skin": w.skin,
                       "minimiser": "CollectionNLCGV (fixed box), dt 0.1, secmax 10, seceps 1e-4, kmax 1000",
                       "tol_mixed": tol32, "tol_fp64": tol64, "step_cap_mixed": cap32, "step_cap_fp64": cap64,
-                      "mixed_phase_end": "max|F| < tol_mixed, or less than a factor 2 over 4 checks",
+                      "mixed_phase_end": "max|F| < tol_mixed",
                       "steps_per_check": chunk, "kernel_variant": r["variant"], "autotune": tuned},
            "wall_s": wall, "mixed_s": r["t32"], "fp64_s": r["t64"],
            "converged": int(conv.sum()), "converged_fraction": float(conv.mean()),
@@ -698,13 +698,13 @@ def run_replicas(args):
 
     def make(ws):
         g = make_system(ws, "mixed", 0)
-        g.set_graph_steps(50)
+        g.set_graph_steps(args.graph_steps)
         return g
     w, cscale, tuned = _tuned(w, make, lambda g, k: g.sol(dt, damping, T, seed, k), (0.1, 0.2, 0.3, 0.45))
     res["autotune"] = tuned
     for prec, nst in (("mixed", steps), ("fp64", steps64)):
         g = make_system(w, prec, 0)
-        g.set_graph_steps(50)
+        g.set_graph_steps(args.graph_steps)
         if cscale != 1.0:
             g.set_cell_scale(cscale)
             g.nlist_update(False)
@@ -721,7 +721,7 @@ def run_replicas(args):
             done += k
             msd.append(_msd(g.get_atoms(1)["x"], x0, w.sizes))
             pe.append(g.energy() / np.array(w.sizes))
-        res[prec] = {"atom_steps_per_s": w.n * nst / tt, "steps": nst, "seconds": tt,
+        res[prec] = {"atom_steps_per_s": w.n * nst / tt, "steps": nst, "seconds": tt, "launches": g.last_launches(),
                      "msd": np.array(msd), "pe": np.array(pe)}
         g.close()
     k = len(res["fp64"]["msd"])
@@ -735,7 +735,9 @@ def run_replicas(args):
            "data": "synthetic",
            "config": {"workload": f"wca_replicas_{nrep}", "replicas": nrep, "atoms": w.n, "n_range": [256, 32768],
                       "rho_range": [0.5, 0.9], "T": T, "damping": damping, "dt": dt, "steps": steps,
-                      "fp64_steps": steps64, "kernel": res["kernel"], "skin": w.skin, "autotune": res["autotune"]},
+                      "fp64_steps": steps64, "kernel": res["kernel"], "skin": w.skin, "autotune": res["autotune"],
+                      "steps_per_graph": args.graph_steps},
+           "ms_per_step": 1e3 * res["mixed"]["seconds"] / res["mixed"]["steps"],
            "fp64_value": res["fp64"]["atom_steps_per_s"],
            "mixed_vs_fp64": res["mixed"]["atom_steps_per_s"] / res["fp64"]["atom_steps_per_s"],
            "msd_batch_mean_rel_diff": [float(q) for q in msd_rel],
@@ -797,7 +799,7 @@ def main():
                     help="lj1m: the headline line; the others print their own line")
     ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workloads")
     ap.add_argument("--min-steps", type=int, default=20000, help="step cap of each minimisation phase")
-    ap.add_argument("--fp64-cap", type=int, default=10000, help="packings: step cap of the FP64 phase")
+    ap.add_argument("--fp64-cap", type=int, default=5000, help="packings: step cap of the FP64 phase")
     ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin of the packing workloads")
     ap.add_argument("--fp64-steps", type=int, default=0,
                     help="lj1m: timed FP64 steps (default 200); replicas: FP64 steps of the comparison (2000)")

@@ -323,6 +323,10 @@ int parm_debug_remainder(const double* d, const double* L, double* out, uint32_t
 int parm_debug_philox(const uint32_t* in, uint32_t* out, uint32_t n);
 int parm_debug_normals(uint64_t seed, uint32_t sys, uint64_t step, uint32_t natoms, double* out);
 
+/* Test hook: the per-atom update's float <-> double conversions on bit
+ * patterns, on the GPU: d2f[i] = (float)d[i], f2d[i] = (double)f[i]. */
+int parm_debug_fpbits(const double* d, const float* f, uint32_t n, float* d2f, double* f2d);
+
 /* Test hook: atoms staged in shared memory per cell block (the rest of a
  * block's neighbourhood is read from global memory); 0 restores the size
  * chosen from the density.  Results do not depend on it. */

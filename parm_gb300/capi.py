@@ -95,6 +95,7 @@ SIGNATURES = {
     "parm_host_free": (C.c_int, [C.c_void_p]),
     "parm_debug_remainder": (C.c_int, [_dp, _dp, _dp, C.c_uint32]),
     "parm_debug_philox": (C.c_int, [_u32p, _u32p, C.c_uint32]),
+    "parm_debug_fpbits": (C.c_int, [_dp, C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float), _dp]),
     "parm_nlcg_init": (C.c_int, [_h, C.c_int, _dp]),
     "parm_nlcg_set_params": (C.c_int, [_h, _dp]),
     "parm_nlcg_get_state": (C.c_int, [_h, _dp]),

@@ -2230,6 +2230,28 @@ int parm_debug_philox(const uint32_t* in, uint32_t* out, uint32_t n) {
     return PARM_OK;
 }
 
+int parm_debug_fpbits(const double* d, const float* f, uint32_t n, float* d2f, double* f2d) {
+    if (!d || !f || !d2f || !f2d) return fail(PARM_ERR_ARG, "NULL argument");
+    if (n == 0) return PARM_OK;
+    char* buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, 24 * (size_t)n));
+    double* dd = reinterpret_cast<double*>(buf);
+    double* df2d = dd + n;
+    float* df = reinterpret_cast<float*>(df2d + n);
+    float* dd2f = df + n;
+    cudaError_t e = cudaMemcpy(dd, d, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(df, f, 4 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_fpbits_test(dd, df, n, dd2f, df2d, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(d2f, dd2f, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f2d, df2d, 8 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(PARM_ERR_CUDA, cudaGetErrorString(e));
+    return PARM_OK;
+}
+
 int parm_debug_normals(uint64_t seed, uint32_t sys, uint64_t step, uint32_t natoms, double* out) {
     if (!out) return fail(PARM_ERR_ARG, "NULL argument");
     if (natoms == 0) return PARM_OK;

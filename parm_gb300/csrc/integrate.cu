@@ -9,6 +9,7 @@
 //   CollectionSol::timestep     265-322  (first loop, BivariateGauss noise)
 // The second half of step k (a = f/m and the final velocity update) is fused
 // with the first half of step k+1 in k_kickdrift; a call ends with k_kick.
+#include "fpbits.cuh"
 #include "parm_check.cuh"
 
 namespace parm {
@@ -112,7 +113,7 @@ __device__ __forceinline__ void kick(const DevCtx& c, uint32_t i, double m, doub
     if constexpr (MIXED) {
         const float im = mobile(m) ? c.invm32[i] : (float)(1.0 / m);
 #pragma unroll
-        for (int d = 0; d < ND; d++) a[d] = (double)(fm[d] * im);
+        for (int d = 0; d < ND; d++) a[d] = f2d_bits(fm[d] * im);
     } else {
 #pragma unroll
         for (int d = 0; d < ND; d++) a[d] = f[d] / m;
@@ -154,9 +155,9 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
                 if constexpr (KICK) {
                     const float4 q = c.f32[i];
                     const float im = c.invm32[i];
-                    a[0] = (double)(q.x * im);
-                    a[1] = (double)(q.y * im);
-                    if constexpr (ND == 3) a[2] = (double)(q.z * im);
+                    a[0] = f2d_bits(q.x * im);
+                    a[1] = f2d_bits(q.y * im);
+                    if constexpr (ND == 3) a[2] = f2d_bits(q.z * im);
                 } else {
                     av = static_cast<const V*>(c.a)[i];
                 }
@@ -230,12 +231,14 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
             // at the last rebuild or upload (x - X is exact in FP64); an atom
             // that has moved more than 1/4 from its coarse point is re-anchored
             // (any multiple of 1/8 is a valid coarse point)
+            // (the conversions on the bit patterns: integer instructions, the
+            // same values as the FP64 conversion instructions)
             float4 A = c.pos[2 * (size_t)i];
             float4 B;
-            B.x = (float)(x[0] - (double)A.x);
-            B.y = (float)(x[1] - (double)A.y);
+            B.x = d2f_bits(x[0] - f2d_bits(A.x));
+            B.y = d2f_bits(x[1] - f2d_bits(A.y));
             B.z = 0.f;
-            if constexpr (ND == 3) B.z = (float)(x[2] - (double)A.z);
+            if constexpr (ND == 3) B.z = d2f_bits(x[2] - f2d_bits(A.z));
             B.w = 0.f;
             if (fabsf(B.x) > 0.25f || fabsf(B.y) > 0.25f || fabsf(B.z) > 0.25f) {
                 posq_split2(x[0], A.x, B.x);
@@ -260,12 +263,17 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
             } else {
                 dsq = disp_sq<ND>(xv, l);
             }
-            valid = !(dsq != dsq);
+            // dsq is a sum of squares: +0, positive, +inf or NaN, so the tests
+            // compare bit patterns (integer instructions, not the FP64 pipe)
+            const unsigned long long db = (unsigned long long)__double_as_longlong(dsq);
+            valid = (db & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
             // the cell-block records hold atoms within 2 skin + 1/2 of their
             // position at the last build (far more than the rebuild test lets
             // them move)
             if constexpr (MIXED)
-                if (c.staged && dsq > c.sys[s].rec_lim2) atomicOr(c.status, ST_IMAGE_RANGE);
+                if (c.staged && valid &&
+                    db > (unsigned long long)__double_as_longlong(c.sys[s].rec_lim2))
+                    atomicOr(c.status, ST_IMAGE_RANGE);
         }
     }
     check_accumulate(c, s, valid, dsq);
@@ -644,6 +652,18 @@ __global__ void k_normals_test(unsigned long long key, unsigned long long step, 
     normals6(key, step, i, g);
 #pragma unroll
     for (int q = 0; q < 6; q++) out[6 * (size_t)i + q] = g[q];
+}
+
+// the bit-pattern conversions of the per-atom update on n values of each kind
+__global__ void k_fpbits_test(const double* d, const float* f, uint32_t n, float* d2f, double* f2d) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d2f[i] = d2f_bits(d[i]);
+    f2d[i] = f2d_bits(f[i]);
+}
+
+void launch_fpbits_test(const double* d, const float* f, uint32_t n, float* d2f, double* f2d, cudaStream_t s) {
+    if (n) k_fpbits_test<<<grid_for(n), BLOCK, 0, s>>>(d, f, n, d2f, f2d);
 }
 
 void launch_philox_test(const uint32_t* in, uint32_t* out, uint32_t n, cudaStream_t s) {

@@ -41,7 +41,9 @@ __device__ __forceinline__ void check_accumulate(const DevCtx& c, uint32_t sys_i
     __shared__ unsigned long long s1[BLOCK / 32], s2[BLOCK / 32];
     __shared__ uint32_t ssys[BLOCK / 32];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    unsigned long long v1 = (valid && dsq > 0.0) ? (unsigned long long)__double_as_longlong(dsq) : 0ull;
+    // dsq >= 0 (a sum of squares) when valid: its bit pattern orders like its
+    // value, and +0 is the pattern 0
+    unsigned long long v1 = valid ? (unsigned long long)__double_as_longlong(dsq) : 0ull;
     unsigned long long v2 = 0ull;
     uint32_t sid = valid ? sys_id : 0xFFFFFFFFu;
     // warp-level: lanes that hold no value adopt the warp's first valid system

@@ -238,6 +238,7 @@ void launch_remainder_test(const double* d, const double* L, double* out, uint32
                            cudaStream_t s);
 // test hooks of the Langevin generator (integrate.cu)
 void launch_philox_test(const uint32_t* in, uint32_t* out, uint32_t n, cudaStream_t s);
+void launch_fpbits_test(const double* d, const float* f, uint32_t n, float* d2f, double* f2d, cudaStream_t s);
 void launch_normals_test(unsigned long long key, unsigned long long step, uint32_t n, double* out,
                          cudaStream_t s);
 

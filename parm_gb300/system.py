@@ -332,6 +332,20 @@ def debug_philox(ctr_key) -> np.ndarray:
     return out
 
 
+def debug_fpbits(d, f):
+    """The per-atom update's bit-pattern conversions on the GPU: ((float)d, (double)f)."""
+    import ctypes as C
+    lib = capi.load()
+    d = np.ascontiguousarray(np.asarray(d, dtype=np.float64).ravel())
+    f = np.ascontiguousarray(np.asarray(f, dtype=np.float32).ravel())
+    n = min(d.size, f.size)
+    d2f = np.zeros(n, dtype=np.float32)
+    f2d = np.zeros(n)
+    fp = C.POINTER(C.c_float)
+    check(lib.parm_debug_fpbits(dptr(d), f.ctypes.data_as(fp), n, d2f.ctypes.data_as(fp), dptr(f2d)))
+    return d2f, f2d
+
+
 def debug_normals(seed: int, sys: int, step: int, natoms: int) -> np.ndarray:
     """The (natoms, 6) standard normals parm_sol draws for system `sys` at counter `step`."""
     lib = capi.load()

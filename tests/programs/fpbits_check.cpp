@@ -1,0 +1,98 @@
+// Checks the bit-pattern conversions of parm_gb300/csrc/fpbits.cuh against
+// the host's own float <-> double conversions (IEEE 754, round to nearest
+// even) on edge cases and on seeded random values; prints "ok <count>" or the
+// first mismatch.  Test infrastructure.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+
+#include "fpbits.cuh"
+
+using parm::d2f_bits;
+using parm::f2d_bits;
+
+static uint64_t sm_state = 0x2545F4914F6CDD1Dull;
+static uint64_t next64() {   // splitmix64
+    uint64_t z = (sm_state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static bool same_f(float a, float b) {
+    if (std::isnan(a) && std::isnan(b)) return true;
+    return std::memcmp(&a, &b, 4) == 0;
+}
+static bool same_d(double a, double b) {
+    if (std::isnan(a) && std::isnan(b)) return true;
+    return std::memcmp(&a, &b, 8) == 0;
+}
+
+static long count = 0;
+static bool check_d(double d) {
+    count++;
+    const float want = (float)d, got = d2f_bits(d);
+    if (!same_f(want, got)) {
+        std::printf("d2f mismatch: %.17g -> %.9g, want %.9g\n", d, got, want);
+        return false;
+    }
+    return true;
+}
+static bool check_f(float f) {
+    count++;
+    const double want = (double)f, got = f2d_bits(f);
+    if (!same_d(want, got)) {
+        std::printf("f2d mismatch: %.9g -> %.17g, want %.17g\n", f, got, want);
+        return false;
+    }
+    return true;
+}
+static double from_bits(uint64_t b) {
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+}
+static float from_bits32(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+int main() {
+    const double dl[] = {0.0, -0.0, 1.0, -1.0, 0.1, 1e-40, -1e-40, 1e-45, 1.1754943508222875e-38,
+                         1.1754942106924411e-38, 3.4028234663852886e38, 3.4028235677973366e38,
+                         3.4028236e38, 1e39, -1e39, std::numeric_limits<double>::infinity(),
+                         -std::numeric_limits<double>::infinity(), std::numeric_limits<double>::quiet_NaN(),
+                         std::numeric_limits<double>::denorm_min(), 0.24999999999999997, 0.125, 2.0 / 3.0};
+    for (double d : dl)
+        if (!check_d(d)) return 1;
+    const float fl[] = {0.0f, -0.0f, 1.0f, -1.0f, 0.1f, 1e-40f, -1e-40f, 1.17549435e-38f,
+                        std::numeric_limits<float>::max(), std::numeric_limits<float>::infinity(),
+                        -std::numeric_limits<float>::infinity(), std::numeric_limits<float>::quiet_NaN(),
+                        std::numeric_limits<float>::denorm_min()};
+    for (float f : fl)
+        if (!check_f(f)) return 1;
+    for (long i = 0; i < 4000000; i++) {
+        const uint64_t r = next64();
+        // any bit pattern
+        if (!check_d(from_bits(r))) return 1;
+        if (!check_f(from_bits32((uint32_t)r))) return 1;
+        // doubles of moderate magnitude, as positions, fine parts and forces are
+        const int e = (int)(r % 120) - 60;
+        if (!check_d(std::ldexp((double)(next64() >> 11) * 0x1p-53, e) * ((r >> 40) & 1 ? -1.0 : 1.0))) return 1;
+        // exact ties and their neighbours: the 29 dropped fraction bits at 0x10000000 (+-1)
+        const uint64_t t = (r & 0xFFFFFFFFE0000000ull & ~(0x7FFull << 52)) | ((uint64_t)(1023 + e) << 52);
+        if (!check_d(from_bits(t | 0x10000000ull))) return 1;
+        if (!check_d(from_bits(t | 0x0FFFFFFFull))) return 1;
+        if (!check_d(from_bits(t | 0x10000001ull))) return 1;
+        // all-ones fractions (the carry into the exponent)
+        if (!check_d(from_bits(((uint64_t)(1023 + e) << 52) | 0xFFFFFFFFFFFFFull))) return 1;
+        // around the float normal range's ends
+        const uint64_t lowe = (uint64_t)(896 + (r >> 50) % 3) << 52, high = (uint64_t)(1149 + (r >> 52) % 3) << 52;
+        if (!check_d(from_bits(lowe | (next64() & 0xFFFFFFFFFFFFFull)))) return 1;
+        if (!check_d(from_bits(high | (next64() & 0xFFFFFFFFFFFFFull)))) return 1;
+    }
+    std::printf("ok %ld\n", count);
+    return 0;
+}
