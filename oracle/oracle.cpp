@@ -37,7 +37,13 @@
 
 namespace {
 
-enum PairKind { LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3 };
+enum PairKind {
+    LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3,
+    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7
+};
+
+// kinds whose atoms carry four parameters
+inline bool four_params(int kind) { return kind >= LOISOHERN; }
 
 struct V3 {
     double c[3] = {0, 0, 0};
@@ -52,12 +58,15 @@ inline double dotv(const double* a, const double* b, int nd) {
 }
 
 struct AtomParams {
-    double p0 = 0, p1 = 0, p2 = 0;  // kind-dependent (eps, sigma, sigcut|exponent)
+    // kind-dependent: (eps, sigma, sigcut|exponent) or, for the Lois kinds,
+    // (eps, sigma, C, l) / (eps, sigma, f, l)
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
 };
 
 struct PairConst {
-    // LennardJonesCutPair / RepulsionPair / LJRepulsePair constructor outputs
-    double eps, sig, third, cut_energy;
+    // the pair constructors' outputs; for the Lois kinds third = C (or f),
+    // fourth = l and cut = sigcut
+    double eps, sig, third, cut_energy, fourth = 0, cut = 0;
 };
 
 struct System {
@@ -123,6 +132,34 @@ struct System {
             pc.sig = (A.p1 + B.p1) / 2.0;
             pc.third = (A.p2 + B.p2) / 2.0;
             pc.cut_energy = 0;
+        } else if (kind == LOISOHERN || kind == LOISOHERN_MIN) {
+            // LoisOhernPair(LoisOhernAtom, LoisOhernAtom) (interaction.hpp:1693-1703) and
+            // LoisOhernPairMinCLs (1746-1751): averages, or the smaller C and l
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2.0;
+            if (kind == LOISOHERN) {
+                pc.third = (A.p2 + B.p2) / 2.0;
+                pc.fourth = (A.p3 + B.p3) / 2.0;
+            } else {
+                pc.third = A.p2 < B.p2 ? A.p2 : B.p2;
+                pc.fourth = A.p3 < B.p3 ? A.p3 : B.p3;
+            }
+            pc.cut = pc.sig * (1 + pc.third + pc.fourth);
+            pc.cut_energy = 0;
+        } else if (kind == LOISLIN || kind == LOISLIN_MIN) {
+            // LoisLinPair(LoisLinAtom, LoisLinAtom) (interaction.hpp:1782-1800) and
+            // LoisLinPairMin (1831-1836)
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2.0;
+            if (kind == LOISLIN) {
+                pc.third = (A.p2 + B.p2) / 2.0;
+                pc.fourth = (A.p3 + B.p3) / 2.0;
+            } else {
+                pc.third = A.p2 < B.p2 ? A.p2 : B.p2;
+                pc.fourth = A.p3 < B.p3 ? A.p3 : B.p3;
+            }
+            pc.cut = pc.sig + pc.fourth;
+            pc.cut_energy = 0;
         } else {
             // LJRepulsePair(EpsSigAtom, EpsSigAtom) (interaction.hpp:875-880)
             pc.eps = std::sqrt(A.p0 * B.p0);
@@ -162,6 +199,27 @@ struct System {
             if (dsq > pc.sig * pc.sig) return 0.0;
             double R = std::sqrt(dsq);
             return pc.eps * std::pow(1.0 - (R / pc.sig), pc.third) / pc.third;
+        } else if (kind == LOISOHERN || kind == LOISOHERN_MIN) {
+            // LoisOhernPair::energy (interaction.hpp:1713-1727)
+            const double C = pc.third, l = pc.fourth;
+            if (dsq >= pc.cut * pc.cut) return 0.0;
+            double R = std::sqrt(dsq) / pc.sig;
+            if (R <= 1 + C) {
+                double dR = R - 1;
+                return -pc.eps * pc.sig / 2 * (C * (C + l) - dR * dR);
+            }
+            double dR2 = C + l + 1 - R;
+            return -C * pc.eps * pc.sig / 2 / l * dR2 * dR2;
+        } else if (kind == LOISLIN || kind == LOISLIN_MIN) {
+            // LoisLinPair::energy (interaction.hpp:1802-1815)
+            const double f = pc.third, l = pc.fourth;
+            if (dsq >= pc.cut * pc.cut) return 0.0;
+            double R = std::sqrt(dsq);
+            if (R <= pc.sig) {
+                double dR = 1.0 - (R / pc.sig);
+                return pc.eps / 2 * dR * dR - f * l;
+            }
+            return -f * (pc.sig + l - R);
         } else {
             // LJRepulsive::energy (interaction.hpp:127-134)
             double rsq = dsq / (pc.sig * pc.sig);
@@ -198,6 +256,30 @@ struct System {
             if (dsq > pc.sig * pc.sig) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
             double R = std::sqrt(dsq);
             s = pc.eps * std::pow(1.0 - (R / pc.sig), pc.third - 1) / pc.sig / R;
+        } else if (kind == LOISOHERN || kind == LOISOHERN_MIN) {
+            // LoisOhernPair::forces (interaction.hpp:1729-1743)
+            const double C = pc.third, l = pc.fourth;
+            if (dsq >= pc.cut * pc.cut) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double R = std::sqrt(dsq);
+            double rsig = R / pc.sig;
+            if (rsig <= 1 + C) {
+                double dR = rsig - 1;
+                s = -pc.eps * dR / R;
+            } else {
+                double dR2 = rsig - (C + l + 1);
+                s = C * pc.eps / l * dR2 / R;
+            }
+        } else if (kind == LOISLIN || kind == LOISLIN_MIN) {
+            // LoisLinPair::forces (interaction.hpp:1817-1828); -rij * (f / R) is rij * -(f / R)
+            const double f = pc.third;
+            if (dsq >= pc.cut * pc.cut) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double R = std::sqrt(dsq);
+            if (R <= pc.sig) {
+                double dR = 1.0 - (R / pc.sig);
+                s = pc.eps * dR / pc.sig / R;
+            } else {
+                s = -(f / R);
+            }
         } else {
             // LJRepulsive::forces (interaction.hpp:136-150)
             double rsq = dsq / (pc.sig * pc.sig);
@@ -213,6 +295,9 @@ struct System {
     double max_size(uint32_t i) const {
         // EpsSigCutAtom::max_size (interaction.hpp:904), EpsSigExpAtom (1464), EpsSigAtom (864)
         if (kind == LJCUT || kind == LJATTRACT) return params[i].p1 * params[i].p2;
+        // LoisOhernAtom::max_size (interaction.hpp:1691), LoisLinAtom::max_size (1780)
+        if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
+        if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
         return params[i].p1;
     }
 
@@ -759,7 +844,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 3) return -1;
+    if (kind < 0 || kind > 7) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;
@@ -773,6 +858,7 @@ int orc_add_atom(void* s, uint32_t i, const double* p) {
     S->params[i].p0 = p[0];
     S->params[i].p1 = p[1];
     S->params[i].p2 = (S->kind == LJREPULSE) ? 0.0 : p[2];
+    S->params[i].p3 = four_params(S->kind) ? p[3] : 0.0;
     S->has_params[i] = 1;
     S->members.push_back(i);
     S->diameters.push_back(S->max_size(i));

@@ -3,12 +3,15 @@
 // parity tests compare, with 17 significant digits.  Test infrastructure.
 //
 // Input (whitespace separated): kind integrator nsteps dt damping T skin
-//   L[NDIM]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2
+//   L[NDIM]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2 (and p3 for kinds 4-7)
 //   norder order[norder]   nign (a b)[nign]   nout out_steps[nout]
 //   integrators 3 and 4 add one line: dt P0 kappa kmax secmax seceps alphamax afrac
 //   dxmax stepmax maxdV
 // kind: 0 NListed<EpsSigCutAtom,LennardJonesCutPair>, 1 <EpsSigExpAtom,RepulsionPair>,
-//       2 <EpsSigAtom,LJRepulsePair>, 3 <EpsSigCutAtom,LJAttractCutPair>;  integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
+//       2 <EpsSigAtom,LJRepulsePair>, 3 <EpsSigCutAtom,LJAttractCutPair>,
+//       4 <LoisOhernAtom,LoisOhernPair>, 5 <LoisOhernAtom,LoisOhernPairMinCLs> (p: eps sigma C l),
+//       6 <LoisLinAtom,LoisLinPair>, 7 <LoisLinAtom,LoisLinPairMin> (p: eps sigma depth width);
+//       integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
 //       4 CollectionNLCGV (constructor, then reset())
@@ -49,18 +52,27 @@ template <>
 EpsSigAtom make_atom<EpsSigAtom>(AtomID id, int, const double* p) {
     return EpsSigAtom(id, p[0], p[1]);
 }
+template <>
+LoisOhernAtom make_atom<LoisOhernAtom>(AtomID id, int, const double* p) {
+    return LoisOhernAtom(id, p[0], p[1], p[2], p[3]);
+}
+template <>
+LoisLinAtom make_atom<LoisLinAtom>(AtomID id, int, const double* p) {
+    return LoisLinAtom(id, p[0], p[1], p[2], p[3]);
+}
 
 template <class A, class P>
 int run(int kind, int integ, int nsteps, double dt, double damping, double T, double skin) {
     Vec L;
     for (int d = 0; d < NDIM; d++) L[d] = rd();
     unsigned N = rdu();
-    std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * 3);
+    const unsigned np = kind >= 4 ? 4 : 3;
+    std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * np);
     for (unsigned i = 0; i < N; i++) {
         for (int d = 0; d < NDIM; d++) xs[i * NDIM + d] = rd();
         for (int d = 0; d < NDIM; d++) vs[i * NDIM + d] = rd();
         ms[i] = rd();
-        for (int k = 0; k < 3; k++) ps[3 * i + k] = rd();
+        for (unsigned k = 0; k < np; k++) ps[np * i + k] = rd();
     }
     std::vector<unsigned> order(rdu());
     for (auto& o : order) o = rdu();
@@ -82,7 +94,7 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
     }
     boost::shared_ptr<NListed<A, P> > inter(new NListed<A, P>(obox, atoms, skin));
     boost::shared_ptr<NeighborList> nl = inter->neighbor_list();
-    for (unsigned i : order) inter->add(make_atom<A>(atoms->get_id(i), kind, &ps[3 * i]));
+    for (unsigned i : order) inter->add(make_atom<A>(atoms->get_id(i), kind, &ps[np * i]));
     for (size_t q = 0; q < ign.size() / 2; q++) nl->ignore(atoms->get_id(ign[2 * q]), atoms->get_id(ign[2 * q + 1]));
     nl->update_list(true);
     std::printf("PAIRS %u\n", nl->numpairs());
@@ -167,5 +179,9 @@ int main() {
     if (kind == 0) return run<EpsSigCutAtom, LennardJonesCutPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 1) return run<EpsSigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 3) return run<EpsSigCutAtom, LJAttractCutPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 4) return run<LoisOhernAtom, LoisOhernPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 5) return run<LoisOhernAtom, LoisOhernPairMinCLs>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 6) return run<LoisLinAtom, LoisLinPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 7) return run<LoisLinAtom, LoisLinPairMin>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

@@ -35,6 +35,7 @@ REFOUT = ROOT / "oracle" / "_ref"
 
 VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
+LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN = 4, 5, 6, 7
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -43,7 +44,8 @@ def _deck(c: dict) -> str:
     out = [f"{c['kind']} {c['integ']} {c['nsteps']} {c['dt']!r} {c['damping']!r} {c['T']!r} {c['skin']!r}",
            " ".join(repr(float(q)) for q in c["L"]), str(len(c["m"]))]
     for i in range(len(c["m"])):
-        vals = list(c["x"][i]) + list(c["v"][i]) + [c["m"][i]] + list(c["params"][i])
+        prm = c["deck_params"][i] if "deck_params" in c else c["params"][i]
+        vals = list(c["x"][i]) + list(c["v"][i]) + [c["m"][i]] + list(prm)
         out.append(" ".join(repr(float(q)) for q in vals))
     out.append(f"{len(c['order'])} " + " ".join(str(int(q)) for q in c["order"]))
     ig = c["ignores"].reshape(-1)
@@ -98,14 +100,18 @@ def _parse(text: str, n: int, nd: int) -> dict:
 
 
 def _case(name, kind, integ, nsteps, dt, L, x, v, m, params, skin, out_steps, damping=0.0, T=0.0,
-          order=None, ignores=None, cg=None):
+          order=None, ignores=None, cg=None, deck_params=None):
+    """deck_params: the atoms' constructor arguments when they differ from the stored fields
+    (LoisLinAtom takes depth and width and stores f = depth / width and l = width)."""
     n = len(m)
     extra = {} if cg is None else {"cg": np.asarray(cg, dtype=np.float64)}
+    if deck_params is not None:
+        extra["deck_params"] = np.asarray(deck_params, dtype=np.float64).reshape(n, -1)
     return {**extra, "name": name, "kind": kind, "integ": integ, "nsteps": nsteps, "dt": float(dt),
             "damping": float(damping), "T": float(T), "skin": float(skin),
             "L": np.asarray(L, dtype=np.float64), "x": np.asarray(x, dtype=np.float64),
             "v": np.asarray(v, dtype=np.float64), "m": np.asarray(m, dtype=np.float64),
-            "params": np.asarray(params, dtype=np.float64).reshape(n, 3),
+            "params": np.asarray(params, dtype=np.float64).reshape(n, -1),
             "order": np.arange(n, dtype=np.int64) if order is None else np.asarray(order, dtype=np.int64),
             "ignores": np.zeros((0, 2), np.int64) if ignores is None else np.asarray(ignores, np.int64),
             "out_steps": np.asarray(out_steps, dtype=np.int64)}
@@ -243,6 +249,53 @@ def cases() -> list[dict]:
     out.append(_case("nlcgv100_fixed", REPULSION, NLCGV, 200, 0.01, [Lv] * 3, rng.uniform(0, Lv, (n, 3)),
                      np.zeros((n, 3)), np.ones(n), np.stack([np.ones(n), sig, np.full(n, 2.0)], 1), 0.3,
                      [0, 1, 2, 5, 10, 50, 200], cg=cg))
+    # 13. LoisOhernPair (sticky spheres: harmonic repulsion, linear attraction out to
+    #     sigma (1 + C + l)), per-atom C and l averaged, 3D, damped from random positions
+    rng = np.random.default_rng(61)
+    n = 216
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lo = (np.sum(np.pi * sig ** 3 / 6) / 0.5) ** (1 / 3)
+    C = rng.choice([0.05, 0.1], n)
+    ll = rng.choice([0.02, 0.05], n)
+    out.append(_case("loisohern216_damped", LOISOHERN, DAMPED, 300, 0.01, [Lo] * 3, rng.uniform(0, Lo, (n, 3)),
+                     rng.normal(0, 0.05, (n, 3)), np.ones(n), np.stack([np.ones(n), sig, C, ll], 1), 0.2,
+                     [1, 10, 100, 300], damping=0.5))
+    # 14. LoisOhernPairMinCLs (the smaller C and l of the two atoms) in 2D, Verlet
+    rng = np.random.default_rng(62)
+    n = 150
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lo2 = np.sqrt(np.sum(np.pi * sig ** 2 / 4) / 0.7)
+    C = rng.choice([0.04, 0.08], n)
+    ll = rng.choice([0.03, 0.06], n)
+    eps = rng.choice([0.5, 2.0], n)
+    out.append(_case("loisohernmin150_2d_verlet", LOISOHERN_MIN, VERLET, 400, 0.005, [Lo2, Lo2],
+                     rng.uniform(0, Lo2, (n, 2)), rng.normal(0, 0.1, (n, 2)), np.ones(n),
+                     np.stack([eps, sig, C, ll], 1), 0.2, [1, 10, 100, 400]))
+    # 15. LoisLinPair (harmonic repulsion, a fixed attractive force f = depth / width out to
+    #     sigma + width), 3D, damped; the fixture keeps the atoms' fields (eps, sigma, f, l)
+    rng = np.random.default_rng(63)
+    n = 200
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Ll = (np.sum(np.pi * sig ** 3 / 6) / 0.55) ** (1 / 3)
+    depth = rng.choice([0.001, 0.003], n)
+    width = rng.choice([0.05, 0.1], n)
+    f = depth / width
+    out.append(_case("loislin200_damped", LOISLIN, DAMPED, 300, 0.01, [Ll] * 3, rng.uniform(0, Ll, (n, 3)),
+                     np.zeros((n, 3)), np.ones(n), np.stack([np.ones(n), sig, f, width], 1), 0.2,
+                     [1, 10, 100, 300], damping=0.5, deck_params=np.stack([np.ones(n), sig, depth, width], 1)))
+    # 16. LoisLinPairMin (the smaller f and l) in 2D, Verlet, one atom with width 0 (f = 0)
+    rng = np.random.default_rng(64)
+    n = 120
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Ll2 = np.sqrt(np.sum(np.pi * sig ** 2 / 4) / 0.75)
+    depth = rng.choice([0.002, 0.004], n)
+    width = rng.choice([0.04, 0.08], n)
+    width[7] = 0.0
+    f = np.where(width > 0, depth / np.where(width > 0, width, 1.0), 0.0)
+    out.append(_case("loislinmin120_2d_verlet", LOISLIN_MIN, VERLET, 400, 0.005, [Ll2, Ll2],
+                     rng.uniform(0, Ll2, (n, 2)), rng.normal(0, 0.1, (n, 2)), np.ones(n),
+                     np.stack([np.ones(n), sig, f, width], 1), 0.2, [1, 10, 100, 400],
+                     deck_params=np.stack([np.ones(n), sig, depth, width], 1)))
     return out
 
 
