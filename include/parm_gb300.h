@@ -44,6 +44,17 @@ extern "C" {
                                LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
+/* Four-parameter atoms (params: natoms*4 doubles, the atoms' fields); FP64
+ * handles only (a mixed-precision handle rejects them). */
+#define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
+                                1679-1744): params (eps, sigma, C, l), C and l averaged */
+#define PARM_LOISOHERN_MIN 5 /* NListed<LoisOhernAtom, LoisOhernPairMinCLs> (1746-1751): the smaller C, l */
+#define PARM_LOISLIN 6       /* NListed<LoisLinAtom, LoisLinPair> (1764-1829): params (eps, sigma, f, l),
+                                the fields LoisLinAtom(eps, sigma, depth, width) stores:
+                                f = depth / width (0 for width 0), l = width; f and l averaged */
+#define PARM_LOISLIN_MIN 7   /* NListed<LoisLinAtom, LoisLinPairMin> (1831-1836): the smaller f, l */
+/* doubles per atom in parm_set_interaction's params */
+#define PARM_NPARAM(kind) ((kind) >= PARM_LOISOHERN ? 4 : 3)
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u
@@ -99,7 +110,7 @@ int parm_get_atoms(parm_system* s, double* atoms, uint64_t stride, uint32_t fiel
 /* Install the pair interaction and its neighbour list:
  *   NListed<A,P>(box, atoms, skin) + NListed::add(A) for every atom with
  *   rank[i] != PARM_NOT_MEMBER (src/interaction.hpp:1902-1914).
- * params: natoms*3 doubles per kind (see PARM_LJCUT..).  rank[i] is the atom's
+ * params: natoms*PARM_NPARAM(kind) doubles (see PARM_LJCUT..).  rank[i] is the atom's
  * position in the NeighborList (its insertion order, src/trackers.hpp:194-201),
  * which fixes the reference's pair order; pass NULL for rank[i] = local index.
  * Marks the list for a rebuild on the next update (ignorechanged = true). */

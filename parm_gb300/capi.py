@@ -27,6 +27,15 @@ LJCUT = 0
 REPULSION = 1
 LJREPULSE = 2
 LJATTRACTCUT = 3
+LOISOHERN = 4       # params (eps, sigma, C, l); FP64 handles
+LOISOHERN_MIN = 5
+LOISLIN = 6         # params (eps, sigma, f, l); FP64 handles
+LOISLIN_MIN = 7
+
+
+def nparam(kind: int) -> int:
+    """Doubles per atom in parm_set_interaction's params."""
+    return 4 if kind >= LOISOHERN else 3
 
 X, V, A, F, M = 1, 2, 4, 8, 16
 

@@ -27,6 +27,23 @@ using namespace parm;
 namespace {
 thread_local std::string g_err;
 
+// A::max_size() of the atom types (src/interaction.hpp: EpsSigCutAtom 904,
+// EpsSigExpAtom 1464, EpsSigAtom 864, LoisOhernAtom 1691, LoisLinAtom 1780):
+// the atom's diameter in its neighbour list
+double atom_max_size(int kind, const double* p) {
+    if (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) return p[1] * p[2];
+    if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return p[1] * (1 + p[2] + p[3]);
+    if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return p[1] * (1 + p[3]);
+    return p[1];
+}
+
+// device pair law of an API kind (the Lois "Min" variants are a combination flag)
+int device_kind(int kind) {
+    if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return KIND_LOISOHERN;
+    if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return KIND_LOISLIN;
+    return kind;
+}
+
 int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;
@@ -201,8 +218,8 @@ struct parm_system {
         for (uint32_t i = 0; i < n; i++) {
             if (kind < 0 || rank_in[i] == PARM_NOT_MEMBER) continue;
             any_member = true;
-            const double* p = &prm_in[3 * (size_t)i];
-            double d = (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) ? p[1] * p[2] : p[1];
+            const double* p = &prm_in[(size_t)PARM_NPARAM(kind) * i];
+            double d = atom_max_size(kind, p);
             if (!ldiam.empty() && std::isfinite(ldiam[i])) d = ldiam[i];
             dmax = std::max(dmax, d);
         }
@@ -1319,14 +1336,17 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > 3) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > PARM_LOISLIN_MIN) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
+        return fail(PARM_ERR_ARG, "the Lois-O'Hern and Lois-Lin pairs run on FP64 handles only");
     if (!(skin >= 0.0) || !std::isfinite(skin)) return fail(PARM_ERR_ARG, "skin must be >= 0");
     TRY(S->flush());
     CUDA_TRY(cudaStreamSynchronize(S->st));
     const uint32_t n = S->n;
     S->kind = kind;
     S->skin = skin;
-    S->prm_in.assign(params, params + 3 * (size_t)n);
+    const size_t np = PARM_NPARAM(kind);
+    S->prm_in.assign(params, params + np * n);
     S->rank_in.resize(n);
     for (uint32_t s = 0; s < S->nsys; s++) {
         std::set<uint32_t> seen;
@@ -1344,14 +1364,14 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     std::vector<double> diam(n);
     std::vector<uint32_t> nmr(n, 0);
     bool first = true;
-    double e0 = 0, s0 = 0, t0 = 0;
-    uint32_t uni = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_SIG_ONE;
+    double e0 = 0, s0 = 0, t0 = 0, u0 = 0;
+    uint32_t uni = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_FOURTH | UNI_SIG_ONE;
     for (uint32_t s = 0; s < S->nsys; s++) {
         uint32_t nm = 0;
         for (uint32_t i = 0; i < S->natoms[s]; i++) {
             uint32_t g = S->off[s] + i;
-            const double* p = &params[3 * (size_t)g];
-            AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], 0.0};
+            const double* p = &params[np * g];
+            AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], np == 4 ? p[3] : 0.0};
             if (kind == PARM_LJCUT) a.p3 = 1 - 1 / std::pow(a.p2, 6);  // LennardJonesCut ctor
             if (kind == PARM_LJATTRACTCUT) {
                 // LJAttract::energy(cut) (interaction.hpp:170-177), times epsilon in the pair
@@ -1367,7 +1387,7 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             }
             prm[g] = a;
             prm32[g] = make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
-            diam[g] = (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) ? a.p1 * a.p2 : a.p1;   // A::max_size()
+            diam[g] = atom_max_size(kind, p);
             const bool explicit_d = !S->ldiam.empty() && std::isfinite(S->ldiam[g]);
             if (explicit_d) diam[g] = S->ldiam[g];   // NeighborList::add(atom, diameter)
             if (S->rank_in[g] == PARM_NOT_MEMBER) {
@@ -1376,15 +1396,19 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             }
             if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0)))
                 return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
+            if (np == 4 && !(std::isfinite(a.p2) && std::isfinite(a.p3) && a.p2 >= 0.0 && a.p3 >= 0.0))
+                return fail(PARM_ERR_ARG, "C (or f) and l must be finite and >= 0");
             if (first) {
                 e0 = a.p0;
                 s0 = a.p1;
                 t0 = a.p2;
+                u0 = a.p3;
                 first = false;
             }
             if (a.p0 != e0) uni &= ~UNI_EPS;
             if (a.p1 != s0) uni &= ~UNI_SIG;
             if (a.p2 != t0) uni &= ~UNI_THIRD;
+            if (a.p3 != u0) uni &= ~UNI_FOURTH;
             if (a.p1 != 1.0) uni &= ~UNI_SIG_ONE;
         }
     }
@@ -1410,7 +1434,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     CUDA_TRY(cudaMemcpy(S->c.diam, diam_k.data(), 8 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.rank, rank_k.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.nm_rank, nmr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
-    S->c.kind = kind;
+    if (kind == PARM_LOISOHERN_MIN || kind == PARM_LOISLIN_MIN) uni |= COMB_MIN;
+    S->c.kind = device_kind(kind);
     S->c.uniform = uni;
     launch_posq(S->c, S->st);
     CUDA_TRY(cudaGetLastError());

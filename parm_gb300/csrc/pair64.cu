@@ -8,6 +8,8 @@
 //   RepulsionPair                           1528-1590
 //   LJRepulsive + LJRepulsePair             119-152, 875-891
 //   LJAttractCut + LJAttractCutPair         154-236, 1020-1050
+//   LoisOhernPair, LoisOhernPairMinCLs      1679-1751
+//   LoisLinPair, LoisLinPairMin             1764-1836
 //
 // Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
 // scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
@@ -26,7 +28,8 @@ namespace parm {
 __device__ __forceinline__ bool mobile64(double m) { return !(m <= 0.0 || isinf(m)); }
 
 struct PairC {
-    double eps, sig, third, m6;
+    double eps, sig, third, m6;   // the Lois kinds: third = C (or f), m6 = l
+    double cut;                   // the Lois kinds: sigcut
 };
 
 template <int KIND>
@@ -43,10 +46,24 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
     } else if constexpr (KIND == KIND_REPULSION) {
         p.third = (uni & UNI_THIRD) ? A.p2 : (A.p2 + B.p2) / 2.0;
         p.m6 = 0.0;
+    } else if constexpr (lois_kind<KIND>()) {
+        // LoisOhernPair (interaction.hpp:1693-1703) / LoisLinPair (1782-1800): averages;
+        // LoisOhernPairMinCLs (1746-1751) / LoisLinPairMin (1831-1836): the smaller values
+        if (uni & COMB_MIN) {
+            p.third = A.p2 < B.p2 ? A.p2 : B.p2;
+            p.m6 = A.p3 < B.p3 ? A.p3 : B.p3;
+        } else {
+            p.third = (uni & UNI_THIRD) ? A.p2 : (A.p2 + B.p2) / 2.0;
+            p.m6 = (uni & UNI_FOURTH) ? A.p3 : (A.p3 + B.p3) / 2.0;
+        }
+        // sigcut: sig * (1 + C + l) (LoisOhern), sig + l (LoisLin)
+        p.cut = (KIND == KIND_LOISOHERN) ? p.sig * (1 + p.third + p.m6) : p.sig + p.m6;
+        return p;
     } else {
         p.third = 0.0;
         p.m6 = 0.0;
     }
+    p.cut = 0.0;
     return p;
 }
 
@@ -75,6 +92,32 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
         double rsix = rsq * rsq * rsq;
         double fmagTimesR = 12 * p.eps / rsix * (1 / rsix - 1);
         s = fmagTimesR / dsq;
+        return true;
+    } else if constexpr (KIND == KIND_LOISOHERN) {
+        // LoisOhernPair::forces (interaction.hpp:1729-1743): harmonic to (1 + C) sigma,
+        // then a linear return to zero at sigcut
+        const double C = p.third, l = p.m6;
+        if (dsq >= p.cut * p.cut) return false;
+        double R = sqrt(dsq);
+        double rsig = R / p.sig;
+        if (rsig <= 1 + C) {
+            double dR = rsig - 1;
+            s = -p.eps * dR / R;
+        } else {
+            double dR2 = rsig - (C + l + 1);
+            s = C * p.eps / l * dR2 / R;
+        }
+        return true;
+    } else if constexpr (KIND == KIND_LOISLIN) {
+        // LoisLinPair::forces (interaction.hpp:1817-1828); -rij * (f / R) == rij * -(f / R)
+        if (dsq >= p.cut * p.cut) return false;
+        double R = sqrt(dsq);
+        if (R <= p.sig) {
+            double dR = 1.0 - (R / p.sig);
+            s = p.eps * dR / p.sig / R;
+        } else {
+            s = -(p.third / R);
+        }
         return true;
     } else {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
@@ -115,6 +158,27 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
             e = p.eps * (mid * mid - 1);
         }
         return e - p.m6 * p.eps;
+    } else if constexpr (KIND == KIND_LOISOHERN) {
+        // LoisOhernPair::energy (interaction.hpp:1713-1727)
+        const double C = p.third, l = p.m6;
+        if (dsq >= p.cut * p.cut) return 0.0;
+        double R = sqrt(dsq) / p.sig;
+        if (R <= 1 + C) {
+            double dR = R - 1;
+            return -p.eps * p.sig / 2 * (C * (C + l) - dR * dR);
+        }
+        double dR2 = C + l + 1 - R;
+        return -C * p.eps * p.sig / 2 / l * dR2 * dR2;
+    } else if constexpr (KIND == KIND_LOISLIN) {
+        // LoisLinPair::energy (interaction.hpp:1802-1815)
+        const double f = p.third, l = p.m6;
+        if (dsq >= p.cut * p.cut) return 0.0;
+        double R = sqrt(dsq);
+        if (R <= p.sig) {
+            double dR = 1.0 - (R / p.sig);
+            return p.eps / 2 * dR * dR - f * l;
+        }
+        return -f * (p.sig + l - R);
     } else {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
         if (rsq > 1) return 0.0;
@@ -125,13 +189,21 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
 }
 
 // FP32 screen: true when the pair is certainly beyond the cut-off
+// (Q = (sqrt(eps), sigma, third, fourth) in FP32)
 template <int KIND>
-__device__ __forceinline__ bool beyond32(float d2, float sig32i, float sig32j, float th32i,
-                                         float th32j, uint32_t uni) {
-    float sg = (uni & UNI_SIG) ? sig32i : 0.5f * (sig32i + sig32j);
+__device__ __forceinline__ bool beyond32(float d2, const float4& Qi, const float4& Qj, uint32_t uni) {
+    float sg = (uni & UNI_SIG) ? Qi.y : 0.5f * (Qi.y + Qj.y);
     float rc;
-    if constexpr (cut_kind<KIND>()) rc = sg * fmaxf(th32i, th32j);
-    else rc = sg;
+    if constexpr (cut_kind<KIND>()) {
+        rc = sg * fmaxf(Qi.z, Qj.z);
+    } else if constexpr (lois_kind<KIND>()) {
+        const bool mn = uni & COMB_MIN;
+        const float th = mn ? fminf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
+        const float l = mn ? fminf(Qi.w, Qj.w) : 0.5f * (Qi.w + Qj.w);
+        rc = (KIND == KIND_LOISOHERN) ? sg * (1.0f + th + l) : sg + l;
+    } else {
+        rc = sg;
+    }
     return d2 > rc * rc * 1.0002f;
 }
 
@@ -193,8 +265,8 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             float4 Aj, Bj;
             ld_pos(c.pos, j, Aj, Bj);
             float4 Qj = Qi;
-            if ((uni & (UNI_SIG | UNI_THIRD)) != (UNI_SIG | UNI_THIRD)) Qj = c.prm32[j];
-            if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi.y, Qj.y, Qi.z, Qj.z, uni)) continue;
+            if ((uni & (UNI_SIG | UNI_THIRD | UNI_FOURTH)) != (UNI_SIG | UNI_THIRD | UNI_FOURTH)) Qj = c.prm32[j];
+            if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi, Qj, uni)) continue;
             double xj[3] = {0, 0, 0};
             load3<ND>(c.x, j, xj);
             double r[3] = {0, 0, 0};
@@ -203,7 +275,7 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             double dsq = r[0] * r[0] + r[1] * r[1];
             if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
             AtomPrm Pj = Pi;
-            if ((uni & (UNI_EPS | UNI_SIG | UNI_THIRD)) != (UNI_EPS | UNI_SIG | UNI_THIRD)) Pj = c.prm[j];
+            if ((uni & UNI_ALL) != UNI_ALL) Pj = c.prm[j];
             const PairC pc = combine<KIND>(Pi, Pj, uni);
             double sc;
             if (!force_scale<KIND>(pc, dsq, uni, sc)) continue;
@@ -293,6 +365,8 @@ template <int ND>
 static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     if (c.kind == KIND_LJCUT) force64_nd_kind<ND, KIND_LJCUT>(c, s, mode);
     else if (c.kind == KIND_LJATTRACT) force64_nd_kind<ND, KIND_LJATTRACT>(c, s, mode);
+    else if (c.kind == KIND_LOISOHERN) force64_nd_kind<ND, KIND_LOISOHERN>(c, s, mode);
+    else if (c.kind == KIND_LOISLIN) force64_nd_kind<ND, KIND_LOISLIN>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -306,6 +380,8 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     unsigned g = grid_for(c.n);
     if (c.kind == KIND_LJCUT) k_eval64<ND, KIND_LJCUT><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LJATTRACT) k_eval64<ND, KIND_LJATTRACT><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LOISOHERN) k_eval64<ND, KIND_LOISOHERN><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LOISLIN) k_eval64<ND, KIND_LOISLIN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

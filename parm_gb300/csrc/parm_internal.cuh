@@ -22,7 +22,13 @@
 
 namespace parm {
 
-enum PairKind : int { KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2, KIND_LJATTRACT = 3 };
+enum PairKind : int {
+    KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2, KIND_LJATTRACT = 3,
+    // four-parameter atoms (eps, sigma, C, l) / (eps, sigma, f, l); FP64 path only
+    KIND_LOISOHERN = 4, KIND_LOISLIN = 5
+};
+template <int KIND>
+__host__ __device__ constexpr bool lois_kind() { return KIND == KIND_LOISOHERN || KIND == KIND_LOISLIN; }
 // kinds whose pair cut-off is max(sigcut_i, sigcut_j) sigma_ij, with a force
 // that jumps there (LJ truncated without shift)
 template <int KIND>
@@ -77,6 +83,12 @@ enum UniformFlags : uint32_t {
     UNI_SIG = 1u << 1,     // all members share sigma   -> sig_ij = sig
     UNI_THIRD = 1u << 2,   // all members share sigcut / exponent
     UNI_SIG_ONE = 1u << 3, // sigma == 1 exactly -> dsq / (sig*sig) == dsq
+    UNI_FOURTH = 1u << 4,  // all members share the fourth parameter (p3)
+    UNI_ALL = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_FOURTH,
+    // not a uniformity flag: the Lois pairs combine C (or f) and l as the
+    // smaller of the two atoms' values (LoisOhernPairMinCLs, LoisLinPairMin)
+    // instead of their average
+    COMB_MIN = 1u << 5,
 };
 
 template <int ND> struct DVec;

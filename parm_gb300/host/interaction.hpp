@@ -230,6 +230,124 @@ struct LJAttractCutPair {
     }
 };
 
+//! Sticky spheres (src/interaction.hpp:1679-1691): repulsive epsilon, sigma,
+//! and the widths C and l of the two halves of the attractive well.
+struct LoisOhernAtom : public AtomID {
+    flt eps, sigma, C, l;
+    LoisOhernAtom() : eps(0), sigma(0), C(0), l(0) {}
+    LoisOhernAtom(AtomID a, flt eps, flt sigma, flt C, flt l) : AtomID(a), eps(eps), sigma(sigma), C(C), l(l) {}
+    LoisOhernAtom(AtomID a, LoisOhernAtom other)
+        : AtomID(a), eps(other.eps), sigma(other.sigma), C(other.C), l(other.l) {}
+    flt max_size() { return sigma * (1 + C + l); }
+};
+
+//! Lois-O'Hern pair (src/interaction.hpp:1693-1744): harmonic about sigma out
+//! to (1 + C) sigma, then a linear return to zero force at sigcut =
+//! sigma (1 + C + l); epsilon geometric mean, the rest averaged.
+struct LoisOhernPair {
+    static const int kind = PARM_LOISOHERN;
+    static void params(const LoisOhernAtom& a, double p[4]) {
+        p[0] = a.eps;
+        p[1] = a.sigma;
+        p[2] = a.C;
+        p[3] = a.l;
+    }
+    flt eps, sig, C, l, sigcut;
+    AtomID atom1, atom2;
+    LoisOhernPair(LoisOhernAtom a1, LoisOhernAtom a2)
+        : LoisOhernPair(a1, a2, std::sqrt(a1.eps * a2.eps), (a1.sigma + a2.sigma) / 2.0, (a1.C + a2.C) / 2.0,
+                        (a1.l + a2.l) / 2.0) {}
+    LoisOhernPair(LoisOhernAtom a1, LoisOhernAtom a2, flt eps, flt sig, flt C, flt l)
+        : eps(eps), sig(sig), C(C), l(l), sigcut(sig * (1 + C + l)), atom1(a1), atom2(a2) {}
+    flt energy(Box& box) {
+        const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
+        if (dsq >= sigcut * sigcut) return 0.0;
+        const flt R = std::sqrt(dsq) / sig;
+        if (R <= 1 + C) {
+            const flt dR = R - 1;
+            return -eps * sig / 2 * (C * (C + l) - dR * dR);
+        }
+        const flt dR2 = C + l + 1 - R;
+        return -C * eps * sig / 2 / l * dR2 * dR2;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq >= sigcut * sigcut) return Vec::Zero();
+        const flt R = std::sqrt(dsq);
+        const flt rsig = R / sig;
+        if (rsig <= 1 + C) return rij * (-eps * (rsig - 1) / R);
+        return rij * (C * eps / l * (rsig - (C + l + 1)) / R);
+    }
+};
+
+//! Lois-O'Hern pair with the smaller C and l of the two atoms
+//! (src/interaction.hpp:1746-1751).
+struct LoisOhernPairMinCLs : public LoisOhernPair {
+    static const int kind = PARM_LOISOHERN_MIN;
+    LoisOhernPairMinCLs(LoisOhernAtom a1, LoisOhernAtom a2)
+        : LoisOhernPair(a1, a2, std::sqrt(a1.eps * a2.eps), (a1.sigma + a2.sigma) / 2.0, (a1.C < a2.C ? a1.C : a2.C),
+                        (a1.l < a2.l ? a1.l : a2.l)) {}
+};
+
+//! Harmonic repulsion with a fixed attractive force (src/interaction.hpp:
+//! 1764-1780): the constructor takes the well's depth and width and keeps
+//! f = depth / width (0 for width 0) and l = width.
+struct LoisLinAtom : public AtomID {
+    flt eps, sigma, f, l;
+    LoisLinAtom() : eps(0), sigma(0), f(0), l(0) {}
+    LoisLinAtom(AtomID a, flt eps, flt sigma, flt depth, flt width)
+        : AtomID(a), eps(eps), sigma(sigma), f(width > 0 ? depth / width : 0), l(width) {}
+    LoisLinAtom(AtomID a, LoisLinAtom other) : AtomID(a), eps(other.eps), sigma(other.sigma), f(other.f), l(other.l) {}
+    flt max_size() { return sigma * (1 + l); }
+};
+
+//! Lois-Lin pair (src/interaction.hpp:1782-1829): harmonic inside sigma, a
+//! constant attractive force f out to sigcut = sigma + l.
+struct LoisLinPair {
+    static const int kind = PARM_LOISLIN;
+    static void params(const LoisLinAtom& a, double p[4]) {
+        p[0] = a.eps;
+        p[1] = a.sigma;
+        p[2] = a.f;
+        p[3] = a.l;
+    }
+    flt eps, sig, f, l, sigcut;
+    AtomID atom1, atom2;
+    LoisLinPair(LoisLinAtom a1, LoisLinAtom a2)
+        : LoisLinPair(a1, a2, std::sqrt(a1.eps * a2.eps), (a1.sigma + a2.sigma) / 2.0, (a1.f + a2.f) / 2.0,
+                      (a1.l + a2.l) / 2.0) {}
+    LoisLinPair(LoisLinAtom a1, LoisLinAtom a2, flt eps, flt sig, flt f, flt l)
+        : eps(eps), sig(sig), f(f), l(l), sigcut(sig + l), atom1(a1), atom2(a2) {}
+    flt energy(Box& box) {
+        const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
+        if (dsq >= sigcut * sigcut) return 0.0;
+        const flt R = std::sqrt(dsq);
+        if (R <= sig) {
+            const flt dR = 1.0 - (R / sig);
+            return eps / 2 * dR * dR - f * l;
+        }
+        return -f * (sig + l - R);
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq >= sigcut * sigcut) return Vec::Zero();
+        const flt R = std::sqrt(dsq);
+        if (R <= sig) return rij * (eps * (1.0 - (R / sig)) / sig / R);
+        return rij * -(f / R);
+    }
+};
+
+//! Lois-Lin pair with the smaller f and l of the two atoms
+//! (src/interaction.hpp:1831-1836).
+struct LoisLinPairMin : public LoisLinPair {
+    static const int kind = PARM_LOISLIN_MIN;
+    LoisLinPairMin(LoisLinAtom a1, LoisLinAtom a2)
+        : LoisLinPair(a1, a2, std::sqrt(a1.eps * a2.eps), (a1.sigma + a2.sigma) / 2.0, (a1.f < a2.f ? a1.f : a2.f),
+                      (a1.l < a2.l ? a1.l : a2.l)) {}
+};
+
 // GPU-evaluated quantities of the handle's interaction
 flt gpu_evaluate(GpuLink& link, int what);
 Matrix gpu_stress(GpuLink& link);
@@ -252,7 +370,7 @@ class NListed : public Interaction, public GpuInteraction {
         init_atoms(*atomv);
     }
     void add(A atm) {
-        double p[3];
+        double p[4] = {0.0, 0.0, 0.0, 0.0};
         P::params(atm, p);
         link->add(atm.n(), P::kind, p, this);
         atoms.at(atm.n()) = atm;

@@ -115,7 +115,7 @@ void parm_host_check(int rc, const char* what) {
 GpuLink::GpuLink(sptr<Box> box, sptr<AtomVec> atoms, flt skin) : bx(box), atomv(atoms), skin_(skin) {
     if (!std::dynamic_pointer_cast<OriginBox>(bx))
         throw std::invalid_argument("parm_gb300: the GPU path supports periodic OriginBox boxes");
-    params.assign(3 * (size_t)atomv->size(), 0.0);
+    params.assign(4 * (size_t)atomv->size(), 0.0);
     rank.assign(atomv->size(), PARM_NOT_MEMBER);
     ldiam.assign(atomv->size(), std::nan(""));
 }
@@ -124,7 +124,7 @@ GpuLink::~GpuLink() {
     if (h) parm_destroy(h);
 }
 
-void GpuLink::add(uint atom, int k, const double p[3], const void* owner) {
+void GpuLink::add(uint atom, int k, const double p[4], const void* owner) {
     if (atom >= atomv->size()) throw std::out_of_range("NListed::add: atom not in this AtomVec");
     if (owner_ && owner != owner_)
         throw std::invalid_argument("parm_gb300: one NListed interaction per NeighborList");
@@ -132,7 +132,7 @@ void GpuLink::add(uint atom, int k, const double p[3], const void* owner) {
     if (rank[atom] != PARM_NOT_MEMBER) throw std::invalid_argument("NListed::add: atom added twice");
     owner_ = owner;
     kind = k;
-    for (int q = 0; q < 3; q++) params[3 * (size_t)atom + q] = p[q];
+    for (int q = 0; q < PARM_NPARAM(k); q++) params[4 * (size_t)atom + q] = p[q];
     rank[atom] = nmembers++;
     interaction_dirty = true;
 }
@@ -168,8 +168,12 @@ void GpuLink::push() {
         if (any_ldiam) parm_host_check(parm_set_list_diameters(h, ldiam.data()), "parm_set_list_diameters");
         // members without an NListed carry no parameters: any law with zero
         // epsilon gives them no force
-        parm_host_check(parm_set_interaction(h, kind >= 0 ? kind : PARM_REPULSION, params.data(), rank.data(), skin_),
-                        "parm_set_interaction");
+        const int k = kind >= 0 ? kind : PARM_REPULSION;
+        const size_t np = PARM_NPARAM(k), n = atomv->size();
+        std::vector<double> packed(np * n);
+        for (size_t i = 0; i < n; i++)
+            for (size_t q = 0; q < np; q++) packed[np * i + q] = params[4 * i + q];
+        parm_host_check(parm_set_interaction(h, k, packed.data(), rank.data(), skin_), "parm_set_interaction");
         interaction_dirty = false;
     }
     for (auto& pr : pending_ignores) parm_host_check(parm_nlist_ignore(h, pr.first, pr.second), "parm_nlist_ignore");

@@ -31,10 +31,11 @@ class GpuLink {
     GpuLink(const GpuLink&) = delete;
     GpuLink& operator=(const GpuLink&) = delete;
 
-    //! NListed::add: per-atom parameters (kind: PARM_LJCUT, ...) and the
-    //! atom's position in the neighbour list (insertion order); `owner` is
-    //! the NListed adding it (one NListed per neighbour list)
-    void add(uint atom, int kind, const double p[3], const void* owner);
+    //! NListed::add: per-atom parameters (kind: PARM_LJCUT, ...; the first
+    //! PARM_NPARAM(kind) of p) and the atom's position in the neighbour list
+    //! (insertion order); `owner` is the NListed adding it (one NListed per
+    //! neighbour list)
+    void add(uint atom, int kind, const double p[4], const void* owner);
     //! NeighborList::add(atom, diameter): a list member with its own list
     //! diameter and no pair parameters (its pairs carry no force)
     void add_member(uint atom, double diameter);
@@ -61,7 +62,7 @@ class GpuLink {
     flt skin_;
     parm_system* h = nullptr;
     int kind = -1;
-    std::vector<double> params;
+    std::vector<double> params;   // four per atom
     std::vector<uint32_t> rank;
     std::vector<double> ldiam;   // explicit list diameters (NaN: the parameters' max_size())
     bool any_ldiam = false;

@@ -95,7 +95,7 @@ class System:
 
     # -- interaction / neighbour list --
     def set_interaction(self, kind: int, params, skin: float, rank=None) -> None:
-        p = _as_f64(params, (self.n, 3))
+        p = _as_f64(params, (self.n, capi.nparam(kind)))
         rk = None
         if rank is not None:
             rk = np.ascontiguousarray(np.asarray(rank, dtype=np.uint32))

@@ -115,3 +115,53 @@ def test_cell_scale_leaves_results_unchanged(precision):
             np.testing.assert_array_equal(out[0][2][k], out[1][2][k])
     else:
         assert force_error(out[1][1], out[0][1]) <= 1e-5
+
+
+@pytest.mark.parametrize("kind", [4, 5, 6, 7])
+def test_lois_uniform_parameters_match_oracle(kind):
+    """The Lois-O'Hern / Lois-Lin pairs with shared C (or f) and l, and with only l varying: pair list,
+    forces and 50 Verlet steps bit-exact against the oracle (the uniform-parameter shortcuts of the FP64
+    kernels and the list build)."""
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    rng = np.random.default_rng(70 + kind)
+    n = 300
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    L = (np.sum(np.pi * sig ** 3 / 6) / 0.55) ** (1 / 3)
+    x = rng.uniform(0, L, (n, 3))
+    v = rng.normal(0, 0.05, (n, 3))
+    third = 0.08 if kind < 6 else 0.04
+    for lvals in (np.full(n, 0.05), rng.choice([0.03, 0.06], n)):
+        params = np.stack([np.ones(n), sig, np.full(n, third), lvals], 1)
+        g = System(n, ndim=3, precision="fp64")
+        g.set_boxes(np.full((1, 3), L))
+        g.set_atoms(x=x, v=v, a=np.zeros((n, 3)), f=np.zeros((n, 3)), m=np.ones(n))
+        g.set_interaction(kind, params, 0.2)
+        o = Oracle(n, 3)
+        o.set_box(np.full(3, L))
+        o.set_state(x=x, v=v, m=np.ones(n))
+        o.set_interaction(kind, params, 0.2)
+        g.nlist_update(True)
+        o.nl_update(True)
+        assert np.array_equal(g.pairs(), o.pairs())
+        g.set_forces(True)
+        o.set_forces(True)
+        assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+        g.verlet(0.005, 50)
+        o.verlet(0.005, 50)
+        st, ref = g.get_atoms(), o.get_state()
+        for k in ("x", "v", "f"):
+            assert np.array_equal(st[k], ref[k]), k
+        assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-13)
+        g.close()
+
+
+def test_lois_kinds_need_fp64_handles():
+    from parm_gb300 import System
+    w = W.small_random(n=64, ndim=3, kind=1, seed=3)
+    g = System(w.n, ndim=3, precision="mixed")
+    g.set_boxes(w.L)
+    g.set_atoms(x=w.x, v=w.v, a=np.zeros_like(w.x), f=np.zeros_like(w.x), m=w.m)
+    with pytest.raises(ValueError, match="FP64"):
+        g.set_interaction(4, np.tile([1.0, 1.0, 0.1, 0.05], (w.n, 1)), 0.2)
+    g.close()

@@ -63,7 +63,7 @@ def _close(got, want, exact, what):
 def test_host_api_matches_reference(drivers, name):
     d = load(name)
     case = {k: d[k] for k in ("kind", "integ", "nsteps", "dt", "damping", "T", "skin", "L", "x", "v", "m",
-                              "params", "order", "ignores", "out_steps", "cg") if k in d}
+                              "params", "deck_params", "order", "ignores", "out_steps", "cg") if k in d}
     deck = MG._deck(case)
     r = subprocess.run([str(drivers[d["ndim"]])], input=deck, capture_output=True, text=True, timeout=600,
                        env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
