@@ -45,7 +45,7 @@ extern "C" {
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
 /* Four-parameter atoms (params: natoms*4 doubles, the atoms' fields); FP64
- * handles only (a mixed-precision handle rejects them). */
+ * handles only (a mixed-precision handle rejects them, and PARM_EISMCLACHLAN). */
 #define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
                                 1679-1744): params (eps, sigma, C, l), C and l averaged */
 #define PARM_LOISOHERN_MIN 5 /* NListed<LoisOhernAtom, LoisOhernPairMinCLs> (1746-1751): the smaller C, l */
@@ -53,8 +53,11 @@ extern "C" {
                                 the fields LoisLinAtom(eps, sigma, depth, width) stores:
                                 f = depth / width (0 for width 0), l = width; f and l averaged */
 #define PARM_LOISLIN_MIN 7   /* NListed<LoisLinAtom, LoisLinPairMin> (1831-1836): the smaller f, l */
+#define PARM_EISMCLACHLAN 8  /* NListed<EisMclachlanAtom, EisMclachlanPair> (implicit solvation,
+                                src/interaction.hpp:1415-1452): params (dist, sigmai, unused);
+                                FP64 handles only */
 /* doubles per atom in parm_set_interaction's params */
-#define PARM_NPARAM(kind) ((kind) >= PARM_LOISOHERN ? 4 : 3)
+#define PARM_NPARAM(kind) (((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) ? 4 : 3)
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u

@@ -39,11 +39,11 @@ namespace {
 
 enum PairKind {
     LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3,
-    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7
+    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7, EISMCLACHLAN = 8
 };
 
 // kinds whose atoms carry four parameters
-inline bool four_params(int kind) { return kind >= LOISOHERN; }
+inline bool four_params(int kind) { return kind >= LOISOHERN && kind <= LOISLIN_MIN; }
 
 struct V3 {
     double c[3] = {0, 0, 0};
@@ -160,6 +160,14 @@ struct System {
             }
             pc.cut = pc.sig + pc.fourth;
             pc.cut_energy = 0;
+        } else if (kind == EISMCLACHLAN) {
+            // EisMclachlanPair(EisMclachlanAtom, EisMclachlanAtom) (interaction.hpp:1425-1438):
+            // E = c0/R + c1 + c2 R out to dist1 + dist2 (atom fields p0 = dist, p1 = sigmai)
+            pc.eps = -M_PI * (A.p1 * B.p0 - B.p1 * A.p0) * (A.p0 * A.p0 - B.p0 * B.p0);      // c0
+            pc.sig = -2 * M_PI * (A.p1 * B.p0 * B.p0 + B.p1 * A.p0 * A.p0);                // c1
+            pc.third = M_PI * (A.p1 * B.p0 + B.p1 * A.p0);                                 // c2
+            pc.cut = A.p0 + B.p0;
+            pc.cut_energy = 0;
         } else {
             // LJRepulsePair(EpsSigAtom, EpsSigAtom) (interaction.hpp:875-880)
             pc.eps = std::sqrt(A.p0 * B.p0);
@@ -220,6 +228,11 @@ struct System {
                 return pc.eps / 2 * dR * dR - f * l;
             }
             return -f * (pc.sig + l - R);
+        } else if (kind == EISMCLACHLAN) {
+            // EisMclachlanPair::energy (interaction.hpp:1439-1444)
+            double R = std::sqrt(dsq);
+            if (R > pc.cut) return 0;
+            return pc.eps / R + pc.sig + pc.third * R;
         } else {
             // LJRepulsive::energy (interaction.hpp:127-134)
             double rsq = dsq / (pc.sig * pc.sig);
@@ -280,6 +293,11 @@ struct System {
             } else {
                 s = -(f / R);
             }
+        } else if (kind == EISMCLACHLAN) {
+            // EisMclachlanPair::forces (interaction.hpp:1445-1451)
+            if (dsq > (pc.cut * pc.cut)) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double R = std::sqrt(dsq);
+            s = (pc.eps / dsq - pc.third) / R;
         } else {
             // LJRepulsive::forces (interaction.hpp:136-150)
             double rsq = dsq / (pc.sig * pc.sig);
@@ -298,6 +316,7 @@ struct System {
         // LoisOhernAtom::max_size (interaction.hpp:1691), LoisLinAtom::max_size (1780)
         if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
         if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
+        if (kind == EISMCLACHLAN) return params[i].p0;   // EisMclachlanAtom::max_size (1423)
         return params[i].p1;
     }
 
@@ -844,7 +863,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 7) return -1;
+    if (kind < 0 || kind > 8) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;

@@ -28,12 +28,14 @@ namespace {
 thread_local std::string g_err;
 
 // A::max_size() of the atom types (src/interaction.hpp: EpsSigCutAtom 904,
-// EpsSigExpAtom 1464, EpsSigAtom 864, LoisOhernAtom 1691, LoisLinAtom 1780):
+// EpsSigExpAtom 1464, EpsSigAtom 864, LoisOhernAtom 1691, LoisLinAtom 1780,
+// EisMclachlanAtom 1423):
 // the atom's diameter in its neighbour list
 double atom_max_size(int kind, const double* p) {
     if (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) return p[1] * p[2];
     if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return p[1] * (1 + p[2] + p[3]);
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return p[1] * (1 + p[3]);
+    if (kind == PARM_EISMCLACHLAN) return p[0];
     return p[1];
 }
 
@@ -41,6 +43,7 @@ double atom_max_size(int kind, const double* p) {
 int device_kind(int kind) {
     if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return KIND_LOISOHERN;
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return KIND_LOISLIN;
+    if (kind == PARM_EISMCLACHLAN) return KIND_EISMCLACHLAN;
     return kind;
 }
 
@@ -1336,9 +1339,9 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > PARM_LOISLIN_MIN) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > PARM_EISMCLACHLAN) return fail(PARM_ERR_ARG, "unknown pair kind");
     if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
-        return fail(PARM_ERR_ARG, "the Lois-O'Hern and Lois-Lin pairs run on FP64 handles only");
+        return fail(PARM_ERR_ARG, "the Lois-O'Hern, Lois-Lin and Eis-Mclachlan pairs run on FP64 handles only");
     if (!(skin >= 0.0) || !std::isfinite(skin)) return fail(PARM_ERR_ARG, "skin must be >= 0");
     TRY(S->flush());
     CUDA_TRY(cudaStreamSynchronize(S->st));
@@ -1365,7 +1368,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     std::vector<uint32_t> nmr(n, 0);
     bool first = true;
     double e0 = 0, s0 = 0, t0 = 0, u0 = 0;
-    uint32_t uni = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_FOURTH | UNI_SIG_ONE;
+    uint32_t uni = UNI_EPS | UNI_SIG | UNI_THIRD | UNI_FOURTH | UNI_SIG_ONE | UNI_DIAM;
+    double d0 = 0;
     for (uint32_t s = 0; s < S->nsys; s++) {
         uint32_t nm = 0;
         for (uint32_t i = 0; i < S->natoms[s]; i++) {
@@ -1386,7 +1390,9 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 }
             }
             prm[g] = a;
-            prm32[g] = make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
+            prm32[g] = (kind == PARM_EISMCLACHLAN)
+                           ? make_float4((float)a.p0, (float)a.p1, 0.f, 0.f)   // (dist, sigmai)
+                           : make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
             diam[g] = atom_max_size(kind, p);
             const bool explicit_d = !S->ldiam.empty() && std::isfinite(S->ldiam[g]);
             if (explicit_d) diam[g] = S->ldiam[g];   // NeighborList::add(atom, diameter)
@@ -1394,8 +1400,12 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 nmr[g] = nm++;
                 continue;
             }
-            if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0)))
+            if (kind == PARM_EISMCLACHLAN) {
+                if (!(a.p0 >= 0.0 && std::isfinite(a.p0) && std::isfinite(a.p1)))
+                    return fail(PARM_ERR_ARG, "dist must be finite and >= 0, sigmai finite");
+            } else if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0))) {
                 return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
+            }
             if (np == 4 && !(std::isfinite(a.p2) && std::isfinite(a.p3) && a.p2 >= 0.0 && a.p3 >= 0.0))
                 return fail(PARM_ERR_ARG, "C (or f) and l must be finite and >= 0");
             if (first) {
@@ -1403,8 +1413,10 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 s0 = a.p1;
                 t0 = a.p2;
                 u0 = a.p3;
+                d0 = diam[g];
                 first = false;
             }
+            if (diam[g] != d0) uni &= ~UNI_DIAM;
             if (a.p0 != e0) uni &= ~UNI_EPS;
             if (a.p1 != s0) uni &= ~UNI_SIG;
             if (a.p2 != t0) uni &= ~UNI_THIRD;

@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(DevCtx c) {
     const bool wrap0 = WRAP && r0 == 0, wrap1 = WRAP && r1 == 0, wrap2 = WRAP && (ND == 3) && r2 == 0;
     const float kShift = 12582912.0f;
     const float skin32 = (float)S.skin;
-    const bool uni_thr = (c.uniform & UNI_SIG) && (c.uniform & UNI_THIRD) && (c.uniform & UNI_FOURTH);
+    const bool uni_thr = c.uniform & UNI_DIAM;
     const uint32_t maxnb = c.maxnb;
     for (uint32_t hb = cs; hb < ce; hb += 32) {
         const uint32_t mh = min(32u, ce - hb);

@@ -10,6 +10,7 @@
 //   LJAttractCut + LJAttractCutPair         154-236, 1020-1050
 //   LoisOhernPair, LoisOhernPairMinCLs      1679-1751
 //   LoisLinPair, LoisLinPairMin             1764-1836
+//   EisMclachlanPair                        1415-1452
 //
 // Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
 // scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
@@ -59,6 +60,15 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
         // sigcut: sig * (1 + C + l) (LoisOhern), sig + l (LoisLin)
         p.cut = (KIND == KIND_LOISOHERN) ? p.sig * (1 + p.third + p.m6) : p.sig + p.m6;
         return p;
+    } else if constexpr (KIND == KIND_EISMCLACHLAN) {
+        // EisMclachlanPair(a1, a2) (interaction.hpp:1425-1438), atoms (dist, sigmai) =
+        // (p0, p1): E = c0/R + c1 + c2 R with c0, c1, c2 in eps, sig, third; cut-off d1 + d2
+        p.eps = -M_PI * (A.p1 * B.p0 - B.p1 * A.p0) * (A.p0 * A.p0 - B.p0 * B.p0);
+        p.sig = -2 * M_PI * (A.p1 * B.p0 * B.p0 + B.p1 * A.p0 * A.p0);
+        p.third = M_PI * (A.p1 * B.p0 + B.p1 * A.p0);
+        p.m6 = 0.0;
+        p.cut = A.p0 + B.p0;
+        return p;
     } else {
         p.third = 0.0;
         p.m6 = 0.0;
@@ -107,6 +117,12 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
             double dR2 = rsig - (C + l + 1);
             s = C * p.eps / l * dR2 / R;
         }
+        return true;
+    } else if constexpr (KIND == KIND_EISMCLACHLAN) {
+        // EisMclachlanPair::forces (interaction.hpp:1445-1451)
+        if (dsq > (p.cut * p.cut)) return false;
+        double R = sqrt(dsq);
+        s = (p.eps / dsq - p.third) / R;
         return true;
     } else if constexpr (KIND == KIND_LOISLIN) {
         // LoisLinPair::forces (interaction.hpp:1817-1828); -rij * (f / R) == rij * -(f / R)
@@ -169,6 +185,11 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         }
         double dR2 = C + l + 1 - R;
         return -C * p.eps * p.sig / 2 / l * dR2 * dR2;
+    } else if constexpr (KIND == KIND_EISMCLACHLAN) {
+        // EisMclachlanPair::energy (interaction.hpp:1439-1444)
+        double R = sqrt(dsq);
+        if (R > p.cut) return 0.0;
+        return p.eps / R + p.sig + p.third * R;
     } else if constexpr (KIND == KIND_LOISLIN) {
         // LoisLinPair::energy (interaction.hpp:1802-1815)
         const double f = p.third, l = p.m6;
@@ -201,6 +222,8 @@ __device__ __forceinline__ bool beyond32(float d2, const float4& Qi, const float
         const float th = mn ? fminf(Qi.z, Qj.z) : 0.5f * (Qi.z + Qj.z);
         const float l = mn ? fminf(Qi.w, Qj.w) : 0.5f * (Qi.w + Qj.w);
         rc = (KIND == KIND_LOISOHERN) ? sg * (1.0f + th + l) : sg + l;
+    } else if constexpr (KIND == KIND_EISMCLACHLAN) {
+        rc = Qi.x + Qj.x;   // dist_i + dist_j
     } else {
         rc = sg;
     }
@@ -265,7 +288,7 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             float4 Aj, Bj;
             ld_pos(c.pos, j, Aj, Bj);
             float4 Qj = Qi;
-            if ((uni & (UNI_SIG | UNI_THIRD | UNI_FOURTH)) != (UNI_SIG | UNI_THIRD | UNI_FOURTH)) Qj = c.prm32[j];
+            if ((uni & UNI_ALL) != UNI_ALL) Qj = c.prm32[j];
             if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi, Qj, uni)) continue;
             double xj[3] = {0, 0, 0};
             load3<ND>(c.x, j, xj);
@@ -367,6 +390,7 @@ static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     else if (c.kind == KIND_LJATTRACT) force64_nd_kind<ND, KIND_LJATTRACT>(c, s, mode);
     else if (c.kind == KIND_LOISOHERN) force64_nd_kind<ND, KIND_LOISOHERN>(c, s, mode);
     else if (c.kind == KIND_LOISLIN) force64_nd_kind<ND, KIND_LOISLIN>(c, s, mode);
+    else if (c.kind == KIND_EISMCLACHLAN) force64_nd_kind<ND, KIND_EISMCLACHLAN>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -382,6 +406,7 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     else if (c.kind == KIND_LJATTRACT) k_eval64<ND, KIND_LJATTRACT><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LOISOHERN) k_eval64<ND, KIND_LOISOHERN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LOISLIN) k_eval64<ND, KIND_LOISLIN><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_EISMCLACHLAN) k_eval64<ND, KIND_EISMCLACHLAN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

@@ -25,7 +25,9 @@ namespace parm {
 enum PairKind : int {
     KIND_LJCUT = 0, KIND_REPULSION = 1, KIND_LJREPULSE = 2, KIND_LJATTRACT = 3,
     // four-parameter atoms (eps, sigma, C, l) / (eps, sigma, f, l); FP64 path only
-    KIND_LOISOHERN = 4, KIND_LOISLIN = 5
+    KIND_LOISOHERN = 4, KIND_LOISLIN = 5,
+    // (dist, sigmai) atoms, E = c0/R + c1 + c2 R; FP64 path only
+    KIND_EISMCLACHLAN = 6
 };
 template <int KIND>
 __host__ __device__ constexpr bool lois_kind() { return KIND == KIND_LOISOHERN || KIND == KIND_LOISLIN; }
@@ -89,6 +91,7 @@ enum UniformFlags : uint32_t {
     // smaller of the two atoms' values (LoisOhernPairMinCLs, LoisLinPairMin)
     // instead of their average
     COMB_MIN = 1u << 5,
+    UNI_DIAM = 1u << 6,    // all members share their list diameter
 };
 
 template <int ND> struct DVec;

@@ -348,6 +348,48 @@ struct LoisLinPairMin : public LoisLinPair {
                       (a1.l < a2.l ? a1.l : a2.l)) {}
 };
 
+//! Implicit-solvation atom (src/interaction.hpp:1415-1423): dist = the
+//! atom's radius plus the water radius, sigmai its solvation parameter.
+struct EisMclachlanAtom : public AtomID {
+    flt dist, sigmai;
+    EisMclachlanAtom() : dist(0), sigmai(0) {}
+    EisMclachlanAtom(AtomID a, flt dist, flt sigmai) : AtomID(a), dist(dist), sigmai(sigmai) {}
+    EisMclachlanAtom(AtomID a, EisMclachlanAtom other) : AtomID(a), dist(other.dist), sigmai(other.sigmai) {}
+    flt max_size() { return dist; }
+};
+
+//! Eisenberg-McLachlan pair (src/interaction.hpp:1425-1452): E = c0/R + c1 +
+//! c2 R out to dist_1 + dist_2.
+struct EisMclachlanPair {
+    static const int kind = PARM_EISMCLACHLAN;
+    static void params(const EisMclachlanAtom& a, double p[4]) {
+        p[0] = a.dist;
+        p[1] = a.sigmai;
+        p[2] = 0.0;
+    }
+    flt c0, c1, c2, cutoff;
+    AtomID atom1, atom2;
+    EisMclachlanPair(EisMclachlanAtom a1, EisMclachlanAtom a2)
+        : c0(-M_PI * (a1.sigmai * a2.dist - a2.sigmai * a1.dist) * (a1.dist * a1.dist - a2.dist * a2.dist)),
+          c1(-2 * M_PI * (a1.sigmai * a2.dist * a2.dist + a2.sigmai * a1.dist * a1.dist)),
+          c2(M_PI * (a1.sigmai * a2.dist + a2.sigmai * a1.dist)),
+          cutoff(a1.dist + a2.dist),
+          atom1(a1),
+          atom2(a2) {}
+    flt energy(Box& box) {
+        const flt R = box.diff(atom1->x, atom2->x).norm();
+        if (R > cutoff) return 0;
+        return c0 / R + c1 + c2 * R;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq > (cutoff * cutoff)) return Vec::Zero();
+        const flt R = std::sqrt(dsq);
+        return rij * ((c0 / dsq - c2) / R);
+    }
+};
+
 // GPU-evaluated quantities of the handle's interaction
 flt gpu_evaluate(GpuLink& link, int what);
 Matrix gpu_stress(GpuLink& link);

@@ -35,7 +35,7 @@ REFOUT = ROOT / "oracle" / "_ref"
 
 VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
-LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN = 4, 5, 6, 7
+LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN = 4, 5, 6, 7, 8
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -296,6 +296,16 @@ def cases() -> list[dict]:
                      rng.uniform(0, Ll2, (n, 2)), rng.normal(0, 0.1, (n, 2)), np.ones(n),
                      np.stack([np.ones(n), sig, f, width], 1), 0.2, [1, 10, 100, 400],
                      deck_params=np.stack([np.ones(n), sig, depth, width], 1)))
+    # 17. EisMclachlanPair (implicit solvation, E = c0/R + c1 + c2 R out to dist_i + dist_j),
+    #     per-atom dist and solvation parameter of either sign, 3D, damped
+    rng = np.random.default_rng(65)
+    n = 180
+    Le = 9.0
+    dist = rng.choice([1.6, 1.9, 2.2], n)
+    sigi = rng.choice([-0.012, 0.006, 0.018], n)
+    out.append(_case("eismclachlan180_damped", EISMCLACHLAN, DAMPED, 200, 0.005, [Le] * 3,
+                     rng.uniform(0, Le, (n, 3)), rng.normal(0, 0.02, (n, 3)), np.ones(n),
+                     np.stack([dist, sigi, np.zeros(n)], 1), 0.3, [1, 10, 100, 200], damping=0.5))
     return out
 
 

@@ -165,3 +165,36 @@ def test_lois_kinds_need_fp64_handles():
     with pytest.raises(ValueError, match="FP64"):
         g.set_interaction(4, np.tile([1.0, 1.0, 0.1, 0.05], (w.n, 1)), 0.2)
     g.close()
+
+
+def test_eismclachlan_uniform_dist_matches_oracle():
+    """Eis-Mclachlan atoms sharing their dist (the uniform list-diameter path of the FP64 list build)
+    with solvation parameters of either sign: pairs, forces and 50 damped steps bit-exact against the
+    oracle."""
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    rng = np.random.default_rng(81)
+    n, L = 250, 10.0
+    x = rng.uniform(0, L, (n, 3))
+    params = np.stack([np.full(n, 1.8), rng.choice([-0.01, 0.015], n), np.zeros(n)], 1)
+    g = System(n, ndim=3, precision="fp64")
+    g.set_boxes(np.full((1, 3), L))
+    g.set_atoms(x=x, v=np.zeros((n, 3)), a=np.zeros((n, 3)), f=np.zeros((n, 3)), m=np.ones(n))
+    g.set_interaction(8, params, 0.3)
+    o = Oracle(n, 3)
+    o.set_box(np.full(3, L))
+    o.set_state(x=x, v=np.zeros((n, 3)), m=np.ones(n))
+    o.set_interaction(8, params, 0.3)
+    g.nlist_update(True)
+    o.nl_update(True)
+    assert np.array_equal(g.pairs(), o.pairs())
+    g.set_forces(True)
+    o.set_forces(True)
+    assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+    g.damped(0.002, 0.5, 50)
+    o.damped(0.002, 0.5, 50)
+    st, ref = g.get_atoms(), o.get_state()
+    for k in ("x", "v", "f"):
+        assert np.array_equal(st[k], ref[k]), k
+    assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-12)
+    g.close()
