@@ -44,8 +44,8 @@ extern "C" {
                                LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
-/* Four-parameter atoms (params: natoms*4 doubles, the atoms' fields); FP64
- * handles only (a mixed-precision handle rejects them, and PARM_EISMCLACHLAN). */
+/* Kinds 4-9 run on FP64 handles only (a mixed-precision handle rejects
+ * them); kinds 4-7 and 9 take four parameters per atom (the atoms' fields). */
 #define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
                                 1679-1744): params (eps, sigma, C, l), C and l averaged */
 #define PARM_LOISOHERN_MIN 5 /* NListed<LoisOhernAtom, LoisOhernPairMinCLs> (1746-1751): the smaller C, l */
@@ -56,8 +56,14 @@ extern "C" {
 #define PARM_EISMCLACHLAN 8  /* NListed<EisMclachlanAtom, EisMclachlanPair> (implicit solvation,
                                 src/interaction.hpp:1415-1452): params (dist, sigmai, unused);
                                 FP64 handles only */
+#define PARM_REPULSIONDRAG 9 /* NListed<EpsSigExpDragAtom, RepulsionDragPair> (src/interaction.hpp:
+                                1598-1640): soft repulsion minus gamma times the relative normal
+                                velocity; params (eps, sigma, exponent, gamma), the fields
+                                EpsSigExpDragAtom(eps, sigma, gamma, exponent) stores; FP64 handles
+                                only */
 /* doubles per atom in parm_set_interaction's params */
-#define PARM_NPARAM(kind) (((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) ? 4 : 3)
+#define PARM_NPARAM(kind) \
+    ((((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) || (kind) == PARM_REPULSIONDRAG) ? 4 : 3)
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u

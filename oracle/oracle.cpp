@@ -39,11 +39,11 @@ namespace {
 
 enum PairKind {
     LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3,
-    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7, EISMCLACHLAN = 8
+    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7, EISMCLACHLAN = 8, REPULSIONDRAG = 9
 };
 
 // kinds whose atoms carry four parameters
-inline bool four_params(int kind) { return kind >= LOISOHERN && kind <= LOISLIN_MIN; }
+inline bool four_params(int kind) { return (kind >= LOISOHERN && kind <= LOISLIN_MIN) || kind == REPULSIONDRAG; }
 
 struct V3 {
     double c[3] = {0, 0, 0};
@@ -160,6 +160,14 @@ struct System {
             }
             pc.cut = pc.sig + pc.fourth;
             pc.cut_energy = 0;
+        } else if (kind == REPULSIONDRAG) {
+            // RepulsionDragPair(EpsSigExpDragAtom, EpsSigExpDragAtom) (interaction.hpp:1613-1621):
+            // atom fields (eps, sigma, exponent, gamma)
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.sig = (A.p1 + B.p1) / 2.0;
+            pc.third = (A.p2 + B.p2) / 2.0;
+            pc.fourth = (A.p3 + B.p3) / 2;
+            pc.cut_energy = 0;
         } else if (kind == EISMCLACHLAN) {
             // EisMclachlanPair(EisMclachlanAtom, EisMclachlanAtom) (interaction.hpp:1425-1438):
             // E = c0/R + c1 + c2 R out to dist1 + dist2 (atom fields p0 = dist, p1 = sigmai)
@@ -228,6 +236,11 @@ struct System {
                 return pc.eps / 2 * dR * dR - f * l;
             }
             return -f * (pc.sig + l - R);
+        } else if (kind == REPULSIONDRAG) {
+            // RepulsionDragPair::energy (interaction.hpp:1622-1628)
+            if (dsq > pc.sig * pc.sig) return 0.0;
+            double R = std::sqrt(dsq);
+            return pc.eps * std::pow(1.0 - (R / pc.sig), pc.third) / pc.third;
         } else if (kind == EISMCLACHLAN) {
             // EisMclachlanPair::energy (interaction.hpp:1439-1444)
             double R = std::sqrt(dsq);
@@ -243,10 +256,25 @@ struct System {
         }
     }
 
-    // P::forces(box); returns false when the pair is beyond its cutoff (force = 0)
-    bool pair_force(const PairConst& pc, const double* rij, double* fo) const {
+    // P::forces(box) of the pair (i, j); returns false when the pair is beyond its cutoff (force = 0)
+    bool pair_force(const PairConst& pc, const double* rij, double* fo, uint32_t i, uint32_t j) const {
         double dsq = dotv(rij, rij, nd);
         double s;
+        if (kind == REPULSIONDRAG) {
+            // RepulsionDragPair::forces (interaction.hpp:1629-1639): the repulsion minus gamma
+            // times the relative velocity's component along rij
+            double vij[3];
+            for (int d = 0; d < nd; d++) vij[d] = v[i * nd + d] - v[j * nd + d];
+            if (dsq > pc.sig * pc.sig) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double R = std::sqrt(dsq);
+            double vdot = dotv(vij, rij, nd);
+            double sr = pc.eps * std::pow(1.0 - (R / pc.sig), pc.third - 1) / pc.sig / R;
+            for (int d = 0; d < nd; d++) {
+                double vperp = rij[d] * vdot / dsq;
+                fo[d] = rij[d] * sr - vperp * pc.fourth;
+            }
+            return true;
+        }
         if (kind == LJCUT) {
             // LennardJonesCut::forces (interaction.hpp:263-271)
             double rsq = dsq / (pc.sig * pc.sig);
@@ -317,6 +345,7 @@ struct System {
         if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
         if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
         if (kind == EISMCLACHLAN) return params[i].p0;   // EisMclachlanAtom::max_size (1423)
+        // EpsSigExpDragAtom::max_size (1611) is sigma, as below
         return params[i].p1;
     }
 
@@ -376,7 +405,7 @@ struct System {
             PairConst pc = pair_const(pr.first, pr.second);
             double r[3], fo[3];
             diff(&x[pr.first * nd], &x[pr.second * nd], r);
-            pair_force(pc, r, fo);
+            pair_force(pc, r, fo, pr.first, pr.second);
             for (int d = 0; d < nd; d++) {
                 f[pr.first * nd + d] += fo[d];
                 f[pr.second * nd + d] -= fo[d];
@@ -412,7 +441,7 @@ struct System {
             PairConst pc = pair_const(pr.first, pr.second);
             double r[3], fo[3];
             diff(&x[pr.first * nd], &x[pr.second * nd], r);
-            pair_force(pc, r, fo);
+            pair_force(pc, r, fo, pr.first, pr.second);
             p += dotv(r, fo, nd);
             for (int aa = 0; aa < nd; aa++)
                 for (int bb = 0; bb < nd; bb++) st[aa * nd + bb] += r[aa] * fo[bb];
@@ -863,7 +892,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 8) return -1;
+    if (kind < 0 || kind > 9) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;

@@ -148,7 +148,7 @@ class Oracle:
     def set_interaction(self, kind, params, skin, order=None):
         """NListed(box, atoms, skin) and add() of every atom in `order`."""
         assert self.L_.orc_set_interaction(self.h, kind, float(skin)) == 0
-        params = np.asarray(params, dtype=np.float64).reshape(self.n, 4 if 4 <= kind <= 7 else 3)
+        params = np.asarray(params, dtype=np.float64).reshape(self.n, 4 if (4 <= kind <= 7 or kind == 9) else 3)
         order = range(self.n) if order is None else order
         for i in order:
             p = np.ascontiguousarray(params[i])

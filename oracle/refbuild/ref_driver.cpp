@@ -11,7 +11,8 @@
 //       2 <EpsSigAtom,LJRepulsePair>, 3 <EpsSigCutAtom,LJAttractCutPair>,
 //       4 <LoisOhernAtom,LoisOhernPair>, 5 <LoisOhernAtom,LoisOhernPairMinCLs> (p: eps sigma C l),
 //       6 <LoisLinAtom,LoisLinPair>, 7 <LoisLinAtom,LoisLinPairMin> (p: eps sigma depth width),
-//       8 <EisMclachlanAtom,EisMclachlanPair> (p: dist sigmai unused);
+//       8 <EisMclachlanAtom,EisMclachlanPair> (p: dist sigmai unused),
+//       9 <EpsSigExpDragAtom,RepulsionDragPair> (p: eps sigma gamma exponent);
 //       integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
@@ -65,13 +66,17 @@ template <>
 EisMclachlanAtom make_atom<EisMclachlanAtom>(AtomID id, int, const double* p) {
     return EisMclachlanAtom(id, p[0], p[1]);
 }
+template <>
+EpsSigExpDragAtom make_atom<EpsSigExpDragAtom>(AtomID id, int, const double* p) {
+    return EpsSigExpDragAtom(id, p[0], p[1], p[2], p[3]);
+}
 
 template <class A, class P>
 int run(int kind, int integ, int nsteps, double dt, double damping, double T, double skin) {
     Vec L;
     for (int d = 0; d < NDIM; d++) L[d] = rd();
     unsigned N = rdu();
-    const unsigned np = (kind >= 4 && kind <= 7) ? 4 : 3;
+    const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9) ? 4 : 3;
     std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * np);
     for (unsigned i = 0; i < N; i++) {
         for (int d = 0; d < NDIM; d++) xs[i * NDIM + d] = rd();
@@ -189,5 +194,6 @@ int main() {
     if (kind == 6) return run<LoisLinAtom, LoisLinPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 7) return run<LoisLinAtom, LoisLinPairMin>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 8) return run<EisMclachlanAtom, EisMclachlanPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 9) return run<EpsSigExpDragAtom, RepulsionDragPair>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

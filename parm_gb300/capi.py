@@ -32,11 +32,12 @@ LOISOHERN_MIN = 5
 LOISLIN = 6         # params (eps, sigma, f, l); FP64 handles
 LOISLIN_MIN = 7
 EISMCLACHLAN = 8    # params (dist, sigmai, unused); FP64 handles
+REPULSIONDRAG = 9   # params (eps, sigma, exponent, gamma); FP64 handles
 
 
 def nparam(kind: int) -> int:
     """Doubles per atom in parm_set_interaction's params."""
-    return 4 if LOISOHERN <= kind <= LOISLIN_MIN else 3
+    return 4 if (LOISOHERN <= kind <= LOISLIN_MIN or kind == REPULSIONDRAG) else 3
 
 X, V, A, F, M = 1, 2, 4, 8, 16
 

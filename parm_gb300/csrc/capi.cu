@@ -44,6 +44,7 @@ int device_kind(int kind) {
     if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return KIND_LOISOHERN;
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return KIND_LOISLIN;
     if (kind == PARM_EISMCLACHLAN) return KIND_EISMCLACHLAN;
+    if (kind == PARM_REPULSIONDRAG) return KIND_REPULSIONDRAG;
     return kind;
 }
 
@@ -1339,9 +1340,10 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > PARM_EISMCLACHLAN) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > PARM_REPULSIONDRAG) return fail(PARM_ERR_ARG, "unknown pair kind");
     if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
-        return fail(PARM_ERR_ARG, "the Lois-O'Hern, Lois-Lin and Eis-Mclachlan pairs run on FP64 handles only");
+        return fail(PARM_ERR_ARG,
+                    "the Lois-O'Hern, Lois-Lin, Eis-Mclachlan and drag pairs run on FP64 handles only");
     if (!(skin >= 0.0) || !std::isfinite(skin)) return fail(PARM_ERR_ARG, "skin must be >= 0");
     TRY(S->flush());
     CUDA_TRY(cudaStreamSynchronize(S->st));
@@ -1407,7 +1409,7 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
             }
             if (np == 4 && !(std::isfinite(a.p2) && std::isfinite(a.p3) && a.p2 >= 0.0 && a.p3 >= 0.0))
-                return fail(PARM_ERR_ARG, "C (or f) and l must be finite and >= 0");
+                return fail(PARM_ERR_ARG, "the third and fourth parameters must be finite and >= 0");
             if (first) {
                 e0 = a.p0;
                 s0 = a.p1;

@@ -11,6 +11,7 @@
 //   LoisOhernPair, LoisOhernPairMinCLs      1679-1751
 //   LoisLinPair, LoisLinPairMin             1764-1836
 //   EisMclachlanPair                        1415-1452
+//   RepulsionDragPair                       1598-1640
 //
 // Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
 // scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
@@ -47,6 +48,10 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
     } else if constexpr (KIND == KIND_REPULSION) {
         p.third = (uni & UNI_THIRD) ? A.p2 : (A.p2 + B.p2) / 2.0;
         p.m6 = 0.0;
+    } else if constexpr (KIND == KIND_REPULSIONDRAG) {
+        // RepulsionDragPair(a1, a2) (interaction.hpp:1613-1621): exponent and gamma averaged
+        p.third = (uni & UNI_THIRD) ? A.p2 : (A.p2 + B.p2) / 2.0;
+        p.m6 = (uni & UNI_FOURTH) ? A.p3 : (A.p3 + B.p3) / 2;
     } else if constexpr (lois_kind<KIND>()) {
         // LoisOhernPair (interaction.hpp:1693-1703) / LoisLinPair (1782-1800): averages;
         // LoisOhernPairMinCLs (1746-1751) / LoisLinPairMin (1831-1836): the smaller values
@@ -154,7 +159,8 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         double mid = (1 - 1 / rsix);
         double cut_energy = p.eps * (p.m6 * p.m6 - 1);
         return p.eps * (mid * mid - 1) - cut_energy;
-    } else if constexpr (KIND == KIND_REPULSION) {
+    } else if constexpr (KIND == KIND_REPULSION || KIND == KIND_REPULSIONDRAG) {
+        // RepulsionPair::energy (1544-1550), RepulsionDragPair::energy (1622-1628)
         if (dsq > p.sig * p.sig) return 0.0;
         double R = sqrt(dsq);
         double b = 1.0 - (R / p.sig);
@@ -207,6 +213,30 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         double mid = (1 - 1 / rsix);
         return p.eps * (mid * mid);
     }
+}
+
+// RepulsionDragPair::forces (interaction.hpp:1629-1639): the soft repulsion
+// minus gamma times the relative velocity's component along r; false beyond
+// the cut-off.  F(i, j) == -F(j, i) bit for bit (r and v_i - v_j both flip).
+template <int ND>
+__device__ __forceinline__ bool drag_force(const PairC& p, const double* r, double dsq, const double* vi,
+                                           const double* vj, double* fo) {
+    if (dsq > p.sig * p.sig) return false;
+    double R = sqrt(dsq);
+    double vij[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < ND; d++) vij[d] = vi[d] - vj[d];
+    double vdot = vij[0] * r[0] + vij[1] * r[1];
+    if constexpr (ND == 3) vdot = vdot + vij[2] * r[2];
+    double b = 1.0 - (R / p.sig);
+    double pw = (p.third == 2.0) ? b : pow(b, p.third - 1);   // pow(b, 1) == b exactly
+    double sr = p.eps * pw / p.sig / R;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        double vperp = r[d] * vdot / dsq;
+        fo[d] = r[d] * sr - vperp * p.m6;
+    }
+    return true;
 }
 
 // FP32 screen: true when the pair is certainly beyond the cut-off
@@ -276,8 +306,9 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
     }
     if (member) {
         const SysConst& S = c.sys[s];
-        double xi[3] = {0, 0, 0};
+        double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
         load3<ND>(c.x, i, xi);
+        if constexpr (KIND == KIND_REPULSIONDRAG) load3<ND>(c.v, i, vi);
         const float4 Ai = c.pos[2 * (size_t)(i)], Bi = c.pos[2 * (size_t)(i) + 1];
         const AtomPrm Pi = c.prm[i];
         const float4 Qi = c.prm32[i];
@@ -300,10 +331,18 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             AtomPrm Pj = Pi;
             if ((uni & UNI_ALL) != UNI_ALL) Pj = c.prm[j];
             const PairC pc = combine<KIND>(Pi, Pj, uni);
-            double sc;
-            if (!force_scale<KIND>(pc, dsq, uni, sc)) continue;
+            if constexpr (KIND == KIND_REPULSIONDRAG) {
+                double vj[3] = {0, 0, 0}, fo[3];
+                load3<ND>(c.v, j, vj);
+                if (!drag_force<ND>(pc, r, dsq, vi, vj, fo)) continue;
 #pragma unroll
-            for (int d = 0; d < ND; d++) f[d] = f[d] + r[d] * sc;
+                for (int d = 0; d < ND; d++) f[d] = f[d] + fo[d];
+            } else {
+                double sc;
+                if (!force_scale<KIND>(pc, dsq, uni, sc)) continue;
+#pragma unroll
+                for (int d = 0; d < ND; d++) f[d] = f[d] + r[d] * sc;
+            }
         }
     }
     if (active) {
@@ -357,7 +396,13 @@ __global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
             } else {
                 double sc;
                 double fo[3] = {0, 0, 0};
-                if (force_scale<KIND>(pc, dsq, uni, sc)) {
+                if constexpr (KIND == KIND_REPULSIONDRAG) {
+                    double vi[3] = {0, 0, 0}, vj[3] = {0, 0, 0};
+                    load3<ND>(c.v, i, vi);
+                    load3<ND>(c.v, j, vj);
+                    if (!drag_force<ND>(pc, r, dsq, vi, vj, fo))
+                        for (int d = 0; d < 3; d++) fo[d] = 0.0;
+                } else if (force_scale<KIND>(pc, dsq, uni, sc)) {
 #pragma unroll
                     for (int d = 0; d < ND; d++) fo[d] = r[d] * sc;
                 }
@@ -391,6 +436,7 @@ static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     else if (c.kind == KIND_LOISOHERN) force64_nd_kind<ND, KIND_LOISOHERN>(c, s, mode);
     else if (c.kind == KIND_LOISLIN) force64_nd_kind<ND, KIND_LOISLIN>(c, s, mode);
     else if (c.kind == KIND_EISMCLACHLAN) force64_nd_kind<ND, KIND_EISMCLACHLAN>(c, s, mode);
+    else if (c.kind == KIND_REPULSIONDRAG) force64_nd_kind<ND, KIND_REPULSIONDRAG>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -407,6 +453,7 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     else if (c.kind == KIND_LOISOHERN) k_eval64<ND, KIND_LOISOHERN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LOISLIN) k_eval64<ND, KIND_LOISLIN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_EISMCLACHLAN) k_eval64<ND, KIND_EISMCLACHLAN><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_REPULSIONDRAG) k_eval64<ND, KIND_REPULSIONDRAG><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

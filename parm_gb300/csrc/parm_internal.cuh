@@ -27,7 +27,10 @@ enum PairKind : int {
     // four-parameter atoms (eps, sigma, C, l) / (eps, sigma, f, l); FP64 path only
     KIND_LOISOHERN = 4, KIND_LOISLIN = 5,
     // (dist, sigmai) atoms, E = c0/R + c1 + c2 R; FP64 path only
-    KIND_EISMCLACHLAN = 6
+    KIND_EISMCLACHLAN = 6,
+    // (eps, sigma, exponent, gamma) atoms: soft repulsion with a drag on the
+    // relative normal velocity; FP64 path only
+    KIND_REPULSIONDRAG = 7
 };
 template <int KIND>
 __host__ __device__ constexpr bool lois_kind() { return KIND == KIND_LOISOHERN || KIND == KIND_LOISLIN; }

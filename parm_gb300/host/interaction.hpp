@@ -348,6 +348,56 @@ struct LoisLinPairMin : public LoisLinPair {
                       (a1.l < a2.l ? a1.l : a2.l)) {}
 };
 
+//! (epsilon, sigma, exponent, drag coefficient gamma) per atom
+//! (src/interaction.hpp:1598-1611); the constructor takes gamma before the
+//! exponent.
+struct EpsSigExpDragAtom : public AtomID {
+    flt eps, sigma, exponent, gamma;
+    EpsSigExpDragAtom() : eps(0), sigma(0), exponent(2.5), gamma(0) {}
+    EpsSigExpDragAtom(AtomID a, flt eps, flt sigma, flt gamma, flt exponent = 2.5)
+        : AtomID(a), eps(eps), sigma(sigma), exponent(exponent), gamma(gamma) {}
+    EpsSigExpDragAtom(AtomID a, EpsSigExpDragAtom other)
+        : AtomID(a), eps(other.eps), sigma(other.sigma), exponent(other.exponent), gamma(other.gamma) {}
+    flt max_size() { return sigma; }
+};
+
+//! Soft repulsion with a drag on the relative normal velocity
+//! (src/interaction.hpp:1613-1640): F = r eps (1 - r/sigma)^(n-1) / (sigma r)
+//! - gamma v_perp, v_perp = r ((v1 - v2) . r) / r^2.
+struct RepulsionDragPair {
+    static const int kind = PARM_REPULSIONDRAG;
+    static void params(const EpsSigExpDragAtom& a, double p[4]) {
+        p[0] = a.eps;
+        p[1] = a.sigma;
+        p[2] = a.exponent;
+        p[3] = a.gamma;
+    }
+    flt eps, sig, exponent, gamma;
+    AtomID atom1, atom2;
+    RepulsionDragPair(EpsSigExpDragAtom a1, EpsSigExpDragAtom a2)
+        : eps(std::sqrt(a1.eps * a2.eps)),
+          sig((a1.sigma + a2.sigma) / 2.0),
+          exponent((a1.exponent + a2.exponent) / 2.0),
+          gamma((a1.gamma + a2.gamma) / 2),
+          atom1(a1),
+          atom2(a2) {}
+    flt energy(Box& box) {
+        const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
+        if (dsq > sig * sig) return 0.0;
+        const flt R = std::sqrt(dsq);
+        return eps * std::pow(1.0 - (R / sig), exponent) / exponent;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const Vec vij = atom1->v - atom2->v;
+        const flt dsq = rij.squaredNorm();
+        if (dsq > sig * sig) return Vec::Zero();
+        const flt R = std::sqrt(dsq);
+        const Vec v_perp = rij * (vij.dot(rij)) / dsq;
+        return rij * (eps * std::pow(1.0 - (R / sig), exponent - 1) / sig / R) - (v_perp * gamma);
+    }
+};
+
 //! Implicit-solvation atom (src/interaction.hpp:1415-1423): dist = the
 //! atom's radius plus the water radius, sigmai its solvation parameter.
 struct EisMclachlanAtom : public AtomID {

@@ -35,7 +35,7 @@ REFOUT = ROOT / "oracle" / "_ref"
 
 VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
-LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN = 4, 5, 6, 7, 8
+LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN, REPULSIONDRAG = 4, 5, 6, 7, 8, 9
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -306,6 +306,21 @@ def cases() -> list[dict]:
     out.append(_case("eismclachlan180_damped", EISMCLACHLAN, DAMPED, 200, 0.005, [Le] * 3,
                      rng.uniform(0, Le, (n, 3)), rng.normal(0, 0.02, (n, 3)), np.ones(n),
                      np.stack([dist, sigi, np.zeros(n)], 1), 0.3, [1, 10, 100, 200], damping=0.5))
+    # 18. RepulsionDragPair (soft repulsion with a drag on the relative normal velocity),
+    #     per-atom exponent 2 or 2.5 and gamma, 3D Verlet from random positions and velocities;
+    #     the constructor takes (eps, sigma, gamma, exponent), the fixture keeps the fields
+    #     (eps, sigma, exponent, gamma)
+    rng = np.random.default_rng(66)
+    n = 160
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lr = (np.sum(np.pi * sig ** 3 / 6) / 0.6) ** (1 / 3)
+    expo = rng.choice([2.0, 2.5], n)
+    gam = rng.choice([0.1, 0.3], n)
+    eps = rng.choice([1.0, 2.0], n)
+    out.append(_case("repulsiondrag160_verlet", REPULSIONDRAG, VERLET, 300, 0.01, [Lr] * 3,
+                     rng.uniform(0, Lr, (n, 3)), rng.normal(0, 0.3, (n, 3)), np.ones(n),
+                     np.stack([eps, sig, expo, gam], 1), 0.3, [1, 10, 100, 300],
+                     deck_params=np.stack([eps, sig, gam, expo], 1)))
     return out
 
 

@@ -198,3 +198,41 @@ def test_eismclachlan_uniform_dist_matches_oracle():
         assert np.array_equal(st[k], ref[k]), k
     assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-12)
     g.close()
+
+
+@pytest.mark.parametrize("vary_gamma", [False, True])
+def test_repulsion_drag_matches_oracle(vary_gamma):
+    """RepulsionDragPair (velocity-dependent pair forces) with exponent 2: pairs, forces, virial and 100
+    Verlet steps bit-exact against the oracle, with a shared drag coefficient (the uniform-parameter
+    shortcut) and with per-atom ones."""
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    rng = np.random.default_rng(90 + vary_gamma)
+    n = 240
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    L = (np.sum(np.pi * sig ** 3 / 6) / 0.6) ** (1 / 3)
+    x = rng.uniform(0, L, (n, 3))
+    v = rng.normal(0, 0.3, (n, 3))
+    gam = rng.choice([0.1, 0.4], n) if vary_gamma else np.full(n, 0.2)
+    params = np.stack([np.ones(n), sig, np.full(n, 2.0), gam], 1)
+    g = System(n, ndim=3, precision="fp64")
+    g.set_boxes(np.full((1, 3), L))
+    g.set_atoms(x=x, v=v, a=np.zeros((n, 3)), f=np.zeros((n, 3)), m=np.ones(n))
+    g.set_interaction(9, params, 0.3)
+    o = Oracle(n, 3)
+    o.set_box(np.full(3, L))
+    o.set_state(x=x, v=v, m=np.ones(n))
+    o.set_interaction(9, params, 0.3)
+    g.nlist_update(True)
+    o.nl_update(True)
+    assert np.array_equal(g.pairs(), o.pairs())
+    g.set_forces(True)
+    o.set_forces(True)
+    assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+    g.verlet(0.01, 100)
+    o.verlet(0.01, 100)
+    st, ref = g.get_atoms(), o.get_state()
+    for k in ("x", "v", "f"):
+        assert np.array_equal(st[k], ref[k]), k
+    assert g.virial()[0] == pytest.approx(o.pressure(), rel=1e-12, abs=1e-12)
+    g.close()
