@@ -39,8 +39,14 @@ namespace {
 
 enum PairKind {
     LJCUT = 0, REPULSION = 1, LJREPULSE = 2, LJATTRACT = 3,
-    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7, EISMCLACHLAN = 8, REPULSIONDRAG = 9
+    LOISOHERN = 4, LOISOHERN_MIN = 5, LOISLIN = 6, LOISLIN_MIN = 7, EISMCLACHLAN = 8, REPULSIONDRAG = 9,
+    // indexed pair epsilons (and sigmas): the pair's values come from a table by the two atoms'
+    // type indices, first atom's row (IEps*Atom::get_epsilon)
+    LJCUT_IEPSISIG = 10, LJATTRACT_IEPSISIG = 11, LJATTRACT_IEPS = 12, LJATTRACTREPULSE = 13,
+    LJATTRACTFIXEDREPULSE = 14, LJISH = 15
 };
+
+inline bool indexed_kind(int kind) { return kind >= LJCUT_IEPSISIG && kind <= LJISH; }
 
 // kinds whose atoms carry four parameters
 inline bool four_params(int kind) { return (kind >= LOISOHERN && kind <= LOISLIN_MIN) || kind == REPULSIONDRAG; }
@@ -59,8 +65,10 @@ inline double dotv(const double* a, const double* b, int nd) {
 
 struct AtomParams {
     // kind-dependent: (eps, sigma, sigcut|exponent) or, for the Lois kinds,
-    // (eps, sigma, C, l) / (eps, sigma, f, l)
+    // (eps, sigma, C, l) / (eps, sigma, f, l); the indexed kinds: type t and
+    // (repeps, sigma, sigcut, exponent)
     double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    uint32_t t = 0;
 };
 
 struct PairConst {
@@ -82,6 +90,8 @@ struct System {
     std::vector<double> diameters;      // A::max_size() per member
     std::vector<double> lastlocs;       // per member
     std::vector<AtomParams> params;     // indexed by AtomVec index
+    uint32_t ntypes = 0;
+    std::vector<double> teps, tsig;     // ntypes x ntypes: row = first atom's type
     std::vector<uint8_t> has_params;
     std::vector<std::pair<uint32_t, uint32_t>> curpairs;  // (first.n, last.n)
     std::set<std::pair<uint32_t, uint32_t>> ignored;      // (max, min) by AtomVec index
@@ -160,6 +170,77 @@ struct System {
             }
             pc.cut = pc.sig + pc.fourth;
             pc.cut_energy = 0;
+        } else if (indexed_kind(kind)) {
+            const double te = teps[A.t * ntypes + B.t];   // a1.get_epsilon(a2)
+            pc.cut = 0;
+            if (kind == LJCUT_IEPSISIG) {
+                // LennardJonesCutPair(IEpsISigCutAtom, IEpsISigCutAtom) (interaction.hpp:977-982)
+                pc.eps = te;
+                pc.sig = tsig[A.t * ntypes + B.t];
+                pc.third = std::max(A.p2, B.p2);
+                double rsix = std::pow(pc.third, 6);
+                double mid = (1 - 1 / rsix);
+                pc.cut_energy = pc.eps * (mid * mid - 1);
+            } else if (kind == LJATTRACT_IEPSISIG || kind == LJATTRACT_IEPS) {
+                // LJAttractCutPair(IEpsISigCutAtom...) / (IEpsSigCutAtom...) (interaction.hpp:1028-1037)
+                pc.eps = te;
+                pc.sig = (kind == LJATTRACT_IEPSISIG) ? tsig[A.t * ntypes + B.t] : (A.p1 + B.p1) / 2;
+                pc.third = std::max(A.p2, B.p2);
+                double e;
+                if (pc.third < 1) {
+                    e = -1;
+                } else {
+                    double rsq = pc.third * pc.third;
+                    double rsix = rsq * rsq * rsq;
+                    double mid = (1 - 1 / rsix);
+                    e = mid * mid - 1;
+                }
+                pc.cut_energy = e * pc.eps;
+            } else if (kind == LJATTRACTREPULSE) {
+                // LJAttractRepulsePair(IEpsSigCutAtom, IEpsSigCutAtom) (interaction.hpp:1255-1268)
+                pc.eps = te;
+                pc.sig = (A.p1 + B.p1) / 2.0;
+                pc.third = std::max(A.p2, B.p2);
+                if (pc.eps <= 0) {
+                    pc.third = 1;
+                    pc.cut_energy = 0;
+                    pc.eps = std::abs(pc.eps);
+                } else {
+                    double mid = (1 - std::pow(pc.third, -6));
+                    pc.cut_energy = pc.eps * (mid * mid);
+                }
+            } else if (kind == LJATTRACTFIXEDREPULSE) {
+                // LJAttractFixedRepulsePair(IEpsRepsSigCutAtom...) (interaction.hpp:1349-1365); fourth = repeps
+                pc.eps = std::abs(te);
+                pc.fourth = std::sqrt(A.p0 * B.p0);
+                pc.sig = (A.p1 + B.p1) / 2.0;
+                pc.third = std::max(A.p2, B.p2);
+                bool attract = te > 0;
+                if (!attract || pc.eps == 0) {
+                    pc.third = 1;
+                    pc.cut_energy = 0;
+                    pc.eps = 0;
+                } else {
+                    double mid = (1 - std::pow(pc.third, -6.0));
+                    pc.cut_energy = pc.eps * (mid * mid);
+                }
+            } else {
+                // LJishPair(IEpsRepsSigExpCutAtom...) (interaction.hpp:1098-1114); fourth = repeps,
+                // cut = the exponent n
+                pc.eps = te;
+                pc.fourth = std::sqrt(A.p0 * B.p0);
+                pc.sig = (A.p1 + B.p1) / 2.0;
+                pc.cut = (A.p3 + B.p3) / 2;
+                pc.third = std::max(A.p2, B.p2);
+                if (pc.eps <= 0) {
+                    pc.third = 1;
+                    pc.cut_energy = 0;
+                    pc.eps = 0;
+                } else {
+                    double mid = (1 - std::pow(pc.third, -pc.cut));
+                    pc.cut_energy = pc.eps * (mid * mid);
+                }
+            }
         } else if (kind == REPULSIONDRAG) {
             // RepulsionDragPair(EpsSigExpDragAtom, EpsSigExpDragAtom) (interaction.hpp:1613-1621):
             // atom fields (eps, sigma, exponent, gamma)
@@ -236,6 +317,45 @@ struct System {
                 return pc.eps / 2 * dR * dR - f * l;
             }
             return -f * (pc.sig + l - R);
+        } else if (kind == LJCUT_IEPSISIG) {
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > (pc.third * pc.third)) return 0;
+            double rsix = rsq * rsq * rsq;
+            double mid = (1 - 1 / rsix);
+            return pc.eps * (mid * mid - 1) - pc.cut_energy;
+        } else if (kind == LJATTRACT_IEPSISIG || kind == LJATTRACT_IEPS) {
+            if (pc.eps == 0) return 0;
+            if (dsq > (pc.third * pc.third * pc.sig * pc.sig)) return 0;
+            double rsq = dsq / (pc.sig * pc.sig);
+            double e;
+            if (rsq < 1) {
+                e = -pc.eps;
+            } else {
+                double rsix = rsq * rsq * rsq;
+                double mid = (1 - 1 / rsix);
+                e = pc.eps * (mid * mid - 1);
+            }
+            return e - pc.cut_energy;
+        } else if (kind == LJATTRACTREPULSE) {
+            // LJAttractRepulsePair::energy (interaction.hpp:1269-1286)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > pc.third * pc.third) return 0;
+            double mid = (1 - std::pow(rsq, -3));
+            return pc.eps * (mid * mid) - pc.cut_energy;
+        } else if (kind == LJATTRACTFIXEDREPULSE) {
+            // LJAttractFixedRepulsePair::energy (interaction.hpp:1366-1389)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > pc.third * pc.third) return 0;
+            double mid = (1 - std::pow(rsq, -3));
+            if (rsq > 1) return pc.eps * (mid * mid) - pc.cut_energy;
+            return pc.fourth * (mid * mid) - pc.cut_energy;
+        } else if (kind == LJISH) {
+            // LJishPair::energy (interaction.hpp:1115-1129)
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > pc.third * pc.third) return 0;
+            double mid = (1 - std::pow(rsq, -pc.cut / 2));
+            if (rsq > 1) return pc.eps * (mid * mid) - pc.cut_energy;
+            return pc.fourth * (mid * mid) - pc.cut_energy;
         } else if (kind == REPULSIONDRAG) {
             // RepulsionDragPair::energy (interaction.hpp:1622-1628)
             if (dsq > pc.sig * pc.sig) return 0.0;
@@ -260,6 +380,43 @@ struct System {
     bool pair_force(const PairConst& pc, const double* rij, double* fo, uint32_t i, uint32_t j) const {
         double dsq = dotv(rij, rij, nd);
         double s;
+        if (kind == LJCUT_IEPSISIG || kind == LJATTRACT_IEPSISIG || kind == LJATTRACT_IEPS) {
+            // LennardJonesCut::forces (263-271), LJAttractCut::forces (219-229)
+            const bool attr = kind != LJCUT_IEPSISIG;
+            double rsq = dsq / (pc.sig * pc.sig);
+            if ((attr && (pc.eps == 0 || rsq < 1)) || rsq > (pc.third * pc.third)) {
+                for (int d = 0; d < nd; d++) fo[d] = 0;
+                return false;
+            }
+            double rsix = rsq * rsq * rsq;
+            double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
+            s = fmagTimesR / dsq;
+            for (int d = 0; d < nd; d++) fo[d] = rij[d] * s;
+            return true;
+        }
+        if (kind == LJATTRACTREPULSE || kind == LJATTRACTFIXEDREPULSE || kind == LJISH) {
+            // LJAttractRepulsePair::forces (1287-1297), LJAttractFixedRepulsePair::forces (1390-1398),
+            // LJishPair::forces (1130-1140)
+            if (kind == LJATTRACTREPULSE && pc.eps == 0) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            double rsq = dsq / (pc.sig * pc.sig);
+            if (rsq > (pc.third * pc.third)) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            if (kind == LJATTRACTREPULSE) {
+                double rsix = std::pow(rsq, -3);
+                double fmagTimesR = 12 * pc.eps * rsix * (rsix - 1);
+                s = fmagTimesR / dsq;
+            } else if (kind == LJATTRACTFIXEDREPULSE) {
+                double rsix = std::pow(rsq, -3);
+                double fmagTimesR = 12 * rsix * (rsix - 1);
+                s = (rsq < 1) ? pc.fourth * fmagTimesR / dsq : pc.eps * fmagTimesR / dsq;
+            } else {
+                double n = pc.cut;
+                double rmid = std::pow(rsq, -n / 2);
+                double fmagTimesR = 2 * n * rmid * (rmid - 1);
+                s = (rsq < 1) ? pc.fourth * fmagTimesR / dsq : pc.eps * fmagTimesR / dsq;
+            }
+            for (int d = 0; d < nd; d++) fo[d] = rij[d] * s;
+            return true;
+        }
         if (kind == REPULSIONDRAG) {
             // RepulsionDragPair::forces (interaction.hpp:1629-1639): the repulsion minus gamma
             // times the relative velocity's component along rij
@@ -345,6 +502,16 @@ struct System {
         if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
         if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
         if (kind == EISMCLACHLAN) return params[i].p0;   // EisMclachlanAtom::max_size (1423)
+        if (kind == LJCUT_IEPSISIG || kind == LJATTRACT_IEPSISIG) {
+            // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut
+            const double* row = &tsig[params[i].t * ntypes];
+            double sg = row[0];
+            for (uint32_t k = 1; k < ntypes; ++k)
+                if (sg < row[k]) sg = row[k];
+            return sg * params[i].p2;
+        }
+        // IEpsSigCutAtom (1017), IEpsRepsSigCutAtom (1335), IEpsRepsSigExpCutAtom (1091): sigma * sigcut
+        if (indexed_kind(kind)) return params[i].p1 * params[i].p2;
         // EpsSigExpDragAtom::max_size (1611) is sigma, as below
         return params[i].p1;
     }
@@ -892,7 +1059,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 9) return -1;
+    if (kind < 0 || kind > 15) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;
@@ -903,15 +1070,41 @@ int orc_set_interaction(void* s, int kind, double skin) {
 int orc_add_atom(void* s, uint32_t i, const double* p) {
     System* S = static_cast<System*>(s);
     if (i >= S->n || S->has_params[i]) return -1;
-    S->params[i].p0 = p[0];
-    S->params[i].p1 = p[1];
-    S->params[i].p2 = (S->kind == LJREPULSE) ? 0.0 : p[2];
-    S->params[i].p3 = four_params(S->kind) ? p[3] : 0.0;
+    if (indexed_kind(S->kind)) {
+        // params: (indx, sigcut) for IEpsISigCutAtom, (indx, sigma, sigcut) for IEpsSigCutAtom,
+        // (indx, repeps, sigma, sigcut) for IEpsRepsSigCutAtom, (indx, repeps, sigma, n, sigcut)
+        // for IEpsRepsSigExpCutAtom
+        AtomParams& a = S->params[i];
+        a.t = (uint32_t)p[0];
+        if (a.t >= S->ntypes) return -1;
+        const int k = S->kind;
+        if (k == LJCUT_IEPSISIG || k == LJATTRACT_IEPSISIG) a.p2 = p[1];
+        else if (k == LJATTRACT_IEPS || k == LJATTRACTREPULSE) { a.p1 = p[1]; a.p2 = p[2]; }
+        else if (k == LJATTRACTFIXEDREPULSE) { a.p0 = p[1]; a.p1 = p[2]; a.p2 = p[3]; }
+        else { a.p0 = p[1]; a.p1 = p[2]; a.p3 = p[3]; a.p2 = p[4]; }
+    } else {
+        S->params[i].p0 = p[0];
+        S->params[i].p1 = p[1];
+        S->params[i].p2 = (S->kind == LJREPULSE) ? 0.0 : p[2];
+        S->params[i].p3 = four_params(S->kind) ? p[3] : 0.0;
+    }
     S->has_params[i] = 1;
     S->members.push_back(i);
     S->diameters.push_back(S->max_size(i));
     for (int d = 0; d < S->nd; d++) S->lastlocs.push_back(S->x[i * S->nd + d]);
     S->ignorechanged = true;
+    return 0;
+}
+
+// the pair tables of the indexed kinds: eps[a * ntypes + b] = the epsilon of
+// a pair whose first atom has type a and second type b (first.epsilons[b]);
+// sig likewise (IEpsISigCutAtom), may be NULL
+int orc_set_pair_table(void* s, uint32_t ntypes, const double* eps, const double* sig) {
+    System* S = static_cast<System*>(s);
+    S->ntypes = ntypes;
+    S->teps.assign(eps, eps + (size_t)ntypes * ntypes);
+    if (sig) S->tsig.assign(sig, sig + (size_t)ntypes * ntypes);
+    else S->tsig.assign((size_t)ntypes * ntypes, 0.0);
     return 0;
 }
 

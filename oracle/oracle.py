@@ -34,6 +34,8 @@ def lib() -> C.CDLL:
             "orc_add_atom": (C.c_int, [C.c_void_p, C.c_uint32, _dp]),
             "orc_ignore": (None, [C.c_void_p, C.c_uint32, C.c_uint32]),
             "orc_add_member": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double]),
+            "orc_set_pair_table": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_double)]),
             "orc_nl_update": (C.c_int, [C.c_void_p, C.c_int]),
             "orc_nl_which": (C.c_uint32, [C.c_void_p]),
             "orc_nl_numpairs": (C.c_uint64, [C.c_void_p]),
@@ -117,6 +119,15 @@ def sol_constants(dt: float, damping: float):
     return c0, c1, c2, sr, sv * corr, sv * math.sqrt(1 - corr * corr)
 
 
+
+def nparam(kind: int) -> int:
+    """Doubles per atom of a pair kind's parameters (the C ABI's PARM_NPARAM)."""
+    if 4 <= kind <= 7 or kind in (9, 14):
+        return 4
+    if kind == 15:
+        return 5
+    return 3
+
 class Oracle:
     def __init__(self, n: int, ndim: int = 3):
         self.L_ = lib()
@@ -148,11 +159,22 @@ class Oracle:
     def set_interaction(self, kind, params, skin, order=None):
         """NListed(box, atoms, skin) and add() of every atom in `order`."""
         assert self.L_.orc_set_interaction(self.h, kind, float(skin)) == 0
-        params = np.asarray(params, dtype=np.float64).reshape(self.n, 4 if (4 <= kind <= 7 or kind == 9) else 3)
+        params = np.asarray(params, dtype=np.float64).reshape(self.n, nparam(kind))
         order = range(self.n) if order is None else order
         for i in order:
             p = np.ascontiguousarray(params[i])
             assert self.L_.orc_add_atom(self.h, int(i), _d(p)) == 0
+
+    def set_pair_table(self, eps, sig=None):
+        """Pair tables of the indexed kinds (10-15): eps[a, b] = first atom's epsilons[b] for a
+        first atom of type a."""
+        eps = np.ascontiguousarray(np.asarray(eps, dtype=np.float64))
+        nt = eps.shape[0]
+        sp = None
+        if sig is not None:
+            sig = np.ascontiguousarray(np.asarray(sig, dtype=np.float64).reshape(nt, nt))
+            sp = _d(sig)
+        assert self.L_.orc_set_pair_table(self.h, nt, _d(eps), sp) == 0
 
     def add_member(self, i, diameter):
         """NeighborList::add(atom, diameter): a list member without pair parameters."""

@@ -12,7 +12,13 @@
 //       4 <LoisOhernAtom,LoisOhernPair>, 5 <LoisOhernAtom,LoisOhernPairMinCLs> (p: eps sigma C l),
 //       6 <LoisLinAtom,LoisLinPair>, 7 <LoisLinAtom,LoisLinPairMin> (p: eps sigma depth width),
 //       8 <EisMclachlanAtom,EisMclachlanPair> (p: dist sigmai unused),
-//       9 <EpsSigExpDragAtom,RepulsionDragPair> (p: eps sigma gamma exponent);
+//       9 <EpsSigExpDragAtom,RepulsionDragPair> (p: eps sigma gamma exponent),
+//       indexed epsilons (the deck adds "nt eps[nt*nt] sig[nt*nt]" after the atoms; an atom of
+//       type t gets row t): 10 <IEpsISigCutAtom,LennardJonesCutPair> (p: t sigcut unused),
+//       11 <IEpsISigCutAtom,LJAttractCutPair> (same), 12 <IEpsSigCutAtom,LJAttractCutPair>
+//       (p: t sigma sigcut), 13 <IEpsSigCutAtom,LJAttractRepulsePair> (same),
+//       14 <IEpsRepsSigCutAtom,LJAttractFixedRepulsePair> (p: t repeps sigma sigcut),
+//       15 <IEpsRepsSigExpCutAtom,LJishPair> (p: t repeps sigma n sigcut);
 //       integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
@@ -38,6 +44,13 @@ static unsigned rdu() { return (unsigned)rd(); }
 
 static void pvec(const Vec& v) {
     for (int d = 0; d < NDIM; d++) std::printf(" %.17g", v[d]);
+}
+
+// the pair tables of the indexed kinds
+static unsigned g_nt = 0;
+static std::vector<double> g_eps, g_sig;
+static std::vector<flt> row_of(const std::vector<double>& t, unsigned r) {
+    return std::vector<flt>(t.begin() + (size_t)r * g_nt, t.begin() + (size_t)(r + 1) * g_nt);
 }
 
 template <class A>
@@ -70,19 +83,46 @@ template <>
 EpsSigExpDragAtom make_atom<EpsSigExpDragAtom>(AtomID id, int, const double* p) {
     return EpsSigExpDragAtom(id, p[0], p[1], p[2], p[3]);
 }
+template <>
+IEpsISigCutAtom make_atom<IEpsISigCutAtom>(AtomID id, int, const double* p) {
+    const unsigned t = (unsigned)p[0];
+    return IEpsISigCutAtom(id, row_of(g_eps, t), row_of(g_sig, t), t, p[1]);
+}
+template <>
+IEpsSigCutAtom make_atom<IEpsSigCutAtom>(AtomID id, int, const double* p) {
+    const unsigned t = (unsigned)p[0];
+    return IEpsSigCutAtom(id, row_of(g_eps, t), t, p[1], p[2]);
+}
+template <>
+IEpsRepsSigCutAtom make_atom<IEpsRepsSigCutAtom>(AtomID id, int, const double* p) {
+    const unsigned t = (unsigned)p[0];
+    return IEpsRepsSigCutAtom(id, row_of(g_eps, t), p[1], p[2], t, p[3]);
+}
+template <>
+IEpsRepsSigExpCutAtom make_atom<IEpsRepsSigExpCutAtom>(AtomID id, int, const double* p) {
+    const unsigned t = (unsigned)p[0];
+    return IEpsRepsSigExpCutAtom(id, row_of(g_eps, t), p[1], p[2], p[3], t, p[4]);
+}
 
 template <class A, class P>
 int run(int kind, int integ, int nsteps, double dt, double damping, double T, double skin) {
     Vec L;
     for (int d = 0; d < NDIM; d++) L[d] = rd();
     unsigned N = rdu();
-    const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9) ? 4 : 3;
+    const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9 || kind == 14) ? 4 : (kind == 15 ? 5 : 3);
     std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * np);
     for (unsigned i = 0; i < N; i++) {
         for (int d = 0; d < NDIM; d++) xs[i * NDIM + d] = rd();
         for (int d = 0; d < NDIM; d++) vs[i * NDIM + d] = rd();
         ms[i] = rd();
         for (unsigned k = 0; k < np; k++) ps[np * i + k] = rd();
+    }
+    if (kind >= 10) {
+        g_nt = rdu();
+        g_eps.resize((size_t)g_nt * g_nt);
+        g_sig.resize((size_t)g_nt * g_nt);
+        for (auto& q : g_eps) q = rd();
+        for (auto& q : g_sig) q = rd();
     }
     std::vector<unsigned> order(rdu());
     for (auto& o : order) o = rdu();
@@ -195,5 +235,12 @@ int main() {
     if (kind == 7) return run<LoisLinAtom, LoisLinPairMin>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 8) return run<EisMclachlanAtom, EisMclachlanPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 9) return run<EpsSigExpDragAtom, RepulsionDragPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 10) return run<IEpsISigCutAtom, LennardJonesCutPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 11) return run<IEpsISigCutAtom, LJAttractCutPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 12) return run<IEpsSigCutAtom, LJAttractCutPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 13) return run<IEpsSigCutAtom, LJAttractRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 14)
+        return run<IEpsRepsSigCutAtom, LJAttractFixedRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 15) return run<IEpsRepsSigExpCutAtom, LJishPair>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

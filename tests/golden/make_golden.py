@@ -36,6 +36,7 @@ REFOUT = ROOT / "oracle" / "_ref"
 VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
 LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN, REPULSIONDRAG = 4, 5, 6, 7, 8, 9
+LJCUT_IEPSISIG, LJATTRACT_IEPSISIG, LJATTRACT_IEPS, LJATTRACTREPULSE, LJATTRACTFIXEDREPULSE, LJISH = range(10, 16)
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -47,6 +48,10 @@ def _deck(c: dict) -> str:
         prm = c["deck_params"][i] if "deck_params" in c else c["params"][i]
         vals = list(c["x"][i]) + list(c["v"][i]) + [c["m"][i]] + list(prm)
         out.append(" ".join(repr(float(q)) for q in vals))
+    if "pair_eps" in c:   # the indexed kinds' tables
+        nt = c["pair_eps"].shape[0]
+        out.append(f"{nt} " + " ".join(repr(float(q)) for q in c["pair_eps"].reshape(-1)) + " "
+                   + " ".join(repr(float(q)) for q in c["pair_sig"].reshape(-1)))
     out.append(f"{len(c['order'])} " + " ".join(str(int(q)) for q in c["order"]))
     ig = c["ignores"].reshape(-1)
     out.append(f"{len(ig) // 2} " + " ".join(str(int(q)) for q in ig))
@@ -100,13 +105,17 @@ def _parse(text: str, n: int, nd: int) -> dict:
 
 
 def _case(name, kind, integ, nsteps, dt, L, x, v, m, params, skin, out_steps, damping=0.0, T=0.0,
-          order=None, ignores=None, cg=None, deck_params=None):
+          order=None, ignores=None, cg=None, deck_params=None, pair_eps=None, pair_sig=None):
     """deck_params: the atoms' constructor arguments when they differ from the stored fields
     (LoisLinAtom takes depth and width and stores f = depth / width and l = width)."""
     n = len(m)
     extra = {} if cg is None else {"cg": np.asarray(cg, dtype=np.float64)}
     if deck_params is not None:
         extra["deck_params"] = np.asarray(deck_params, dtype=np.float64).reshape(n, -1)
+    if pair_eps is not None:
+        extra["pair_eps"] = np.asarray(pair_eps, dtype=np.float64)
+        extra["pair_sig"] = (np.asarray(pair_sig, dtype=np.float64) if pair_sig is not None
+                             else np.zeros_like(extra["pair_eps"]))
     return {**extra, "name": name, "kind": kind, "integ": integ, "nsteps": nsteps, "dt": float(dt),
             "damping": float(damping), "T": float(T), "skin": float(skin),
             "L": np.asarray(L, dtype=np.float64), "x": np.asarray(x, dtype=np.float64),
@@ -321,6 +330,33 @@ def cases() -> list[dict]:
                      rng.uniform(0, Lr, (n, 3)), rng.normal(0, 0.3, (n, 3)), np.ones(n),
                      np.stack([eps, sig, expo, gam], 1), 0.3, [1, 10, 100, 300],
                      deck_params=np.stack([eps, sig, gam, expo], 1)))
+    # 19-24. indexed pair epsilons (and sigmas): three atom types, a symmetric table with one
+    #        non-positive entry (the repulsion-only branch of the kinds that have one)
+    L, x, v = lj_lattice_deck((6, 6, 6), 71)
+    n = len(x)
+    rng = np.random.default_rng(71)
+    t = rng.integers(0, 3, n).astype(np.float64)
+    teps = np.array([[1.0, 0.6, 0.3], [0.6, 1.3, -0.5], [0.3, -0.5, 0.8]])
+    tsig = np.array([[1.0, 1.1, 1.05], [1.1, 1.2, 1.15], [1.05, 1.15, 0.95]])
+    cutv = rng.choice([2.0, 2.5], n)
+    out.append(_case("ljcut_iepsisig216_verlet", LJCUT_IEPSISIG, VERLET, 300, 0.002, L * 1.1, x * 1.1, v,
+                     np.ones(n), np.stack([t, cutv, np.zeros(n)], 1), 0.3, [1, 10, 100, 300],
+                     pair_eps=np.abs(teps), pair_sig=tsig))
+    out.append(_case("ljattract_iepsisig216_verlet", LJATTRACT_IEPSISIG, VERLET, 300, 0.002, L * 1.1, x * 1.1,
+                     v, np.ones(n), np.stack([t, cutv, np.zeros(n)], 1), 0.3, [1, 10, 100, 300],
+                     pair_eps=np.abs(teps), pair_sig=tsig))
+    sgv = rng.choice([1.0, 1.2], n)
+    out.append(_case("ljattract_ieps216_verlet", LJATTRACT_IEPS, VERLET, 300, 0.002, L * 1.1, x * 1.1, v,
+                     np.ones(n), np.stack([t, sgv, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=np.abs(teps)))
+    out.append(_case("ljattractrepulse216_verlet", LJATTRACTREPULSE, VERLET, 300, 0.002, L * 1.1, x * 1.1, v,
+                     np.ones(n), np.stack([t, sgv, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=teps))
+    rep = rng.choice([0.5, 2.0], n)
+    out.append(_case("ljattractfixedrepulse216_verlet", LJATTRACTFIXEDREPULSE, VERLET, 300, 0.002, L * 1.1,
+                     x * 1.1, v, np.ones(n), np.stack([t, rep, sgv, cutv], 1), 0.3, [1, 10, 100, 300],
+                     pair_eps=teps))
+    nexp = rng.choice([8.0, 12.0], n)
+    out.append(_case("ljish216_verlet", LJISH, VERLET, 300, 0.002, L * 1.1, x * 1.1, v, np.ones(n),
+                     np.stack([t, rep, sgv, nexp, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=teps))
     return out
 
 

@@ -21,6 +21,8 @@ def replay(d):
     o = Oracle(d["n"], d["ndim"])
     o.set_box(d["L"])
     o.set_state(x=d["x"], v=d["v"], m=d["m"])
+    if "pair_eps" in d:
+        o.set_pair_table(d["pair_eps"], d["pair_sig"])
     o.set_interaction(d["kind"], d["params"], d["skin"], order=[int(i) for i in d["order"]])
     for a, b in d["ignores"]:
         o.ignore(int(a), int(b))
