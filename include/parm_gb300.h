@@ -44,7 +44,7 @@ extern "C" {
                                LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
-/* Kinds 4-9 run on FP64 handles only (a mixed-precision handle rejects
+/* Kinds 4-15 run on FP64 handles only (a mixed-precision handle rejects
  * them); kinds 4-7 and 9 take four parameters per atom (the atoms' fields). */
 #define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
                                 1679-1744): params (eps, sigma, C, l), C and l averaged */
@@ -61,9 +61,27 @@ extern "C" {
                                 velocity; params (eps, sigma, exponent, gamma), the fields
                                 EpsSigExpDragAtom(eps, sigma, gamma, exponent) stores; FP64 handles
                                 only */
+/* Indexed epsilons (the IEps*Atom types): the pair's epsilon (and for kinds
+ * 10-11 its sigma) comes from the tables of parm_set_pair_table by the two
+ * atoms' types, the first atom's row (IEps*Atom::get_epsilon, the first atom
+ * being the later one in the neighbour list); params begin with the atom's
+ * type index (indx).  FP64 handles only. */
+#define PARM_LJCUT_IEPSISIG 10    /* NListed<IEpsISigCutAtom, LennardJonesCutPair> (src/interaction.hpp:
+                                     911-954, 977-982): params (indx, sigcut, unused) */
+#define PARM_LJATTRACTCUT_IEPSISIG 11 /* NListed<IEpsISigCutAtom, LJAttractCutPair> (1028-1032): same */
+#define PARM_LJATTRACTCUT_IEPS 12 /* NListed<IEpsSigCutAtom, LJAttractCutPair> (989-1018, 1033-1037):
+                                     params (indx, sigma, sigcut) */
+#define PARM_LJATTRACTREPULSE 13  /* NListed<IEpsSigCutAtom, LJAttractRepulsePair> (1251-1298): same */
+#define PARM_LJATTRACTFIXEDREPULSE 14 /* NListed<IEpsRepsSigCutAtom, LJAttractFixedRepulsePair>
+                                     (1307-1399): params (indx, repeps, sigma, sigcut) */
+#define PARM_LJISH 15             /* NListed<IEpsRepsSigExpCutAtom, LJishPair> (1051-1141):
+                                     params (indx, repeps, sigma, n, sigcut) */
 /* doubles per atom in parm_set_interaction's params */
-#define PARM_NPARAM(kind) \
-    ((((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) || (kind) == PARM_REPULSIONDRAG) ? 4 : 3)
+#define PARM_NPARAM(kind)                                                                             \
+    ((((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) || (kind) == PARM_REPULSIONDRAG ||    \
+      (kind) == PARM_LJATTRACTFIXEDREPULSE)                                                           \
+         ? 4                                                                                          \
+         : ((kind) == PARM_LJISH ? 5 : 3))
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u
@@ -125,6 +143,13 @@ int parm_get_atoms(parm_system* s, double* atoms, uint64_t stride, uint32_t fiel
  * Marks the list for a rebuild on the next update (ignorechanged = true). */
 int parm_set_interaction(parm_system* s, int kind, const double* params, const uint32_t* rank,
                          double skin);
+
+/* Tables of the indexed kinds (PARM_LJCUT_IEPSISIG ..): eps[a * ntypes + b]
+ * is epsilons[b] of the atoms of type a (IEps*Atom::epsilons), sig likewise
+ * (IEpsISigCutAtom::sigmas; NULL when no kind in use reads it).  Set before
+ * parm_set_interaction with an indexed kind; the next parm_set_interaction
+ * applies a change. */
+int parm_set_pair_table(parm_system* s, uint32_t ntypes, const double* eps, const double* sig);
 
 /* List diameters given to NeighborList::add(atom, diameter)
  * (src/trackers.hpp:194-201) instead of the pair parameters' max_size():

@@ -33,11 +33,20 @@ LOISLIN = 6         # params (eps, sigma, f, l); FP64 handles
 LOISLIN_MIN = 7
 EISMCLACHLAN = 8    # params (dist, sigmai, unused); FP64 handles
 REPULSIONDRAG = 9   # params (eps, sigma, exponent, gamma); FP64 handles
+# indexed epsilons (parm_set_pair_table first); params begin with the type index; FP64 handles
+LJCUT_IEPSISIG = 10             # (indx, sigcut, unused)
+LJATTRACTCUT_IEPSISIG = 11      # (indx, sigcut, unused)
+LJATTRACTCUT_IEPS = 12          # (indx, sigma, sigcut)
+LJATTRACTREPULSE = 13           # (indx, sigma, sigcut)
+LJATTRACTFIXEDREPULSE = 14      # (indx, repeps, sigma, sigcut)
+LJISH = 15                      # (indx, repeps, sigma, n, sigcut)
 
 
 def nparam(kind: int) -> int:
-    """Doubles per atom in parm_set_interaction's params."""
-    return 4 if (LOISOHERN <= kind <= LOISLIN_MIN or kind == REPULSIONDRAG) else 3
+    """Doubles per atom in parm_set_interaction's params (PARM_NPARAM)."""
+    if LOISOHERN <= kind <= LOISLIN_MIN or kind in (REPULSIONDRAG, LJATTRACTFIXEDREPULSE):
+        return 4
+    return 5 if kind == LJISH else 3
 
 X, V, A, F, M = 1, 2, 4, 8, 16
 
@@ -68,6 +77,7 @@ SIGNATURES = {
     "parm_set_atoms": (C.c_int, [_h, _dp, C.c_uint64, C.c_uint32]),
     "parm_get_atoms": (C.c_int, [_h, _dp, C.c_uint64, C.c_uint32]),
     "parm_set_interaction": (C.c_int, [_h, C.c_int, _dp, _u32p, C.c_double]),
+    "parm_set_pair_table": (C.c_int, [_h, C.c_uint32, _dp, _dp]),
     "parm_nlist_ignore": (C.c_int, [_h, C.c_uint32, C.c_uint32]),
     "parm_set_list_diameters": (C.c_int, [_h, _dp]),
     "parm_nlist_update": (C.c_int, [_h, C.c_int, _u8p]),

@@ -31,7 +31,19 @@ thread_local std::string g_err;
 // EpsSigExpAtom 1464, EpsSigAtom 864, LoisOhernAtom 1691, LoisLinAtom 1780,
 // EisMclachlanAtom 1423):
 // the atom's diameter in its neighbour list
-double atom_max_size(int kind, const double* p) {
+double atom_max_size(int kind, const double* p, const std::vector<double>& tsig, uint32_t ntypes) {
+    if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) {
+        // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut
+        const uint32_t t = (uint32_t)p[0];
+        if (t >= ntypes || tsig.size() < (size_t)ntypes * ntypes) return 0.0;
+        double sg = tsig[(size_t)t * ntypes];
+        for (uint32_t k = 1; k < ntypes; ++k)
+            if (sg < tsig[(size_t)t * ntypes + k]) sg = tsig[(size_t)t * ntypes + k];
+        return sg * p[1];
+    }
+    if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE) return p[1] * p[2];
+    if (kind == PARM_LJATTRACTFIXEDREPULSE) return p[2] * p[3];
+    if (kind == PARM_LJISH) return p[2] * p[4];
     if (kind == PARM_LJCUT || kind == PARM_LJATTRACTCUT) return p[1] * p[2];
     if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return p[1] * (1 + p[2] + p[3]);
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return p[1] * (1 + p[3]);
@@ -45,6 +57,11 @@ int device_kind(int kind) {
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return KIND_LOISLIN;
     if (kind == PARM_EISMCLACHLAN) return KIND_EISMCLACHLAN;
     if (kind == PARM_REPULSIONDRAG) return KIND_REPULSIONDRAG;
+    if (kind == PARM_LJCUT_IEPSISIG) return KIND_LJCUT_IDX;
+    if (kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPS) return KIND_LJATTRACT_IDX;
+    if (kind == PARM_LJATTRACTREPULSE) return KIND_LJATTRACTREPULSE;
+    if (kind == PARM_LJATTRACTFIXEDREPULSE) return KIND_LJFIXEDREPULSE;
+    if (kind == PARM_LJISH) return KIND_LJISH;
     return kind;
 }
 
@@ -100,6 +117,9 @@ struct parm_system {
     double skin = 0.0;
     std::vector<double> prm_in;      // n*3 (global order)
     std::vector<double> ldiam;       // explicit list diameters (global order; NaN: from the parameters), or empty
+    uint32_t ntypes = 0;             // indexed kinds: the pair tables (eps then sig, ntypes^2 each)
+    std::vector<double> teps, tsig;
+    double* ptab_mem = nullptr;
     std::vector<uint32_t> rank_in;   // global order
     std::vector<std::set<uint32_t>> excl;
     bool have_excl = false, excl_dirty = false;
@@ -149,6 +169,7 @@ struct parm_system {
         if (nbr16_mem) cudaFree(nbr16_mem);
         if (rsq_mem) cudaFree(rsq_mem);
         if (nlcg_mem) cudaFree(nlcg_mem);
+        if (ptab_mem) cudaFree(ptab_mem);
         if (excl_mem) cudaFree(excl_mem);
         if (staging) cudaFree(staging);
         if (h_params) cudaFreeHost(h_params);
@@ -223,7 +244,7 @@ struct parm_system {
             if (kind < 0 || rank_in[i] == PARM_NOT_MEMBER) continue;
             any_member = true;
             const double* p = &prm_in[(size_t)PARM_NPARAM(kind) * i];
-            double d = atom_max_size(kind, p);
+            double d = atom_max_size(kind, p, tsig, ntypes);
             if (!ldiam.empty() && std::isfinite(ldiam[i])) d = ldiam[i];
             dmax = std::max(dmax, d);
         }
@@ -1340,7 +1361,9 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > PARM_REPULSIONDRAG) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > PARM_LJISH) return fail(PARM_ERR_ARG, "unknown pair kind");
+    const bool indexed = kind >= PARM_LJCUT_IEPSISIG;
+    if (indexed && S->ntypes == 0) return fail(PARM_ERR_ARG, "indexed pair kinds need parm_set_pair_table first");
     if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
         return fail(PARM_ERR_ARG,
                     "the Lois-O'Hern, Lois-Lin, Eis-Mclachlan and drag pairs run on FP64 handles only");
@@ -1378,8 +1401,23 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             uint32_t g = S->off[s] + i;
             const double* p = &params[np * g];
             AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], np == 4 ? p[3] : 0.0};
+            uint32_t ptype = 0;
+            if (indexed) {
+                // records (repeps, sigma, sigcut, p3), the type apart
+                const bool member = S->rank_in[g] != PARM_NOT_MEMBER;
+                if (member && !(p[0] >= 0.0 && p[0] < (double)S->ntypes && p[0] == std::floor(p[0])))
+                    return fail(PARM_ERR_ARG, "type index out of range");
+                ptype = member ? (uint32_t)p[0] : 0u;
+                if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) a = AtomPrm{0.0, 0.0, p[1], 0.0};
+                else if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE) a = AtomPrm{0.0, p[1], p[2], 0.0};
+                else if (kind == PARM_LJATTRACTFIXEDREPULSE) a = AtomPrm{p[1], p[2], p[3], 0.0};
+                else a = AtomPrm{p[1], p[2], p[4], p[3]};
+                if (kind == PARM_LJCUT_IEPSISIG) a.p3 = 1 - 1 / std::pow(a.p2, 6);      // LennardJonesCut ctor
+                if (kind == PARM_LJATTRACTREPULSE) a.p3 = 1 - std::pow(a.p2, -6);      // its cut energy term
+                if (kind == PARM_LJATTRACTFIXEDREPULSE) a.p3 = 1 - std::pow(a.p2, -6.0);
+            }
             if (kind == PARM_LJCUT) a.p3 = 1 - 1 / std::pow(a.p2, 6);  // LennardJonesCut ctor
-            if (kind == PARM_LJATTRACTCUT) {
+            if (kind == PARM_LJATTRACTCUT || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPS) {
                 // LJAttract::energy(cut) (interaction.hpp:170-177), times epsilon in the pair
                 const double rsig = a.p2;
                 if (rsig < 1) {
@@ -1395,7 +1433,12 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             prm32[g] = (kind == PARM_EISMCLACHLAN)
                            ? make_float4((float)a.p0, (float)a.p1, 0.f, 0.f)   // (dist, sigmai)
                            : make_float4((float)std::sqrt(a.p0), (float)a.p1, (float)a.p2, (float)a.p3);
-            diam[g] = atom_max_size(kind, p);
+            if (indexed) {
+                float tf;
+                std::memcpy(&tf, &ptype, 4);
+                prm32[g].x = tf;   // the type's bit pattern
+            }
+            diam[g] = atom_max_size(kind, p, S->tsig, S->ntypes);
             const bool explicit_d = !S->ldiam.empty() && std::isfinite(S->ldiam[g]);
             if (explicit_d) diam[g] = S->ldiam[g];   // NeighborList::add(atom, diameter)
             if (S->rank_in[g] == PARM_NOT_MEMBER) {
@@ -1405,6 +1448,10 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             if (kind == PARM_EISMCLACHLAN) {
                 if (!(a.p0 >= 0.0 && std::isfinite(a.p0) && std::isfinite(a.p1)))
                     return fail(PARM_ERR_ARG, "dist must be finite and >= 0, sigmai finite");
+            } else if (indexed) {
+                const bool sig_ok = (kind <= PARM_LJATTRACTCUT_IEPSISIG) || a.p1 > 0.0;
+                if (!(sig_ok && a.p0 >= 0.0 && a.p2 >= 0.0 && std::isfinite(a.p2) && (kind != PARM_LJISH || a.p3 > 0.0)))
+                    return fail(PARM_ERR_ARG, "sigma and n must be > 0, repeps and sigcut >= 0");
             } else if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0))) {
                 return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
             }
@@ -1449,6 +1496,11 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     CUDA_TRY(cudaMemcpy(S->c.rank, rank_k.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.nm_rank, nmr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     if (kind == PARM_LOISOHERN_MIN || kind == PARM_LOISLIN_MIN) uni |= COMB_MIN;
+    if (indexed) {
+        // per-pair values come from the tables: no per-atom shortcuts
+        uni &= ~(UNI_EPS | UNI_SIG_ONE);
+        if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) uni |= IDX_SIG;
+    }
     S->c.kind = device_kind(kind);
     S->c.uniform = uni;
     launch_posq(S->c, S->st);
@@ -1462,6 +1514,28 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     S->stg_pending = false;
     if (S->c.staged != was) S->clear_graphs();
     return S->request_rebuild_all();  // ignorechanged = true
+}
+
+int parm_set_pair_table(parm_system* S, uint32_t ntypes, const double* eps, const double* sig) {
+    if (!S || !eps) return fail(PARM_ERR_ARG, "NULL argument");
+    if (ntypes == 0 || ntypes > 4096) return fail(PARM_ERR_ARG, "ntypes must be 1 .. 4096");
+    const size_t nn = (size_t)ntypes * ntypes;
+    for (size_t k = 0; k < nn; k++)
+        if (!std::isfinite(eps[k]) || (sig && !std::isfinite(sig[k]))) return fail(PARM_ERR_ARG, "non-finite table entry");
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    S->ntypes = ntypes;
+    S->teps.assign(eps, eps + nn);
+    if (sig) S->tsig.assign(sig, sig + nn);
+    else S->tsig.assign(nn, 0.0);
+    if (S->ptab_mem) cudaFree(S->ptab_mem);
+    S->ptab_mem = nullptr;
+    CUDA_TRY(cudaMalloc(&S->ptab_mem, 16 * nn));
+    CUDA_TRY(cudaMemcpy(S->ptab_mem, S->teps.data(), 8 * nn, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(S->ptab_mem + nn, S->tsig.data(), 8 * nn, cudaMemcpyHostToDevice));
+    S->c.ptab = S->ptab_mem;
+    S->c.ptab_n = ntypes;
+    return PARM_OK;
 }
 
 int parm_set_list_diameters(parm_system* S, const double* diam) {

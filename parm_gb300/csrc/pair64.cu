@@ -12,6 +12,9 @@
 //   LoisLinPair, LoisLinPairMin             1764-1836
 //   EisMclachlanPair                        1415-1452
 //   RepulsionDragPair                       1598-1640
+//   indexed epsilons: LennardJonesCutPair / LJAttractCutPair on IEps*Atoms
+//   977-982, 1028-1037; LJAttractRepulsePair 1251-1298; LJishPair 1095-1141;
+//   LJAttractFixedRepulsePair 1343-1399
 //
 // Summation order: the reference visits pairs (i, j<i) in ascending (i, j) and
 // scatters +F to i and -F to j.  For atom k this is: neighbours j<k in
@@ -30,9 +33,58 @@ namespace parm {
 __device__ __forceinline__ bool mobile64(double m) { return !(m <= 0.0 || isinf(m)); }
 
 struct PairC {
-    double eps, sig, third, m6;   // the Lois kinds: third = C (or f), m6 = l
-    double cut;                   // the Lois kinds: sigcut
+    double eps, sig, third, m6;   // the Lois kinds: third = C (or f), m6 = l; LJish: m6 = n
+    double cut;                   // the Lois kinds: sigcut; LJAttractRepulse, LJAttractFixedRepulse,
+                                  // LJish: the cut energy
+    double rep;                   // LJAttractFixedRepulse, LJish: the repulsive epsilon
 };
+
+// Pair constants of the indexed kinds, A the pair's first atom (the later one
+// in the neighbour list: its row of the table is used, IEps*Atom::get_epsilon).
+// Atom records: (repeps, sigma, sigcut, p3) with p3 = 1 - 1/sigcut^6
+// (LennardJonesCut), LJAttract::energy(sigcut), 1 - sigcut^-6 (the attractive-
+// repulsive pairs) or the exponent n (LJish).
+template <int KIND>
+__device__ __forceinline__ PairC combine_idx(const DevCtx& c, const AtomPrm& A, const AtomPrm& B, uint32_t ta,
+                                             uint32_t tb, uint32_t uni) {
+    PairC p;
+    const uint32_t n = c.ptab_n;
+    const double te = c.ptab[(size_t)ta * n + tb];
+    p.sig = (uni & IDX_SIG) ? c.ptab[(size_t)n * n + (size_t)ta * n + tb] : (A.p1 + B.p1) / 2.0;
+    const bool b_larger = B.p2 > A.p2;
+    p.third = b_larger ? B.p2 : A.p2;            // max(a1.sigcut, a2.sigcut)
+    const double pc3 = b_larger ? B.p3 : A.p3;   // its per-atom cut term
+    p.rep = sqrt(A.p0 * B.p0);
+    p.cut = 0.0;
+    p.m6 = pc3;
+    p.eps = te;
+    if constexpr (KIND == KIND_LJATTRACTREPULSE) {
+        if (te <= 0) {
+            p.third = 1;
+            p.eps = fabs(te);
+        } else {
+            p.cut = te * (pc3 * pc3);
+        }
+    } else if constexpr (KIND == KIND_LJFIXEDREPULSE) {
+        p.eps = fabs(te);
+        if (!(te > 0) || p.eps == 0) {
+            p.third = 1;
+            p.eps = 0;
+        } else {
+            p.cut = p.eps * (pc3 * pc3);
+        }
+    } else if constexpr (KIND == KIND_LJISH) {
+        p.m6 = (A.p3 + B.p3) / 2;
+        if (te <= 0) {
+            p.third = 1;
+            p.eps = 0;
+        } else {
+            const double mid = (1 - pow(p.third, -p.m6));
+            p.cut = te * (mid * mid);
+        }
+    }
+    return p;
+}
 
 template <int KIND>
 __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uint32_t uni) {
@@ -85,7 +137,31 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
 // pair force scale s (F = r * s); returns false beyond the cut-off
 template <int KIND>
 __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t uni, double& s) {
-    if constexpr (KIND == KIND_LJCUT) {
+    if constexpr (KIND == KIND_LJATTRACTREPULSE) {
+        // LJAttractRepulsePair::forces (interaction.hpp:1287-1297)
+        if (p.eps == 0) return false;
+        double rsq = dsq / (p.sig * p.sig);
+        if (rsq > (p.third * p.third)) return false;
+        double rsix = pow(rsq, -3.0);
+        double fmagTimesR = 12 * p.eps * rsix * (rsix - 1);
+        s = fmagTimesR / dsq;
+        return true;
+    } else if constexpr (KIND == KIND_LJFIXEDREPULSE || KIND == KIND_LJISH) {
+        // LJAttractFixedRepulsePair::forces (1390-1398), LJishPair::forces (1130-1140)
+        double rsq = dsq / (p.sig * p.sig);
+        if (rsq > (p.third * p.third)) return false;
+        double fmagTimesR;
+        if constexpr (KIND == KIND_LJFIXEDREPULSE) {
+            double rsix = pow(rsq, -3.0);
+            fmagTimesR = 12 * rsix * (rsix - 1);
+        } else {
+            double n = p.m6;
+            double rmid = pow(rsq, -n / 2);
+            fmagTimesR = 2 * n * rmid * (rmid - 1);
+        }
+        s = (rsq < 1) ? p.rep * fmagTimesR / dsq : p.eps * fmagTimesR / dsq;
+        return true;
+    } else if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJCUT_IDX) {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
         if (rsq > (p.third * p.third)) return false;
         double rsix = rsq * rsq * rsq;
@@ -99,7 +175,7 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
         double pw = (p.third == 2.0) ? b : pow(b, p.third - 1);   // pow(b, 1) == b exactly
         s = p.eps * pw / p.sig / R;
         return true;
-    } else if constexpr (KIND == KIND_LJATTRACT) {
+    } else if constexpr (KIND == KIND_LJATTRACT || KIND == KIND_LJATTRACT_IDX) {
         // LJAttractCut::forces (interaction.hpp:219-229)
         if (p.eps == 0) return false;
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
@@ -152,7 +228,16 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
 
 template <int KIND>
 __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32_t uni) {
-    if constexpr (KIND == KIND_LJCUT) {
+    if constexpr (KIND == KIND_LJATTRACTREPULSE || KIND == KIND_LJFIXEDREPULSE || KIND == KIND_LJISH) {
+        // LJAttractRepulsePair::energy (1269-1286), LJAttractFixedRepulsePair::energy (1366-1389),
+        // LJishPair::energy (1115-1129)
+        double rsq = dsq / (p.sig * p.sig);
+        if (rsq > p.third * p.third) return 0.0;
+        double mid = (KIND == KIND_LJISH) ? (1 - pow(rsq, -p.m6 / 2)) : (1 - pow(rsq, -3.0));
+        if constexpr (KIND == KIND_LJATTRACTREPULSE) return p.eps * (mid * mid) - p.cut;
+        if (rsq > 1) return p.eps * (mid * mid) - p.cut;
+        return p.rep * (mid * mid) - p.cut;
+    } else if constexpr (KIND == KIND_LJCUT || KIND == KIND_LJCUT_IDX) {
         double rsq = (uni & UNI_SIG_ONE) ? dsq : dsq / (p.sig * p.sig);
         if (rsq > (p.third * p.third)) return 0.0;
         double rsix = rsq * rsq * rsq;
@@ -166,7 +251,7 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         double b = 1.0 - (R / p.sig);
         double pw = (p.third == 2.0) ? b * b : pow(b, p.third);   // pow(b, 2) == b*b exactly
         return p.eps * pw / p.third;
-    } else if constexpr (KIND == KIND_LJATTRACT) {
+    } else if constexpr (KIND == KIND_LJATTRACT || KIND == KIND_LJATTRACT_IDX) {
         // LJAttractCut::energy (interaction.hpp:211-216) with LJAttract::energy (162-169)
         if (p.eps == 0) return 0.0;
         if (dsq > (p.third * p.third * p.sig * p.sig)) return 0.0;
@@ -243,6 +328,7 @@ __device__ __forceinline__ bool drag_force(const PairC& p, const double* r, doub
 // (Q = (sqrt(eps), sigma, third, fourth) in FP32)
 template <int KIND>
 __device__ __forceinline__ bool beyond32(float d2, const float4& Qi, const float4& Qj, uint32_t uni) {
+    if constexpr (idx_kind<KIND>()) return false;   // the table decides sigma: every pair takes the exact test
     float sg = (uni & UNI_SIG) ? Qi.y : 0.5f * (Qi.y + Qj.y);
     float rc;
     if constexpr (cut_kind<KIND>()) {
@@ -330,7 +416,15 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
             AtomPrm Pj = Pi;
             if ((uni & UNI_ALL) != UNI_ALL) Pj = c.prm[j];
-            const PairC pc = combine<KIND>(Pi, Pj, uni);
+            PairC pc;
+            if constexpr (idx_kind<KIND>()) {
+                // the pair's first atom is the one of higher neighbour-list rank
+                const uint32_t ti = __float_as_uint(Qi.x), tj = __float_as_uint(Qj.x);
+                pc = (c.rank[i] > c.rank[j]) ? combine_idx<KIND>(c, Pi, Pj, ti, tj, uni)
+                                             : combine_idx<KIND>(c, Pj, Pi, tj, ti, uni);
+            } else {
+                pc = combine<KIND>(Pi, Pj, uni);
+            }
             if constexpr (KIND == KIND_REPULSIONDRAG) {
                 double vj[3] = {0, 0, 0}, fo[3];
                 load3<ND>(c.v, j, vj);
@@ -387,7 +481,12 @@ __global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
             for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
             double dsq = r[0] * r[0] + r[1] * r[1];
             if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
-            const PairC pc = combine<KIND>(Pi, c.prm[j], uni);
+            PairC pc;
+            if constexpr (idx_kind<KIND>())   // i is the pair's first atom (higher rank)
+                pc = combine_idx<KIND>(c, Pi, c.prm[j], __float_as_uint(c.prm32[i].x),
+                                       __float_as_uint(c.prm32[j].x), uni);
+            else
+                pc = combine<KIND>(Pi, c.prm[j], uni);
             if (what == EV_ENERGY || what == EV_CONTACTS || what == EV_OVERLAPS) {
                 double e = pair_energy<KIND>(pc, dsq, uni);
                 if (what == EV_ENERGY) acc[0] = acc[0] + e;
@@ -437,6 +536,11 @@ static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     else if (c.kind == KIND_LOISLIN) force64_nd_kind<ND, KIND_LOISLIN>(c, s, mode);
     else if (c.kind == KIND_EISMCLACHLAN) force64_nd_kind<ND, KIND_EISMCLACHLAN>(c, s, mode);
     else if (c.kind == KIND_REPULSIONDRAG) force64_nd_kind<ND, KIND_REPULSIONDRAG>(c, s, mode);
+    else if (c.kind == KIND_LJCUT_IDX) force64_nd_kind<ND, KIND_LJCUT_IDX>(c, s, mode);
+    else if (c.kind == KIND_LJATTRACT_IDX) force64_nd_kind<ND, KIND_LJATTRACT_IDX>(c, s, mode);
+    else if (c.kind == KIND_LJATTRACTREPULSE) force64_nd_kind<ND, KIND_LJATTRACTREPULSE>(c, s, mode);
+    else if (c.kind == KIND_LJFIXEDREPULSE) force64_nd_kind<ND, KIND_LJFIXEDREPULSE>(c, s, mode);
+    else if (c.kind == KIND_LJISH) force64_nd_kind<ND, KIND_LJISH>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -454,6 +558,11 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     else if (c.kind == KIND_LOISLIN) k_eval64<ND, KIND_LOISLIN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_EISMCLACHLAN) k_eval64<ND, KIND_EISMCLACHLAN><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSIONDRAG) k_eval64<ND, KIND_REPULSIONDRAG><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJCUT_IDX) k_eval64<ND, KIND_LJCUT_IDX><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJATTRACT_IDX) k_eval64<ND, KIND_LJATTRACT_IDX><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJATTRACTREPULSE) k_eval64<ND, KIND_LJATTRACTREPULSE><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJFIXEDREPULSE) k_eval64<ND, KIND_LJFIXEDREPULSE><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJISH) k_eval64<ND, KIND_LJISH><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

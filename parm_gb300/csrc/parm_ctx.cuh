@@ -71,7 +71,10 @@ struct DevCtx {
     double* m;
     float* invm32;        // mixed path: 1/m in FP32 (0 for immobile atoms)
     AtomPrm* prm;
-    float4* prm32;        // (sqrt(eps), sigma, third, unused) in FP32
+    float4* prm32;        // (sqrt(eps), sigma, third, unused) in FP32; the indexed
+                          // kinds keep the atom's type in x (its bit pattern)
+    const double* ptab;   // indexed kinds: ptab_n x ptab_n epsilons, then sigmas
+    uint32_t ptab_n;
     double* diam;         // A::max_size()
     uint32_t* rank;       // NeighborList position, NOT_MEMBER if not added
     uint32_t* orig;       // caller's atom index (global)

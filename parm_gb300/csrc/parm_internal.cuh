@@ -30,8 +30,17 @@ enum PairKind : int {
     KIND_EISMCLACHLAN = 6,
     // (eps, sigma, exponent, gamma) atoms: soft repulsion with a drag on the
     // relative normal velocity; FP64 path only
-    KIND_REPULSIONDRAG = 7
+    KIND_REPULSIONDRAG = 7,
+    // indexed pair epsilons (IEps* atoms; FP64 path only): the pair's epsilon
+    // (and sigma, flag IDX_SIG) from a table by the two atoms' types
+    KIND_LJCUT_IDX = 8,          // LennardJonesCutPair(IEpsISigCutAtom)
+    KIND_LJATTRACT_IDX = 9,      // LJAttractCutPair(IEpsISigCutAtom / IEpsSigCutAtom)
+    KIND_LJATTRACTREPULSE = 10,  // LJAttractRepulsePair(IEpsSigCutAtom)
+    KIND_LJFIXEDREPULSE = 11,    // LJAttractFixedRepulsePair(IEpsRepsSigCutAtom)
+    KIND_LJISH = 12              // LJishPair(IEpsRepsSigExpCutAtom)
 };
+template <int KIND>
+__host__ __device__ constexpr bool idx_kind() { return KIND >= KIND_LJCUT_IDX && KIND <= KIND_LJISH; }
 template <int KIND>
 __host__ __device__ constexpr bool lois_kind() { return KIND == KIND_LOISOHERN || KIND == KIND_LOISLIN; }
 // kinds whose pair cut-off is max(sigcut_i, sigcut_j) sigma_ij, with a force
@@ -95,6 +104,7 @@ enum UniformFlags : uint32_t {
     // instead of their average
     COMB_MIN = 1u << 5,
     UNI_DIAM = 1u << 6,    // all members share their list diameter
+    IDX_SIG = 1u << 7,     // indexed kinds: the pair sigma comes from the table too
 };
 
 template <int ND> struct DVec;

@@ -76,6 +76,83 @@ struct EpsSigExpAtom : public AtomID {
     flt max_size() { return sigma; }
 };
 
+//! Indexed epsilons and sigmas (src/interaction.hpp:911-954): the pair's
+//! values are a1.epsilons[a2.indx], a1.sigmas[a2.indx].
+struct IEpsISigCutAtom : public AtomID {
+    std::vector<flt> epsilons, sigmas;
+    uint indx;
+    flt sigcut;
+    IEpsISigCutAtom() : indx(0), sigcut(0) {}
+    IEpsISigCutAtom(AtomID a, std::vector<flt> epsilons, std::vector<flt> sigmas, uint indx, flt cut)
+        : AtomID(a), epsilons(epsilons), sigmas(sigmas), indx(indx), sigcut(cut) {}
+    IEpsISigCutAtom(AtomID a, IEpsISigCutAtom other)
+        : AtomID(a), epsilons(other.epsilons), sigmas(other.sigmas), indx(other.indx), sigcut(other.sigcut) {}
+    flt get_epsilon(IEpsISigCutAtom& other) { return epsilons.at(other.indx); }
+    flt get_sigma(IEpsISigCutAtom& other) { return sigmas.at(other.indx); }
+    flt max_size() {
+        flt sg = sigmas.at(0);
+        for (uint i = 1; i < sigmas.size(); ++i)
+            if (sg < sigmas[i]) sg = sigmas[i];
+        return sg * sigcut;
+    }
+};
+
+//! Indexed epsilons, own sigma (src/interaction.hpp:989-1018).
+struct IEpsSigCutAtom : public AtomID {
+    std::vector<flt> epsilons;
+    uint indx;
+    flt sigma, sigcut;
+    IEpsSigCutAtom() : indx(0), sigma(0), sigcut(0) {}
+    IEpsSigCutAtom(AtomID a, std::vector<flt> epsilons, uint indx, flt sigma, flt cut)
+        : AtomID(a), epsilons(epsilons), indx(indx), sigma(sigma), sigcut(cut) {}
+    IEpsSigCutAtom(AtomID a, IEpsSigCutAtom other)
+        : AtomID(a), epsilons(other.epsilons), indx(other.indx), sigma(other.sigma), sigcut(other.sigcut) {}
+    flt get_epsilon(IEpsSigCutAtom& other) { return epsilons.at(other.indx); }
+    flt max_size() { return sigma * sigcut; }
+};
+
+//! Indexed attractive epsilons with a repulsive epsilon (src/interaction.hpp:1307-1336).
+struct IEpsRepsSigCutAtom : public AtomID {
+    std::vector<flt> epsilons;
+    flt repeps, sig;
+    uint indx;
+    flt sigcut;
+    IEpsRepsSigCutAtom() : repeps(0), sig(0), indx(0), sigcut(0) {}
+    IEpsRepsSigCutAtom(AtomID a, std::vector<flt> epsilons, flt repeps, flt sigma, uint indx, flt cut)
+        : AtomID(a), epsilons(epsilons), repeps(repeps), sig(sigma), indx(indx), sigcut(cut) {}
+    IEpsRepsSigCutAtom(AtomID a, IEpsRepsSigCutAtom other)
+        : AtomID(a), epsilons(other.epsilons), repeps(other.repeps), sig(other.sig), indx(other.indx),
+          sigcut(other.sigcut) {}
+    flt get_epsilon(IEpsRepsSigCutAtom& other) { return epsilons.at(other.indx); }
+    flt max_size() { return sig * sigcut; }
+};
+
+//! Indexed epsilons, repulsive epsilon and exponent (src/interaction.hpp:1051-1092).
+struct IEpsRepsSigExpCutAtom : public AtomID {
+    std::vector<flt> epsilons;
+    flt repeps, sigma, exponent;
+    uint indx;
+    flt sigcut;
+    IEpsRepsSigExpCutAtom() : repeps(0), sigma(0), exponent(0), indx(0), sigcut(0) {}
+    IEpsRepsSigExpCutAtom(AtomID a, std::vector<flt> epsilons, flt repeps, flt sigma, flt n, uint indx, flt cut)
+        : AtomID(a), epsilons(epsilons), repeps(repeps), sigma(sigma), exponent(n), indx(indx), sigcut(cut) {}
+    IEpsRepsSigExpCutAtom(AtomID a, IEpsRepsSigExpCutAtom other)
+        : AtomID(a), epsilons(other.epsilons), repeps(other.repeps), sigma(other.sigma), exponent(other.exponent),
+          indx(other.indx), sigcut(other.sigcut) {}
+    flt get_epsilon(IEpsRepsSigExpCutAtom& other) { return epsilons.at(other.indx); }
+    flt get_sigma(IEpsRepsSigExpCutAtom& other) { return (sigma + other.sigma) / 2.0; }
+    flt max_size() { return sigma * sigcut; }
+};
+
+// the table rows an indexed atom brings to its neighbour list's GPU handle
+inline void register_types(GpuLink&, const AtomID&) {}
+inline void register_types(GpuLink& l, const IEpsISigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, &a.sigmas); }
+inline void register_types(GpuLink& l, const IEpsSigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, nullptr); }
+inline void register_types(GpuLink& l, const IEpsRepsSigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, nullptr); }
+inline void register_types(GpuLink& l, const IEpsRepsSigExpCutAtom& a) {
+    l.set_type_row(a.indx, a.epsilons, nullptr);
+}
+
 // Pair laws.  Each pair type holds its pair's constants (combined from the
 // two atoms as the reference combines them) and its two atoms; `kind` and
 // `params` tell the GPU which law and which per-atom numbers to use.
@@ -89,6 +166,13 @@ struct LennardJonesCutPair {
         p[1] = a.sigma;
         p[2] = a.sigcut;
     }
+    static int kind_of(const EpsSigCutAtom&) { return PARM_LJCUT; }
+    static int kind_of(const IEpsISigCutAtom&) { return PARM_LJCUT_IEPSISIG; }
+    static void params(const IEpsISigCutAtom& a, double p[3]) {
+        p[0] = a.indx;
+        p[1] = a.sigcut;
+        p[2] = 0.0;
+    }
     flt epsilon, sigma, cut_distance, cut_energy;
     AtomID atom1, atom2;
     LennardJonesCutPair(EpsSigCutAtom a1, EpsSigCutAtom a2)
@@ -97,6 +181,18 @@ struct LennardJonesCutPair {
           cut_distance(std::max(a1.sigcut, a2.sigcut)),
           atom1(a1),
           atom2(a2) {
+        set_cut_energy();
+    }
+    //! indexed epsilon and sigma (src/interaction.hpp:977-982)
+    LennardJonesCutPair(IEpsISigCutAtom a1, IEpsISigCutAtom a2)
+        : epsilon(a1.get_epsilon(a2)),
+          sigma(a1.get_sigma(a2)),
+          cut_distance(std::max(a1.sigcut, a2.sigcut)),
+          atom1(a1),
+          atom2(a2) {
+        set_cut_energy();
+    }
+    void set_cut_energy() {
         const flt rsix = std::pow(cut_distance, 6);
         const flt mid = (1 - 1 / rsix);
         cut_energy = epsilon * (mid * mid - 1);
@@ -191,14 +287,32 @@ struct LJAttractCutPair {
         p[1] = a.sigma;
         p[2] = a.sigcut;
     }
+    static int kind_of(const EpsSigCutAtom&) { return PARM_LJATTRACTCUT; }
+    static int kind_of(const IEpsISigCutAtom&) { return PARM_LJATTRACTCUT_IEPSISIG; }
+    static int kind_of(const IEpsSigCutAtom&) { return PARM_LJATTRACTCUT_IEPS; }
+    static void params(const IEpsISigCutAtom& a, double p[3]) {
+        p[0] = a.indx;
+        p[1] = a.sigcut;
+        p[2] = 0.0;
+    }
+    static void params(const IEpsSigCutAtom& a, double p[3]) {
+        p[0] = a.indx;
+        p[1] = a.sigma;
+        p[2] = a.sigcut;
+    }
     flt epsilon, sigma, cut_distance, cut_energy;
     AtomID atom1, atom2;
     LJAttractCutPair(EpsSigCutAtom a1, EpsSigCutAtom a2)
-        : epsilon(std::sqrt(a1.epsilon * a2.epsilon)),
-          sigma((a1.sigma + a2.sigma) / 2),
-          cut_distance(std::max(a1.sigcut, a2.sigcut)),
-          atom1(a1),
-          atom2(a2) {
+        : LJAttractCutPair(a1, a2, std::sqrt(a1.epsilon * a2.epsilon), (a1.sigma + a2.sigma) / 2,
+                           std::max(a1.sigcut, a2.sigcut)) {}
+    //! indexed epsilon and sigma (src/interaction.hpp:1028-1032)
+    LJAttractCutPair(IEpsISigCutAtom a1, IEpsISigCutAtom a2)
+        : LJAttractCutPair(a1, a2, a1.get_epsilon(a2), a1.get_sigma(a2), std::max(a1.sigcut, a2.sigcut)) {}
+    //! indexed epsilon (src/interaction.hpp:1033-1037)
+    LJAttractCutPair(IEpsSigCutAtom a1, IEpsSigCutAtom a2)
+        : LJAttractCutPair(a1, a2, a1.get_epsilon(a2), (a1.sigma + a2.sigma) / 2, std::max(a1.sigcut, a2.sigcut)) {}
+    LJAttractCutPair(AtomID a1, AtomID a2, flt eps, flt sig, flt cut)
+        : epsilon(eps), sigma(sig), cut_distance(cut), atom1(a1), atom2(a2) {
         flt e = -1;   // the unit-epsilon attraction at the cut
         if (cut_distance >= 1) {
             const flt rsq = cut_distance * cut_distance;
@@ -440,6 +554,147 @@ struct EisMclachlanPair {
     }
 };
 
+//! LJ with an indexed epsilon; repulsion only (|eps|, cut at sigma) when
+//! the table's entry is not positive (src/interaction.hpp:1251-1298).
+struct LJAttractRepulsePair {
+    static const int kind = PARM_LJATTRACTREPULSE;
+    static void params(const IEpsSigCutAtom& a, double p[3]) {
+        p[0] = a.indx;
+        p[1] = a.sigma;
+        p[2] = a.sigcut;
+    }
+    flt eps, sig, cut_distance, cut_energy;
+    AtomID atom1, atom2;
+    LJAttractRepulsePair(IEpsSigCutAtom a1, IEpsSigCutAtom a2)
+        : eps(a1.get_epsilon(a2)), sig((a1.sigma + a2.sigma) / 2.0), cut_distance(std::max(a1.sigcut, a2.sigcut)),
+          atom1(a1), atom2(a2) {
+        if (eps <= 0) {
+            cut_distance = 1;
+            cut_energy = 0;
+            eps = std::abs(eps);
+            return;
+        }
+        const flt mid = (1 - std::pow(cut_distance, -6));
+        cut_energy = eps * (mid * mid);
+    }
+    flt energy(Box& box) {
+        const flt rsq = box.diff(atom1->x, atom2->x).squaredNorm() / (sig * sig);
+        if (rsq > cut_distance * cut_distance) return 0;
+        const flt mid = (1 - std::pow(rsq, -3));
+        return eps * (mid * mid) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        if (eps == 0) return Vec::Zero();
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        const flt rsq = dsq / (sig * sig);
+        if (rsq > (cut_distance * cut_distance)) return Vec::Zero();
+        const flt rsix = std::pow(rsq, -3);
+        return rij * (12 * eps * rsix * (rsix - 1) / dsq);
+    }
+};
+
+//! LJ with an indexed attractive epsilon (none when the entry is not
+//! positive) and a repulsive epsilon inside sigma
+//! (src/interaction.hpp:1343-1399).
+struct LJAttractFixedRepulsePair {
+    static const int kind = PARM_LJATTRACTFIXEDREPULSE;
+    static void params(const IEpsRepsSigCutAtom& a, double p[4]) {
+        p[0] = a.indx;
+        p[1] = a.repeps;
+        p[2] = a.sig;
+        p[3] = a.sigcut;
+    }
+    flt eps, repeps, sig, cut_distance, cut_energy;
+    bool attract;
+    AtomID atom1, atom2;
+    LJAttractFixedRepulsePair(IEpsRepsSigCutAtom a1, IEpsRepsSigCutAtom a2)
+        : eps(std::abs(a1.get_epsilon(a2))), repeps(std::sqrt(a1.repeps * a2.repeps)), sig((a1.sig + a2.sig) / 2.0),
+          cut_distance(std::max(a1.sigcut, a2.sigcut)), attract(a1.get_epsilon(a2) > 0), atom1(a1), atom2(a2) {
+        if (!attract || eps == 0) {
+            cut_distance = 1;
+            cut_energy = 0;
+            eps = 0;
+            attract = false;
+            return;
+        }
+        const flt mid = (1 - std::pow(cut_distance, -6.0));
+        cut_energy = eps * (mid * mid);
+    }
+    flt energy(Box& box) {
+        const flt rsq = box.diff(atom1->x, atom2->x).squaredNorm() / (sig * sig);
+        if (rsq > cut_distance * cut_distance) return 0;
+        const flt mid = (1 - std::pow(rsq, -3));
+        if (rsq > 1) return eps * (mid * mid) - cut_energy;
+        return repeps * (mid * mid) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        const flt rsq = dsq / (sig * sig);
+        if (rsq > (cut_distance * cut_distance)) return Vec::Zero();
+        const flt rsix = std::pow(rsq, -3);
+        const flt fmagTimesR = 12 * rsix * (rsix - 1);
+        if (rsq < 1) return rij * (repeps * fmagTimesR / dsq);
+        return rij * (eps * fmagTimesR / dsq);
+    }
+};
+
+//! LJ-like law with exponent n, indexed epsilon, repulsive epsilon inside
+//! sigma (src/interaction.hpp:1095-1141).
+struct LJishPair {
+    static const int kind = PARM_LJISH;
+    static void params(const IEpsRepsSigExpCutAtom& a, double p[5]) {
+        p[0] = a.indx;
+        p[1] = a.repeps;
+        p[2] = a.sigma;
+        p[3] = a.exponent;
+        p[4] = a.sigcut;
+    }
+    flt epsilon, repeps, sigma, n, cut_distance, cut_energy;
+    AtomID atom1, atom2;
+    LJishPair(IEpsRepsSigExpCutAtom a1, IEpsRepsSigExpCutAtom a2)
+        : epsilon(a1.get_epsilon(a2)), repeps(std::sqrt(a1.repeps * a2.repeps)), sigma(a1.get_sigma(a2)),
+          n((a1.exponent + a2.exponent) / 2), cut_distance(std::max(a1.sigcut, a2.sigcut)), atom1(a1), atom2(a2) {
+        if (epsilon <= 0) {
+            cut_distance = 1;
+            cut_energy = 0;
+            epsilon = 0;
+            return;
+        }
+        const flt mid = (1 - std::pow(cut_distance, -n));
+        cut_energy = epsilon * (mid * mid);
+    }
+    flt energy(Box& box) {
+        const flt rsq = box.diff(atom1->x, atom2->x).squaredNorm() / (sigma * sigma);
+        if (rsq > cut_distance * cut_distance) return 0;
+        const flt mid = (1 - std::pow(rsq, -n / 2));
+        if (rsq > 1) return epsilon * (mid * mid) - cut_energy;
+        return repeps * (mid * mid) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        const flt rsq = dsq / (sigma * sigma);
+        if (rsq > cut_distance * cut_distance) return Vec::Zero();
+        const flt rmid = std::pow(rsq, -n / 2);
+        const flt fmagTimesR = 2 * n * rmid * (rmid - 1);
+        if (rsq < 1) return rij * (repeps * fmagTimesR / dsq);
+        return rij * (epsilon * fmagTimesR / dsq);
+    }
+};
+
+// the pair law (PARM_* kind) of pair type P for atom type A: P::kind_of(A)
+// where a pair type serves several atom types, else P::kind
+template <class P, class A>
+auto pair_kind(const A& a, int) -> decltype(P::kind_of(a)) {
+    return P::kind_of(a);
+}
+template <class P, class A>
+int pair_kind(const A&, long) {
+    return P::kind;
+}
+
 // GPU-evaluated quantities of the handle's interaction
 flt gpu_evaluate(GpuLink& link, int what);
 Matrix gpu_stress(GpuLink& link);
@@ -462,9 +717,10 @@ class NListed : public Interaction, public GpuInteraction {
         init_atoms(*atomv);
     }
     void add(A atm) {
-        double p[4] = {0.0, 0.0, 0.0, 0.0};
+        double p[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         P::params(atm, p);
-        link->add(atm.n(), P::kind, p, this);
+        register_types(*link, atm);
+        link->add(atm.n(), pair_kind<P>(atm, 0), p, this);
         atoms.at(atm.n()) = atm;
     }
     //! the pair of an IDPair of the neighbour list, with its constants

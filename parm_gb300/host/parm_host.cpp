@@ -1,6 +1,7 @@
 // parm_gb300 host API implementation: the reference's C++ classes
 // (wackywendell/parm src/box.*, src/trackers.*, src/interaction.hpp,
 // src/collection.*) on top of the C ABI of include/parm_gb300.h.
+#include <algorithm>
 #include <cstdlib>
 #include <functional>
 #include <cstring>
@@ -115,7 +116,7 @@ void parm_host_check(int rc, const char* what) {
 GpuLink::GpuLink(sptr<Box> box, sptr<AtomVec> atoms, flt skin) : bx(box), atomv(atoms), skin_(skin) {
     if (!std::dynamic_pointer_cast<OriginBox>(bx))
         throw std::invalid_argument("parm_gb300: the GPU path supports periodic OriginBox boxes");
-    params.assign(4 * (size_t)atomv->size(), 0.0);
+    params.assign(5 * (size_t)atomv->size(), 0.0);
     rank.assign(atomv->size(), PARM_NOT_MEMBER);
     ldiam.assign(atomv->size(), std::nan(""));
 }
@@ -124,7 +125,7 @@ GpuLink::~GpuLink() {
     if (h) parm_destroy(h);
 }
 
-void GpuLink::add(uint atom, int k, const double p[4], const void* owner) {
+void GpuLink::add(uint atom, int k, const double p[5], const void* owner) {
     if (atom >= atomv->size()) throw std::out_of_range("NListed::add: atom not in this AtomVec");
     if (owner_ && owner != owner_)
         throw std::invalid_argument("parm_gb300: one NListed interaction per NeighborList");
@@ -132,9 +133,28 @@ void GpuLink::add(uint atom, int k, const double p[4], const void* owner) {
     if (rank[atom] != PARM_NOT_MEMBER) throw std::invalid_argument("NListed::add: atom added twice");
     owner_ = owner;
     kind = k;
-    for (int q = 0; q < PARM_NPARAM(k); q++) params[4 * (size_t)atom + q] = p[q];
+    for (int q = 0; q < PARM_NPARAM(k); q++) params[5 * (size_t)atom + q] = p[q];
     rank[atom] = nmembers++;
     interaction_dirty = true;
+}
+
+void GpuLink::set_type_row(uint type, const std::vector<flt>& eps, const std::vector<flt>* sig) {
+    if (type >= eps.size()) throw std::invalid_argument("NListed::add: the atom's index is not in its epsilons");
+    std::vector<double> e(eps.begin(), eps.end());
+    std::vector<double> sg;
+    if (sig) sg.assign(sig->begin(), sig->end());
+    if (type >= eps_rows.size()) {
+        eps_rows.resize(type + 1);
+        sig_rows.resize(type + 1);
+    }
+    if (!eps_rows[type].empty()) {
+        if (eps_rows[type] != e || sig_rows[type] != sg)
+            throw std::invalid_argument("parm_gb300: atoms of one type index must share their epsilons and sigmas");
+        return;
+    }
+    eps_rows[type] = e;
+    sig_rows[type] = sg;
+    rows_dirty = true;
 }
 
 void GpuLink::add_member(uint atom, double diameter) {
@@ -164,6 +184,22 @@ void GpuLink::push() {
         parm_host_check(parm_set_boxes(h, lv.data()), "parm_set_boxes");
         lastbox = lv;
     }
+    if (rows_dirty) {
+        // the table of the indexed kinds: row a = the epsilons of the atoms of type a
+        size_t nt = eps_rows.size();
+        for (auto& r : eps_rows) nt = std::max(nt, r.size());
+        std::vector<double> te(nt * nt, 0.0), ts(nt * nt, 0.0);
+        bool any_sig = false;
+        for (size_t a = 0; a < eps_rows.size(); a++) {
+            for (size_t b = 0; b < eps_rows[a].size(); b++) te[a * nt + b] = eps_rows[a][b];
+            for (size_t b = 0; b < sig_rows[a].size(); b++) ts[a * nt + b] = sig_rows[a][b];
+            any_sig = any_sig || !sig_rows[a].empty();
+        }
+        parm_host_check(parm_set_pair_table(h, (uint32_t)nt, te.data(), any_sig ? ts.data() : nullptr),
+                        "parm_set_pair_table");
+        rows_dirty = false;
+        interaction_dirty = true;
+    }
     if (interaction_dirty && nmembers > 0) {
         if (any_ldiam) parm_host_check(parm_set_list_diameters(h, ldiam.data()), "parm_set_list_diameters");
         // members without an NListed carry no parameters: any law with zero
@@ -172,7 +208,7 @@ void GpuLink::push() {
         const size_t np = PARM_NPARAM(k), n = atomv->size();
         std::vector<double> packed(np * n);
         for (size_t i = 0; i < n; i++)
-            for (size_t q = 0; q < np; q++) packed[np * i + q] = params[4 * i + q];
+            for (size_t q = 0; q < np; q++) packed[np * i + q] = params[5 * i + q];
         parm_host_check(parm_set_interaction(h, k, packed.data(), rank.data(), skin_), "parm_set_interaction");
         interaction_dirty = false;
     }

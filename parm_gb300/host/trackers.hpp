@@ -35,7 +35,10 @@ class GpuLink {
     //! PARM_NPARAM(kind) of p) and the atom's position in the neighbour list
     //! (insertion order); `owner` is the NListed adding it (one NListed per
     //! neighbour list)
-    void add(uint atom, int kind, const double p[4], const void* owner);
+    void add(uint atom, int kind, const double p[5], const void* owner);
+    //! the pair tables of the indexed kinds: the epsilons (and sigmas, or
+    //! NULL) of the atoms of type `type`; atoms of one type must share them
+    void set_type_row(uint type, const std::vector<flt>& eps, const std::vector<flt>* sig);
     //! NeighborList::add(atom, diameter): a list member with its own list
     //! diameter and no pair parameters (its pairs carry no force)
     void add_member(uint atom, double diameter);
@@ -62,7 +65,9 @@ class GpuLink {
     flt skin_;
     parm_system* h = nullptr;
     int kind = -1;
-    std::vector<double> params;   // four per atom
+    std::vector<double> params;   // five per atom
+    std::vector<std::vector<double>> eps_rows, sig_rows;   // by type index (indexed kinds)
+    bool rows_dirty = false;
     std::vector<uint32_t> rank;
     std::vector<double> ldiam;   // explicit list diameters (NaN: the parameters' max_size())
     bool any_ldiam = false;

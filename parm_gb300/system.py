@@ -102,6 +102,15 @@ class System:
         check(self.lib.parm_set_interaction(self.h, kind, dptr(p), u32ptr(rk) if rk is not None else None,
                                             float(skin)))
 
+    def set_pair_table(self, eps, sig=None) -> None:
+        """Pair tables of the indexed kinds: eps[a, b] = epsilons[b] of the atoms of type a
+        (IEps*Atom), sig likewise (IEpsISigCutAtom::sigmas)."""
+        e = np.ascontiguousarray(np.asarray(eps, dtype=np.float64))
+        nt = e.shape[0]
+        e = _as_f64(e, (nt, nt))
+        sg = _as_f64(sig, (nt, nt)) if sig is not None else None
+        check(self.lib.parm_set_pair_table(self.h, nt, dptr(e), dptr(sg) if sg is not None else None))
+
     def set_list_diameters(self, diam) -> None:
         """NeighborList::add(atom, diameter): explicit list diameters (NaN: from the parameters); None clears."""
         if diam is None:

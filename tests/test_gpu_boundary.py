@@ -236,3 +236,49 @@ def test_repulsion_drag_matches_oracle(vary_gamma):
         assert np.array_equal(st[k], ref[k]), k
     assert g.virial()[0] == pytest.approx(o.pressure()[0], rel=1e-12, abs=1e-12)
     g.close()
+
+
+@pytest.mark.parametrize("kind", [10, 12])
+def test_indexed_asymmetric_table_matches_oracle(kind):
+    """Indexed epsilons with an asymmetric table and a shuffled insertion order: each pair takes the row
+    of its first atom (the later one in the neighbour list), as IEps*Atom::get_epsilon does.  Pairs,
+    forces and 50 Verlet steps bit-exact against the oracle."""
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    L, x, v = None, None, None
+    w = W.lj_lattice(shape=(6, 6, 6), skin_prime=0.3, seed=83)
+    n = w.n
+    x, v, L = w.x * 1.1, w.v, w.L[0] * 1.1
+    rng = np.random.default_rng(83)
+    t = rng.integers(0, 3, n).astype(np.float64)
+    teps = np.array([[1.0, 0.7, 0.4], [0.5, 1.2, 0.9], [0.3, 0.8, 0.6]])
+    tsig = np.array([[1.0, 1.1, 1.05], [1.08, 1.2, 1.12], [1.02, 1.17, 0.95]])
+    cutv = rng.choice([2.0, 2.5], n)
+    params = (np.stack([t, cutv, np.zeros(n)], 1) if kind == 10
+              else np.stack([t, rng.choice([1.0, 1.2], n), cutv], 1))
+    order = rng.permutation(n)
+    rank = np.empty(n, dtype=np.uint32)
+    rank[order] = np.arange(n, dtype=np.uint32)
+    g = System(n, ndim=3, precision="fp64")
+    g.set_boxes(L[None, :])
+    g.set_atoms(x=x, v=v, a=np.zeros((n, 3)), f=np.zeros((n, 3)), m=np.ones(n))
+    g.set_pair_table(teps, tsig)
+    g.set_interaction(kind, params, w.skin, rank=rank)
+    o = Oracle(n, 3)
+    o.set_box(L)
+    o.set_state(x=x, v=v, m=np.ones(n))
+    o.set_pair_table(teps, tsig)
+    o.set_interaction(kind, params, w.skin, order=[int(i) for i in order])
+    g.nlist_update(True)
+    o.nl_update(True)
+    assert np.array_equal(g.pairs(), o.pairs())
+    g.set_forces(True)
+    o.set_forces(True)
+    assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+    g.verlet(0.002, 50)
+    o.verlet(0.002, 50)
+    st, ref = g.get_atoms(), o.get_state()
+    for k in ("x", "v", "f"):
+        assert np.array_equal(st[k], ref[k]), k
+    assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-12)
+    g.close()

@@ -63,7 +63,8 @@ def _close(got, want, exact, what):
 def test_host_api_matches_reference(drivers, name):
     d = load(name)
     case = {k: d[k] for k in ("kind", "integ", "nsteps", "dt", "damping", "T", "skin", "L", "x", "v", "m",
-                              "params", "deck_params", "order", "ignores", "out_steps", "cg") if k in d}
+                              "params", "deck_params", "pair_eps", "pair_sig", "order", "ignores", "out_steps", "cg")
+            if k in d}
     deck = MG._deck(case)
     r = subprocess.run([str(drivers[d["ndim"]])], input=deck, capture_output=True, text=True, timeout=600,
                        env={"PARM_PRECISION": "fp64", "PATH": "/usr/bin:/bin"})
@@ -72,7 +73,8 @@ def test_host_api_matches_reference(drivers, name):
     if d["integ"] >= NLCG:
         _check_minimiser(got, d)
         return
-    exact = not (d["kind"] in (1, 9) and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
+    exact = not ((d["kind"] in (1, 9) and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
+                 or d["kind"] in (13, 14, 15))   # laws that call the device pow
     np.testing.assert_array_equal(got["pairs"], d["pairs"])
     np.testing.assert_array_equal(got["init_counts"], d["init_counts"])
     np.testing.assert_allclose(got["init"], d["init"], rtol=1e-12, atol=1e-13)
