@@ -339,9 +339,12 @@ def cases() -> list[dict]:
     teps = np.array([[1.0, 0.6, 0.3], [0.6, 1.3, -0.5], [0.3, -0.5, 0.8]])
     tsig = np.array([[1.0, 1.1, 1.05], [1.1, 1.2, 1.15], [1.05, 1.15, 0.95]])
     cutv = rng.choice([2.0, 2.5], n)
+    # (an asymmetric table: a pair takes its first atom's row, the later one in the list)
+    teps_a = np.array([[1.0, 0.7, 0.4], [0.5, 1.2, 0.9], [0.3, 0.8, 0.6]])
+    tsig_a = np.array([[1.0, 1.1, 1.05], [1.08, 1.2, 1.12], [1.02, 1.17, 0.95]])
     out.append(_case("ljcut_iepsisig216_verlet", LJCUT_IEPSISIG, VERLET, 300, 0.002, L * 1.1, x * 1.1, v,
                      np.ones(n), np.stack([t, cutv, np.zeros(n)], 1), 0.3, [1, 10, 100, 300],
-                     pair_eps=np.abs(teps), pair_sig=tsig))
+                     order=rng.permutation(n), pair_eps=teps_a, pair_sig=tsig_a))
     out.append(_case("ljattract_iepsisig216_verlet", LJATTRACT_IEPSISIG, VERLET, 300, 0.002, L * 1.1, x * 1.1,
                      v, np.ones(n), np.stack([t, cutv, np.zeros(n)], 1), 0.3, [1, 10, 100, 300],
                      pair_eps=np.abs(teps), pair_sig=tsig))
@@ -355,8 +358,10 @@ def cases() -> list[dict]:
                      x * 1.1, v, np.ones(n), np.stack([t, rep, sgv, cutv], 1), 0.3, [1, 10, 100, 300],
                      pair_eps=teps))
     nexp = rng.choice([8.0, 12.0], n)
+    teps_b = teps.copy()
+    teps_b[0, 2] = -0.2   # asymmetric, and not positive in one order only
     out.append(_case("ljish216_verlet", LJISH, VERLET, 300, 0.002, L * 1.1, x * 1.1, v, np.ones(n),
-                     np.stack([t, rep, sgv, nexp, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=teps))
+                     np.stack([t, rep, sgv, nexp, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=teps_b))
     return out
 
 
