@@ -44,7 +44,7 @@ extern "C" {
                                LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
-/* Kinds 4-15 run on FP64 handles only (a mixed-precision handle rejects
+/* Kinds 4-16 run on FP64 handles only (a mixed-precision handle rejects
  * them); kinds 4-7 and 9 take four parameters per atom (the atoms' fields). */
 #define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
                                 1679-1744): params (eps, sigma, C, l), C and l averaged */
@@ -76,6 +76,8 @@ extern "C" {
                                      (1307-1399): params (indx, repeps, sigma, sigcut) */
 #define PARM_LJISH 15             /* NListed<IEpsRepsSigExpCutAtom, LJishPair> (1051-1141):
                                      params (indx, repeps, sigma, n, sigcut) */
+#define PARM_REPULSION_IEPSISIG 16 /* NListed<IEpsISigExpAtom, RepulsionPair> (pyparm's RepulsionII,
+                                     1477-1543): params (indx, exponent, unused) */
 /* doubles per atom in parm_set_interaction's params */
 #define PARM_NPARAM(kind)                                                                             \
     ((((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) || (kind) == PARM_REPULSIONDRAG ||    \

@@ -43,10 +43,10 @@ enum PairKind {
     // indexed pair epsilons (and sigmas): the pair's values come from a table by the two atoms'
     // type indices, first atom's row (IEps*Atom::get_epsilon)
     LJCUT_IEPSISIG = 10, LJATTRACT_IEPSISIG = 11, LJATTRACT_IEPS = 12, LJATTRACTREPULSE = 13,
-    LJATTRACTFIXEDREPULSE = 14, LJISH = 15
+    LJATTRACTFIXEDREPULSE = 14, LJISH = 15, REPULSION_IEPSISIG = 16
 };
 
-inline bool indexed_kind(int kind) { return kind >= LJCUT_IEPSISIG && kind <= LJISH; }
+inline bool indexed_kind(int kind) { return kind >= LJCUT_IEPSISIG && kind <= REPULSION_IEPSISIG; }
 
 // kinds whose atoms carry four parameters
 inline bool four_params(int kind) { return (kind >= LOISOHERN && kind <= LOISLIN_MIN) || kind == REPULSIONDRAG; }
@@ -173,7 +173,13 @@ struct System {
         } else if (indexed_kind(kind)) {
             const double te = teps[A.t * ntypes + B.t];   // a1.get_epsilon(a2)
             pc.cut = 0;
-            if (kind == LJCUT_IEPSISIG) {
+            if (kind == REPULSION_IEPSISIG) {
+                // RepulsionPair(IEpsISigExpAtom, IEpsISigExpAtom) (interaction.hpp:1538-1543)
+                pc.eps = te;
+                pc.sig = tsig[A.t * ntypes + B.t];
+                pc.third = (A.p2 + B.p2) / 2.0;
+                pc.cut_energy = 0;
+            } else if (kind == LJCUT_IEPSISIG) {
                 // LennardJonesCutPair(IEpsISigCutAtom, IEpsISigCutAtom) (interaction.hpp:977-982)
                 pc.eps = te;
                 pc.sig = tsig[A.t * ntypes + B.t];
@@ -291,7 +297,7 @@ struct System {
                 e = pc.eps * (mid * mid - 1);
             }
             return e - pc.cut_energy;
-        } else if (kind == REPULSION) {
+        } else if (kind == REPULSION || kind == REPULSION_IEPSISIG) {
             // RepulsionPair::energy (interaction.hpp:1544-1550)
             if (dsq > pc.sig * pc.sig) return 0.0;
             double R = std::sqrt(dsq);
@@ -449,7 +455,7 @@ struct System {
             double rsix = rsq * rsq * rsq;
             double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
             s = fmagTimesR / dsq;
-        } else if (kind == REPULSION) {
+        } else if (kind == REPULSION || kind == REPULSION_IEPSISIG) {
             // RepulsionPair::forces (interaction.hpp:1551-1556)
             if (dsq > pc.sig * pc.sig) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
             double R = std::sqrt(dsq);
@@ -502,13 +508,14 @@ struct System {
         if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
         if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
         if (kind == EISMCLACHLAN) return params[i].p0;   // EisMclachlanAtom::max_size (1423)
-        if (kind == LJCUT_IEPSISIG || kind == LJATTRACT_IEPSISIG) {
-            // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut
+        if (kind == LJCUT_IEPSISIG || kind == LJATTRACT_IEPSISIG || kind == REPULSION_IEPSISIG) {
+            // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut;
+            // IEpsISigExpAtom::max_size (1505-1511): the largest sigma
             const double* row = &tsig[params[i].t * ntypes];
             double sg = row[0];
             for (uint32_t k = 1; k < ntypes; ++k)
                 if (sg < row[k]) sg = row[k];
-            return sg * params[i].p2;
+            return kind == REPULSION_IEPSISIG ? sg : sg * params[i].p2;
         }
         // IEpsSigCutAtom (1017), IEpsRepsSigCutAtom (1335), IEpsRepsSigExpCutAtom (1091): sigma * sigcut
         if (indexed_kind(kind)) return params[i].p1 * params[i].p2;
@@ -1059,7 +1066,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 15) return -1;
+    if (kind < 0 || kind > 16) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;
@@ -1078,7 +1085,7 @@ int orc_add_atom(void* s, uint32_t i, const double* p) {
         a.t = (uint32_t)p[0];
         if (a.t >= S->ntypes) return -1;
         const int k = S->kind;
-        if (k == LJCUT_IEPSISIG || k == LJATTRACT_IEPSISIG) a.p2 = p[1];
+        if (k == LJCUT_IEPSISIG || k == LJATTRACT_IEPSISIG || k == REPULSION_IEPSISIG) a.p2 = p[1];
         else if (k == LJATTRACT_IEPS || k == LJATTRACTREPULSE) { a.p1 = p[1]; a.p2 = p[2]; }
         else if (k == LJATTRACTFIXEDREPULSE) { a.p0 = p[1]; a.p1 = p[2]; a.p2 = p[3]; }
         else { a.p0 = p[1]; a.p1 = p[2]; a.p3 = p[3]; a.p2 = p[4]; }

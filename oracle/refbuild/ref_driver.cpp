@@ -18,7 +18,8 @@
 //       11 <IEpsISigCutAtom,LJAttractCutPair> (same), 12 <IEpsSigCutAtom,LJAttractCutPair>
 //       (p: t sigma sigcut), 13 <IEpsSigCutAtom,LJAttractRepulsePair> (same),
 //       14 <IEpsRepsSigCutAtom,LJAttractFixedRepulsePair> (p: t repeps sigma sigcut),
-//       15 <IEpsRepsSigExpCutAtom,LJishPair> (p: t repeps sigma n sigcut);
+//       15 <IEpsRepsSigExpCutAtom,LJishPair> (p: t repeps sigma n sigcut),
+//       16 <IEpsISigExpAtom,RepulsionPair> (p: t exponent unused);
 //       integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
@@ -97,6 +98,11 @@ template <>
 IEpsRepsSigCutAtom make_atom<IEpsRepsSigCutAtom>(AtomID id, int, const double* p) {
     const unsigned t = (unsigned)p[0];
     return IEpsRepsSigCutAtom(id, row_of(g_eps, t), p[1], p[2], t, p[3]);
+}
+template <>
+IEpsISigExpAtom make_atom<IEpsISigExpAtom>(AtomID id, int, const double* p) {
+    const unsigned t = (unsigned)p[0];
+    return IEpsISigExpAtom(id, row_of(g_eps, t), row_of(g_sig, t), t, p[1]);
 }
 template <>
 IEpsRepsSigExpCutAtom make_atom<IEpsRepsSigExpCutAtom>(AtomID id, int, const double* p) {
@@ -242,5 +248,6 @@ int main() {
     if (kind == 14)
         return run<IEpsRepsSigCutAtom, LJAttractFixedRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 15) return run<IEpsRepsSigExpCutAtom, LJishPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 16) return run<IEpsISigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

@@ -40,6 +40,7 @@ LJATTRACTCUT_IEPS = 12          # (indx, sigma, sigcut)
 LJATTRACTREPULSE = 13           # (indx, sigma, sigcut)
 LJATTRACTFIXEDREPULSE = 14      # (indx, repeps, sigma, sigcut)
 LJISH = 15                      # (indx, repeps, sigma, n, sigcut)
+REPULSION_IEPSISIG = 16         # (indx, exponent, unused)
 
 
 def nparam(kind: int) -> int:

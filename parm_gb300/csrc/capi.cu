@@ -32,14 +32,15 @@ thread_local std::string g_err;
 // EisMclachlanAtom 1423):
 // the atom's diameter in its neighbour list
 double atom_max_size(int kind, const double* p, const std::vector<double>& tsig, uint32_t ntypes) {
-    if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) {
-        // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut
+    if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG) {
+        // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut;
+        // IEpsISigExpAtom::max_size (1505-1511): the largest sigma
         const uint32_t t = (uint32_t)p[0];
         if (t >= ntypes || tsig.size() < (size_t)ntypes * ntypes) return 0.0;
         double sg = tsig[(size_t)t * ntypes];
         for (uint32_t k = 1; k < ntypes; ++k)
             if (sg < tsig[(size_t)t * ntypes + k]) sg = tsig[(size_t)t * ntypes + k];
-        return sg * p[1];
+        return kind == PARM_REPULSION_IEPSISIG ? sg : sg * p[1];
     }
     if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE) return p[1] * p[2];
     if (kind == PARM_LJATTRACTFIXEDREPULSE) return p[2] * p[3];
@@ -62,6 +63,7 @@ int device_kind(int kind) {
     if (kind == PARM_LJATTRACTREPULSE) return KIND_LJATTRACTREPULSE;
     if (kind == PARM_LJATTRACTFIXEDREPULSE) return KIND_LJFIXEDREPULSE;
     if (kind == PARM_LJISH) return KIND_LJISH;
+    if (kind == PARM_REPULSION_IEPSISIG) return KIND_REPULSION_IDX;
     return kind;
 }
 
@@ -1361,7 +1363,7 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > PARM_LJISH) return fail(PARM_ERR_ARG, "unknown pair kind");
+    if (kind < 0 || kind > PARM_REPULSION_IEPSISIG) return fail(PARM_ERR_ARG, "unknown pair kind");
     const bool indexed = kind >= PARM_LJCUT_IEPSISIG;
     if (indexed && S->ntypes == 0) return fail(PARM_ERR_ARG, "indexed pair kinds need parm_set_pair_table first");
     if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
@@ -1408,7 +1410,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 if (member && !(p[0] >= 0.0 && p[0] < (double)S->ntypes && p[0] == std::floor(p[0])))
                     return fail(PARM_ERR_ARG, "type index out of range");
                 ptype = member ? (uint32_t)p[0] : 0u;
-                if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) a = AtomPrm{0.0, 0.0, p[1], 0.0};
+                if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG)
+                    a = AtomPrm{0.0, 0.0, p[1], 0.0};   // sigcut, or the exponent
                 else if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE) a = AtomPrm{0.0, p[1], p[2], 0.0};
                 else if (kind == PARM_LJATTRACTFIXEDREPULSE) a = AtomPrm{p[1], p[2], p[3], 0.0};
                 else a = AtomPrm{p[1], p[2], p[4], p[3]};
@@ -1449,7 +1452,7 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                 if (!(a.p0 >= 0.0 && std::isfinite(a.p0) && std::isfinite(a.p1)))
                     return fail(PARM_ERR_ARG, "dist must be finite and >= 0, sigmai finite");
             } else if (indexed) {
-                const bool sig_ok = (kind <= PARM_LJATTRACTCUT_IEPSISIG) || a.p1 > 0.0;
+                const bool sig_ok = (kind <= PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG) || a.p1 > 0.0;
                 if (!(sig_ok && a.p0 >= 0.0 && a.p2 >= 0.0 && std::isfinite(a.p2) && (kind != PARM_LJISH || a.p3 > 0.0)))
                     return fail(PARM_ERR_ARG, "sigma and n must be > 0, repeps and sigcut >= 0");
             } else if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0))) {
@@ -1499,7 +1502,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     if (indexed) {
         // per-pair values come from the tables: no per-atom shortcuts
         uni &= ~(UNI_EPS | UNI_SIG_ONE);
-        if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG) uni |= IDX_SIG;
+        if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG)
+            uni |= IDX_SIG;
     }
     S->c.kind = device_kind(kind);
     S->c.uniform = uni;

@@ -58,7 +58,11 @@ __device__ __forceinline__ PairC combine_idx(const DevCtx& c, const AtomPrm& A, 
     p.cut = 0.0;
     p.m6 = pc3;
     p.eps = te;
-    if constexpr (KIND == KIND_LJATTRACTREPULSE) {
+    if constexpr (KIND == KIND_REPULSION_IDX) {
+        // RepulsionPair(IEpsISigExpAtom...) (interaction.hpp:1538-1543): the exponent averaged
+        p.third = (A.p2 + B.p2) / 2.0;
+        p.m6 = 0.0;
+    } else if constexpr (KIND == KIND_LJATTRACTREPULSE) {
         if (te <= 0) {
             p.third = 1;
             p.eps = fabs(te);
@@ -168,7 +172,7 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
         double fmagTimesR = 12 * p.eps / rsix * (1 / rsix - 1);
         s = fmagTimesR / dsq;
         return true;
-    } else if constexpr (KIND == KIND_REPULSION) {
+    } else if constexpr (KIND == KIND_REPULSION || KIND == KIND_REPULSION_IDX) {
         if (dsq > p.sig * p.sig) return false;
         double R = sqrt(dsq);
         double b = 1.0 - (R / p.sig);
@@ -244,7 +248,7 @@ __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32
         double mid = (1 - 1 / rsix);
         double cut_energy = p.eps * (p.m6 * p.m6 - 1);
         return p.eps * (mid * mid - 1) - cut_energy;
-    } else if constexpr (KIND == KIND_REPULSION || KIND == KIND_REPULSIONDRAG) {
+    } else if constexpr (KIND == KIND_REPULSION || KIND == KIND_REPULSIONDRAG || KIND == KIND_REPULSION_IDX) {
         // RepulsionPair::energy (1544-1550), RepulsionDragPair::energy (1622-1628)
         if (dsq > p.sig * p.sig) return 0.0;
         double R = sqrt(dsq);
@@ -541,6 +545,7 @@ static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     else if (c.kind == KIND_LJATTRACTREPULSE) force64_nd_kind<ND, KIND_LJATTRACTREPULSE>(c, s, mode);
     else if (c.kind == KIND_LJFIXEDREPULSE) force64_nd_kind<ND, KIND_LJFIXEDREPULSE>(c, s, mode);
     else if (c.kind == KIND_LJISH) force64_nd_kind<ND, KIND_LJISH>(c, s, mode);
+    else if (c.kind == KIND_REPULSION_IDX) force64_nd_kind<ND, KIND_REPULSION_IDX>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -563,6 +568,7 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     else if (c.kind == KIND_LJATTRACTREPULSE) k_eval64<ND, KIND_LJATTRACTREPULSE><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LJFIXEDREPULSE) k_eval64<ND, KIND_LJFIXEDREPULSE><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LJISH) k_eval64<ND, KIND_LJISH><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_REPULSION_IDX) k_eval64<ND, KIND_REPULSION_IDX><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

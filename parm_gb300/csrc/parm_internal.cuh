@@ -37,10 +37,11 @@ enum PairKind : int {
     KIND_LJATTRACT_IDX = 9,      // LJAttractCutPair(IEpsISigCutAtom / IEpsSigCutAtom)
     KIND_LJATTRACTREPULSE = 10,  // LJAttractRepulsePair(IEpsSigCutAtom)
     KIND_LJFIXEDREPULSE = 11,    // LJAttractFixedRepulsePair(IEpsRepsSigCutAtom)
-    KIND_LJISH = 12              // LJishPair(IEpsRepsSigExpCutAtom)
+    KIND_LJISH = 12,             // LJishPair(IEpsRepsSigExpCutAtom)
+    KIND_REPULSION_IDX = 13      // RepulsionPair(IEpsISigExpAtom)
 };
 template <int KIND>
-__host__ __device__ constexpr bool idx_kind() { return KIND >= KIND_LJCUT_IDX && KIND <= KIND_LJISH; }
+__host__ __device__ constexpr bool idx_kind() { return KIND >= KIND_LJCUT_IDX && KIND <= KIND_REPULSION_IDX; }
 template <int KIND>
 __host__ __device__ constexpr bool lois_kind() { return KIND == KIND_LOISOHERN || KIND == KIND_LOISLIN; }
 // kinds whose pair cut-off is max(sigcut_i, sigcut_j) sigma_ij, with a force

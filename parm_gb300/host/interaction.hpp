@@ -144,14 +144,55 @@ struct IEpsRepsSigExpCutAtom : public AtomID {
     flt max_size() { return sigma * sigcut; }
 };
 
+//! Indexed epsilons and sigmas with an exponent (src/interaction.hpp:1477-1511).
+struct IEpsISigExpAtom : public AtomID {
+    std::vector<flt> epsilons, sigmas;
+    flt exponent;
+    uint indx;
+    IEpsISigExpAtom() : exponent(2.5), indx(0) {}
+    IEpsISigExpAtom(AtomID a, std::vector<flt> epsilons, std::vector<flt> sigmas, uint indx, flt exponent = 2.5)
+        : AtomID(a), epsilons(epsilons), sigmas(sigmas), exponent(exponent), indx(indx) {}
+    IEpsISigExpAtom(AtomID a, IEpsISigExpAtom other)
+        : AtomID(a), epsilons(other.epsilons), sigmas(other.sigmas), exponent(other.exponent), indx(other.indx) {}
+    flt get_epsilon(IEpsISigExpAtom& other) { return epsilons.at(other.indx); }
+    flt get_sigma(IEpsISigExpAtom& other) { return sigmas.at(other.indx); }
+    flt max_size() {
+        flt sg = sigmas.at(0);
+        for (uint i = 1; i < sigmas.size(); ++i)
+            if (sg < sigmas[i]) sg = sigmas[i];
+        return sg;
+    }
+};
+
 // the table rows an indexed atom brings to its neighbour list's GPU handle
 inline void register_types(GpuLink&, const AtomID&) {}
 inline void register_types(GpuLink& l, const IEpsISigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, &a.sigmas); }
 inline void register_types(GpuLink& l, const IEpsSigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, nullptr); }
+inline void register_types(GpuLink& l, const IEpsISigExpAtom& a) { l.set_type_row(a.indx, a.epsilons, &a.sigmas); }
 inline void register_types(GpuLink& l, const IEpsRepsSigCutAtom& a) { l.set_type_row(a.indx, a.epsilons, nullptr); }
 inline void register_types(GpuLink& l, const IEpsRepsSigExpCutAtom& a) {
     l.set_type_row(a.indx, a.epsilons, nullptr);
 }
+
+//! A pair's force and energy (src/interaction.hpp:1467-1472).
+struct EnergyForce {
+    Vec f;
+    flt E;
+    EnergyForce(Vec f, flt E) : f(f), E(E) {}
+};
+
+//! A pair, its force and its stiffness term, handed to an FPairXFunct
+//! (src/interaction.hpp:822-836).
+struct ForcePairX {
+    AtomID a1, a2;
+    flt xij;
+    Vec fij;
+};
+class FPairXFunct {
+   public:
+    virtual void run(ForcePairX*) = 0;
+    virtual ~FPairXFunct() {}
+};
 
 // Pair laws.  Each pair type holds its pair's constants (combined from the
 // two atoms as the reference combines them) and its two atoms; `kind` and
@@ -224,6 +265,13 @@ struct RepulsionPair {
         p[1] = a.sigma;
         p[2] = a.exponent;
     }
+    static int kind_of(const EpsSigExpAtom&) { return PARM_REPULSION; }
+    static int kind_of(const IEpsISigExpAtom&) { return PARM_REPULSION_IEPSISIG; }
+    static void params(const IEpsISigExpAtom& a, double p[3]) {
+        p[0] = a.indx;
+        p[1] = a.exponent;
+        p[2] = 0.0;
+    }
     flt eps, sig, exponent;
     AtomID atom1, atom2;
     RepulsionPair(EpsSigExpAtom a1, EpsSigExpAtom a2)
@@ -232,6 +280,38 @@ struct RepulsionPair {
           exponent((a1.exponent + a2.exponent) / 2.0),
           atom1(a1),
           atom2(a2) {}
+    //! indexed epsilon and sigma (src/interaction.hpp:1538-1543)
+    RepulsionPair(IEpsISigExpAtom a1, IEpsISigExpAtom a2)
+        : eps(a1.get_epsilon(a2)),
+          sig(a1.get_sigma(a2)),
+          exponent((a1.exponent + a2.exponent) / 2.0),
+          atom1(a1),
+          atom2(a2) {}
+    //! the pair force and energy together (src/interaction.hpp:1557-1567)
+    EnergyForce get_energy_forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq > sig * sig) return EnergyForce(Vec::Zero(), 0);
+        const flt R = std::sqrt(dsq);
+        return EnergyForce(rij * (eps * std::pow(1.0 - (R / sig), exponent - 1) / sig / R),
+                           eps * std::pow(1.0 - (R / sig), exponent) / exponent);
+    }
+    //! the pair force and its pair stiffness term for NListedVirial's callback (1574-1589)
+    void fill(Box& box, ForcePairX& fpair) {
+        fpair.a1 = atom1;
+        fpair.a2 = atom2;
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt dsq = rij.squaredNorm();
+        if (dsq > sig * sig) {
+            fpair.fij = Vec::Zero();
+            fpair.xij = 0.0;
+            return;
+        }
+        const flt R = std::sqrt(dsq);
+        fpair.fij = rij * (eps * std::pow(1.0 - (R / sig), exponent - 1) / sig / R);
+        const flt Rs = R / sig;
+        fpair.xij = -Rs * eps * std::pow(1.0 - (R / sig), exponent - 2) * (1 - exponent * Rs);
+    }
     flt energy(Box& box) {
         const flt dsq = box.diff(atom1->x, atom2->x).squaredNorm();
         if (dsq > sig * sig) return 0.0;
@@ -772,6 +852,57 @@ class NListed : public Interaction, public GpuInteraction {
     sptr<NeighborList> neighbors;
     std::vector<A> atoms;   // indexed by AtomVec index
     std::vector<P> pairs;
+};
+
+//! Interactions that can hand every pair's force to a callback
+//! (src/interaction.hpp:838-843).
+class InteractionPairsX : public Interaction {
+   public:
+    using Interaction::set_forces;
+    virtual void set_forces(Box& box, FPairXFunct*) = 0;
+    virtual ~InteractionPairsX() {}
+};
+
+//! NListed with per-pair callbacks (pyparm's HertzianVirial,
+//! src/interaction.hpp:1948-1968, 2178-2229): the forces are the NListed's
+//! (on the GPU); set_forces(box, funct) and setForcesGetEnergy walk the pairs
+//! on the host with the pair type's fill / get_energy_forces and add the
+//! forces to the host Atom records, as the reference does.
+template <class A, class P>
+class NListedVirial : public InteractionPairsX, public GpuInteraction {
+   public:
+    NListedVirial(sptr<AtomVec> vec, sptr<NeighborList> neighbors) : vec(vec), nlisted(vec, neighbors) {}
+    using InteractionPairsX::set_forces;
+    void set_forces(Box& box) override { nlisted.set_forces(box); }
+    void set_forces(Box& box, FPairXFunct* funct) override {
+        for (P& pr : nlisted.pair_iter()) {
+            ForcePairX fp;
+            pr.fill(box, fp);
+            funct->run(&fp);
+            pr.atom1->f += fp.fij;
+            pr.atom2->f -= fp.fij;
+        }
+    }
+    flt set_forces_get_pressure(Box& box) override { return nlisted.set_forces_get_pressure(box); }
+    virtual flt setForcesGetEnergy(Box& box) {
+        flt E = 0;
+        for (P& pr : nlisted.pair_iter()) {
+            EnergyForce ef = pr.get_energy_forces(box);
+            pr.atom1->f += ef.f;
+            pr.atom2->f -= ef.f;
+            E += ef.E;
+        }
+        return E;
+    }
+    flt energy(Box& box) override { return nlisted.energy(box); }
+    flt pressure(Box& box) override { return nlisted.pressure(box); }
+    void add(A atm) { nlisted.add(atm); }
+    sptr<NeighborList> neighbor_list() { return nlisted.neighbor_list(); }
+    sptr<GpuLink> gpu() override { return nlisted.gpu(); }
+
+   private:
+    sptr<AtomVec> vec;
+    NListed<A, P> nlisted;
 };
 
 #endif

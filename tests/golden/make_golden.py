@@ -37,6 +37,7 @@ VERLET, DAMPED, SOL, NLCG, NLCGV = 0, 1, 2, 3, 4
 LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
 LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN, REPULSIONDRAG = 4, 5, 6, 7, 8, 9
 LJCUT_IEPSISIG, LJATTRACT_IEPSISIG, LJATTRACT_IEPS, LJATTRACTREPULSE, LJATTRACTFIXEDREPULSE, LJISH = range(10, 16)
+REPULSION_IEPSISIG = 16
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -362,6 +363,18 @@ def cases() -> list[dict]:
     teps_b[0, 2] = -0.2   # asymmetric, and not positive in one order only
     out.append(_case("ljish216_verlet", LJISH, VERLET, 300, 0.002, L * 1.1, x * 1.1, v, np.ones(n),
                      np.stack([t, rep, sgv, nexp, cutv], 1), 0.3, [1, 10, 100, 300], pair_eps=teps_b))
+    # 25. RepulsionPair on IEpsISigExpAtom (pyparm's RepulsionII): indexed epsilon and sigma,
+    #     per-atom exponent 2 or 2.5 (averaged), 3D soft spheres, damped
+    rng = np.random.default_rng(72)
+    n = 200
+    t = rng.integers(0, 3, n).astype(np.float64)
+    teps = np.array([[1.0, 0.8, 1.1], [0.8, 1.4, 0.9], [1.1, 0.9, 0.7]])
+    tsig = np.array([[1.0, 1.2, 1.1], [1.2, 1.4, 1.3], [1.1, 1.3, 1.2]])
+    Lr2 = (200 * np.pi * 1.2 ** 3 / 6 / 0.6) ** (1 / 3)
+    out.append(_case("repulsion_iepsisig200_damped", REPULSION_IEPSISIG, DAMPED, 300, 0.01, [Lr2] * 3,
+                     rng.uniform(0, Lr2, (n, 3)), np.zeros((n, 3)), np.ones(n),
+                     np.stack([t, rng.choice([2.0, 2.5], n), np.zeros(n)], 1), 0.2, [1, 10, 100, 300],
+                     damping=0.5, pair_eps=teps, pair_sig=tsig))
     return out
 
 

@@ -8,8 +8,11 @@
 //  * set_forces_get_stress and the virtual Interaction::stress;
 //  * an Interaction subclass of the program's own (compiles; a Collection
 //    rejects it with an exception, as its time steps run on the GPU);
-//  * a second NListed on the same NeighborList is rejected.
+//  * a second NListed on the same NeighborList is rejected;
+//  * NListedVirial (pyparm's HertzianVirial): the per-pair callback and
+//    setForcesGetEnergy on the host against the GPU forces and energy.
 // Prints "check <name> <ok>" lines and the largest relative differences.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <memory>
@@ -112,5 +115,37 @@ int main() {
     const flt E1 = col.energy();
     std::printf("verlet_energy_rel_change %.3e\n", std::fabs(E1 - E0) / std::fabs(E0));
     check("verlet_runs", std::isfinite(E1) && std::fabs(E1 - E0) <= 1e-3 * std::fabs(E0));
+
+    // NListedVirial on a list of its own: the callback sees every pair; the forces it adds
+    // and setForcesGetEnergy's energy equal the GPU's
+    sptr<NeighborList> nl2(new NeighborList(box, atoms, 0.3));
+    NListedVirial<EpsSigExpAtom, RepulsionPair> vir(atoms, nl2);
+    for (uint i = 0; i < N; i++) vir.add(EpsSigExpAtom(atoms->get_id(i), 1.0, i % 2 ? 1.0 : 1.4, 2.5));
+    nl2->update_list(true);
+    struct Count : public FPairXFunct {
+        uint n = 0;
+        flt xsum = 0;
+        void run(ForcePairX* fp) override {
+            n++;
+            xsum += fp->xij;
+        }
+    } counter;
+    for (uint i = 0; i < atoms->size(); i++) (*atoms)[i].f = Vec::Zero();
+    vir.set_forces(*box, &counter);
+    std::vector<Vec> fhost(atoms->size());
+    for (uint i = 0; i < atoms->size(); i++) fhost[i] = (*atoms)[i].f;
+    for (uint i = 0; i < atoms->size(); i++) (*atoms)[i].f = Vec::Zero();
+    vir.set_forces(*box);
+    flt fdiff = 0, fmax = 0;
+    for (uint i = 0; i < atoms->size(); i++) {
+        fdiff = std::max(fdiff, ((*atoms)[i].f - fhost[i]).norm());
+        fmax = std::max(fmax, fhost[i].norm());
+    }
+    std::printf("virial_callback_pairs %u force_rel_diff %.3e\n", counter.n, fdiff / fmax);
+    check("virial_callback_sees_every_pair", counter.n == nl2->numpairs() && std::isfinite(counter.xsum));
+    check("virial_callback_forces", fdiff <= 1e-12 * fmax);
+    for (uint i = 0; i < atoms->size(); i++) (*atoms)[i].f = Vec::Zero();
+    const flt Ev = vir.setForcesGetEnergy(*box), Eg = vir.energy(*box);
+    check("virial_energy", std::fabs(Ev - Eg) <= 1e-12 * std::fabs(Eg));
     return 0;
 }

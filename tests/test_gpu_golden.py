@@ -17,15 +17,22 @@ pytestmark = pytest.mark.gpu
 
 CASES = [n for n in names() if load(n)["integ"] < NLCG]   # the minimiser cases: test_gpu_nlcg.py
 RTOL = 1e-12
+POW_KINDS = (13, 14, 15)   # LJAttractRepulse, LJAttractFixedRepulse, LJish: pow at every pair
 
 
-def _close(got, want, exact, what):
+def step_tol(kind, step):
+    """The laws that call pow at every pair: the device's pow and the host's differ by an ulp now and
+    then, and the dynamics amplifies that (LJish: ~1e-11 after 300 steps); 1e-12 through step 100."""
+    return 1e-9 if (kind in POW_KINDS and step > 100) else RTOL
+
+
+def _close(got, want, exact, what, tol=RTOL):
     if exact:
         np.testing.assert_array_equal(got, want, err_msg=what)
     else:
         scale = max(float(np.abs(want).max()), 1e-300)
         err = float(np.abs(got - want).max()) / scale
-        assert err <= RTOL, f"{what}: relative error {err:.3e}"
+        assert err <= tol, f"{what}: relative error {err:.3e}"
 
 
 def _gpu(d):
@@ -47,7 +54,8 @@ def _gpu(d):
 @pytest.mark.parametrize("name", CASES)
 def test_gpu_fp64_matches_reference(name):
     d = load(name)
-    exact = not ((d["kind"] in (1, 9) and np.any(d["params"][:, 2] != np.rint(d["params"][:, 2])))
+    ecol = 1 if d["kind"] == 16 else 2   # the exponent's column
+    exact = not ((d["kind"] in (1, 9, 16) and np.any(d["params"][:, ecol] != np.rint(d["params"][:, ecol])))
                  or d["kind"] in (13, 14, 15))   # laws that call the device pow
     s = _gpu(d)
     s.nlist_update(True)
@@ -73,9 +81,10 @@ def test_gpu_fp64_matches_reference(name):
             s.sol(d["dt"], d["damping"], 0.0, seed=1, nsteps=k)
         done = int(step)
         st = s.get_atoms()
+        tol = step_tol(d["kind"], int(step))
         for key in ("x", "v", "a", "f"):
-            _close(st[key], d[f"{key}_steps"][i], exact, f"{key} at step {step}")
+            _close(st[key], d[f"{key}_steps"][i], exact, f"{key} at step {step}", tol)
         assert s.which()[0] == d["which_steps"][i], f"rebuilds at step {step}"
-        assert s.energy()[0] == pytest.approx(d["energy_steps"][i], rel=RTOL, abs=1e-13)
-        assert s.kinetic_energy()[0] == pytest.approx(d["ke_steps"][i], rel=RTOL, abs=1e-13)
+        assert s.energy()[0] == pytest.approx(d["energy_steps"][i], rel=tol, abs=1e-13)
+        assert s.kinetic_energy()[0] == pytest.approx(d["ke_steps"][i], rel=tol, abs=1e-13)
     s.close()
