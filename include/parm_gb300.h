@@ -44,7 +44,7 @@ extern "C" {
                                LJ attraction only, zero force inside sigma (src/interaction.hpp:154-236,
                                1020-1050); params (epsilon, sigma, sigcut); the mixed path runs it
                                on the per-atom kernels */
-/* Kinds 4-16 run on FP64 handles only (a mixed-precision handle rejects
+/* Kinds 4-17 run on FP64 handles only (a mixed-precision handle rejects
  * them); kinds 4-7 and 9 take four parameters per atom (the atoms' fields). */
 #define PARM_LOISOHERN 4     /* NListed<LoisOhernAtom, LoisOhernPair> (sticky spheres, src/interaction.hpp:
                                 1679-1744): params (eps, sigma, C, l), C and l averaged */
@@ -78,12 +78,15 @@ extern "C" {
                                      params (indx, repeps, sigma, n, sigcut) */
 #define PARM_REPULSION_IEPSISIG 16 /* NListed<IEpsISigExpAtom, RepulsionPair> (pyparm's RepulsionII,
                                      1477-1543): params (indx, exponent, unused) */
+#define PARM_LJATTRACTREPULSESIGS 17 /* NListed<EpsEpsSigSigCutAtom, LJAttractRepulseSigsPair>
+                                     (1149-1239): params (eps_r, eps_a, sig_r, sig_a, sigcut); FP64
+                                     handles only */
 /* doubles per atom in parm_set_interaction's params */
 #define PARM_NPARAM(kind)                                                                             \
     ((((kind) >= PARM_LOISOHERN && (kind) <= PARM_LOISLIN_MIN) || (kind) == PARM_REPULSIONDRAG ||    \
       (kind) == PARM_LJATTRACTFIXEDREPULSE)                                                           \
          ? 4                                                                                          \
-         : ((kind) == PARM_LJISH ? 5 : 3))
+         : (((kind) == PARM_LJISH || (kind) == PARM_LJATTRACTREPULSESIGS) ? 5 : 3))
 
 /* fields of the reference's struct Atom {Vec x, v, a, f; flt m;} (src/box.hpp:234-249) */
 #define PARM_X 1u

@@ -43,7 +43,8 @@ enum PairKind {
     // indexed pair epsilons (and sigmas): the pair's values come from a table by the two atoms'
     // type indices, first atom's row (IEps*Atom::get_epsilon)
     LJCUT_IEPSISIG = 10, LJATTRACT_IEPSISIG = 11, LJATTRACT_IEPS = 12, LJATTRACTREPULSE = 13,
-    LJATTRACTFIXEDREPULSE = 14, LJISH = 15, REPULSION_IEPSISIG = 16
+    LJATTRACTFIXEDREPULSE = 14, LJISH = 15, REPULSION_IEPSISIG = 16,
+    LJATTRACTREPULSESIGS = 17   // EpsEpsSigSigCutAtom: (eps_r, eps_a, sig_r, sig_a, sigcut)
 };
 
 inline bool indexed_kind(int kind) { return kind >= LJCUT_IEPSISIG && kind <= REPULSION_IEPSISIG; }
@@ -67,7 +68,7 @@ struct AtomParams {
     // kind-dependent: (eps, sigma, sigcut|exponent) or, for the Lois kinds,
     // (eps, sigma, C, l) / (eps, sigma, f, l); the indexed kinds: type t and
     // (repeps, sigma, sigcut, exponent)
-    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0;
     uint32_t t = 0;
 };
 
@@ -247,6 +248,16 @@ struct System {
                     pc.cut_energy = pc.eps * (mid * mid);
                 }
             }
+        } else if (kind == LJATTRACTREPULSESIGS) {
+            // LJAttractRepulseSigsPair(a1, a2) (interaction.hpp:1171-1190): eps = eps_r, fourth = eps_a,
+            // sig = sig_r, cut = sig_a, third = the cut in sigma units, cut_energy as constructed
+            pc.eps = std::sqrt(A.p0 * B.p0);
+            pc.fourth = std::sqrt(A.p1 * B.p1);
+            pc.sig = (A.p2 + B.p2) / 2.0;
+            pc.cut = (A.p3 + B.p3) / 2.0;
+            pc.third = std::max(A.p4, B.p4);
+            const double cu = pc.sig + pc.cut * (pc.third - 1);
+            pc.cut_energy = (pc.third >= 1) ? sigs_attract_energy(pc, cu) : sigs_repulse_energy(pc, cu);
         } else if (kind == REPULSIONDRAG) {
             // RepulsionDragPair(EpsSigExpDragAtom, EpsSigExpDragAtom) (interaction.hpp:1613-1621):
             // atom fields (eps, sigma, exponent, gamma)
@@ -271,6 +282,18 @@ struct System {
             pc.cut_energy = 0;
         }
         return pc;
+    }
+
+    // LJAttractRepulseSigsPair::attract_energy / repulse_energy (interaction.hpp:1192-1202)
+    static double sigs_attract_energy(const PairConst& pc, double r) {
+        double r_over_sig = (r - pc.sig + pc.cut) / pc.cut;
+        double mid = (1 - std::pow(r_over_sig, -6));
+        return pc.fourth * (mid * mid) - pc.fourth;
+    }
+    static double sigs_repulse_energy(const PairConst& pc, double r) {
+        double r_over_sig = r / pc.sig;
+        double mid = (1 - std::pow(r_over_sig, -6));
+        return pc.eps * (mid * mid) - pc.fourth;
     }
 
     // P::energy(box) for the three pair kinds
@@ -323,6 +346,13 @@ struct System {
                 return pc.eps / 2 * dR * dR - f * l;
             }
             return -f * (pc.sig + l - R);
+        } else if (kind == LJATTRACTREPULSESIGS) {
+            // LJAttractRepulseSigsPair::energy (interaction.hpp:1204-1216)
+            double dist = std::sqrt(dsq);
+            double cu = pc.sig + pc.cut * (pc.third - 1);
+            if (pc.third > 0 && dist > cu) return 0;
+            if (dist <= pc.sig) return sigs_repulse_energy(pc, dist) - pc.cut_energy;
+            return sigs_attract_energy(pc, dist) - pc.cut_energy;
         } else if (kind == LJCUT_IEPSISIG) {
             double rsq = dsq / (pc.sig * pc.sig);
             if (rsq > (pc.third * pc.third)) return 0;
@@ -397,6 +427,26 @@ struct System {
             double rsix = rsq * rsq * rsq;
             double fmagTimesR = 12 * pc.eps / rsix * (1 / rsix - 1);
             s = fmagTimesR / dsq;
+            for (int d = 0; d < nd; d++) fo[d] = rij[d] * s;
+            return true;
+        }
+        if (kind == LJATTRACTREPULSESIGS) {
+            // LJAttractRepulseSigsPair::forces (interaction.hpp:1218-1238)
+            double cu = pc.sig + pc.cut * (pc.third - 1);
+            if (pc.third > 0 && dsq > cu * cu) { for (int d = 0; d < nd; d++) fo[d] = 0; return false; }
+            if (dsq > pc.sig * pc.sig) {
+                double dist = std::sqrt(dsq);
+                double rminus = dist - pc.sig + pc.cut;
+                double r_over_sig = rminus / pc.cut;
+                double rsix = std::pow(r_over_sig, -6);
+                double fmag_over_r = 12 * rsix * (rsix - 1) / (dist * rminus);
+                s = pc.fourth * fmag_over_r;
+            } else {
+                double r_over_sigsq = dsq / (pc.sig * pc.sig);
+                double rsix = std::pow(r_over_sigsq, -3);
+                double fmagTimesR = 12 * rsix * (rsix - 1);
+                s = pc.eps * fmagTimesR / dsq;
+            }
             for (int d = 0; d < nd; d++) fo[d] = rij[d] * s;
             return true;
         }
@@ -508,6 +558,8 @@ struct System {
         if (kind == LOISOHERN || kind == LOISOHERN_MIN) return params[i].p1 * (1 + params[i].p2 + params[i].p3);
         if (kind == LOISLIN || kind == LOISLIN_MIN) return params[i].p1 * (1 + params[i].p3);
         if (kind == EISMCLACHLAN) return params[i].p0;   // EisMclachlanAtom::max_size (1423)
+        // EpsEpsSigSigCutAtom::max_size (1169): sig_r + sig_a (sigcut - 1)
+        if (kind == LJATTRACTREPULSESIGS) return params[i].p2 + params[i].p3 * (params[i].p4 - 1);
         if (kind == LJCUT_IEPSISIG || kind == LJATTRACT_IEPSISIG || kind == REPULSION_IEPSISIG) {
             // IEpsISigCutAtom::max_size (947-953): the largest sigma of the atom's row times sigcut;
             // IEpsISigExpAtom::max_size (1505-1511): the largest sigma
@@ -1066,7 +1118,7 @@ void orc_get_state(void* s, double* x, double* v, double* a, double* f, double* 
 // NListed(box, atoms, skin) (interaction.hpp:1911-1914)
 int orc_set_interaction(void* s, int kind, double skin) {
     System* S = static_cast<System*>(s);
-    if (kind < 0 || kind > 16) return -1;
+    if (kind < 0 || kind > 17) return -1;
     S->kind = kind;
     S->skin = skin;
     return 0;
@@ -1089,6 +1141,9 @@ int orc_add_atom(void* s, uint32_t i, const double* p) {
         else if (k == LJATTRACT_IEPS || k == LJATTRACTREPULSE) { a.p1 = p[1]; a.p2 = p[2]; }
         else if (k == LJATTRACTFIXEDREPULSE) { a.p0 = p[1]; a.p1 = p[2]; a.p2 = p[3]; }
         else { a.p0 = p[1]; a.p1 = p[2]; a.p3 = p[3]; a.p2 = p[4]; }
+    } else if (S->kind == LJATTRACTREPULSESIGS) {
+        AtomParams& a = S->params[i];
+        a.p0 = p[0]; a.p1 = p[1]; a.p2 = p[2]; a.p3 = p[3]; a.p4 = p[4];
     } else {
         S->params[i].p0 = p[0];
         S->params[i].p1 = p[1];

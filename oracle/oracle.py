@@ -124,7 +124,7 @@ def nparam(kind: int) -> int:
     """Doubles per atom of a pair kind's parameters (the C ABI's PARM_NPARAM)."""
     if 4 <= kind <= 7 or kind in (9, 14):
         return 4
-    if kind == 15:
+    if kind in (15, 17):
         return 5
     return 3
 

@@ -19,7 +19,8 @@
 //       (p: t sigma sigcut), 13 <IEpsSigCutAtom,LJAttractRepulsePair> (same),
 //       14 <IEpsRepsSigCutAtom,LJAttractFixedRepulsePair> (p: t repeps sigma sigcut),
 //       15 <IEpsRepsSigExpCutAtom,LJishPair> (p: t repeps sigma n sigcut),
-//       16 <IEpsISigExpAtom,RepulsionPair> (p: t exponent unused);
+//       16 <IEpsISigExpAtom,RepulsionPair> (p: t exponent unused),
+//       17 <EpsEpsSigSigCutAtom,LJAttractRepulseSigsPair> (p: eps_r eps_a sig_r sig_a sigcut);
 //       integrator: 0 Verlet, 1 Damped, 2 Sol (T = 0),
 //       3 CollectionNLCG (set up as pyparm's packmin.Minimizer does: constructor,
 //       set_max_alpha / set_max_dx / set_max_step, set_forces(true, true)),
@@ -100,6 +101,10 @@ IEpsRepsSigCutAtom make_atom<IEpsRepsSigCutAtom>(AtomID id, int, const double* p
     return IEpsRepsSigCutAtom(id, row_of(g_eps, t), p[1], p[2], t, p[3]);
 }
 template <>
+EpsEpsSigSigCutAtom make_atom<EpsEpsSigSigCutAtom>(AtomID id, int, const double* p) {
+    return EpsEpsSigSigCutAtom(id, p[0], p[1], p[2], p[3], p[4]);
+}
+template <>
 IEpsISigExpAtom make_atom<IEpsISigExpAtom>(AtomID id, int, const double* p) {
     const unsigned t = (unsigned)p[0];
     return IEpsISigExpAtom(id, row_of(g_eps, t), row_of(g_sig, t), t, p[1]);
@@ -115,7 +120,7 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
     Vec L;
     for (int d = 0; d < NDIM; d++) L[d] = rd();
     unsigned N = rdu();
-    const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9 || kind == 14) ? 4 : (kind == 15 ? 5 : 3);
+    const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9 || kind == 14) ? 4 : ((kind == 15 || kind == 17) ? 5 : 3);
     std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * np);
     for (unsigned i = 0; i < N; i++) {
         for (int d = 0; d < NDIM; d++) xs[i * NDIM + d] = rd();
@@ -123,7 +128,7 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
         ms[i] = rd();
         for (unsigned k = 0; k < np; k++) ps[np * i + k] = rd();
     }
-    if (kind >= 10) {
+    if (kind >= 10 && kind <= 16) {
         g_nt = rdu();
         g_eps.resize((size_t)g_nt * g_nt);
         g_sig.resize((size_t)g_nt * g_nt);
@@ -249,5 +254,7 @@ int main() {
         return run<IEpsRepsSigCutAtom, LJAttractFixedRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 15) return run<IEpsRepsSigExpCutAtom, LJishPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 16) return run<IEpsISigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);
+    if (kind == 17)
+        return run<EpsEpsSigSigCutAtom, LJAttractRepulseSigsPair>(kind, integ, nsteps, dt, damping, T, skin);
     return run<EpsSigAtom, LJRepulsePair>(kind, integ, nsteps, dt, damping, T, skin);
 }

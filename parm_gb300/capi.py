@@ -41,13 +41,14 @@ LJATTRACTREPULSE = 13           # (indx, sigma, sigcut)
 LJATTRACTFIXEDREPULSE = 14      # (indx, repeps, sigma, sigcut)
 LJISH = 15                      # (indx, repeps, sigma, n, sigcut)
 REPULSION_IEPSISIG = 16         # (indx, exponent, unused)
+LJATTRACTREPULSESIGS = 17       # (eps_r, eps_a, sig_r, sig_a, sigcut); FP64 handles
 
 
 def nparam(kind: int) -> int:
     """Doubles per atom in parm_set_interaction's params (PARM_NPARAM)."""
     if LOISOHERN <= kind <= LOISLIN_MIN or kind in (REPULSIONDRAG, LJATTRACTFIXEDREPULSE):
         return 4
-    return 5 if kind == LJISH else 3
+    return 5 if kind in (LJISH, LJATTRACTREPULSESIGS) else 3
 
 X, V, A, F, M = 1, 2, 4, 8, 16
 

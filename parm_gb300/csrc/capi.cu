@@ -49,6 +49,7 @@ double atom_max_size(int kind, const double* p, const std::vector<double>& tsig,
     if (kind == PARM_LOISOHERN || kind == PARM_LOISOHERN_MIN) return p[1] * (1 + p[2] + p[3]);
     if (kind == PARM_LOISLIN || kind == PARM_LOISLIN_MIN) return p[1] * (1 + p[3]);
     if (kind == PARM_EISMCLACHLAN) return p[0];
+    if (kind == PARM_LJATTRACTREPULSESIGS) return p[2] + p[3] * (p[4] - 1);   // EpsEpsSigSigCutAtom (1169)
     return p[1];
 }
 
@@ -64,6 +65,7 @@ int device_kind(int kind) {
     if (kind == PARM_LJATTRACTFIXEDREPULSE) return KIND_LJFIXEDREPULSE;
     if (kind == PARM_LJISH) return KIND_LJISH;
     if (kind == PARM_REPULSION_IEPSISIG) return KIND_REPULSION_IDX;
+    if (kind == PARM_LJATTRACTREPULSESIGS) return KIND_LJATTREPSIGS;
     return kind;
 }
 
@@ -1363,8 +1365,8 @@ int parm_get_atoms(parm_system* S, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* S, int kind, const double* params, const uint32_t* rank,
                          double skin) {
     if (!S || !params) return fail(PARM_ERR_ARG, "NULL argument");
-    if (kind < 0 || kind > PARM_REPULSION_IEPSISIG) return fail(PARM_ERR_ARG, "unknown pair kind");
-    const bool indexed = kind >= PARM_LJCUT_IEPSISIG;
+    if (kind < 0 || kind > PARM_LJATTRACTREPULSESIGS) return fail(PARM_ERR_ARG, "unknown pair kind");
+    const bool indexed = kind >= PARM_LJCUT_IEPSISIG && kind <= PARM_REPULSION_IEPSISIG;
     if (indexed && S->ntypes == 0) return fail(PARM_ERR_ARG, "indexed pair kinds need parm_set_pair_table first");
     if (kind >= PARM_LOISOHERN && S->prec == PREC_MIXED)
         return fail(PARM_ERR_ARG,
@@ -1402,7 +1404,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
         for (uint32_t i = 0; i < S->natoms[s]; i++) {
             uint32_t g = S->off[s] + i;
             const double* p = &params[np * g];
-            AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], np == 4 ? p[3] : 0.0};
+            AtomPrm a{p[0], p[1], kind == PARM_LJREPULSE ? 0.0 : p[2], np >= 4 ? p[3] : 0.0,
+                      (kind == PARM_LJATTRACTREPULSESIGS) ? p[4] : 0.0};
             uint32_t ptype = 0;
             if (indexed) {
                 // records (repeps, sigma, sigcut, p3), the type apart
@@ -1411,10 +1414,11 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
                     return fail(PARM_ERR_ARG, "type index out of range");
                 ptype = member ? (uint32_t)p[0] : 0u;
                 if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG)
-                    a = AtomPrm{0.0, 0.0, p[1], 0.0};   // sigcut, or the exponent
-                else if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE) a = AtomPrm{0.0, p[1], p[2], 0.0};
-                else if (kind == PARM_LJATTRACTFIXEDREPULSE) a = AtomPrm{p[1], p[2], p[3], 0.0};
-                else a = AtomPrm{p[1], p[2], p[4], p[3]};
+                    a = AtomPrm{0.0, 0.0, p[1], 0.0, 0.0};   // sigcut, or the exponent
+                else if (kind == PARM_LJATTRACTCUT_IEPS || kind == PARM_LJATTRACTREPULSE)
+                    a = AtomPrm{0.0, p[1], p[2], 0.0, 0.0};
+                else if (kind == PARM_LJATTRACTFIXEDREPULSE) a = AtomPrm{p[1], p[2], p[3], 0.0, 0.0};
+                else a = AtomPrm{p[1], p[2], p[4], p[3], 0.0};
                 if (kind == PARM_LJCUT_IEPSISIG) a.p3 = 1 - 1 / std::pow(a.p2, 6);      // LennardJonesCut ctor
                 if (kind == PARM_LJATTRACTREPULSE) a.p3 = 1 - std::pow(a.p2, -6);      // its cut energy term
                 if (kind == PARM_LJATTRACTFIXEDREPULSE) a.p3 = 1 - std::pow(a.p2, -6.0);
@@ -1451,6 +1455,9 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             if (kind == PARM_EISMCLACHLAN) {
                 if (!(a.p0 >= 0.0 && std::isfinite(a.p0) && std::isfinite(a.p1)))
                     return fail(PARM_ERR_ARG, "dist must be finite and >= 0, sigmai finite");
+            } else if (kind == PARM_LJATTRACTREPULSESIGS) {
+                if (!(a.p0 >= 0.0 && a.p1 >= 0.0 && a.p2 > 0.0 && a.p3 > 0.0 && a.p4 > 0.0 && std::isfinite(a.p4)))
+                    return fail(PARM_ERR_ARG, "epsilons must be >= 0, sigmas and sigcut > 0");
             } else if (indexed) {
                 const bool sig_ok = (kind <= PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG) || a.p1 > 0.0;
                 if (!(sig_ok && a.p0 >= 0.0 && a.p2 >= 0.0 && std::isfinite(a.p2) && (kind != PARM_LJISH || a.p3 > 0.0)))
@@ -1458,7 +1465,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
             } else if (!(a.p0 >= 0.0) || !(a.p1 > 0.0 || (explicit_d && a.p1 == 0.0 && a.p0 == 0.0))) {
                 return fail(PARM_ERR_ARG, "sigma must be > 0, epsilon >= 0");
             }
-            if (np == 4 && !(std::isfinite(a.p2) && std::isfinite(a.p3) && a.p2 >= 0.0 && a.p3 >= 0.0))
+            if (np == 4 && !indexed &&
+                !(std::isfinite(a.p2) && std::isfinite(a.p3) && a.p2 >= 0.0 && a.p3 >= 0.0))
                 return fail(PARM_ERR_ARG, "the third and fourth parameters must be finite and >= 0");
             if (first) {
                 e0 = a.p0;
@@ -1499,8 +1507,8 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     CUDA_TRY(cudaMemcpy(S->c.rank, rank_k.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.nm_rank, nmr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     if (kind == PARM_LOISOHERN_MIN || kind == PARM_LOISLIN_MIN) uni |= COMB_MIN;
-    if (indexed) {
-        // per-pair values come from the tables: no per-atom shortcuts
+    if (indexed || kind == PARM_LJATTRACTREPULSESIGS) {
+        // per-pair values from the tables, or a fifth parameter: no per-atom shortcuts
         uni &= ~(UNI_EPS | UNI_SIG_ONE);
         if (kind == PARM_LJCUT_IEPSISIG || kind == PARM_LJATTRACTCUT_IEPSISIG || kind == PARM_REPULSION_IEPSISIG)
             uni |= IDX_SIG;

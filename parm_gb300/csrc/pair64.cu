@@ -12,6 +12,7 @@
 //   LoisLinPair, LoisLinPairMin             1764-1836
 //   EisMclachlanPair                        1415-1452
 //   RepulsionDragPair                       1598-1640
+//   LJAttractRepulseSigsPair                1149-1239
 //   indexed epsilons: LennardJonesCutPair / LJAttractCutPair on IEps*Atoms
 //   977-982, 1028-1037; LJAttractRepulsePair 1251-1298; LJishPair 1095-1141;
 //   LJAttractFixedRepulsePair 1343-1399
@@ -36,7 +37,9 @@ struct PairC {
     double eps, sig, third, m6;   // the Lois kinds: third = C (or f), m6 = l; LJish: m6 = n
     double cut;                   // the Lois kinds: sigcut; LJAttractRepulse, LJAttractFixedRepulse,
                                   // LJish: the cut energy
-    double rep;                   // LJAttractFixedRepulse, LJish: the repulsive epsilon
+    double rep;                   // LJAttractFixedRepulse, LJish: the repulsive epsilon;
+                                  // LJAttractRepulseSigs: the attractive one (eps_r in eps,
+                                  // sig_a in m6)
 };
 
 // Pair constants of the indexed kinds, A the pair's first atom (the later one
@@ -90,6 +93,18 @@ __device__ __forceinline__ PairC combine_idx(const DevCtx& c, const AtomPrm& A, 
     return p;
 }
 
+// LJAttractRepulseSigsPair::attract_energy / repulse_energy (interaction.hpp:1192-1202)
+__device__ __forceinline__ double sigs_attract(const PairC& p, double r) {
+    double r_over_sig = (r - p.sig + p.m6) / p.m6;
+    double mid = (1 - pow(r_over_sig, -6.0));
+    return p.rep * (mid * mid) - p.rep;
+}
+__device__ __forceinline__ double sigs_repulse(const PairC& p, double r) {
+    double r_over_sig = r / p.sig;
+    double mid = (1 - pow(r_over_sig, -6.0));
+    return p.eps * (mid * mid) - p.rep;
+}
+
 template <int KIND>
 __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uint32_t uni) {
     PairC p;
@@ -121,6 +136,18 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
         // sigcut: sig * (1 + C + l) (LoisOhern), sig + l (LoisLin)
         p.cut = (KIND == KIND_LOISOHERN) ? p.sig * (1 + p.third + p.m6) : p.sig + p.m6;
         return p;
+    } else if constexpr (KIND == KIND_LJATTREPSIGS) {
+        // LJAttractRepulseSigsPair(a1, a2) (interaction.hpp:1171-1190), atoms (eps_r, eps_a,
+        // sig_r, sig_a, sigcut): eps = eps_r, rep = eps_a, sig = sig_r, m6 = sig_a, third =
+        // sigcut (max), cut = the cut energy
+        p.eps = sqrt(A.p0 * B.p0);
+        p.rep = sqrt(A.p1 * B.p1);
+        p.sig = (A.p2 + B.p2) / 2.0;
+        p.m6 = (A.p3 + B.p3) / 2.0;
+        p.third = B.p4 > A.p4 ? B.p4 : A.p4;
+        const double cu = p.sig + p.m6 * (p.third - 1);
+        p.cut = (p.third >= 1) ? sigs_attract(p, cu) : sigs_repulse(p, cu);
+        return p;
     } else if constexpr (KIND == KIND_EISMCLACHLAN) {
         // EisMclachlanPair(a1, a2) (interaction.hpp:1425-1438), atoms (dist, sigmai) =
         // (p0, p1): E = c0/R + c1 + c2 R with c0, c1, c2 in eps, sig, third; cut-off d1 + d2
@@ -141,7 +168,25 @@ __device__ __forceinline__ PairC combine(const AtomPrm& A, const AtomPrm& B, uin
 // pair force scale s (F = r * s); returns false beyond the cut-off
 template <int KIND>
 __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t uni, double& s) {
-    if constexpr (KIND == KIND_LJATTRACTREPULSE) {
+    if constexpr (KIND == KIND_LJATTREPSIGS) {
+        // LJAttractRepulseSigsPair::forces (interaction.hpp:1218-1238)
+        double cu = p.sig + p.m6 * (p.third - 1);
+        if (p.third > 0 && dsq > cu * cu) return false;
+        if (dsq > p.sig * p.sig) {
+            double dist = sqrt(dsq);
+            double rminus = dist - p.sig + p.m6;
+            double r_over_sig = rminus / p.m6;
+            double rsix = pow(r_over_sig, -6.0);
+            double fmag_over_r = 12 * rsix * (rsix - 1) / (dist * rminus);
+            s = p.rep * fmag_over_r;
+        } else {
+            double r_over_sigsq = dsq / (p.sig * p.sig);
+            double rsix = pow(r_over_sigsq, -3.0);
+            double fmagTimesR = 12 * rsix * (rsix - 1);
+            s = p.eps * fmagTimesR / dsq;
+        }
+        return true;
+    } else if constexpr (KIND == KIND_LJATTRACTREPULSE) {
         // LJAttractRepulsePair::forces (interaction.hpp:1287-1297)
         if (p.eps == 0) return false;
         double rsq = dsq / (p.sig * p.sig);
@@ -232,7 +277,14 @@ __device__ __forceinline__ bool force_scale(const PairC& p, double dsq, uint32_t
 
 template <int KIND>
 __device__ __forceinline__ double pair_energy(const PairC& p, double dsq, uint32_t uni) {
-    if constexpr (KIND == KIND_LJATTRACTREPULSE || KIND == KIND_LJFIXEDREPULSE || KIND == KIND_LJISH) {
+    if constexpr (KIND == KIND_LJATTREPSIGS) {
+        // LJAttractRepulseSigsPair::energy (interaction.hpp:1204-1216)
+        double dist = sqrt(dsq);
+        double cu = p.sig + p.m6 * (p.third - 1);
+        if (p.third > 0 && dist > cu) return 0.0;
+        if (dist <= p.sig) return sigs_repulse(p, dist) - p.cut;
+        return sigs_attract(p, dist) - p.cut;
+    } else if constexpr (KIND == KIND_LJATTRACTREPULSE || KIND == KIND_LJFIXEDREPULSE || KIND == KIND_LJISH) {
         // LJAttractRepulsePair::energy (1269-1286), LJAttractFixedRepulsePair::energy (1366-1389),
         // LJishPair::energy (1115-1129)
         double rsq = dsq / (p.sig * p.sig);
@@ -332,7 +384,7 @@ __device__ __forceinline__ bool drag_force(const PairC& p, const double* r, doub
 // (Q = (sqrt(eps), sigma, third, fourth) in FP32)
 template <int KIND>
 __device__ __forceinline__ bool beyond32(float d2, const float4& Qi, const float4& Qj, uint32_t uni) {
-    if constexpr (idx_kind<KIND>()) return false;   // the table decides sigma: every pair takes the exact test
+    if constexpr (idx_kind<KIND>() || KIND == KIND_LJATTREPSIGS) return false;   // every pair takes the exact test
     float sg = (uni & UNI_SIG) ? Qi.y : 0.5f * (Qi.y + Qj.y);
     float rc;
     if constexpr (cut_kind<KIND>()) {
@@ -546,6 +598,7 @@ static void force64_nd(const DevCtx& c, cudaStream_t s, int mode) {
     else if (c.kind == KIND_LJFIXEDREPULSE) force64_nd_kind<ND, KIND_LJFIXEDREPULSE>(c, s, mode);
     else if (c.kind == KIND_LJISH) force64_nd_kind<ND, KIND_LJISH>(c, s, mode);
     else if (c.kind == KIND_REPULSION_IDX) force64_nd_kind<ND, KIND_REPULSION_IDX>(c, s, mode);
+    else if (c.kind == KIND_LJATTREPSIGS) force64_nd_kind<ND, KIND_LJATTREPSIGS>(c, s, mode);
     else if (c.kind == KIND_REPULSION) force64_nd_kind<ND, KIND_REPULSION>(c, s, mode);
     else force64_nd_kind<ND, KIND_LJREPULSE>(c, s, mode);
 }
@@ -569,6 +622,7 @@ static void eval64_nd(const DevCtx& c, cudaStream_t s, int what) {
     else if (c.kind == KIND_LJFIXEDREPULSE) k_eval64<ND, KIND_LJFIXEDREPULSE><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_LJISH) k_eval64<ND, KIND_LJISH><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION_IDX) k_eval64<ND, KIND_REPULSION_IDX><<<g, BLOCK, 0, s>>>(c, what);
+    else if (c.kind == KIND_LJATTREPSIGS) k_eval64<ND, KIND_LJATTREPSIGS><<<g, BLOCK, 0, s>>>(c, what);
     else if (c.kind == KIND_REPULSION) k_eval64<ND, KIND_REPULSION><<<g, BLOCK, 0, s>>>(c, what);
     else k_eval64<ND, KIND_LJREPULSE><<<g, BLOCK, 0, s>>>(c, what);
 }

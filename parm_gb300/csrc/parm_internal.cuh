@@ -38,7 +38,9 @@ enum PairKind : int {
     KIND_LJATTRACTREPULSE = 10,  // LJAttractRepulsePair(IEpsSigCutAtom)
     KIND_LJFIXEDREPULSE = 11,    // LJAttractFixedRepulsePair(IEpsRepsSigCutAtom)
     KIND_LJISH = 12,             // LJishPair(IEpsRepsSigExpCutAtom)
-    KIND_REPULSION_IDX = 13      // RepulsionPair(IEpsISigExpAtom)
+    KIND_REPULSION_IDX = 13,     // RepulsionPair(IEpsISigExpAtom)
+    // (eps_r, eps_a, sig_r, sig_a, sigcut) atoms; FP64 path only
+    KIND_LJATTREPSIGS = 14       // LJAttractRepulseSigsPair(EpsEpsSigSigCutAtom)
 };
 template <int KIND>
 __host__ __device__ constexpr bool idx_kind() { return KIND >= KIND_LJCUT_IDX && KIND <= KIND_REPULSION_IDX; }
@@ -90,6 +92,7 @@ struct SysConst {
 //   LJREPULSE: p0 = epsilon, p1 = sigma
 struct AtomPrm {
     double p0, p1, p2, p3;
+    double p4;   // the fifth parameter (LJAttractRepulseSigs' sigcut), else 0
 };
 
 // flags that let the FP64 kernel skip combinations that are exact identities

@@ -592,6 +592,72 @@ struct RepulsionDragPair {
     }
 };
 
+//! Separate repulsive and attractive epsilons and lengths
+//! (src/interaction.hpp:1149-1169).
+struct EpsEpsSigSigCutAtom : public AtomID {
+    flt eps_r, eps_a, sig_r, sig_a, sigcut;
+    EpsEpsSigSigCutAtom() : eps_r(0), eps_a(0), sig_r(0), sig_a(0), sigcut(0) {}
+    EpsEpsSigSigCutAtom(AtomID a, flt eps_r, flt eps_a, flt sigma_r, flt sigma_a, flt cut)
+        : AtomID(a), eps_r(eps_r), eps_a(eps_a), sig_r(sigma_r), sig_a(sigma_a), sigcut(cut) {}
+    EpsEpsSigSigCutAtom(AtomID a, EpsEpsSigSigCutAtom other)
+        : AtomID(a), eps_r(other.eps_r), eps_a(other.eps_a), sig_r(other.sig_r), sig_a(other.sig_a),
+          sigcut(other.sigcut) {}
+    flt max_size() { return sig_r + sig_a * (sigcut - 1); }
+};
+
+//! LJ repulsion eps_r (1 - (sig_r/r)^6)^2 inside sig_r and an LJ attraction
+//! of depth eps_a and width sig_a beyond it, cut at sig_r + sig_a (sigcut - 1)
+//! (src/interaction.hpp:1171-1239).
+struct LJAttractRepulseSigsPair {
+    static const int kind = PARM_LJATTRACTREPULSESIGS;
+    static void params(const EpsEpsSigSigCutAtom& a, double p[5]) {
+        p[0] = a.eps_r;
+        p[1] = a.eps_a;
+        p[2] = a.sig_r;
+        p[3] = a.sig_a;
+        p[4] = a.sigcut;
+    }
+    flt eps_r, eps_a, sig_r, sig_a, cut_distance, cut_energy;
+    AtomID atom1, atom2;
+    LJAttractRepulseSigsPair(EpsEpsSigSigCutAtom a1, EpsEpsSigSigCutAtom a2)
+        : eps_r(std::sqrt(a1.eps_r * a2.eps_r)), eps_a(std::sqrt(a1.eps_a * a2.eps_a)),
+          sig_r((a1.sig_r + a2.sig_r) / 2.0), sig_a((a1.sig_a + a2.sig_a) / 2.0),
+          cut_distance(std::max(a1.sigcut, a2.sigcut)), cut_energy(0), atom1(a1), atom2(a2) {
+        if (cut_distance <= 0) return;
+        const flt cu = sig_r + sig_a * (cut_distance - 1);
+        cut_energy = (cut_distance >= 1) ? attract_energy(cu) : repulse_energy(cu);
+    }
+    flt attract_energy(flt r) {
+        const flt mid = (1 - std::pow((r - sig_r + sig_a) / sig_a, -6));
+        return eps_a * (mid * mid) - eps_a;
+    }
+    flt repulse_energy(flt r) {
+        const flt mid = (1 - std::pow(r / sig_r, -6));
+        return eps_r * (mid * mid) - eps_a;
+    }
+    flt energy(Box& box) {
+        const flt dist = box.diff(atom1->x, atom2->x).norm();
+        const flt cu = sig_r + sig_a * (cut_distance - 1);
+        if (cut_distance > 0 && dist > cu) return 0;
+        if (dist <= sig_r) return repulse_energy(dist) - cut_energy;
+        return attract_energy(dist) - cut_energy;
+    }
+    Vec forces(Box& box) {
+        const Vec rij = box.diff(atom1->x, atom2->x);
+        const flt rsq = rij.squaredNorm();
+        const flt cu = sig_r + sig_a * (cut_distance - 1);
+        if (cut_distance > 0 && rsq > cu * cu) return Vec::Zero();
+        if (rsq > sig_r * sig_r) {
+            const flt dist = std::sqrt(rsq);
+            const flt rminus = dist - sig_r + sig_a;
+            const flt rsix = std::pow(rminus / sig_a, -6);
+            return rij * (eps_a * (12 * rsix * (rsix - 1) / (dist * rminus)));
+        }
+        const flt rsix = std::pow(rsq / (sig_r * sig_r), -3);
+        return rij * (eps_r * (12 * rsix * (rsix - 1)) / rsq);
+    }
+};
+
 //! Implicit-solvation atom (src/interaction.hpp:1415-1423): dist = the
 //! atom's radius plus the water radius, sigmai its solvation parameter.
 struct EisMclachlanAtom : public AtomID {

@@ -38,6 +38,7 @@ LJCUT, REPULSION, LJREPULSE, LJATTRACT = 0, 1, 2, 3
 LOISOHERN, LOISOHERN_MIN, LOISLIN, LOISLIN_MIN, EISMCLACHLAN, REPULSIONDRAG = 4, 5, 6, 7, 8, 9
 LJCUT_IEPSISIG, LJATTRACT_IEPSISIG, LJATTRACT_IEPS, LJATTRACTREPULSE, LJATTRACTFIXEDREPULSE, LJISH = range(10, 16)
 REPULSION_IEPSISIG = 16
+LJATTRACTREPULSESIGS = 17
 SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 
@@ -375,6 +376,15 @@ def cases() -> list[dict]:
                      rng.uniform(0, Lr2, (n, 3)), np.zeros((n, 3)), np.ones(n),
                      np.stack([t, rng.choice([2.0, 2.5], n), np.zeros(n)], 1), 0.2, [1, 10, 100, 300],
                      damping=0.5, pair_eps=teps, pair_sig=tsig))
+    # 26. LJAttractRepulseSigsPair (separate repulsive and attractive epsilons and lengths),
+    #     per-atom values, cut-offs in both of the constructor's branches (sigcut < 1, >= 1)
+    rng = np.random.default_rng(73)
+    L, x, v = lj_lattice_deck((6, 6, 6), 73)
+    n = len(x)
+    out.append(_case("ljattractrepulsesigs216_verlet", LJATTRACTREPULSESIGS, VERLET, 300, 0.002, L * 1.1, x * 1.1,
+                     v, np.ones(n), np.stack([rng.choice([1.0, 1.5], n), rng.choice([0.5, 0.8], n),
+                                              rng.choice([1.0, 1.1], n), rng.choice([0.9, 1.2], n),
+                                              rng.choice([0.95, 2.0, 2.5], n)], 1), 0.3, [1, 10, 100, 300]))
     return out
 
 

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = [n for n in names() if load(n)["integ"] < NLCG]   # the minimiser cases: test_gpu_nlcg.py
 RTOL = 1e-12
-POW_KINDS = (13, 14, 15)   # LJAttractRepulse, LJAttractFixedRepulse, LJish: pow at every pair
+POW_KINDS = (13, 14, 15, 17)   # LJAttractRepulse, LJAttractFixedRepulse, LJish, LJAttractRepulseSigs
 
 
 def step_tol(kind, step):
@@ -56,7 +56,7 @@ def test_gpu_fp64_matches_reference(name):
     d = load(name)
     ecol = 1 if d["kind"] == 16 else 2   # the exponent's column
     exact = not ((d["kind"] in (1, 9, 16) and np.any(d["params"][:, ecol] != np.rint(d["params"][:, ecol])))
-                 or d["kind"] in (13, 14, 15))   # laws that call the device pow
+                 or d["kind"] in POW_KINDS)   # laws that call the device pow
     s = _gpu(d)
     s.nlist_update(True)
     np.testing.assert_array_equal(s.pairs(), d["pairs"])
