@@ -149,6 +149,15 @@ int parm_get_atoms(parm_system* s, double* atoms, uint64_t stride, uint32_t fiel
 int parm_set_interaction(parm_system* s, int kind, const double* params, const uint32_t* rank,
                          double skin);
 
+/* LeesEdwardsBox (src/box.hpp:165-196, box.cpp:72-135): gamma (nsys values)
+ * turns every system's box into a sheared one whose y image shifts x by
+ * gamma * Lx (LeesEdwardsBox::diff); NULL returns to OriginBoxes.  FP64
+ * handles only; the neighbour lists of a sheared handle are built by an
+ * all-pairs test, as the reference's own list build is.  Shearing the atoms
+ * (LeesEdwardsBox::shear(dgamma, atoms): x += y dgamma) is the caller's:
+ * move them with parm_set_atoms and pass the new gamma here. */
+int parm_set_lees_edwards(parm_system* s, const double* gamma);
+
 /* Tables of the indexed kinds (PARM_LJCUT_IEPSISIG ..): eps[a * ntypes + b]
  * is epsilons[b] of the atoms of type a (IEps*Atom::epsilons), sig likewise
  * (IEpsISigCutAtom::sigmas; NULL when no kind in use reads it).  Set before

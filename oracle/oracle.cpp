@@ -82,6 +82,8 @@ struct System {
     int nd;
     uint32_t n;
     double L[3] = {1, 1, 1};
+    bool lees = false;   // LeesEdwardsBox (box.hpp:165-196) with shear gamma
+    double gamma = 0;
     std::vector<double> x, v, a, f, m;  // n*nd each (AoS of Vec)
 
     // NListed<A,P> + NeighborList state (interaction.hpp:1876-1945, trackers.hpp:157-214)
@@ -104,6 +106,20 @@ struct System {
 
     // OriginBox::diff (box.hpp:103) with vec_mod (box.hpp:68-78)
     inline void diff(const double* r1, const double* r2, double* out) const {
+        if (lees) {
+            // LeesEdwardsBox::diff (box.cpp:72-91): the y image shifts x by im * gamma * Lx
+            const double Ly = L[1];
+            double dy = r1[1] - r2[1];
+            const int im = (int)std::round(dy / Ly);
+            dy = dy - (im * Ly);
+            const double Lx = L[0];
+            double dx = r1[0] - r2[0];
+            dx = dx - std::round((dx / Lx) - im * gamma) * Lx - im * gamma * Lx;
+            out[0] = dx;
+            out[1] = dy;
+            if (nd == 3) out[2] = std::remainder(r1[2] - r2[2], L[2]);
+            return;
+        }
         for (int d = 0; d < nd; d++) out[d] = std::remainder(r1[d] - r2[d], L[d]);
     }
 
@@ -1091,6 +1107,13 @@ void orc_destroy(void* s) { delete static_cast<System*>(s); }
 void orc_set_box(void* s, const double* L) {
     System* S = static_cast<System*>(s);
     for (int d = 0; d < S->nd; d++) S->L[d] = L[d];
+}
+
+// a LeesEdwardsBox of shear gamma (lees != 0) or the OriginBox
+void orc_set_lees(void* s, int lees, double gamma) {
+    System* S = static_cast<System*>(s);
+    S->lees = lees != 0;
+    S->gamma = gamma;
 }
 
 // arrays are (n, ndim) row-major (an AtomVec's x/v/a/f fields), m is (n,)

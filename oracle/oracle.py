@@ -34,6 +34,7 @@ def lib() -> C.CDLL:
             "orc_add_atom": (C.c_int, [C.c_void_p, C.c_uint32, _dp]),
             "orc_ignore": (None, [C.c_void_p, C.c_uint32, C.c_uint32]),
             "orc_add_member": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double]),
+            "orc_set_lees": (None, [C.c_void_p, C.c_int, C.c_double]),
             "orc_set_pair_table": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_double),
                                              C.POINTER(C.c_double)]),
             "orc_nl_update": (C.c_int, [C.c_void_p, C.c_int]),
@@ -164,6 +165,10 @@ class Oracle:
         for i in order:
             p = np.ascontiguousarray(params[i])
             assert self.L_.orc_add_atom(self.h, int(i), _d(p)) == 0
+
+    def set_lees_edwards(self, gamma):
+        """A LeesEdwardsBox of shear gamma (None: the OriginBox)."""
+        self.L_.orc_set_lees(self.h, 0 if gamma is None else 1, 0.0 if gamma is None else float(gamma))
 
     def set_pair_table(self, eps, sig=None):
         """Pair tables of the indexed kinds (10-15): eps[a, b] = first atom's epsilons[b] for a

@@ -3,7 +3,7 @@
 // parity tests compare, with 17 significant digits.  Test infrastructure.
 //
 // Input (whitespace separated): kind integrator nsteps dt damping T skin
-//   L[NDIM]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2 (and p3 for kinds 4-7)
+//   L[NDIM] [gamma: kinds 100 + k, a LeesEdwardsBox of shear gamma]  N  then per atom x[NDIM] v[NDIM] m p0 p1 p2 (and p3 for kinds 4-7)
 //   norder order[norder]   nign (a b)[nign]   nout out_steps[nout]
 //   integrators 3 and 4 add one line: dt P0 kappa kmax secmax seceps alphamax afrac
 //   dxmax stepmax maxdV
@@ -47,6 +47,9 @@ static unsigned rdu() { return (unsigned)rd(); }
 static void pvec(const Vec& v) {
     for (int d = 0; d < NDIM; d++) std::printf(" %.17g", v[d]);
 }
+
+// a LeesEdwardsBox instead of the OriginBox (kinds 100 + k)
+static bool g_lees = false;
 
 // the pair tables of the indexed kinds
 static unsigned g_nt = 0;
@@ -119,6 +122,8 @@ template <class A, class P>
 int run(int kind, int integ, int nsteps, double dt, double damping, double T, double skin) {
     Vec L;
     for (int d = 0; d < NDIM; d++) L[d] = rd();
+    const bool lees = g_lees;
+    const double gamma = lees ? rd() : 0.0;
     unsigned N = rdu();
     const unsigned np = ((kind >= 4 && kind <= 7) || kind == 9 || kind == 14) ? 4 : ((kind == 15 || kind == 17) ? 5 : 3);
     std::vector<double> xs(N * NDIM), vs(N * NDIM), ms(N), ps(N * np);
@@ -145,7 +150,7 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
     if (integ >= 3)
         for (double& q : cg) q = rd();
 
-    boost::shared_ptr<OriginBox> obox(new OriginBox(L));
+    boost::shared_ptr<OriginBox> obox(lees ? new LeesEdwardsBox(L, gamma) : new OriginBox(L));
     boost::shared_ptr<AtomVec> atoms(new AtomVec(ms));
     for (unsigned i = 0; i < N; i++) {
         for (int d = 0; d < NDIM; d++) {
@@ -236,6 +241,10 @@ int run(int kind, int integ, int nsteps, double dt, double damping, double T, do
 
 int main() {
     int kind = (int)rd(), integ = (int)rd(), nsteps = (int)rd();
+    if (kind >= 100) {
+        g_lees = true;
+        kind -= 100;
+    }
     double dt = rd(), damping = rd(), T = rd(), skin = rd();
     if (kind == 0) return run<EpsSigCutAtom, LennardJonesCutPair>(kind, integ, nsteps, dt, damping, T, skin);
     if (kind == 1) return run<EpsSigExpAtom, RepulsionPair>(kind, integ, nsteps, dt, damping, T, skin);

@@ -80,6 +80,7 @@ SIGNATURES = {
     "parm_get_atoms": (C.c_int, [_h, _dp, C.c_uint64, C.c_uint32]),
     "parm_set_interaction": (C.c_int, [_h, C.c_int, _dp, _u32p, C.c_double]),
     "parm_set_pair_table": (C.c_int, [_h, C.c_uint32, _dp, _dp]),
+    "parm_set_lees_edwards": (C.c_int, [_h, _dp]),
     "parm_nlist_ignore": (C.c_int, [_h, C.c_uint32, C.c_uint32]),
     "parm_set_list_diameters": (C.c_int, [_h, _dp]),
     "parm_nlist_update": (C.c_int, [_h, C.c_int, _u8p]),

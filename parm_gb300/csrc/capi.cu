@@ -1528,6 +1528,26 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     return S->request_rebuild_all();  // ignorechanged = true
 }
 
+int parm_set_lees_edwards(parm_system* S, const double* gamma) {
+    if (!S) return fail(PARM_ERR_ARG, "NULL handle");
+    if (gamma && S->prec != PREC_FP64) return fail(PARM_ERR_ARG, "Lees-Edwards boxes run on FP64 handles only");
+    if (gamma && S->nd < 2) return fail(PARM_ERR_ARG, "Lees-Edwards boxes need two or three dimensions");
+    if (gamma)
+        for (uint32_t s = 0; s < S->nsys; s++)
+            if (!std::isfinite(gamma[s])) return fail(PARM_ERR_ARG, "non-finite shear");
+    TRY(S->flush());
+    CUDA_TRY(cudaStreamSynchronize(S->st));
+    S->c.any_lees = gamma ? 1u : 0u;
+    for (uint32_t s = 0; s < S->nsys; s++) {
+        S->sys[s].lees = gamma ? 1 : 0;
+        S->sys[s].gamma = gamma ? gamma[s] : 0.0;
+    }
+    CUDA_TRY(cudaMemcpy(const_cast<SysConst*>(S->c.sys), S->sys.data(), sizeof(SysConst) * S->nsys,
+                        cudaMemcpyHostToDevice));
+    S->clear_graphs();
+    return S->kind >= 0 ? S->request_rebuild_all() : PARM_OK;
+}
+
 int parm_set_pair_table(parm_system* S, uint32_t ntypes, const double* eps, const double* sig) {
     if (!S || !eps) return fail(PARM_ERR_ARG, "NULL argument");
     if (ntypes == 0 || ntypes > 4096) return fail(PARM_ERR_ARG, "ntypes must be 1 .. 4096");

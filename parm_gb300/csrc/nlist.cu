@@ -544,6 +544,53 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(DevCtx c) {
     }
 }
 
+// All-pairs list build of the handles with a LeesEdwardsBox (FP64 path): the
+// sheared images do not follow the cell stencil, so every member atom tests
+// every member of its system with the reference's own test (trackers.cpp:
+// 59-69: diff(x_i, x_j).norm() < (d_i + d_j)/2 + skin), as the reference's
+// O(N^2) list build does; k_sort_lists then orders each list by rank.
+template <int ND>
+__global__ void k_build_lees(DevCtx c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const uint32_t s = c.atom_sys[i];
+    if (!c.flag[s]) return;
+    if (c.rank[i] == NOT_MEMBER) {
+        c.nnb[i] = 0u;
+        return;
+    }
+    const SysConst& S = c.sys[s];
+    typename DVec<ND>::T xv = ldx<ND>(c.x, i);
+    const double* xi = reinterpret_cast<const double*>(&xv);
+    const double di = c.diam[i];
+    const uint32_t maxnb = c.maxnb;
+    uint32_t cnt = 0;
+    for (uint32_t j = S.atom_off; j < S.atom_off + S.natoms; j++) {
+        if (j == i || c.rank[j] == NOT_MEMBER) continue;
+        typename DVec<ND>::T yv = ldx<ND>(c.x, j);
+        const double* xj = reinterpret_cast<const double*>(&yv);
+        double r[3] = {0.0, 0.0, 0.0};
+        if (S.lees) {
+            lees_diff<ND>(S, xi, xj, r);
+        } else {
+#pragma unroll
+            for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+        }
+        double sq = r[0] * r[0] + r[1] * r[1];
+        if constexpr (ND == 3) sq = sq + r[2] * r[2];
+        const double diam = (di + c.diam[j]) / 2;
+        if (!(sqrt(sq) < (diam + S.skin))) continue;
+        if (c.excl_off && is_excluded(c, c.orig[i], c.orig[j])) continue;
+        if (cnt < maxnb) c.nbr[(size_t)i * maxnb + cnt] = j;
+        cnt++;
+    }
+    if (cnt > maxnb) {
+        atomicOr(c.status, ST_NBR_OVERFLOW);
+        cnt = maxnb;
+    }
+    c.nnb[i] = cnt;
+}
+
 // ---------------------------------------------------------------------------
 // Shared-memory tiles for the mixed-precision pair kernel (built after the
 // lists).  A tile is TILE_ATOMS consecutive atoms of one system.  Its frame
@@ -815,6 +862,19 @@ void launch_rebuild(const DevCtx& c, cudaStream_t s) {
             k_copyback<2><<<ga, BLOCK, 0, s>>>(c);
         }
         launch_build_stg(c, s);
+        return;
+    }
+    if (c.any_lees) {   // FP64 handles only
+        if (c.nd == 3) {
+            k_gather<3><<<ga, BLOCK, 0, s>>>(c);
+            k_copyback<3><<<ga, BLOCK, 0, s>>>(c);
+            k_build_lees<3><<<ga, BLOCK, 0, s>>>(c);
+        } else {
+            k_gather<2><<<ga, BLOCK, 0, s>>>(c);
+            k_copyback<2><<<ga, BLOCK, 0, s>>>(c);
+            k_build_lees<2><<<ga, BLOCK, 0, s>>>(c);
+        }
+        k_sort_lists<<<grid_for(c.n, 128), 128, 0, s>>>(c);
         return;
     }
     if (c.nd == 3) {

@@ -462,12 +462,17 @@ __global__ void __launch_bounds__(BLOCK) k_force64(DevCtx c) {
             ld_pos(c.pos, j, Aj, Bj);
             float4 Qj = Qi;
             if ((uni & UNI_ALL) != UNI_ALL) Qj = c.prm32[j];
-            if (beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi, Qj, uni)) continue;
+            // (the FP32 screen is per-axis periodic: not for a sheared box)
+            if (!S.lees && beyond32<KIND>(d2_32<ND>(S, Ai, Bi, Aj, Bj), Qi, Qj, uni)) continue;
             double xj[3] = {0, 0, 0};
             load3<ND>(c.x, j, xj);
             double r[3] = {0, 0, 0};
+            if (S.lees) {
+                lees_diff<ND>(S, xi, xj, r);
+            } else {
 #pragma unroll
-            for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+                for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+            }
             double dsq = r[0] * r[0] + r[1] * r[1];
             if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
             AtomPrm Pj = Pi;
@@ -533,8 +538,12 @@ __global__ void __launch_bounds__(BLOCK) k_eval64(DevCtx c, int what) {
             double xj[3] = {0, 0, 0};
             load3<ND>(c.x, j, xj);
             double r[3] = {0, 0, 0};
+            if (S.lees) {
+                lees_diff<ND>(S, xi, xj, r);
+            } else {
 #pragma unroll
-            for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+                for (int d = 0; d < ND; d++) r[d] = remainder_exact(xi[d] - xj[d], S.L[d], S.invL[d], S.halfL[d]);
+            }
             double dsq = r[0] * r[0] + r[1] * r[1];
             if constexpr (ND == 3) dsq = dsq + r[2] * r[2];
             PairC pc;

@@ -57,6 +57,7 @@ struct DevCtx {
     uint32_t uniform;  // UniformFlags
     uint32_t nbucket;  // total buckets (sum over systems of ncell + 1)
     uint32_t any_wrap; // some system has an axis with a single cell (per-pair minimum image)
+    uint32_t any_lees; // some system is a LeesEdwardsBox: all-pairs list builds
 
     const SysConst* sys;
     const uint32_t* bucket_off;   // per system: first bucket (cells, then the non-member bucket)

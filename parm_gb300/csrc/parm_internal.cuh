@@ -83,6 +83,8 @@ struct SysConst {
     uint32_t ncell;
     uint32_t atom_off;
     uint32_t natoms;
+    int lees;           // a LeesEdwardsBox (FP64 path): the y image shifts x by gamma Lx
+    double gamma;
 };
 
 // per-atom FP64 parameters of the pair interaction (kind dependent)
@@ -148,6 +150,25 @@ __device__ __forceinline__ double remainder_exact(double d, double L, double inv
     }
     if (r == 0.0) r = copysign(0.0, d);
     return r;
+}
+
+// LeesEdwardsBox::diff (reference src/box.cpp:72-91) in its own arithmetic:
+// the y image im = round(dy / Ly) shifts x by im * gamma * Lx, z takes the
+// periodic remainder.  Used by the FP64 units only (compiled with
+// -fmad=false, so no operation is contracted).  diff(b, a) == -diff(a, b)
+// bit for bit (round is odd, and so is every operation on negated inputs).
+template <int ND>
+__device__ __forceinline__ void lees_diff(const SysConst& S, const double* a, const double* b, double* r) {
+    const double Ly = S.L[1];
+    double dy = a[1] - b[1];
+    const int im = (int)round(dy / Ly);
+    dy = dy - (im * Ly);
+    const double Lx = S.L[0];
+    double dx = a[0] - b[0];
+    dx = dx - round((dx / Lx) - im * S.gamma) * Lx - im * S.gamma * Lx;
+    r[0] = dx;
+    r[1] = dy;
+    if constexpr (ND == 3) r[2] = remainder_exact(a[2] - b[2], S.L[2], S.invL[2], S.halfL[2]);
 }
 
 // FP32 minimum-image displacement from the coarse/fine position split.

@@ -74,6 +74,48 @@ class OriginBox : public Box {
     flt resize_to_L(flt newL, AtomGroup& atoms) { return resize(newL / L(), atoms); }
 };
 
+//! Sheared periodic box (src/box.hpp:165-196, box.cpp:72-135): the y image
+//! shifts x by gamma * Lx.  The GPU path (FP64 handles) applies the same
+//! minimum image; shear(dgamma, atoms) moves the host Atom records, which
+//! the next GPU call uploads.
+class LeesEdwardsBox : public OriginBox {
+   protected:
+    flt gamma;
+
+   public:
+    LeesEdwardsBox(Vec size, flt gamma = 0.0) : OriginBox(size), gamma(gamma) {}
+    LeesEdwardsBox(flt L, flt gamma = 0.0) : OriginBox(L), gamma(gamma) {}
+    Vec diff(Vec r1, Vec r2) override {
+        const flt Ly = boxsize[1];
+        flt dy = r1[1] - r2[1];
+        const int im = (int)std::round(dy / Ly);
+        dy = dy - (im * Ly);
+        const flt Lx = boxsize[0];
+        flt dx = r1[0] - r2[0];
+        dx = dx - std::round((dx / Lx) - im * gamma) * Lx - im * gamma * Lx;
+        Vec r = Vec::Zero();
+        r[0] = dx;
+        r[1] = dy;
+#ifndef VEC2D
+        r[2] = std::remainder(r1[2] - r2[2], boxsize[2]);
+#endif
+        return r;
+    }
+    flt get_gamma() { return gamma; }
+    void shear(flt dgamma) { gamma += dgamma; }
+    void shear(flt dgamma, AtomGroup& atoms);
+    void shear_to(flt new_gamma) { gamma = new_gamma; }
+    void shear_to(flt new_gamma, AtomGroup& atoms);
+    Vec non_affine(Vec v) {
+        v[0] -= gamma * v[1];
+        return v;
+    }
+    Vec affine(Vec v) {
+        v[0] += gamma * v[1];
+        return v;
+    }
+};
+
 //! One particle (src/box.hpp:234-249): the layout the C ABI copies.
 struct Atom {
     Vec x;

@@ -88,6 +88,24 @@ flt OriginBox::resize(flt factor, AtomGroup& atoms) {
     return V();
 }
 
+// LeesEdwardsBox::shear / shear_to with the atoms (src/box.cpp:103-135):
+// x += y * dgamma
+void LeesEdwardsBox::shear(flt dgamma, AtomGroup& atoms) {
+    for (uint i = 0; i < atoms.size(); i++) {
+        const flt dy = atoms[i].x[1];
+        atoms[i].x[0] += dy * dgamma;
+    }
+    gamma += dgamma;
+}
+
+void LeesEdwardsBox::shear_to(flt new_gamma, AtomGroup& atoms) {
+    for (uint i = 0; i < atoms.size(); i++) {
+        const flt dy = atoms[i].x[1];
+        atoms[i].x[0] += dy * (new_gamma - gamma);
+    }
+    gamma = new_gamma;
+}
+
 flt OriginBox::resize_to(Vec newsize, AtomGroup& atoms) {
     const Vec scale = newsize.cwiseQuotient(boxsize);
     boxsize = newsize;
@@ -183,6 +201,13 @@ void GpuLink::push() {
     if (lv != lastbox) {
         parm_host_check(parm_set_boxes(h, lv.data()), "parm_set_boxes");
         lastbox = lv;
+    }
+    if (auto le = std::dynamic_pointer_cast<LeesEdwardsBox>(bx)) {
+        const double g = le->get_gamma();
+        if (!(g == lastgamma)) {
+            parm_host_check(parm_set_lees_edwards(h, &g), "parm_set_lees_edwards");
+            lastgamma = g;
+        }
     }
     if (rows_dirty) {
         // the table of the indexed kinds: row a = the epsilons of the atoms of type a

@@ -67,6 +67,7 @@ class GpuLink {
     int kind = -1;
     std::vector<double> params;   // five per atom
     std::vector<std::vector<double>> eps_rows, sig_rows;   // by type index (indexed kinds)
+    double lastgamma = std::nan("");                       // shear sent to the GPU (LeesEdwardsBox)
     bool rows_dirty = false;
     std::vector<uint32_t> rank;
     std::vector<double> ldiam;   // explicit list diameters (NaN: the parameters' max_size())

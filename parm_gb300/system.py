@@ -102,6 +102,14 @@ class System:
         check(self.lib.parm_set_interaction(self.h, kind, dptr(p), u32ptr(rk) if rk is not None else None,
                                             float(skin)))
 
+    def set_lees_edwards(self, gamma) -> None:
+        """LeesEdwardsBox shears, one per system (None: OriginBoxes again); FP64 handles."""
+        if gamma is None:
+            check(self.lib.parm_set_lees_edwards(self.h, None))
+            return
+        g = _as_f64(gamma, (self.nsys,))
+        check(self.lib.parm_set_lees_edwards(self.h, dptr(g)))
+
     def set_pair_table(self, eps, sig=None) -> None:
         """Pair tables of the indexed kinds: eps[a, b] = epsilons[b] of the atoms of type a
         (IEps*Atom), sig likewise (IEpsISigCutAtom::sigmas)."""

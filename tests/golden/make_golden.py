@@ -44,8 +44,11 @@ SIG_PRIME = 2.0 ** (-1.0 / 6.0)
 
 def _deck(c: dict) -> str:
     nd = c["L"].shape[0]
-    out = [f"{c['kind']} {c['integ']} {c['nsteps']} {c['dt']!r} {c['damping']!r} {c['T']!r} {c['skin']!r}",
-           " ".join(repr(float(q)) for q in c["L"]), str(len(c["m"]))]
+    lees = "le_gamma" in c   # a LeesEdwardsBox: kind + 100 and the shear after the box
+    out = [f"{c['kind'] + (100 if lees else 0)} {c['integ']} {c['nsteps']} {c['dt']!r} {c['damping']!r} "
+           f"{c['T']!r} {c['skin']!r}",
+           " ".join(repr(float(q)) for q in c["L"]) + (f" {float(c['le_gamma'])!r}" if lees else ""),
+           str(len(c["m"]))]
     for i in range(len(c["m"])):
         prm = c["deck_params"][i] if "deck_params" in c else c["params"][i]
         vals = list(c["x"][i]) + list(c["v"][i]) + [c["m"][i]] + list(prm)
@@ -107,13 +110,15 @@ def _parse(text: str, n: int, nd: int) -> dict:
 
 
 def _case(name, kind, integ, nsteps, dt, L, x, v, m, params, skin, out_steps, damping=0.0, T=0.0,
-          order=None, ignores=None, cg=None, deck_params=None, pair_eps=None, pair_sig=None):
+          order=None, ignores=None, cg=None, deck_params=None, pair_eps=None, pair_sig=None, le_gamma=None):
     """deck_params: the atoms' constructor arguments when they differ from the stored fields
     (LoisLinAtom takes depth and width and stores f = depth / width and l = width)."""
     n = len(m)
     extra = {} if cg is None else {"cg": np.asarray(cg, dtype=np.float64)}
     if deck_params is not None:
         extra["deck_params"] = np.asarray(deck_params, dtype=np.float64).reshape(n, -1)
+    if le_gamma is not None:
+        extra["le_gamma"] = np.float64(le_gamma)
     if pair_eps is not None:
         extra["pair_eps"] = np.asarray(pair_eps, dtype=np.float64)
         extra["pair_sig"] = (np.asarray(pair_sig, dtype=np.float64) if pair_sig is not None
@@ -385,6 +390,19 @@ def cases() -> list[dict]:
                      v, np.ones(n), np.stack([rng.choice([1.0, 1.5], n), rng.choice([0.5, 0.8], n),
                                               rng.choice([1.0, 1.1], n), rng.choice([0.9, 1.2], n),
                                               rng.choice([0.95, 2.0, 2.5], n)], 1), 0.3, [1, 10, 100, 300]))
+    # 27-28. LeesEdwardsBox: the minimum image across y shifts x by the shear; soft spheres
+    #        (damped) and LJ (Verlet) at shears 0.3 and -0.75 (an image offset past half a box)
+    rng = np.random.default_rng(74)
+    n = 200
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    Lle = (np.sum(np.pi * sig ** 3 / 6) / 0.6) ** (1 / 3)
+    out.append(_case("lees_spheres200_damped", REPULSION, DAMPED, 300, 0.01, [Lle] * 3, rng.uniform(0, Lle, (n, 3)),
+                     np.zeros((n, 3)), np.ones(n), np.stack([np.ones(n), sig, np.full(n, 2.0)], 1), 0.2,
+                     [1, 10, 100, 300], damping=0.5, le_gamma=0.3))
+    L, x, v = lj_lattice_deck((8, 8, 8), 75)
+    n = len(x)
+    out.append(_case("lees_lj512_verlet", LJCUT, VERLET, 300, 0.002, L, x, v, np.ones(n),
+                     np.tile([1.0, 1.0, cut], (n, 1)), 0.3, [1, 10, 100, 300], le_gamma=-0.75))
     return out
 
 

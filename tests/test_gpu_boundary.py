@@ -282,3 +282,58 @@ def test_indexed_asymmetric_table_matches_oracle(kind):
         assert np.array_equal(st[k], ref[k]), k
     assert g.energy()[0] == pytest.approx(o.energy(), rel=1e-12, abs=1e-12)
     g.close()
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_lees_edwards_shear_matches_oracle(ndim):
+    """A LeesEdwardsBox sheared between runs (x += y dgamma, gamma += dgamma, as
+    LeesEdwardsBox::shear(dgamma, atoms) does): pairs, forces and damped steps bit-exact against the
+    oracle before and after the shear, including a shear past half a box."""
+    from oracle.oracle import Oracle
+    from parm_gb300 import System
+    rng = np.random.default_rng(95 + ndim)
+    n = 240
+    sig = np.where(np.arange(n) < n // 2, 1.0, 1.4)
+    vol = np.sum((np.pi * sig ** 2 / 4) if ndim == 2 else (np.pi * sig ** 3 / 6)) / 0.6
+    L = vol ** (1 / ndim)
+    x = rng.uniform(0, L, (n, ndim))
+    params = np.stack([np.ones(n), sig, np.full(n, 2.0)], 1)
+    g = System(n, ndim=ndim, precision="fp64")
+    g.set_boxes(np.full((1, ndim), L))
+    g.set_lees_edwards([0.2])
+    g.set_atoms(x=x, v=np.zeros((n, ndim)), a=np.zeros((n, ndim)), f=np.zeros((n, ndim)), m=np.ones(n))
+    g.set_interaction(1, params, 0.2)
+    o = Oracle(n, ndim)
+    o.set_box(np.full(ndim, L))
+    o.set_lees_edwards(0.2)
+    o.set_state(x=x, v=np.zeros((n, ndim)), m=np.ones(n))
+    o.set_interaction(1, params, 0.2)
+    for gamma_next in (0.35, 0.9):
+        g.nlist_update(True)
+        o.nl_update(True)
+        assert np.array_equal(g.pairs(), o.pairs())
+        g.set_forces(True)
+        o.set_forces(True)
+        assert np.array_equal(g.get_atoms()["f"], o.get_state()["f"])
+        g.damped(0.01, 0.5, 40)
+        o.damped(0.01, 0.5, 40)
+        st, ref = g.get_atoms(), o.get_state()
+        for k in ("x", "v", "f"):
+            assert np.array_equal(st[k], ref[k]), k
+        # shear the box and the atoms
+        gam = 0.2 if gamma_next == 0.35 else 0.35
+        xs = ref["x"].copy()
+        xs[:, 0] += xs[:, 1] * (gamma_next - gam)
+        g.set_atoms(x=xs)
+        g.set_lees_edwards([gamma_next])
+        o.set_state(x=xs, v=ref["v"], a=ref["a"], f=ref["f"], m=np.ones(n))
+        o.set_lees_edwards(gamma_next)
+    g.close()
+
+
+def test_lees_edwards_needs_fp64():
+    from parm_gb300 import System
+    g = System(64, ndim=3, precision="mixed")
+    with pytest.raises(ValueError, match="FP64"):
+        g.set_lees_edwards([0.1])
+    g.close()

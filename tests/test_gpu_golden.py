@@ -40,6 +40,8 @@ def _gpu(d):
     n, nd = d["n"], d["ndim"]
     s = System([n], ndim=nd, precision="fp64")
     s.set_boxes(d["L"][None, :])
+    if "le_gamma" in d:
+        s.set_lees_edwards([float(d["le_gamma"])])
     s.set_atoms(x=d["x"], v=d["v"], a=np.zeros((n, nd)), f=np.zeros((n, nd)), m=d["m"])
     if "pair_eps" in d:
         s.set_pair_table(d["pair_eps"], d["pair_sig"])

@@ -63,7 +63,8 @@ def _close(got, want, exact, what, tol=1e-12):
 def test_host_api_matches_reference(drivers, name):
     d = load(name)
     case = {k: d[k] for k in ("kind", "integ", "nsteps", "dt", "damping", "T", "skin", "L", "x", "v", "m",
-                              "params", "deck_params", "pair_eps", "pair_sig", "order", "ignores", "out_steps", "cg")
+                              "params", "deck_params", "pair_eps", "pair_sig", "le_gamma", "order", "ignores", "out_steps",
+                              "cg")
             if k in d}
     deck = MG._deck(case)
     r = subprocess.run([str(drivers[d["ndim"]])], input=deck, capture_output=True, text=True, timeout=600,

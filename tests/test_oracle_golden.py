@@ -20,6 +20,8 @@ CASES = names()
 def replay(d):
     o = Oracle(d["n"], d["ndim"])
     o.set_box(d["L"])
+    if "le_gamma" in d:
+        o.set_lees_edwards(float(d["le_gamma"]))
     o.set_state(x=d["x"], v=d["v"], m=d["m"])
     if "pair_eps" in d:
         o.set_pair_table(d["pair_eps"], d["pair_sig"])
