@@ -1,0 +1,85 @@
+"""The host side of the pyparm-compatible layer (parm_gb300/pyparm.py): atoms and their pickled
+state, the boxes' minimum images against the C library's round / remainder, shears, atom parameter
+records in the C ABI's layout.  (The GPU side: tests/test_gpu_pyparm.py.)"""
+import ctypes
+import ctypes.util
+import math
+import pickle
+
+import numpy as np
+import pytest
+
+from parm_gb300 import capi, pyparm
+
+libm = ctypes.CDLL(ctypes.util.find_library("m"))
+libm.round.restype = ctypes.c_double
+libm.round.argtypes = [ctypes.c_double]
+
+
+def test_round_half_away_matches_c():
+    rng = np.random.default_rng(1)
+    vals = list(rng.normal(0, 10, 2000)) + [0.5, -0.5, 1.5, -2.5, 0.49999999999999994, -0.49999999999999994,
+                                            2.0 ** 52 + 0.5, 1e300, -0.0, 0.0, 4503599627370495.5]
+    for v in vals:
+        assert pyparm._round_half_away(v) == libm.round(v), v
+
+
+@pytest.mark.parametrize("sim", [pyparm.d2, pyparm.d3])
+def test_atoms_state_and_pickling(sim):
+    nd = sim.NDIM
+    atoms = sim.AtomVec([1.0, 2.0, np.inf])
+    atoms[1].x = np.arange(nd) + 0.5
+    atoms[2].v = np.ones(nd)
+    assert atoms.version > 0 and len(atoms) == 3 and atoms.getmass(1) == 2.0
+    assert [a.n() for a in atoms] == [0, 1, 2]
+    again = pickle.loads(pickle.dumps(atoms))
+    assert np.array_equal(again.rec, atoms.rec)
+    # immobile atoms carry no kinetic energy
+    assert atoms.kinetic_energy() == 0.0
+
+
+@pytest.mark.parametrize("sim", [pyparm.d2, pyparm.d3])
+def test_box_minimum_images(sim):
+    nd = sim.NDIM
+    rng = np.random.default_rng(2)
+    box = sim.OriginBox(7.3)
+    for _ in range(200):
+        r1, r2 = rng.uniform(-20, 20, nd), rng.uniform(-20, 20, nd)
+        d = box.diff(r1, r2)
+        assert np.array_equal(d, [math.remainder(a - b, 7.3) for a, b in zip(r1, r2)])
+    le = sim.LeesEdwardsBox(7.3, 0.35)
+    for _ in range(200):
+        r1, r2 = rng.uniform(-20, 20, nd), rng.uniform(-20, 20, nd)
+        d = le.diff(r1, r2)
+        dy = r1[1] - r2[1]
+        im = int(libm.round(dy / 7.3))
+        want_y = dy - im * 7.3
+        dx = r1[0] - r2[0]
+        want_x = dx - libm.round(dx / 7.3 - im * 0.35) * 7.3 - im * 0.35 * 7.3
+        assert d[0] == want_x and d[1] == want_y
+        assert np.array_equal(le.diff(r2, r1), -d)
+
+
+def test_shear_moves_atoms():
+    sim = pyparm.d3
+    atoms = sim.AtomVec(2)
+    atoms[0].x = [1.0, 2.0, 0.0]
+    le = sim.LeesEdwardsBox(10.0)
+    le.shear(0.25, atoms)
+    assert atoms[0].x[0] == 1.0 + 2.0 * 0.25 and le.get_gamma() == 0.25
+    le.shear_to(0.5, atoms)
+    assert le.get_gamma() == 0.5
+
+
+def test_atom_records_match_the_abi_layout():
+    sim = pyparm.d3
+    atoms = sim.AtomVec(3)
+    assert sim.EpsSigExpAtom(atoms[0], 1.0, 1.4, 2.5).p == [1.0, 1.4, 2.5]
+    assert sim.EpsSigExpDragAtom(atoms[0], 1.0, 1.4, 0.3).p == [1.0, 1.4, 2.5, 0.3]   # exponent default 2.5
+    ll = sim.LoisLinAtom(atoms[0], 1.0, 1.2, 0.004, 0.08)
+    assert ll.p == [1.0, 1.2, 0.004 / 0.08, 0.08] and len(ll.p) == capi.nparam(capi.LOISLIN)
+    ie = sim.IEpsRepsSigExpCutAtom(atoms[1], [1.0, 0.5], 2.0, 1.1, 12.0, 1, 2.5)
+    assert ie.p == [1, 2.0, 1.1, 12.0, 2.5] and ie.rows[0] == 1
+    assert len(ie.p) == capi.nparam(capi.LJISH)
+    with pytest.raises(TypeError):
+        sim.Repulsion(sim.OriginBox(5.0), atoms, 0.3).add(sim.EpsSigAtom(atoms[0], 1.0, 1.0))
