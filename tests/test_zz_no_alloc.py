@@ -67,3 +67,23 @@ def test_noalloc_rejects_oversized_input():
                                          C.c_void_p(buf.data_ptr()), None)
     assert rc == capi.PARM_ERR_ARG
     assert b"262144" in lib.parm_last_error()
+
+
+def test_noalloc_leaves_free_device_memory_unchanged():
+    """After the first call (which looks up the static scratch), repeated calls take no device memory."""
+    torch = pytest.importorskip("torch")
+    w = W.small_random(n=50000, ndim=3, kind=1, seed=72)
+    lib = capi.load()
+    rec = torch.from_numpy(_records(w)).cuda()
+    out = torch.zeros((1,), dtype=torch.float64, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = (C.c_void_p(rec.data_ptr()), 13, w.n, 3, None, C.c_void_p(out.data_ptr()), stream)
+    assert lib.parm_kinetic_energy_noalloc(*args) == capi.PARM_OK
+    torch.cuda.synchronize()
+    first = out.item()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(200):
+        assert lib.parm_kinetic_energy_noalloc(*args) == capi.PARM_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert out.item() == first   # same terms, same order: the same sum
