@@ -54,23 +54,32 @@ def _make(ndim: int):
 
         def __init__(self, masses, mass=1.0):
             m = np.full(int(masses), float(mass)) if np.isscalar(masses) else np.asarray(masses, np.float64)
-            self.rec = np.zeros((len(m), REC))
-            self.rec[:, 4 * NDIM] = m
+            self._rec = np.zeros((len(m), REC))
+            self._rec[:, 4 * NDIM] = m
             self.version = 0
+            self._dev = None   # the NeighborList whose device handle holds newer records
+
+        @property
+        def rec(self):
+            """The records (n, 4*NDIM + 1); read back from the device first when it holds newer ones."""
+            if self._dev is not None:
+                nl, self._dev = self._dev, None
+                nl._fetch()
+            return self._rec
 
         def touch(self):
             self.version += 1
 
         def size(self):
-            return len(self.rec)
+            return len(self._rec)
 
         N = size
 
         def __len__(self):
-            return len(self.rec)
+            return len(self._rec)
 
         def get_id(self, i):
-            if not 0 <= int(i) < len(self.rec):
+            if not 0 <= int(i) < len(self._rec):
                 raise IndexError("atom index out of range")
             return AtomID(self, int(i))
 
@@ -80,14 +89,14 @@ def _make(ndim: int):
             return self.get_id(i)
 
         def __iter__(self):
-            for i in range(len(self.rec)):
+            for i in range(len(self._rec)):
                 yield AtomID(self, i)
 
         def getmass(self, i):
-            return float(self.rec[i, 4 * NDIM])
+            return float(self._rec[i, 4 * NDIM])   # masses change only on the host
 
         def _mobile(self):
-            m = self.rec[:, 4 * NDIM]
+            m = self._rec[:, 4 * NDIM]
             return ~((m <= 0) | np.isinf(m))
 
         def kinetic_energy(self, v0=None):
@@ -101,7 +110,7 @@ def _make(ndim: int):
             return np.sum(self.rec[mob, 4 * NDIM, None] * self.rec[mob, NDIM:2 * NDIM], axis=0)
 
         def mass(self):
-            return float(np.sum(self.rec[self._mobile(), 4 * NDIM]))
+            return float(np.sum(self._rec[self._mobile(), 4 * NDIM]))
 
         def com_velocity(self):
             return self.momentum() / self.mass()
@@ -485,20 +494,29 @@ def _make(ndim: int):
                     s.ignore(a, b)
                 self._dirty = False
                 self._pairs = None
-            if self._pushed[0] != self.atoms.version:
+            if self._pushed[0] != self.atoms.version and self.atoms._dev is not self:
                 r = self.atoms.rec
                 s.set_atoms(x=r[:, 0:NDIM], v=r[:, NDIM:2 * NDIM], a=r[:, 2 * NDIM:3 * NDIM],
                             f=r[:, 3 * NDIM:4 * NDIM], m=r[:, 4 * NDIM])
             self._pushed = (self.atoms.version, L, gamma)
 
         def pull(self):
+            """After a device call: the device holds the newest records; the host reads them back on
+            its next access to AtomVec.rec (so consecutive calls move no records)."""
+            self.atoms._dev = self
+            self._pairs = None
+
+        def _fetch(self):
             st = self.sys.get_atoms()
-            r = self.atoms.rec
+            r = self.atoms._rec
             r[:, 0:NDIM], r[:, NDIM:2 * NDIM] = st["x"], st["v"]
             r[:, 2 * NDIM:3 * NDIM], r[:, 3 * NDIM:4 * NDIM] = st["a"], st["f"]
-            self.atoms.touch()
+            self.atoms.touch()   # other handles on these atoms upload them again
             self._pushed = (self.atoms.version, self._pushed[1], self._pushed[2])
-            self._pairs = None
+
+        def resident(self):
+            """True while the device holds newer Atom records than the host."""
+            return self.atoms._dev is self
 
     # ------------------------------------------------------------ NListed
     class _NListed:
@@ -557,6 +575,7 @@ def _make(ndim: int):
             self.nl.sys.set_forces(False)
             self.nl.pull()
             self.nl.atoms.rec[:, 3 * NDIM:4 * NDIM] += f0
+            self.nl.atoms.touch()
 
     def _nlisted(name, mapping):
         return type(name, (_NListed,), {"kinds": mapping})
@@ -661,8 +680,17 @@ def _make(ndim: int):
         def potential_energy(self):
             return float(sum(i.energy(self.box) for i in self.interactions))
 
+        def _resident(self):
+            return self.nl is not None and self.nl.resident()
+
+        def _ke(self, v0=None):
+            # on the device while it holds the newest velocities (no records move)
+            if self._resident():
+                return float(self.nl.sys.kinetic_energy(None if v0 is None else np.asarray(v0)[None, :])[0])
+            return self.atoms.kinetic_energy(v0)
+
         def kinetic_energy(self):
-            return self.atoms.kinetic_energy()
+            return self._ke()
 
         def energy(self):
             return self.potential_energy() + self.kinetic_energy()
@@ -671,6 +699,9 @@ def _make(ndim: int):
             return NDIM * int(np.sum(self.atoms._mobile()))
 
         def com_velocity(self):
+            if self._resident():
+                mom, mass = self.nl.sys.momentum()
+                return mom[0] / mass[0]
             return self.atoms.com_velocity()
 
         def reset_com_velocity(self):
@@ -679,7 +710,7 @@ def _make(ndim: int):
         def temp(self, minuscomv=True):
             v = self.com_velocity() if minuscomv else None
             ndof = self.degrees_of_freedom() - (NDIM if minuscomv else 0)
-            return self.atoms.kinetic_energy(v) * 2 / ndof
+            return self._ke(v) * 2 / ndof
 
         def pressure(self):
             E = 2.0 * self.kinetic_energy() + sum(i.pressure(self.box) for i in self.interactions)

@@ -92,6 +92,32 @@ def test_random_hertzian_matches_the_c_abi():
     s.close()
 
 
+def test_records_stay_on_the_device_between_calls():
+    t = _RandomHertzianVerlet()
+    nl = t.interaction.neighbor_list()
+    t.collec.timesteps(10)
+    assert nl.resident()
+    ke, T = t.collec.kinetic_energy(), t.collec.temp()
+    assert np.isfinite(t.collec.energy())
+    assert nl.resident()            # kinetic energy and momentum are summed on the device
+    t.collec.timesteps(5)
+    t.collec.timesteps(5)
+    x = t.atoms[0].x                # a host read brings the records back
+    assert not nl.resident()
+    assert np.all(np.isfinite(x))
+    t.collec.timesteps(0)
+    ke_h = t.collec.kinetic_energy()
+    t2 = _RandomHertzianVerlet()     # the same steps with the records read back after each call
+    for _ in range(10):
+        t2.collec.timestep()
+        t2.atoms[0].x
+    assert t2.collec.kinetic_energy() == pytest.approx(ke, rel=1e-13)
+    assert t2.collec.temp() == pytest.approx(T, rel=1e-13)
+    t2.collec.timesteps(10)
+    np.testing.assert_array_equal(t2.atoms.rec, t.atoms.rec)
+    assert ke_h == pytest.approx(t2.collec.kinetic_energy(), rel=1e-13)
+
+
 def _build(d, sim):
     n, nd = d["n"], d["ndim"]
     if "le_gamma" in d:

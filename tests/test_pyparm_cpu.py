@@ -83,3 +83,24 @@ def test_atom_records_match_the_abi_layout():
     assert len(ie.p) == capi.nparam(capi.LJISH)
     with pytest.raises(TypeError):
         sim.Repulsion(sim.OriginBox(5.0), atoms, 0.3).add(sim.EpsSigAtom(atoms[0], 1.0, 1.0))
+
+
+def test_records_are_read_back_only_when_the_host_reads_them():
+    sim = pyparm.d3
+    atoms = sim.AtomVec([1.0, 2.0, 3.0, 4.0])
+
+    class DeviceStub:   # stands in for a NeighborList whose device holds newer records
+        fetches = 0
+
+        def _fetch(self):
+            DeviceStub.fetches += 1
+            atoms._rec[:, 0] = 7.0
+            atoms.touch()
+
+    atoms._dev = DeviceStub()
+    assert len(atoms) == 4 and atoms.getmass(2) == 3.0 and atoms.mass() == 10.0
+    assert DeviceStub.fetches == 0           # sizes and masses never change on the device
+    assert atoms[1].x[0] == 7.0
+    assert DeviceStub.fetches == 1
+    atoms[2].x = [1.0, 2.0, 3.0]
+    assert DeviceStub.fetches == 1 and atoms._dev is None
