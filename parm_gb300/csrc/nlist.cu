@@ -90,17 +90,19 @@ __global__ void k_zero_cells(DevCtx c) {
 
 template <int ND>
 __global__ void k_bin(DevCtx c) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
-    uint32_t s = c.atom_sys[i];
-    if (!c.flag[s]) return;
-    const SysConst& S = c.sys[s];
-    uint32_t b;
-    uint32_t slot;
-    if (c.rank[i] == NOT_MEMBER) {
-        b = c.bucket_off[s] + S.ncell;
+    // every lane of the warp reaches the cell-count update below (the grid is
+    // whole warps), so the lanes that bin a member can be counted by a ballot
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = i < c.n ? c.atom_sys[i] : 0u;
+    const bool live = i < c.n && c.flag[s];
+    const bool member = live && c.rank[i] != NOT_MEMBER;
+    uint32_t b = 0u, slot = 0u;
+    if (live && !member) {
+        b = c.bucket_off[s] + c.sys[s].ncell;
         slot = c.nm_rank[c.orig[i]];
-    } else {
+    }
+    if (member) {
+        const SysConst& S = c.sys[s];
         typename DVec<ND>::T xi = ldx<ND>(c.x, i);
         double xs[3] = {xi.x, xi.y, 0.0};
         if constexpr (ND == 3) xs[2] = reinterpret_cast<const double*>(&xi)[2];
@@ -117,10 +119,24 @@ __global__ void k_bin(DevCtx c) {
         }
         if (bad) atomicOr(c.status, ST_NONFINITE);
         b = c.bucket_off[s] + (uint32_t)((ci[2] * S.nc[1] + ci[1]) * S.nc[0] + ci[0]);
-        slot = atomicAdd(&c.cell_count[b], 1u);
     }
-    c.bucket[i] = b;
-    c.cslot[i] = slot;
+    // one atomic per distinct cell of the warp (atoms arrive in cell order,
+    // so a warp holds two or three cells): the lanes of a cell take
+    // consecutive slots from its count
+    const uint32_t mem = __ballot_sync(0xFFFFFFFFu, member);
+    if (member) {
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t peers = __match_any_sync(mem, b);
+        const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+        uint32_t first = 0u;
+        if (lane == leader) first = atomicAdd(&c.cell_count[b], (uint32_t)__popc(peers));
+        first = __shfl_sync(peers, first, leader);
+        slot = first + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    }
+    if (live) {
+        c.bucket[i] = b;
+        c.cslot[i] = slot;
+    }
 }
 
 // ---------------------------------------------------------------------------

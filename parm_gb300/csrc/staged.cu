@@ -281,6 +281,21 @@ __device__ __forceinline__ float4 stg_plain(const StgTable& T, const float4& rec
     return make_float4(fmaf(qx, 0.125f, rec.x), fmaf(qy, 0.125f, rec.y), fmaf(qz, 0.125f, rec.z), w);
 }
 
+// The plain stage is pair-interleaved: local indices 2k and 2k + 1 share 32
+// bytes, (x0, x1, y0, y1) then (z0, z1, w0, w1), so one 16-byte load gives the
+// x and y of two candidates as packed FP32 pairs.
+__device__ __forceinline__ void stg_put_plain(float4* sp, uint32_t q, const float4& v) {
+    float* f = reinterpret_cast<float*>(sp) + 8u * (q >> 1) + (q & 1u);
+    f[0] = v.x;
+    f[2] = v.y;
+    f[4] = v.z;
+    f[6] = v.w;
+}
+__device__ __forceinline__ float4 stg_at_plain(const float4* sp, uint32_t q) {
+    const float* f = reinterpret_cast<const float*>(sp) + 8u * (q >> 1) + (q & 1u);
+    return make_float4(f[0], f[2], f[4], f[6]);
+}
+
 // list diameter of atom j (the w of its coarse position view)
 __device__ __forceinline__ float stg_diam(const DevCtx& c, uint32_t j) {
     return __ldg(reinterpret_cast<const float*>(c.pos + 2 * (size_t)j) + 3);
@@ -314,7 +329,7 @@ __device__ void stg_load_plain(const DevCtx& c, const StgTable& T, float4* sp, u
         }
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (ok[k]) sp[q[k]] = stg_plain(T, stg_shift(T, pc[k], R[k]), w[k]);
+            if (ok[k]) stg_put_plain(sp, q[k], stg_plain(T, stg_shift(T, pc[k], R[k]), w[k]));
         // pieces longer than 64 atoms (large blocks of sparse systems)
 #pragma unroll 1
         for (int k = 0; k < 2; k++) {
@@ -322,7 +337,7 @@ __device__ void stg_load_plain(const DevCtx& c, const StgTable& T, float4* sp, u
             if (p >= T.npiece) break;
             for (uint32_t t = lane + 64u; t < T.cnt[p] && T.off[p] + t < cap; t += 32u) {
                 const uint32_t j = T.g0[p] + t;
-                sp[T.off[p] + t] = stg_plain(T, stg_shift(T, p, __ldg(&c.rec[j])), diam ? stg_diam(c, j) : 0.f);
+                stg_put_plain(sp, T.off[p] + t, stg_plain(T, stg_shift(T, p, __ldg(&c.rec[j])), diam ? stg_diam(c, j) : 0.f));
             }
         }
     }
@@ -518,6 +533,44 @@ __device__ void stg_nonmembers(const DevCtx& c, uint32_t s, int zero_a) {
     }
 }
 
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// packed pairs of FP32 values (Blackwell's f32x2 add / mul / fma: two lanes
+// of work per instruction)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // list build: one CTA per block, one thread per home atom
 // ---------------------------------------------------------------------------
@@ -525,7 +578,7 @@ __device__ void stg_nonmembers(const DevCtx& c, uint32_t s, int zero_a) {
 template <int ND, int DIA>
 __device__ __forceinline__ float4 stg_get_plain(const DevCtx& c, const SysConst& S, const StgTable& T,
                                                 const float4* sp, uint32_t cap, uint32_t q) {
-    if (q < cap) return sp[q];
+    if (q < cap) return stg_at_plain(sp, q);
     const uint32_t p = stg_piece(T, q);
     const uint32_t j = T.g0[p] + (q - T.off[p]);
     return stg_plain(T, stg_shift(T, p, c.rec[j]), DIA ? stg_diam(c, j) : 0.f);
@@ -537,7 +590,7 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
     const uint32_t maxnb = c.maxnb;
     uint16_t* out = c.nbr16;
     const float skin32 = (float)S.skin;
-    const float4 P = FULL ? sp[a.qi] : stg_get_plain<ND, DIA>(c, S, T, sp, cap, a.qi);
+    const float4 P = FULL ? stg_at_plain(sp, a.qi) : stg_get_plain<ND, DIA>(c, S, T, sp, cap, a.qi);
     const float tu = (DIA ? P.w : stg_diam(c, a.i)) + skin32;
     const float hiu = tu * tu * (1.0f + STG_BAND), lou = tu * tu * (1.0f - STG_BAND);
     const uint32_t oi = c.excl_off ? c.orig[a.i] : 0u;
@@ -547,6 +600,11 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
     uint32_t* const ow = reinterpret_cast<uint32_t*>(ob);
     const uint32_t H2 = 2u * a.H;
     uint32_t k = 0, pend = 0u;
+    // broadcast pairs for the packed screening of FULL stages
+    const f32x2 Px2 = pk2(P.x, P.x), Py2 = pk2(P.y, P.y), Pz2 = pk2(P.z, P.z);
+    const f32x2 HI2 = pk2(hiu, hiu), LO2 = pk2(lou, lou);
+    const f32x2 PW2 = pk2(P.w, P.w), HALF2 = pk2(0.5f, 0.5f), SKIN2 = pk2(skin32, skin32);
+    const f32x2 BH2 = pk2(1.0f + STG_BAND, 1.0f + STG_BAND), BL2 = pk2(1.0f - STG_BAND, 1.0f - STG_BAND);
 #pragma unroll 1
     for (int dz = 0; dz < (ND == 3 ? 3 : 1); dz++) {
 #pragma unroll 1
@@ -558,7 +616,10 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
             // bit per candidate within the widened threshold, then the set
             // bits (the ~15 % that are kept) are settled and written in order
 #pragma unroll 1
-            for (uint32_t base = lo; base < hi; base += 32u) {
+            // FULL stages are screened two candidates at a time in packed
+            // FP32 pairs, so the passes start at an even local index (an odd
+            // row start adds the slot before it, cleared below)
+            for (uint32_t base = FULL ? (lo & ~1u) : lo; base < hi; base += 32u) {
                 const uint32_t m = min(32u, hi - base);
                 uint32_t mask = 0u, sure = 0u;
                 // bit of a candidate within the widened threshold (mask) and
@@ -581,14 +642,43 @@ __device__ __forceinline__ void build_home(const DevCtx& c, const SysConst& S, c
                 };
                 if constexpr (FULL) {
                     // all 32 slots (the stage has 32 records of padding past
-                    // its capacity), then the slots past the row and the
-                    // home atom itself are cleared
-                    const float4* sq = sp + base;
+                    // its capacity), then the slots past the row, the slot
+                    // before an odd row start and the home atom itself are
+                    // cleared.  A candidate's bit is the sign of rr - hi2
+                    // (rr < hi2; equality is far outside the true threshold,
+                    // which lies 2e-5 below hi2) and of rr - lo2 (rr < lo2),
+                    // shifted in from the top candidate down so that bit u
+                    // is candidate base + u.
+                    const ulonglong2* sq = reinterpret_cast<const ulonglong2*>(sp) + base;
 #pragma unroll
-                    for (uint32_t u = 0; u < 16; u++) screen(sq[u], 1u << u);
-#pragma unroll
-                    for (uint32_t u = 0; u < 16; u++) screen(sq[16 + u], 1u << (16 + u));
+                    for (int u2 = 15; u2 >= 0; u2--) {
+                        const ulonglong2 A = sq[2 * u2];   // (x0, x1), (y0, y1)
+                        const f32x2 dx = sub2(Px2, A.x), dy = sub2(Py2, A.y);
+                        f32x2 rr = fma2(dy, dy, mul2(dx, dx));
+                        f32x2 h2 = HI2, l2 = LO2;
+                        if constexpr (ND == 3 || DIA) {
+                            const ulonglong2 B = sq[2 * u2 + 1];   // (z0, z1), (w0, w1)
+                            if constexpr (ND == 3) {
+                                const f32x2 dz = sub2(Pz2, B.x);
+                                rr = fma2(dz, dz, rr);
+                            }
+                            if constexpr (DIA) {
+                                const f32x2 thr = fma2(add2(PW2, B.y), HALF2, SKIN2);
+                                const f32x2 t2 = mul2(thr, thr);
+                                h2 = mul2(t2, BH2);
+                                l2 = mul2(t2, BL2);
+                            }
+                        }
+                        float e0, e1, g0, g1;
+                        upk2(sub2(rr, h2), e0, e1);
+                        upk2(sub2(rr, l2), g0, g1);
+                        mask = __funnelshift_l(__float_as_uint(e1), mask, 1);
+                        sure = __funnelshift_l(__float_as_uint(g1), sure, 1);
+                        mask = __funnelshift_l(__float_as_uint(e0), mask, 1);
+                        sure = __funnelshift_l(__float_as_uint(g0), sure, 1);
+                    }
                     if (m < 32u) mask &= (1u << m) - 1u;
+                    if (base < lo) mask &= ~1u;
                     const uint32_t d = a.qi - base;
                     if (d < 32u) mask &= ~(1u << d);
                 } else {
@@ -686,44 +776,6 @@ __global__ void __launch_bounds__(STG_THREADS, 4) k_build_stg(DevCtx c) {
 // of the home rows' lists into L2, copies the records into shared memory with
 // one bulk asynchronous copy per piece and moves them into the block frame.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float rcp_approx(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// packed pairs of FP32 values (Blackwell's f32x2 add / mul / fma: two lanes
-// of work per instruction)
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 pk2(float a, float b) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
 // pair-law constants of one pair type
 template <int KIND>
 struct Law {
