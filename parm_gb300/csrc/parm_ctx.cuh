@@ -330,8 +330,8 @@ constexpr int STG_KY_MAX = 6;
 constexpr int STG_ROWS_MAX = 3 * (STG_KY_MAX + 2);
 constexpr int STG_PIECES_MAX = 3 * STG_ROWS_MAX;
 constexpr int STG_KX_MAX = 32;
-constexpr int STG_THREADS_HOST = 256;
-constexpr uint32_t STG_TAB_WORDS = 160;   // 16-byte words per block table (>= its size)   // threads per block of the cell-block kernels
+constexpr int STG_THREADS_HOST = 256;     // threads per block of the cell-block kernels
+constexpr uint32_t STG_TAB_WORDS = 160;   // 16-byte words per block table (>= its size)
 
 inline unsigned grid_for(uint32_t n, int block = BLOCK) {
     unsigned g = (unsigned)((n + block - 1) / block);
