@@ -8,9 +8,11 @@
 // of the reference's algorithm on the GPU and downloads the records, so code
 // that reads or edits atoms[i] between steps behaves as with the reference;
 // timesteps(n) runs n steps with one upload and one download, or, when the
-// Collection holds other trackers (RsqTracker, EnergyTracker or the
-// caller's own), one step at a time with the trackers updated after each,
-// as the reference's timestep does.
+// Collection holds trackers of the host (EnergyTracker, the caller's own, or
+// an RsqTracker it could not bind), one step at a time with the trackers
+// updated after each, as the reference's timestep does.  An RsqTracker of
+// the Collection's own AtomVec is bound to its handle when the Collection is
+// made (RsqTracker::bind) and updated inside the GPU steps.
 #ifndef PARM_GB300_COLLECTION_HPP
 #define PARM_GB300_COLLECTION_HPP
 

@@ -315,6 +315,10 @@ RsqTracker::RsqTracker(sptr<AtomGroup> atoms, std::vector<unsigned long> ns, boo
 }
 
 RsqTracker::~RsqTracker() {
+    if (link) {
+        parm_rsq_stop(link->handle());   // no throw from a destructor
+        link->release_rsq(this);
+    }
     if (h) parm_destroy(h);
 }
 
@@ -331,18 +335,52 @@ void RsqTracker::push() {
 }
 
 void RsqTracker::reset() {
-    push();
-    parm_host_check(parm_rsq_start(h, skips.data(), (uint32_t)skips.size(), usecom ? 1 : 0), "parm_rsq_start");
+    if (link) {
+        link->push();
+    } else {
+        push();
+    }
+    parm_host_check(parm_rsq_start(active(), skips.data(), (uint32_t)skips.size(), usecom ? 1 : 0),
+                    "parm_rsq_start");
+    const uint n = atoms->size();
+    start.assign((size_t)n * NDIM, 0.0);
+    for (uint i = 0; i < n; i++)
+        for (int d = 0; d < NDIM; d++) start[(size_t)i * NDIM + d] = (*atoms)[i].x[d];
+    nupdates = 0;
 }
 
 void RsqTracker::update(Box&) {
-    push();
-    parm_host_check(parm_rsq_update(h), "parm_rsq_update");
+    if (link) {
+        link->push();
+    } else {
+        push();
+    }
+    parm_host_check(parm_rsq_update(active()), "parm_rsq_update");
+    nupdates++;
+}
+
+bool RsqTracker::bind(const sptr<GpuLink>& l) {
+    if (link) return link == l;
+    if (!l || static_cast<AtomGroup*>(l->atoms().get()) != atoms.get() || nupdates != 0) return false;
+    const uint n = atoms->size();
+    for (uint i = 0; i < n; i++)
+        for (int d = 0; d < NDIM; d++)
+            if (!((*atoms)[i].x[d] == start[(size_t)i * NDIM + d])) return false;
+    if (!l->claim_rsq(this)) return false;
+    l->push();
+    if (parm_rsq_start(l->handle(), skips.data(), (uint32_t)skips.size(), usecom ? 1 : 0) != PARM_OK) {
+        l->release_rsq(this);
+        return false;
+    }
+    link = l;
+    parm_destroy(h);
+    h = nullptr;
+    return true;
 }
 
 std::vector<double> RsqTracker::get(int what, size_t per_window) {
     std::vector<double> v(skips.size() * per_window);
-    parm_host_check(parm_rsq_get(h, what, v.data()), "parm_rsq_get");
+    parm_host_check(parm_rsq_get(active(), what, v.data()), "parm_rsq_get");
     return v;
 }
 
@@ -472,6 +510,11 @@ void Collection::attach() {
     if (found && found->atoms() != atoms)
         throw std::invalid_argument("parm_gb300: the interaction was built on another AtomVec");
     link = found;
+    // mean-square-displacement trackers of these atoms move onto the
+    // Collection's handle: the time steps update them on the GPU
+    if (link)
+        for (auto& t : trackers)
+            if (auto r = std::dynamic_pointer_cast<RsqTracker>(t)) r->bind(link);
 }
 
 GpuLink& Collection::gpu() {
@@ -585,23 +628,32 @@ bool Collection::has_step_trackers() const {
     return false;
 }
 
+// the trackers that the GPU time steps on handle `g` update themselves: the
+// neighbour list and the mean-square-displacement trackers bound to `g`
+static bool updated_by_steps(const sptr<StateTracker>& t, const GpuLink& g) {
+    if (std::dynamic_pointer_cast<NeighborList>(t)) return true;
+    auto r = std::dynamic_pointer_cast<RsqTracker>(t);
+    return r && r->bound_to(&g);
+}
+
 void Collection::run_steps(uint n, const std::function<void(uint)>& step) {
     if (!n) return;
     GpuLink& g = gpu();
     g.push();
     g.touch();
-    if (!has_step_trackers()) {
+    bool host_trackers = false;
+    for (auto& t : trackers) host_trackers = host_trackers || !updated_by_steps(t, g);
+    if (!host_trackers) {
         step(n);
         g.pull();
         return;
     }
-    // trackers other than the neighbour list (which the GPU steps update
-    // themselves) see the positions at the end of every step
+    // the other trackers see the positions at the end of every step
     for (uint k = 0; k < n; k++) {
         step(1);
         g.pull();
         for (auto& t : trackers)
-            if (!std::dynamic_pointer_cast<NeighborList>(t)) t->update(*box);
+            if (!updated_by_steps(t, g)) t->update(*box);
     }
 }
 

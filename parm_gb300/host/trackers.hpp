@@ -58,6 +58,15 @@ class GpuLink {
     //! advanced by every operation that may change the pair list
     unsigned long long epoch() const { return epoch_; }
     void touch() { epoch_++; }
+    //! the device tracker of this handle (parm_rsq_*) belongs to one RsqTracker
+    bool claim_rsq(const void* who) {
+        if (rsq_owner && rsq_owner != who) return false;
+        rsq_owner = who;
+        return true;
+    }
+    void release_rsq(const void* who) {
+        if (rsq_owner == who) rsq_owner = nullptr;
+    }
 
    private:
     sptr<Box> bx;
@@ -79,6 +88,7 @@ class GpuLink {
     std::vector<std::pair<uint, uint>> pending_ignores;
     std::vector<double> lastbox;
     unsigned long long epoch_ = 0;
+    const void* rsq_owner = nullptr;
 };
 
 //! Something to update before or after each time step (src/trackers.hpp:9-16).
@@ -143,7 +153,10 @@ class NeighborList : public StateTracker {
 //! (src/constraints.hpp:318-361, src/constraints.cpp:404-564), on the GPU
 //! (parm_rsq_*): the tracker holds its own GPU handle and sends it the
 //! atoms' positions and masses at each update.  A Collection updates it at
-//! the end of every time step, as the reference's update_trackers does.
+//! the end of every time step, as the reference's update_trackers does; a
+//! Collection that steps the same AtomVec moves the tracker onto its own
+//! handle (bind), where the time-step graphs update it with no copies and
+//! several steps run in one call.
 class RsqTracker : public StateTracker {
    public:
     RsqTracker(sptr<AtomGroup> atoms, std::vector<unsigned long> ns, bool usecom = true);
@@ -153,6 +166,15 @@ class RsqTracker : public StateTracker {
     //! restart every window at the current positions
     void reset();
     void update(Box& box) override;
+    //! Move the tracker onto the handle of a Collection that steps these
+    //! same atoms on the GPU: the time steps then update it inside their
+    //! graphs, with no records copied.  Done only while the tracker has not
+    //! been updated since its last reset and the atoms have not moved since
+    //! (nothing is lost); false otherwise, and the tracker stays on its own
+    //! handle.
+    bool bind(const sptr<GpuLink>& link);
+    bool bound() const { return (bool)link; }
+    bool bound_to(const GpuLink* l) const { return link.get() == l; }
     std::vector<VecRows> xyz2();
     std::vector<std::vector<flt>> r2();
     std::vector<VecRows> xyz4();
@@ -164,7 +186,11 @@ class RsqTracker : public StateTracker {
     std::vector<uint64_t> skips;
     bool usecom;
     parm_system* h = nullptr;
+    sptr<GpuLink> link;          // the Collection's handle, once bound
     std::vector<double> buf;
+    std::vector<double> start;   // positions at the last reset
+    unsigned long nupdates = 0;  // updates since the last reset
+    parm_system* active() { return link ? link->handle() : h; }
     void push();
     std::vector<double> get(int what, size_t per_window);
     std::vector<VecRows> rows(int what);

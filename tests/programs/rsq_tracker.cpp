@@ -75,7 +75,36 @@ int main() {
             col.timestep();
             positions("X", s, *atoms);
         }
+        std::printf("BOUND COL %d\n", rsq->bound() ? 1 : 0);
         dump("COL", *rsq);
+    }
+    // 3. the same Collection, the twelve steps in one call (the bound tracker
+    //    is updated inside the GPU steps)
+    {
+        const int k = 5;
+        const double a = 1.2, L = k * a;
+        sptr<OriginBox> box(new OriginBox(L));
+        sptr<AtomVec> atoms(new AtomVec(k * k * k, 1.0));
+        uint n = 0;
+        for (int x = 0; x < k; x++)
+            for (int y = 0; y < k; y++)
+                for (int z = 0; z < k; z++, n++) {
+                    (*atoms)[n].x = Vec((x + 0.5) * a, (y + 0.5) * a, (z + 0.5) * a);
+                    (*atoms)[n].v = Vec(0.3 * std::sin(1.0 + n), 0.3 * std::cos(2.0 * n), 0.3 * std::sin(0.5 * n));
+                }
+        sptr<NListed<EpsSigCutAtom, LennardJonesCutPair>> inter(
+            new NListed<EpsSigCutAtom, LennardJonesCutPair>(box, atoms, 0.3));
+        for (uint i = 0; i < atoms->size(); i++) inter->add(EpsSigCutAtom(atoms->get_id(i), 1.0, 1.0, 2.5));
+        sptr<RsqTracker> rsq(new RsqTracker(atoms, std::vector<unsigned long>{1, 3}, true));
+        std::vector<sptr<Interaction>> is(1, inter);
+        std::vector<sptr<StateTracker>> ts;
+        ts.push_back(inter->neighbor_list());
+        ts.push_back(rsq);
+        CollectionVerlet col(box, atoms, 0.002, is, ts);
+        col.timesteps(12);
+        std::printf("BOUND ONE %d\n", rsq->bound() ? 1 : 0);
+        dump("ONE", *rsq);
+        positions("Y", 12, *atoms);
     }
     return 0;
 }

@@ -169,6 +169,16 @@ def test_host_api_rsq_tracker(tmp_path):
     for s in range(1, 13):
         col.update(pos[s])
     _check_program(out, "COL", col, exact=False)
+    # the tracker of the Collection's own atoms is bound to its handle, and
+    # twelve steps in one call update it inside the GPU steps: the same results
+    assert out[("BOUND", "COL")] == 1 and out[("BOUND", "ONE")] == 1
+    ones = {key[1:]: v for key, v in out.items() if key[0] == "ONE"}
+    cols = {key[1:]: v for key, v in out.items() if key[0] == "COL"}
+    assert ones.keys() == cols.keys() and ones
+    for key, v in ones.items():
+        assert abs(v - cols[key]) <= 1e-12 * abs(cols[key]) + 1e-300, key
+    for (name, step, i, d), v in ((k, v) for k, v in out.items() if k[0] == "Y"):
+        assert v == pos[12][i, d]
 
 
 def test_host_api_energy_tracker(tmp_path):
