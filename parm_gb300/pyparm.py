@@ -388,6 +388,7 @@ def _make(ndim: int):
             self.rows = {}
             self.owner = None
             self.sys = None
+            self._rsq = None   # the RsqTracker bound to this handle
             self._dirty = True
             self._pushed = (-1, None, None)
             self._pairs = None
@@ -613,6 +614,72 @@ def _make(ndim: int):
     }.items():
         setattr(mod, name, _nlisted(name, mapping))
 
+    # ------------------------------------------------------------ trackers
+    class RsqTracker:
+        """Mean-square displacement over windows of ns[j] updates (src/constraints.hpp:318-361,
+        src/constraints.cpp:404-564) on the GPU.  Alone it holds its own handle and is sent the
+        positions at each update; a Collection stepping the same AtomVec binds it to its own handle,
+        whose time steps then update it on the device."""
+
+        def __init__(self, atoms, ns, usecom=True):
+            self.atoms, self.ns, self.usecom = atoms, [int(n) for n in ns], bool(usecom)
+            self.nl = None
+            self.sys = System(len(atoms), ndim=NDIM, precision="fp64")
+            self.sys.set_boxes(np.ones((1, NDIM)))   # positions are unwrapped: the box is not used
+            self.reset()
+
+        def _h(self):
+            return self.nl.sys if self.nl is not None else self.sys
+
+        def _push(self):
+            if self.nl is not None:
+                self.nl.push()
+            else:
+                r = self.atoms.rec
+                self.sys.set_atoms(x=r[:, 0:NDIM], m=r[:, 4 * NDIM])
+
+        def reset(self):
+            self._push()
+            self._h().rsq_start(self.ns, self.usecom)
+            self._start = self.atoms.rec[:, 0:NDIM].copy()
+            self._updates = 0
+
+        def update(self, box=None):
+            self._push()
+            self._h().rsq_update()
+            self._updates += 1
+
+        def bind(self, nl):
+            """Move onto `nl`'s handle; only before the first update since the last reset and with
+            the atoms where they were then (nothing is lost), and one tracker per handle."""
+            if self.nl is not None:
+                return self.nl is nl
+            if nl.atoms is not self.atoms or self._updates or getattr(nl, "_rsq", None) is not None:
+                return False
+            if not np.array_equal(self.atoms.rec[:, 0:NDIM], self._start):
+                return False
+            nl.push()
+            nl.sys.rsq_start(self.ns, self.usecom)
+            nl._rsq, self.nl = self, nl
+            self.sys.close()
+            self.sys = None
+            return True
+
+        def xyz2(self):
+            return list(self._h().rsq_get(capi.RSQ_XYZ2))
+
+        def xyz4(self):
+            return list(self._h().rsq_get(capi.RSQ_XYZ4))
+
+        def r2(self):
+            return list(self._h().rsq_get(capi.RSQ_R2))
+
+        def r4(self):
+            return list(self._h().rsq_get(capi.RSQ_R4))
+
+        def counts(self):
+            return list(self._h().rsq_get(capi.RSQ_COUNTS))
+
     # ---------------------------------------------------------- collections
     class Collection:
         """Integrators of the atoms of one NListed interaction (src/collection.hpp:23-131)."""
@@ -629,6 +696,10 @@ def _make(ndim: int):
             self.nl = next(iter(nls.values())) if nls else None
             if self.nl is not None and self.nl.atoms is not atoms:
                 raise ValueError("parm_gb300: the interaction was built on another AtomVec")
+            if self.nl is not None:
+                for t in self.trackers:
+                    if isinstance(t, RsqTracker):
+                        t.bind(self.nl)
             if initialize:
                 self.initialize()
 
@@ -658,17 +729,22 @@ def _make(ndim: int):
         def _steps(self, n):
             raise NotImplementedError
 
+        def _host_trackers(self):
+            # the GPU steps update the neighbour list and the trackers bound to its handle
+            return [t for t in self.trackers
+                    if not isinstance(t, NeighborList) and not (isinstance(t, RsqTracker) and t.nl is self.nl)]
+
         def timesteps(self, n):
             if n <= 0:
                 return
             self.nl.push()
-            if any(not isinstance(t, NeighborList) for t in self.trackers):
-                for _ in range(n):   # trackers of the caller's see every step
+            host = self._host_trackers()
+            if host:
+                for _ in range(n):   # trackers of the host see every step
                     self._steps(1)
                     self.nl.pull()
-                    for t in self.trackers:
-                        if not isinstance(t, NeighborList):
-                            t.update(self.box)
+                    for t in host:
+                        t.update(self.box)
                     self.nl.push()
                 return
             self._steps(n)
@@ -831,9 +907,19 @@ def _make(ndim: int):
         def timesteps(self, n):
             if n <= 0:
                 return
-            s = self._push()
-            s.nlcg_timestep(n)
-            self._pull(s)
+            # the minimiser's steps update no tracker but the neighbour list
+            host = [t for t in self.trackers if not isinstance(t, NeighborList)]
+            if not host:
+                s = self._push()
+                s.nlcg_timestep(n)
+                self._pull(s)
+                return
+            for _ in range(n):
+                s = self._push()
+                s.nlcg_timestep(1)
+                self._pull(s)
+                for t in host:
+                    t.update(self.box)
 
         def set_dt(self, dt):
             self.dt = float(dt)
@@ -886,7 +972,8 @@ def _make(ndim: int):
         def kinetic_energy(self):
             return self.atoms.kinetic_energy()
 
-    for c in (Collection, CollectionVerlet, CollectionDamped, CollectionSol, CollectionNLCG, CollectionNLCGV):
+    for c in (Collection, CollectionVerlet, CollectionDamped, CollectionSol, CollectionNLCG, CollectionNLCGV,
+              RsqTracker):
         setattr(mod, c.__name__, c)
     mod.seed = seed
     # picklable by name: pyparm.d3.AtomVec and so on

@@ -206,3 +206,60 @@ def test_nlcg_packing_matches_reference():
         scale = np.abs(d["x_steps"][i]).max()
         assert np.abs(x - d["x_steps"][i]).max() <= 1e-12 * scale, step
         assert np.abs(box.box_shape() - d["box_steps"][i]).max() <= 1e-12 * d["box_steps"][i].max(), step
+
+
+def test_rsq_tracker_reference_known_answers():
+    """RSQTest (pyparm/tests.py:504-569) through the module: 8 atoms moved by fixed steps."""
+    import itertools
+    sim = pyparm.d3
+    ns = [1, 2, 4, 8, 16, 32]
+    dxs = [[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1], [0, 2, 1], [-2.1, 4, 1]]
+    np.random.seed(13763)
+    radii = np.random.uniform(1.0, 2.0, size=(8,))
+    atoms = sim.AtomVec(radii ** 3)
+    box = sim.OriginBox(float((np.sum(radii ** 3) * 4 / 3 * np.pi / 0.3) ** (1 / 3)))
+    rsqs = sim.RsqTracker(atoms, ns, False)
+    drs = []
+    for t in range(ns[-1] * 4):
+        for i, (a, dr) in enumerate(zip(atoms, itertools.cycle(dxs))):
+            a.x += dr
+            if t == 0:
+                drs.append(dr)
+        rsqs.update(box)
+    drs = np.asarray(drs, dtype=float)
+    for n, r2n, xyz2n, r4n, xyz4n in zip(ns, rsqs.r2(), rsqs.xyz2(), rsqs.r4(), rsqs.xyz4()):
+        d = drs * n
+        np.testing.assert_allclose(r2n, np.sum(d ** 2, axis=-1), rtol=1e-12)
+        np.testing.assert_allclose(xyz2n, d ** 2, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(r4n, np.sum(d ** 2, axis=-1) ** 2, rtol=1e-12)
+        np.testing.assert_allclose(xyz4n, d ** 4, rtol=1e-12, atol=1e-12)
+
+
+def test_rsq_tracker_bound_in_a_collection():
+    """A tracker of the Collection's own atoms is updated inside the GPU steps (one call for twelve
+    steps); the same tracker standing alone, updated by hand after every step, gives the same results."""
+    def run(bound):
+        t = _RandomHertzianVerlet()
+        sim = pyparm.d3
+        rsq = sim.RsqTracker(t.atoms, [1, 3], True)
+        nl = t.interaction.neighbor_list()
+        trackers = [nl, rsq] if bound else [nl]
+        col = sim.CollectionVerlet(t.box, t.atoms, t.dt, [t.interaction], trackers, [])
+        if bound:
+            assert rsq.nl is nl
+            col.timesteps(12)
+        else:
+            assert rsq.nl is None
+            rsq.update(t.box)   # Collection::initialize updates its trackers twice
+            rsq.update(t.box)
+            for _ in range(12):
+                col.timestep()
+                rsq.update(t.box)
+        return rsq, t.atoms.rec[:, 0:3].copy()
+    a, xa = run(True)
+    b, xb = run(False)
+    np.testing.assert_array_equal(xa, xb)
+    assert a.counts() == b.counts()
+    for f in ("r2", "xyz2", "r4", "xyz4"):
+        for u, v in zip(getattr(a, f)(), getattr(b, f)()):
+            np.testing.assert_allclose(u, v, rtol=1e-12, atol=1e-300)
