@@ -12,15 +12,16 @@ names, 621-643, and its Python extensions, 494-667), on this package's C ABI.
     collec = sim.CollectionVerlet(box, atoms, 0.01, [rep], [rep.neighbor_list()], [])
     collec.timestep()
 
-As in the C++ host API (parm_gb300/host), the atoms live in host arrays
-that Python reads and writes between calls (``atoms[i].x = ...``); every call
-that runs on the GPU uploads them first when they changed and a time step
-downloads them after.  One neighbour list carries one GPU handle; an
-NListed interaction evaluates the pairs of its list; a Collection steps the
-atoms of its (single) interaction.  Precision: FP64 (the reference's
-numbers) unless PARM_PRECISION=mixed is set when the list's handle is made.
-Beyond the reference: ``Collection.timesteps(n)`` runs n steps with one
-upload and one download.
+As in the C++ host API (parm_gb300/host), Python reads and writes the atoms
+between calls (``atoms[i].x = ...``).  Every call that runs on the GPU first
+uploads them when they changed.  After a device call the records stay on the
+device and come back only when Python reads them.  One neighbour list
+carries one GPU handle; an NListed interaction evaluates the pairs of its
+list; a Collection steps the atoms of its (single) interaction.  An
+RsqTracker of the Collection's own atoms is updated inside the GPU steps.
+Precision: FP64 (the reference's numbers) unless PARM_PRECISION=mixed is set
+when the list's handle is made.  Beyond the reference,
+``Collection.timesteps(n)`` runs n steps in one call.
 """
 from __future__ import annotations
 
