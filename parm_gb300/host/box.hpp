@@ -70,8 +70,9 @@ class OriginBox : public Box {
     flt resize_to(Vec newsize, AtomGroup& atoms);
     flt resize_to_V(flt newV) { return resize(std::pow(newV / V(), OVERNDIM)); }
     flt resize_to_V(flt newV, AtomGroup& atoms) { return resize(std::pow(newV / V(), OVERNDIM), atoms); }
-    flt resize_to_L(flt newL) { return resize(newL / L()); }
-    flt resize_to_L(flt newL, AtomGroup& atoms) { return resize(newL / L(), atoms); }
+    // the current length is V^(1/NDIM), as src/box.cpp:44-55 takes it (not L())
+    flt resize_to_L(flt newL) { return resize(newL / std::pow(V(), 1.0 / NDIM)); }
+    flt resize_to_L(flt newL, AtomGroup& atoms) { return resize(newL / std::pow(V(), 1.0 / NDIM), atoms); }
 };
 
 //! Sheared periodic box (src/box.hpp:165-196, box.cpp:72-135): the y image

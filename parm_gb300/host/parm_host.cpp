@@ -76,8 +76,10 @@ void AtomGroup::reset_forces() {
 }
 
 void AtomGroup::randomize_velocities(flt T) {
+    // src/box.cpp:419-425: atoms of zero or infinite mass keep their velocity
     for (uint i = 0; i < size(); i++) {
         Atom& a = (*this)[i];
+        if (a.m == 0 || std::isinf(a.m)) continue;
         a.v = rand_vec() * std::sqrt(T / a.m);
     }
 }

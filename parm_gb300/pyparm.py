@@ -117,9 +117,33 @@ def _make(ndim: int):
             return self.momentum() / self.mass()
 
         def reset_com_velocity(self):
-            v = self.com_velocity()
+            # add_velocity(-com_velocity()) (src/box.hpp:426): every atom, immobile ones too
+            self.add_velocity(-self.com_velocity())
+
+        def com(self):
+            """Centre of mass of the mobile atoms (src/box.cpp:228-237)."""
             mob = self._mobile()
-            self.rec[mob, NDIM:2 * NDIM] -= v
+            r = self.rec
+            return np.sum(r[mob, 4 * NDIM, None] * r[mob, 0:NDIM], axis=0) / self.mass()
+
+        def com_force(self):
+            return np.sum(self.rec[:, 3 * NDIM:4 * NDIM], axis=0)
+
+        def gyradius(self):
+            x = self.rec[:, 0:NDIM]
+            return float(np.sqrt(np.sum((x - x.mean(axis=0)) ** 2) / len(x)))
+
+        def add_velocity(self, v):
+            self.rec[:, NDIM:2 * NDIM] += np.asarray(v, np.float64)
+            self.touch()
+
+        def randomize_velocities(self, T):
+            """Normal velocity components of variance T/m (src/box.cpp:419-425, numpy's global
+            generator); atoms of zero or infinite mass keep theirs."""
+            r = self.rec
+            m = r[:, 4 * NDIM]
+            sel = ~((m == 0) | np.isinf(m))
+            r[sel, NDIM:2 * NDIM] = np.random.normal(size=(int(sel.sum()), NDIM)) * np.sqrt(T / m[sel])[:, None]
             self.touch()
 
         def reset_forces(self):
@@ -232,6 +256,10 @@ def _make(ndim: int):
 
         def resize_to_V(self, newV, atoms=None):
             return self.resize((newV / self.V()) ** (1.0 / NDIM), atoms)
+
+        def resize_to_L(self, newL, atoms=None):
+            # the current length is V^(1/NDIM), as src/box.cpp:44-55 takes it
+            return self.resize(newL / self.V() ** (1.0 / NDIM), atoms)
 
     class LeesEdwardsBox(OriginBox):
         """Sheared periodic box (src/box.hpp:165-196, box.cpp:72-135): FP64 handles."""
@@ -774,6 +802,9 @@ def _make(ndim: int):
 
         def degrees_of_freedom(self):
             return NDIM * int(np.sum(self.atoms._mobile()))
+
+        def com(self):
+            return self.atoms.com()
 
         def com_velocity(self):
             if self._resident():

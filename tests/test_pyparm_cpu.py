@@ -104,3 +104,24 @@ def test_records_are_read_back_only_when_the_host_reads_them():
     assert DeviceStub.fetches == 1
     atoms[2].x = [1.0, 2.0, 3.0]
     assert DeviceStub.fetches == 1 and atoms._dev is None
+
+
+def test_atom_group_quantities():
+    sim = pyparm.d3
+    atoms = sim.AtomVec([1.0, 2.0, 0.0, float("inf")])
+    xs = np.array([[1.0, 0, 0], [0, 3.0, 0], [5.0, 5.0, 5.0], [7.0, 7.0, 7.0]])
+    for a, x in zip(atoms, xs):
+        a.x = x
+        a.v = [1.0, 2.0, 3.0]
+    np.testing.assert_allclose(atoms.com(), [1 / 3, 2.0, 0.0])   # mobile atoms only
+    np.random.seed(5)
+    atoms.randomize_velocities(2.0)
+    v = atoms.rec[:, 3:6]
+    assert np.array_equal(v[2], [1.0, 2.0, 3.0]) and np.array_equal(v[3], [1.0, 2.0, 3.0])
+    assert np.all(np.isfinite(v)) and not np.array_equal(v[0], [1.0, 2.0, 3.0])
+    atoms.add_velocity([1.0, 0.0, 0.0])
+    assert atoms.rec[2, 3] == 2.0
+    assert atoms.gyradius() == pytest.approx(np.sqrt(np.sum((xs - xs.mean(axis=0)) ** 2) / 4))
+    box = sim.OriginBox([2.0, 2.0, 4.0])
+    box.resize_to_L(4.0)
+    np.testing.assert_allclose(box.V(), 64.0)
