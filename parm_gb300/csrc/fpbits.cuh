@@ -9,6 +9,7 @@
 // instruction itself.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -89,6 +90,59 @@ PARM_FPB_HD float d2f_bits(double d) {
         return fpb_u2f(f);
     }
     return (float)d;
+}
+
+PARM_FPB_HD float fpb_i2f(int32_t i) {
+#if defined(__CUDA_ARCH__)
+    return __int2float_rn(i);
+#else
+    return (float)i;
+#endif
+}
+
+PARM_FPB_HD float fpb_fma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+
+PARM_FPB_HD float fpb_sub(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
+// The fine part x - X of a position against its coarse point X (a float,
+// a multiple of 1/8 within about 1/4 of x), in FP32 without FP64 arithmetic:
+// x = xh + r with xh = (float)x (the rounding above) and r the 29 dropped
+// fraction bits (signed by the rounding direction: |r| <= ulp(xh) / 2, an
+// integer count of x's ulps, scaled by a power of two), then
+// (xh - X) + r with one rounding (a fused multiply-add).  xh - X is exact
+// when X and xh are within a factor of two (the rule of Sterbenz), so the
+// result is (float)(x - X) but for a rare double rounding near a tie (r is
+// itself rounded to 24 bits); near the origin, where X may lie in another
+// binade, xh - X can round too.  Either way the result is within one ulp of
+// (float)(x - X).  Outside 2^-74 <= |x| < 2^127 the FP64 subtraction is
+// taken.
+PARM_FPB_HD float fine_bits(double x, float X) {
+    uint32_t hi, lo;
+    fpb_d2hilo(x, hi, lo);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if (e - 949u < 200u) {
+        uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+        const uint32_t rem = lo & 0x1FFFFFFFu;
+        const bool up = rem > 0x10000000u || (rem == 0x10000000u && (f & 1u));
+        f += up ? 1u : 0u;
+        // |x| - |xh| in units of 2^(e - 1075), then the sign of x
+        int32_t r = up ? (int32_t)rem - 0x20000000 : (int32_t)rem;
+        if (hi & 0x80000000u) r = -r;
+        return fpb_fma(fpb_i2f(r), fpb_u2f((e - 948u) << 23), fpb_sub(fpb_u2f(f), X));
+    }
+    return d2f_bits(x - f2d_bits(X));
 }
 
 }  // namespace parm

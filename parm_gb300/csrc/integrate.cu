@@ -231,14 +231,19 @@ __global__ void __launch_bounds__(BLOCK) k_kickdrift(DevCtx c) {
             // at the last rebuild or upload (x - X is exact in FP64); an atom
             // that has moved more than 1/4 from its coarse point is re-anchored
             // (any multiple of 1/8 is a valid coarse point)
-            // (the conversions on the bit patterns: integer instructions, the
-            // same values as the FP64 conversion instructions)
+            // (mixed path: on the bit patterns, integer and FP32 instructions
+            // only, within one ulp of (float)(x - X) and equal to it but for
+            // rare roundings; FP64 path: the FP64 subtraction, exact, with the
+            // conversions on the bit patterns)
             float4 A = c.pos[2 * (size_t)i];
             float4 B;
-            B.x = d2f_bits(x[0] - f2d_bits(A.x));
-            B.y = d2f_bits(x[1] - f2d_bits(A.y));
+            auto fine = [](double xd, float Xf) {
+                return MIXED ? fine_bits(xd, Xf) : d2f_bits(xd - f2d_bits(Xf));
+            };
+            B.x = fine(x[0], A.x);
+            B.y = fine(x[1], A.y);
             B.z = 0.f;
-            if constexpr (ND == 3) B.z = d2f_bits(x[2] - f2d_bits(A.z));
+            if constexpr (ND == 3) B.z = fine(x[2], A.z);
             B.w = 0.f;
             if (fabsf(B.x) > 0.25f || fabsf(B.y) > 0.25f || fabsf(B.z) > 0.25f) {
                 posq_split2(x[0], A.x, B.x);
