@@ -263,3 +263,39 @@ def test_rsq_tracker_bound_in_a_collection():
     for f in ("r2", "xyz2", "r4", "xyz4"):
         for u, v in zip(getattr(a, f)(), getattr(b, f)()):
             np.testing.assert_allclose(u, v, rtol=1e-12, atol=1e-300)
+
+
+def test_xyz_frames_of_device_resident_atoms():
+    """Frames written between device calls hold the positions of the last step (one read-back)."""
+    import io
+    from parm_gb300.xyzfile import XYZreader, XYZwriter
+    t = _RandomHertzianVerlet()
+    nl = t.interaction.neighbor_list()
+    f = io.StringIO()
+    w = XYZwriter(f)
+    for k in range(3):
+        t.collec.timesteps(10)
+        assert nl.resident()
+        w.writeframe(t.atoms, time=10 * (k + 1), E=t.collec.energy())
+        assert not nl.resident()
+    f.seek(0)
+    frames = XYZreader(f).all()
+    assert [fr.time for fr in frames] == [10.0, 20.0, 30.0]
+    np.testing.assert_allclose(frames[-1].locs, t.atoms.rec[:, 0:3], atol=5e-5)
+    np.testing.assert_allclose(frames[-1].vels, t.atoms.rec[:, 3:6], atol=5e-5)
+
+
+def test_rsq_tracker_in_a_minimiser():
+    """The conjugate-gradient steps update no tracker themselves: a bound tracker is updated from the
+    host after every step, as the reference's update_trackers does."""
+    d = load("nlcg64_pack")
+    sim = pyparm.d3
+    box, atoms, inter = _build(d, sim)
+    nl = inter.neighbor_list()
+    nl.update_list(True)
+    rsq = sim.RsqTracker(atoms, [1, 2], False)
+    cg = d["cg"]
+    col = sim.CollectionNLCG(box, atoms, cg[0], cg[1], [inter], [nl, rsq], [], cg[2], cg[3], int(cg[4]), cg[5])
+    assert rsq.nl is nl
+    col.timesteps(6)
+    assert rsq.counts() == [8.0, 4.0]   # two updates at construction and one per step, windows of 1 and 2
