@@ -1148,6 +1148,7 @@ int parm_create(parm_system** out, int ndim, uint32_t nsys, const uint32_t* nato
     A(S->alloc(c.which, nsys));
     A(S->alloc(c.seed, nsys));
     A(S->alloc(c.status, 1));
+    A(S->alloc(c.m_mixed, 1));
     A(S->alloc(c.any_flag, 1));
     A(S->alloc(c.chains, 1));
     A(S->alloc(c.params, 1));
@@ -1506,6 +1507,12 @@ int parm_set_interaction(parm_system* S, int kind, const double* params, const u
     CUDA_TRY(cudaMemcpy(S->c.diam, diam_k.data(), 8 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.rank, rank_k.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(S->c.nm_rank, nmr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+    bool same = true;
+    for (uint32_t k = 1; k < n && same; k++)
+        same = std::memcmp(&prm_k[k], &prm_k[0], sizeof(AtomPrm)) == 0 &&
+               std::memcmp(&prm32_k[k], &prm32_k[0], sizeof(float4)) == 0 &&
+               std::memcmp(&diam_k[k], &diam_k[0], sizeof(double)) == 0;
+    S->c.same_prm = same ? 1u : 0u;
     if (kind == PARM_LOISOHERN_MIN || kind == PARM_LOISLIN_MIN) uni |= COMB_MIN;
     if (indexed || kind == PARM_LJATTRACTREPULSESIGS) {
         // per-pair values from the tables, or a fifth parameter: no per-atom shortcuts

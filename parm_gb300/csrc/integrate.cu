@@ -380,6 +380,8 @@ __global__ void k_scatter_in(DevCtx c, const double* st, uint64_t stride, uint32
         double m = r[4 * ND];
         c.m[k] = m;
         c.invm32[k] = mobile(m) ? (float)(1.0 / m) : 0.f;
+        // a mass whose bits differ from the first record's
+        if (__double_as_longlong(m) != __double_as_longlong(st[4 * ND])) atomicOr(c.m_mixed, 1u);
     }
 }
 
@@ -413,6 +415,7 @@ __global__ void k_gather_out(DevCtx c, double* st, uint64_t stride, uint32_t fie
 
 void launch_scatter_in(const DevCtx& c, cudaStream_t s, const double* st, uint64_t stride,
                        uint32_t fields) {
+    if (fields & FB_M) cudaMemsetAsync(c.m_mixed, 0, sizeof(uint32_t), s);   // every mass is uploaded
     if (c.nd == 3) k_scatter_in<3><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
     else k_scatter_in<2><<<grid_for(c.n), BLOCK, 0, s>>>(c, st, stride, fields);
 }

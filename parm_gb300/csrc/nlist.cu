@@ -319,11 +319,16 @@ __global__ void k_gather(DevCtx c) {
     static_cast<V*>(c.a2)[k] = static_cast<const V*>(c.a)[o];
     if (c.prec != PREC_MIXED) static_cast<V*>(c.f2)[k] = static_cast<const V*>(c.f)[o];   // FP64 forces: FP64 path only
     c.f32b[k] = c.f32[o];
-    c.m2[k] = c.m[o];
-    c.invm32b[k] = c.invm32[o];
-    c.prm2[k] = c.prm[o];
-    c.prm32b[k] = c.prm32[o];
-    c.diam2[k] = c.diam[o];
+    // arrays whose entries are all equal are left as they are (copy back too)
+    if (*c.m_mixed) {
+        c.m2[k] = c.m[o];
+        c.invm32b[k] = c.invm32[o];
+    }
+    if (!c.same_prm) {
+        c.prm2[k] = c.prm[o];
+        c.prm32b[k] = c.prm32[o];
+        c.diam2[k] = c.diam[o];
+    }
     c.rank2[k] = c.rank[o];
     c.orig2[k] = c.orig[o];
     c.bucket2[k] = c.bucket[o];
@@ -343,12 +348,19 @@ __global__ void k_copyback(DevCtx c) {
     static_cast<V*>(c.a)[k] = static_cast<const V*>(c.a2)[k];
     if (c.prec != PREC_MIXED) static_cast<V*>(c.f)[k] = static_cast<const V*>(c.f2)[k];
     c.f32[k] = c.f32b[k];
-    c.m[k] = c.m2[k];
-    c.invm32[k] = c.invm32b[k];
-    c.prm[k] = c.prm2[k];
-    c.prm32[k] = c.prm32b[k];
-    double dk = c.diam2[k];
-    c.diam[k] = dk;
+    if (*c.m_mixed) {
+        c.m[k] = c.m2[k];
+        c.invm32[k] = c.invm32b[k];
+    }
+    double dk;
+    if (!c.same_prm) {
+        c.prm[k] = c.prm2[k];
+        c.prm32[k] = c.prm32b[k];
+        dk = c.diam2[k];
+        c.diam[k] = dk;
+    } else {
+        dk = c.diam[k];   // every atom's
+    }
     c.rank[k] = c.rank2[k];
     uint32_t og = c.orig2[k];
     c.orig[k] = og;

@@ -55,6 +55,12 @@ struct DevCtx {
     uint32_t tiled;    // use the shared-memory tiled variant (lists via tiles)
     uint32_t maxnb;    // neighbour capacity per atom
     uint32_t uniform;  // UniformFlags
+    // every atom has the same pair parameters and list diameter (prm, prm32,
+    // diam): a rebuild's permutation leaves those arrays as they are
+    uint32_t same_prm;
+    // device word: nonzero once an upload gave two atoms different masses;
+    // zero, a rebuild's permutation leaves m and invm32 as they are
+    uint32_t* m_mixed;
     uint32_t nbucket;  // total buckets (sum over systems of ncell + 1)
     uint32_t any_wrap; // some system has an axis with a single cell (per-pair minimum image)
     uint32_t any_lees; // some system is a LeesEdwardsBox: all-pairs list builds
