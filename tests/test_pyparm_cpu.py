@@ -125,3 +125,63 @@ def test_atom_group_quantities():
     box = sim.OriginBox([2.0, 2.0, 4.0])
     box.resize_to_L(4.0)
     np.testing.assert_allclose(box.V(), 64.0)
+
+
+def test_interaction_and_collection_checks():
+    """The layer's checks that run before any device call (the C++ host API raises the same ones)."""
+    sim = pyparm.d3
+    box = sim.OriginBox(10.0)
+    atoms = sim.AtomVec([1.0] * 4)
+    rep = sim.Repulsion(box, atoms, 0.3)
+    rep.add(sim.EpsSigExpAtom(atoms[0], 1.0, 1.0, 2.0))
+    with pytest.raises(ValueError):        # an atom added twice
+        rep.add(sim.EpsSigExpAtom(atoms[0], 1.0, 1.0, 2.0))
+    with pytest.raises(TypeError):         # an atom type of another interaction
+        rep.add(sim.EpsSigCutAtom(atoms[1], 1.0, 1.0, 2.5))
+    with pytest.raises(ValueError):        # a second NListed on the same neighbour list
+        other = sim.LJRepulse(atoms, rep.neighbor_list())
+        other.add(sim.EpsSigAtom(atoms[2], 1.0, 1.0))
+    with pytest.raises(ValueError):        # constraints are outside the GPU path
+        sim.CollectionVerlet(box, atoms, 0.01, [rep], [rep.neighbor_list()], [object()])
+    rep2 = sim.Repulsion(box, atoms, 0.3)
+    with pytest.raises(ValueError):        # one neighbour list per Collection
+        sim.CollectionVerlet(box, atoms, 0.01, [rep, rep2], [], [])
+    with pytest.raises(ValueError):        # an interaction of another AtomVec
+        sim.CollectionVerlet(box, sim.AtomVec([1.0] * 4), 0.01, [rep], [], [])
+    ii = sim.LJIICut(box, sim.AtomVec([1.0] * 2), 0.3)
+    a0, a1 = ii.nl.atoms[0], ii.nl.atoms[1]
+    ii.add(sim.IEpsISigCutAtom(a0, [1.0, 0.5], [1.0, 1.1], 0, 2.5))
+    with pytest.raises(ValueError):        # atoms of one type index share their rows
+        ii.add(sim.IEpsISigCutAtom(a1, [0.9, 0.5], [1.0, 1.1], 0, 2.5))
+    with pytest.raises(ValueError):
+        sim.CollectionSol(box, atoms, 0.0, 1.0, 1.0, [rep], [], [])   # dt must be positive
+
+
+def test_records_of_every_atom_type():
+    """Each atom type's C ABI record holds the number of parameters its kind takes."""
+    sim = pyparm.d3
+    atoms = sim.AtomVec([1.0])
+    a = atoms[0]
+    cases = {
+        sim.LJRepulse: sim.EpsSigAtom(a, 1.0, 1.1),
+        sim.LJCut: sim.EpsSigCutAtom(a, 1.0, 1.1, 2.5),
+        sim.Repulsion: sim.EpsSigExpAtom(a, 1.0, 1.1, 2.5),
+        sim.HertzianDrag: sim.EpsSigExpDragAtom(a, 1.0, 1.1, 0.3),
+        sim.LoisOhern: sim.LoisOhernAtom(a, 1.0, 1.1, 0.2, 0.1),
+        sim.LoisLin: sim.LoisLinAtom(a, 1.0, 1.1, 0.2, 0.1),
+        sim.EisMclachlan: sim.EisMclachlanAtom(a, 1.5, 0.2),
+        sim.LJAttractRepulseSigs: sim.EpsEpsSigSigCutAtom(a, 1.0, 0.5, 1.0, 1.2, 2.5),
+        sim.LJAttractICut: sim.IEpsSigCutAtom(a, [1.0, 0.5], 1, 1.1, 2.5),
+        sim.LJAttractFixedRepulse: sim.IEpsRepsSigCutAtom(a, [1.0, 0.5], 0.7, 1.1, 1, 2.5),
+        sim.LJish: sim.IEpsRepsSigExpCutAtom(a, [1.0, 0.5], 0.7, 1.1, 6.0, 1, 2.5),
+        sim.RepulsionII: sim.IEpsISigExpAtom(a, [1.0, 0.5], [1.0, 1.2], 1, 2.0),
+    }
+    for cls, atom in cases.items():
+        kind = next(iter(cls.kinds.values()))
+        assert type(atom) in cls.kinds
+        assert len(atom.p) >= capi.nparam(kind), (cls.__name__, atom.p)
+        assert atom.max_size() > 0
+    drag = cases[sim.HertzianDrag]
+    assert drag.p == [1.0, 1.1, 2.5, 0.3]   # (eps, sigma, exponent, gamma): exponent defaults to 2.5
+    lin = cases[sim.LoisLin]
+    assert lin.p[2] == pytest.approx(2.0) and lin.p[3] == 0.1   # f = depth / width
